@@ -1,0 +1,314 @@
+#!/usr/bin/env python
+"""Benchmark: neutron histories/s of the LET-like chopper-spectrometer chain
+(1e8 histories per step, FP32, reference RNG keying) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one Instrument.execute(1e8) of the LET-like instrument (Maxwellian
+moderator, 4 supermirror guides, 5 disk choppers, 40-line powder sample,
+720 x 1000 banana detector) on the fused path (whole chain in one
+persistent kernel).  The plain path (one kernel per component, neutron
+state in HBM) is timed beside it on the same histories.  The instrument is
+a seeded synthetic stand-in for the reference's LET example.
+
+value: histories/s over all ranks, device-timed (CUDA events per step, L2
+flushed between steps by writing a 256 MiB buffer outside the events).
+e2e:   histories/s through the public API including Instrument
+construction (IDF parse, table upload), execute and the histogram readback.
+roofline: the fused kernel is bound by integer issue (Threefry-4x32-20,
+about 150 integer operations per random draw), not by HBM or tensor cores;
+achieved = draws x ops per draw / kernel time, peak = the same operation
+rate measured by a Threefry-only kernel on this GPU.
+Multi-GPU (torchrun): each rank traces its own 1e8-history slice of one
+chunk of N x 1e8 (weak scaling, no collective in the timed region); the
+histograms are summed once afterwards.
+--impl reference times the CPU restatement of the reference kernels (the
+reference's OpenCL path cannot run here) on a bounded sample with all host
+threads.
+"""
+import argparse
+import json
+import os
+import random
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+N_HIST = 100_000_000
+THREEFRY_OPS = 148          # integer operations per Threefry-4x32-20 draw
+CPU_SAMPLE = 2_000_000      # histories per CPU-baseline step
+
+
+def args_():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=N_HIST)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload_config(n, world):
+    return {"workload": "LET-like chain (MCont 40 K, 4 m=2 guides, 5 choppers at Ei 3.7 meV, "
+                        "40-line powder, 720x1000 banana histogram)",
+            "histories_per_step_per_gpu": n, "global_histories_per_step": n * world,
+            "rng": "reference keying (Threefry-4x32-20, one block per draw)",
+            "path": "fused persistent kernel (plain per-component path reported beside)",
+            "l2": "flushed between steps (256 MiB write)", "parallelism": "dp%d" % world}
+
+
+# ---------------------------------------------------------------- CPU arm
+def cpu_histories_per_s(n, steps=1, warmup=1):
+    import oracle
+    import ramp_gb300 as m
+    from ramp_gb300 import instruments as I
+    inst = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
+    threads = os.cpu_count() or 1
+    for _ in range(warmup):
+        random.seed(1)
+        oracle.run(inst, n, threads=threads)
+    times = []
+    for k in range(steps):
+        random.seed(100 + k)
+        t0 = time.perf_counter()
+        oracle.run(inst, n, threads=threads)
+        times.append(time.perf_counter() - t0)
+    return n / min(times), threads, times
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    steps = max(1, a.steps)
+    v, threads, times = cpu_histories_per_s(CPU_SAMPLE, steps=steps, warmup=max(1, min(a.warmup, 2)))
+    sample = ("%d histories of the LET-like chain per step (a bounded sample of the %d-history "
+              "workload), CPU restatement of the reference kernels in reference sequencing "
+              "(5 passes per component, array-of-structs records), OpenMP" % (CPU_SAMPLE, a.n))
+    line = {"metric": "neutron histories/s", "value": v, "unit": "histories/s",
+            "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
+            "ms_per_step": 1000.0 * statistics.mean(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference", "config": workload_config(CPU_SAMPLE, 1),
+            "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- clocks
+class Clocks:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.index = index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 7:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- GPU arm
+def main():
+    a = args_()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import ramp_gb300 as m
+    from ramp_gb300 import _abi, build, instruments as I
+    build.build()
+    lib = _abi.load()
+    fn, kw = I.path("let_like.json"), I.let_like_kwargs()
+    n = a.n
+    shard = (rank, world) if world > 1 else None
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def timed(inst, path, steps, warmup):
+        for w in range(warmup):
+            random.seed(10 + w)
+            inst.execute(n * world if shard else n, path=path, shard=shard)
+        barrier()
+        torch.cuda.synchronize()
+        ms = []
+        for k in range(steps):
+            flush.fill_(float(k))
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            random.seed(1000 + k)
+            s.record()
+            inst.execute(n * world if shard else n, path=path, shard=shard)
+            e.record()
+            e.synchronize()
+            ms.append(s.elapsed_time(e))
+        torch.cuda.synchronize()
+        barrier()
+        return ms
+
+    inst = m.Instrument(fn, dev, **kw)
+    inst.plan()
+    clocks = Clocks(local)
+    clocks.start()
+    fused_ms = timed(inst, "fused", a.steps, a.warmup)
+    clk = clocks.stop()
+    plain = m.Instrument(fn, dev, **kw)
+    plain_ms = timed(plain, "plain", max(2, a.steps // 2), max(1, min(a.warmup, 2)))
+
+    tot = torch.tensor([sum(fused_ms), sum(plain_ms)], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+        for t in inst.tallies():       # the one exchange step: histogram sum
+            dist.all_reduce(t)
+    fused_total_ms, plain_total_ms = float(tot[0]), float(tot[1])
+    value = world * n * a.steps / (fused_total_ms / 1000.0)
+    plain_value = world * n * len(plain_ms) / (plain_total_ms / 1000.0)
+
+    # ---- roofline of the fused kernel: draws from the plain records ----
+    stream = torch.cuda.current_stream(dev)
+    recs = plain.state[_abi.LANE["mc"], :plain.last_chunk]
+    seed_last = None
+    random.seed(1000 + len(plain_ms) - 1)
+    seed_last = plain.source.next_seed()
+    draws = float((recs.double() - seed_last).sum())
+    kern = []
+    for k in range(3):
+        random.seed(1000 + len(plain_ms) - 1)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        rngd = _abi.RampRng()
+        s.record(stream)
+        rc = lib.ramp_trace_fused(inst.plan(), plain.last_chunk, plain.last_chunk, seed_last,
+                                  _abi.ctypes.byref(rngd), None, None, None,
+                                  _abi.ctypes.c_void_p(stream.cuda_stream))
+        e.record(stream)
+        e.synchronize()
+        _abi.check(lib, rc, "ramp_trace_fused")
+        kern.append(s.elapsed_time(e))
+    kern_ms = statistics.median(kern)
+    out = torch.empty(152 * 2048 * 4, dtype=torch.int32, device=dev)
+    iters = 256
+    for _ in range(2):
+        lib.ramp_debug_rng_peak(out.numel(), iters, out.data_ptr(), _abi.ctypes.c_void_p(stream.cuda_stream))
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    lib.ramp_debug_rng_peak(out.numel(), iters, out.data_ptr(), _abi.ctypes.c_void_p(stream.cuda_stream))
+    e.record(stream)
+    e.synchronize()
+    peak_draws_s = out.numel() * iters * 2 / (s.elapsed_time(e) / 1000.0)
+    achieved_ops = draws * THREEFRY_OPS / (kern_ms / 1000.0)
+    peak_ops = peak_draws_s * THREEFRY_OPS
+    inst._check_status(lib, inst.plan())
+
+    # ---- end to end through the public API ----
+    e2e_steps = max(2, a.steps // 2)
+    e2e_ms, h2d, d2h = [], 0, 0
+    for k in range(e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ei = m.Instrument(fn, dev, **kw)
+        random.seed(5000 + k)
+        ei.execute(n * world if shard else n, path="fused", shard=shard)
+        d = ei.data()
+        t1 = time.perf_counter()
+        if k > 0:
+            e2e_ms.append(1000.0 * (t1 - t0))
+        keep = []
+        src, carr, nc, barr, nb = ei.descriptors(keep)
+        h2d = sum(x.nbytes for x in keep) + _abi.ctypes.sizeof(carr) + _abi.ctypes.sizeof(barr)
+        d2h = sum(t.numel() * t.element_size() for t in ei.tallies())
+        del ei, d
+    e2e = world * n / (statistics.mean(e2e_ms) / 1000.0)
+
+    if rank != 0:
+        return
+    cpu = None
+    if not a.no_cpu_baseline:
+        v, threads, _ = cpu_histories_per_s(CPU_SAMPLE, steps=1, warmup=1)
+        cpu = {"value": v, "unit": "histories/s", "cores": threads, "kind": "port",
+               "sample": "%d LET-like histories, CPU restatement of the reference kernels "
+                         "(reference sequencing), OpenMP, best of 1 after 1 warm-up" % CPU_SAMPLE}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    line = {
+        "metric": "neutron histories/s", "value": value, "unit": "histories/s",
+        "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": fused_total_ms / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(n, world),
+        "plain_path": {"value": plain_value, "unit": "histories/s",
+                       "ms_per_step": plain_total_ms / len(plain_ms)},
+        "fused_over_plain": value / plain_value,
+        "roofline": {"bound": "issue", "achieved": achieved_ops / 1e9, "peak": peak_ops / 1e9,
+                     "unit": "Gop/s", "frac": achieved_ops / peak_ops, "traffic": None,
+                     "kernel": "k_fused", "kernel_ms": kern_ms, "draws_per_launch": draws,
+                     "ops_per_draw": THREEFRY_OPS,
+                     "peak_source": "measured: Threefry-only kernel (ramp_debug_rng_peak), "
+                                    "%d threads x %d x 2 blocks" % (out.numel(), iters),
+                     "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "histories/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "includes": "Instrument(...) parse + plan/table upload, execute, data() readback"},
+        "gpu_launches": a.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

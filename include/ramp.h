@@ -1,0 +1,264 @@
+/*
+ * ramp.h — C ABI of libramp_cuda.so, the GB300 (sm_103a) implementation of
+ * RAMP's per-neutron ray-tracing chain (moderator -> geometry -> scatter ->
+ * detector tally).
+ *
+ * The reference (gcassella/RAMP) has no C ABI: its boundary is the Python
+ * plugin API (mcramp/mcramp.py and the moderator/, geom/, scat/ classes),
+ * which enqueues one OpenCL kernel per plugin call through pyopencl.  Each
+ * entry point below names the reference call sequence it replaces.
+ *
+ * Conventions
+ *   - every function returns 0 on success and a negative RAMP_E* code on
+ *     failure; ramp_last_error() gives a message.  Nothing exits or traps.
+ *   - all neutron state and all tallies are caller-owned device memory
+ *     (plain pointers + sizes); a plan owns only the tables it uploads and a
+ *     small status block.
+ *   - plans are immutable after creation except for ramp_plan_set_*;
+ *     concurrent calls on different streams with distinct state/tallies are
+ *     safe, calls on one plan that share tallies race like the reference's
+ *     float atomics do.
+ *   - streams are passed as void* (a cudaStream_t; NULL = legacy default).
+ */
+#ifndef RAMP_H
+#define RAMP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAMP_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define RAMP_OK              0
+#define RAMP_E_INVALID      -1   /* bad argument or descriptor            */
+#define RAMP_E_CUDA         -2   /* a CUDA runtime call failed            */
+#define RAMP_E_NOMEM        -3   /* device allocation failed              */
+#define RAMP_E_DEVICE       -4   /* a kernel raised a device status flag  */
+#define RAMP_E_UNSUPPORTED  -5   /* component kind not available here     */
+#define RAMP_E_RANGE        -6   /* size beyond a documented maximum      */
+
+/* ---- device status flags (bit set in the plan's status word) ----------- */
+#define RAMP_F_GUIDE_CAP      1u  /* guide bounce loop hit its hard cap     */
+#define RAMP_F_POWDER_CAP     2u  /* powder line walk hit its hard cap      */
+#define RAMP_F_TALLY_OOB      4u  /* a bin index fell outside its buffer    */
+#define RAMP_F_BVH_STACK      8u  /* BVH traversal stack overflow           */
+#define RAMP_F_WORKQ         16u  /* persistent work queue gave up          */
+
+/* ---- neutron record lanes (NOTES:3-14, mcramp/include/consts.h:91-108) - */
+enum RampLane {
+  RAMP_X = 0, RAMP_Y, RAMP_Z, RAMP_VX, RAMP_VY, RAMP_VZ,
+  RAMP_PX, RAMP_PY, RAMP_PZ, RAMP_P, RAMP_TOF,
+  RAMP_MC,        /* sb: RNG draw counter, a float (rand.h:5,18)          */
+  RAMP_PREVCOMP,  /* sc                                                   */
+  RAMP_SD,        /* sd: Q of the last isotropic scatter                  */
+  RAMP_SE,        /* se: omega (isotropic) / counted flag (counter)       */
+  RAMP_DIE,       /* sf: termination flag                                 */
+  RAMP_NLANES
+};
+
+/* ---- component kinds --------------------------------------------------- */
+enum RampSourceKind {
+  RAMP_SRC_FLAT = 1,   /* MFlat  moderator/flat_mod.py:10, flat_mod.cl:4  */
+  RAMP_SRC_CONT = 2    /* MCont  moderator/cont_mod.py:10, cont_mod.cl:11 */
+};
+
+enum RampGeomKind {
+  RAMP_G_PLANE      = 1,  /* GPlane       geom/plane.cl:3               */
+  RAMP_G_CYL_EXT    = 2,  /* GCylinderExt geom/cylinder_ext.cl:3        */
+  RAMP_G_BANANA     = 3,  /* GBanana      geom/banana.cl:3              */
+  RAMP_G_SPHERE     = 4,  /* GSphere      geom/sphere.cl:3              */
+  RAMP_G_SPHERE_INT = 5,  /* GSphereInt   geom/sphere_int.cl:3          */
+  RAMP_G_BOX        = 6,  /* GBox         geom/box.cl:3                 */
+  RAMP_G_ARM        = 7,  /* GArm         geom/arm.cl:3                 */
+  RAMP_G_MESH       = 8   /* GMesh        geom/mesh.cl:3 (BVH on GPU)   */
+};
+
+enum RampScatKind {
+  RAMP_S_ARM       = 1,   /* SArm         scat/arm.cl:3                 */
+  RAMP_S_GUIDE     = 2,   /* SGuide       scat/guide.cl:9               */
+  RAMP_S_CHOPPER   = 3,   /* SChopper     scat/chopper.cl:4             */
+  RAMP_S_ISOTROPIC = 4,   /* SIsotropic   scat/isotropic.cl:75          */
+  RAMP_S_POWDERN   = 5,   /* SPowderN     scat/powderN.cl:5             */
+  RAMP_S_DET1D     = 6,   /* SDetector1D  scat/detector1D.cl:20         */
+  RAMP_S_DET2D     = 7,   /* SDetector2D  scat/detector2D.cl:31         */
+  RAMP_S_COUNTER   = 8,   /* SCounter     scat/counter.cl:18            */
+  RAMP_S_BEAMSTOP  = 9,   /* SBeamstop    scat/beamstop.cl:3            */
+  RAMP_S_ATTENUATE = 10   /* SAttenuate   no reference counterpart: Beer-
+                             Lambert weight over the summed mesh chords */
+};
+
+/* ---- descriptors ------------------------------------------------------- */
+#define RAMP_NGP 12
+#define RAMP_NSP 24
+#define RAMP_NGI 4
+#define RAMP_NSI 12
+#define RAMP_NTAB 12
+
+/* One moderator (the component with "source": true, mcramp.py:58-63).
+ * p[]: mod_dim.x, mod_dim.y, target_dim.x, target_dim.y, target_dist,
+ *      E_min, E_max, T1, I1, T2, I2, T3, I3, str_area               */
+typedef struct RampSource {
+  int32_t kind;
+  int32_t reserved;
+  float p[16];
+} RampSource;
+
+/* One non-source component (mcramp.py:65-108): a geometry kernel and a
+ * scattering kernel sharing a frame (position, rotation) and an index.
+ * Parameter slots per kind are listed in the Python plugin classes
+ * (ramp_gb300/geom, ramp_gb300/scat) that fill them.                      */
+typedef struct RampComp {
+  int32_t geom;                 /* RampGeomKind                          */
+  int32_t scat;                 /* RampScatKind                          */
+  uint32_t idx;                 /* component index (mcramp.py:86,112)    */
+  uint32_t restore;             /* component restore_neutron (:68,104)   */
+  float pos[3];                 /* position (after "relative")           */
+  float rot[3];                 /* Euler angles x,y,z in radians         */
+  float gp[RAMP_NGP];           /* geometry float parameters             */
+  float sp[RAMP_NSP];           /* scatter float parameters              */
+  int32_t gi[RAMP_NGI];         /* geometry integer parameters           */
+  int32_t si[RAMP_NSI];         /* scatter integer parameters            */
+  const float* table[RAMP_NTAB];/* host tables, copied at plan creation  */
+  int64_t table_len[RAMP_NTAB]; /* lengths in floats                     */
+  float* tally;                 /* caller-owned tally (device memory)    */
+  float* tally_err;             /* caller-owned sum of squared weights   */
+  int64_t tally_len;            /* floats in each of tally / tally_err   */
+} RampComp;
+
+/* An execution block (mcramp.py:35-116, 368-382): components
+ * [first, first+count) run linearly, or "multi" events non-linearly.     */
+typedef struct RampBlock {
+  int32_t first;
+  int32_t count;
+  int32_t linear;
+  int32_t multi;
+} RampBlock;
+
+/* Neutron state in HBM, structure of arrays: lane l of neutron i lives at
+ * soa[l*stride + i] (l < RAMP_NLANES); iidx[i] is the intersected-component
+ * index buffer (doc/writing/buffers.rst:84-88).  stride is a multiple of 4
+ * and soa is 16-byte aligned.                                             */
+typedef struct RampState {
+  float* soa;
+  uint32_t* iidx;
+  int64_t stride;
+} RampState;
+
+/* RNG keying.  mode 0 reproduces the reference stream exactly
+ * (mcramp/include/rand.h:4-21): key = {tid, 0xdecafbad, 0xfacebead,
+ * 0x12345678}, counter word 0 = (uint)sb, one Threefry-4x32-20 block per
+ * draw, word x only.  mode 1 ("native") uses all four words of each block:
+ * key = {tid, variant, run_seed, 0x12345678}, counter = {draw/4, ...}.  */
+typedef struct RampRng {
+  int32_t mode;
+  uint32_t run_seed;
+  uint32_t tid_base;   /* global index of neutron 0 of this call: a rank
+                          tracing indices [tid_base, tid_base+n) of a
+                          sharded chunk keys its neutrons exactly as a
+                          single-device run would                         */
+  uint32_t reserved;
+} RampRng;
+
+/* One variant of a batched fused launch: its own components (same kinds
+ * and count as the plan's, different parameters and tallies), its own
+ * neutron count, chunk weight normalisation and per-chunk seed.           */
+typedef struct RampVariant {
+  const RampComp* comps;        /* n_comps entries (host memory)         */
+  RampSource source;            /* the variant's moderator               */
+  int64_t n;                    /* histories in this variant             */
+  int32_t num_sim;              /* p = 1/num_sim (flat_mod.cl:26)        */
+  int32_t seed;                 /* randint(0,4096) stand-in              */
+} RampVariant;
+
+/* Launch configuration chosen by the autotuner (0 = default).             */
+typedef struct RampTune {
+  int32_t block;                /* threads per block                     */
+  int32_t blocks_per_sm;        /* persistent CTAs per SM                */
+  int32_t chunk;                /* neutrons claimed per work-queue grab  */
+  int32_t privatize;            /* 1: shared-memory tally privatisation  */
+} RampTune;
+
+typedef struct RampPlan RampPlan;
+
+/* ---- API --------------------------------------------------------------- */
+
+int ramp_version(void);
+
+/* Host-readable message for the last failing call on this thread.        */
+int ramp_last_error(char* buf, int len);
+
+/* Validate descriptors, precompute frame rotations, upload tables (and a
+ * BVH for meshes).  Replaces the per-plugin constructors that build
+ * OpenCL programs and buffers (mcramp.py:45-116, e.g. plane.py:63-73,
+ * isotropic.py:41-155, powderN.py:50-77, mesh.py:60-81).                 */
+int ramp_plan_create(const RampSource* source, const RampComp* comps,
+                     int n_comps, const RampBlock* blocks, int n_blocks,
+                     RampPlan** out);
+int ramp_plan_destroy(RampPlan* plan);
+
+/* Read and clear the plan's device status flags (RAMP_F_*) and the count
+ * of tally writes that fell outside their buffers.  Synchronises.         */
+int ramp_plan_status(RampPlan* plan, uint32_t* flags, uint64_t* oob_drops);
+
+/* Moderator pass over neutrons [0, n): replaces gen_prg
+ * (flat_mod.py:24-32, cont_mod.py:137-152).  Every record is regenerated
+ * and its counter seeded with seed + previous sb (flat_mod.cl:19).        */
+int ramp_generate(RampPlan* plan, const RampState* st, int64_t n,
+                  int32_t num_sim, int32_t seed, const RampRng* rng,
+                  void* stream);
+
+/* One execution block over neutrons [0, n): replaces
+ * ExecutionBlock.execute (mcramp.py:118-220).  A linear block launches one
+ * kernel per component (transform, intersect, terminate, scatter and
+ * untransform fused); a non-linear block launches one kernel running all
+ * its "multi" events.                                                     */
+int ramp_run_block(RampPlan* plan, int block, const RampState* st,
+                   int64_t n, const RampRng* rng, void* stream);
+
+/* The plain path for one chunk: ramp_generate + ramp_run_block over every
+ * block (one iteration of the chunk loop, mcramp.py:442-455).            */
+int ramp_trace_plain(RampPlan* plan, const RampState* st, int64_t n,
+                     int32_t num_sim, int32_t seed, const RampRng* rng,
+                     void* stream);
+
+/* The fused path for one chunk: the whole chain in one persistent kernel,
+ * each neutron in registers from the moderator to its last component.
+ * sb_carry / iidx_carry (optional, both NULL = all zero, i.e. a fresh
+ * execute()) hold per index the final RNG counter and index-buffer value
+ * of the previous chunk and receive this chunk's; they are what makes
+ * multi-chunk runs reproduce the reference keying (flat_mod.cl:19) with
+ * nothing else of the neutron state in memory.                           */
+int ramp_trace_fused(RampPlan* plan, int64_t n, int32_t num_sim,
+                     int32_t seed, const RampRng* rng, float* sb_carry,
+                     uint32_t* iidx_carry, const RampTune* tune,
+                     void* stream);
+
+/* Batched fused path: n_variants instrument variants with uneven neutron
+ * counts in one persistent launch (no reference counterpart: the
+ * reference runs one Instrument per execute()).                          */
+int ramp_trace_batched(RampPlan* plan, const RampVariant* variants,
+                       int n_variants, const RampRng* rng,
+                       const RampTune* tune, void* stream);
+
+/* Debug/test entry points: evaluate the device RNG and math on a vector
+ * of inputs (used by the parity tests, not by the chain).                 */
+int ramp_debug_threefry(const uint32_t* ctr0_dev, const uint32_t* tid_dev,
+                        uint32_t* out_x_dev, int64_t n, void* stream);
+int ramp_debug_math(int fn, const float* a_dev, const float* b_dev,
+                    float* out_dev, int64_t n, void* stream);
+
+/* Measurement kernel: n_threads threads each evaluate `iters` dependent
+ * Threefry-4x32-20 blocks (two independent chains per thread) and xor the
+ * results into out_dev[thread].  Its rate is the Threefry throughput ceiling
+ * the fused kernel is compared against.                                   */
+int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out_dev,
+                        void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAMP_H */

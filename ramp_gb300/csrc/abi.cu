@@ -1,0 +1,560 @@
+/*
+ * abi.cu — host side of the C ABI declared in include/ramp.h: plan
+ * creation (descriptor validation, frame matrices, table and BVH upload),
+ * the plain and fused launchers, status readback and error messages.
+ */
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ramp.h"
+#include "rmath.h"
+#include "rconst.h"
+#include "plan.h"
+#include "launch.h"
+#include "bvh.h"
+
+static thread_local std::string g_err;
+
+static void set_err(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+
+#define CK(x)                                                                 \
+  do {                                                                        \
+    cudaError_t e_ = (x);                                                     \
+    if (e_ != cudaSuccess) {                                                  \
+      set_err("%s: %s", #x, cudaGetErrorString(e_));                          \
+      return e_ == cudaErrorMemoryAllocation ? RAMP_E_NOMEM : RAMP_E_CUDA;    \
+    }                                                                         \
+  } while (0)
+
+struct BatchCache {
+  std::vector<CompDev> comps_host;   /* n_variants * n_comps              */
+  CompDev* comps_dev = nullptr;
+  size_t comps_cap = 0;
+  VariantDev* vars_dev = nullptr;
+  size_t vars_cap = 0;
+  TaskDev* tasks_dev = nullptr;
+  size_t tasks_cap = 0;
+  std::vector<VariantDev> vars_host;
+  std::vector<TaskDev> tasks_host;
+};
+
+/* device copies of host tables, keyed by (kind, length, content hash) so
+ * variants that share a table share one upload (kind 0 table, 1 BVH) */
+typedef std::tuple<int, int64_t, uint64_t> TabKey;
+
+struct RampPlan {
+  SrcDev src;
+  std::vector<RampComp> comps_in;    /* the caller's descriptors           */
+  std::vector<CompDev> comps;        /* host copy of device descriptors    */
+  CompDev* comps_dev = nullptr;
+  std::vector<RampBlock> blocks;
+  RampBlock* blocks_dev = nullptr;
+  StatusDev* status = nullptr;
+  std::vector<void*> allocs;
+  int sm_count = 0;
+  BatchCache batch;
+  std::map<TabKey, std::pair<void*, void*>> tabs;
+};
+
+/* ---------------------------------------------------------------------- */
+/* host float helpers: the same operations the device uses                 */
+/* ---------------------------------------------------------------------- */
+/* frame matrix, mcramp/include/geom.h:21-53 */
+static void rot_matrix(const float* rot, float* R) {
+  float x_a = rot[0], y_a = rot[1], z_a = rot[2];
+  float cx = rm_cosf(x_a), sx = rm_sinf(x_a);
+  float cy = rm_cosf(y_a), sy = rm_sinf(y_a);
+  float cz = rm_cosf(z_a), sz = rm_sinf(z_a);
+  R[0] = cy * cz;
+  R[1] = -cx * sz + sx * sy * cz;
+  R[2] = sx * sz + cx * sy * cz;
+  R[3] = cy * sz;
+  R[4] = cx * cz + sx * sy * sz;
+  R[5] = -sx * cz + cx * sy * sz;
+  R[6] = -sy;
+  R[7] = sx * cy;
+  R[8] = cx * cy;
+}
+
+/* maxwell_energy_distn, cont_mod.cl:4-9 */
+static float maxwell_h(float E, float T) {
+  float rootE = sqrtf(E);
+  float overKT = 1.0f / (RC_K_B * T);
+  return 2.0f * rootE / sqrtf(RC_PI) * (overKT * sqrtf(overKT)) * rm_expf(-E * overKT);
+}
+
+static int make_src(const RampSource& s, SrcDev& d) {
+  if (s.kind != RAMP_SRC_FLAT && s.kind != RAMP_SRC_CONT) {
+    set_err("unknown source kind %d", s.kind);
+    return RAMP_E_UNSUPPORTED;
+  }
+  memset(&d, 0, sizeof(d));
+  d.kind = s.kind;
+  memcpy(d.p, s.p, sizeof(d.p));
+  if (s.kind == RAMP_SRC_CONT) {
+    d.dmax[0] = maxwell_h(RC_K_B * s.p[7], s.p[7]);
+    d.dmax[1] = maxwell_h(RC_K_B * s.p[9], s.p[9]);
+    d.dmax[2] = maxwell_h(RC_K_B * s.p[11], s.p[11]);
+  }
+  return RAMP_OK;
+}
+
+static int upload(const void* host, size_t bytes, void** dev, std::vector<void*>& owner) {
+  void* p = nullptr;
+  CK(cudaMalloc(&p, bytes > 0 ? bytes : 16));
+  owner.push_back(p);
+  if (bytes) CK(cudaMemcpy(p, host, bytes, cudaMemcpyHostToDevice));
+  *dev = p;
+  return RAMP_OK;
+}
+
+static int validate_comp(const RampComp& c, int j) {
+  if (c.geom < RAMP_G_PLANE || c.geom > RAMP_G_MESH) {
+    set_err("component %d: unknown geometry kind %d", j, c.geom);
+    return RAMP_E_UNSUPPORTED;
+  }
+  if (c.scat < RAMP_S_ARM || c.scat > RAMP_S_ATTENUATE) {
+    set_err("component %d: unknown scatter kind %d", j, c.scat);
+    return RAMP_E_UNSUPPORTED;
+  }
+  if (c.geom == RAMP_G_PLANE && c.gi[0] != 0 && c.gi[0] != 1) {
+    set_err("component %d: plane orientation %d", j, c.gi[0]);
+    return RAMP_E_INVALID;
+  }
+  if (c.geom == RAMP_G_MESH && (c.table_len[0] <= 0 || c.table_len[0] % 9 || !c.table[0])) {
+    set_err("component %d: mesh needs 9*n_tri points", j);
+    return RAMP_E_INVALID;
+  }
+  if (c.scat == RAMP_S_ATTENUATE && c.geom != RAMP_G_MESH) {
+    set_err("component %d: SAttenuate needs a GMesh geometry", j);
+    return RAMP_E_INVALID;
+  }
+  if (c.scat == RAMP_S_POWDERN &&
+      (c.si[0] < 1 || c.table_len[0] < c.si[0] || c.table_len[1] < c.si[0])) {
+    set_err("component %d: powder line tables shorter than num_lines", j);
+    return RAMP_E_INVALID;
+  }
+  if (c.scat == RAMP_S_ISOTROPIC) {
+    for (int ch = 0; ch < 3; ++ch) {
+      int64_t nq = c.si[1 + 2 * ch], nw = c.si[2 + 2 * ch];
+      if (nq < 0 || nw < 0 || c.table_len[4 * ch] < nq || c.table_len[4 * ch + 1] < nw ||
+          c.table_len[4 * ch + 2] < nw || c.table_len[4 * ch + 3] < nq * nw) {
+        set_err("component %d: isotropic channel %d tables inconsistent", j, ch);
+        return RAMP_E_INVALID;
+      }
+    }
+  }
+  if (c.scat == RAMP_S_DET1D && (c.si[2] != c.tally_len || !c.tally || !c.tally_err)) {
+    set_err("component %d: 1-D detector tally length %lld != bins %d", j,
+            (long long)c.tally_len, c.si[2]);
+    return RAMP_E_INVALID;
+  }
+  if (c.scat == RAMP_S_DET2D &&
+      ((int64_t)c.si[2] * c.si[3] != c.tally_len || !c.tally || !c.tally_err)) {
+    set_err("component %d: 2-D detector tally length mismatch", j);
+    return RAMP_E_INVALID;
+  }
+  return RAMP_OK;
+}
+
+static uint64_t fnv1a(const void* data, size_t bytes) {
+  const unsigned char* b = (const unsigned char*)data;
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i < bytes; ++i) { h ^= b[i]; h *= 1099511628211ull; }
+  return h;
+}
+
+static int get_table(RampPlan* p, const float* host, int64_t len, const float** dev) {
+  static const float zero = 0.0f;
+  if (len <= 0 || !host) { host = &zero; len = 1; }
+  TabKey key(0, len, fnv1a(host, (size_t)len * sizeof(float)));
+  auto it = p->tabs.find(key);
+  if (it != p->tabs.end()) { *dev = (const float*)it->second.first; return RAMP_OK; }
+  void* d;
+  int rc = upload(host, (size_t)len * sizeof(float), &d, p->allocs);
+  if (rc) return rc;
+  p->tabs[key] = std::make_pair(d, (void*)nullptr);
+  *dev = (const float*)d;
+  return RAMP_OK;
+}
+
+static int get_bvh(RampPlan* p, const float* pts, int64_t len, const float4** nodes_dev,
+                   const float4** tris_dev) {
+  TabKey key(1, len, fnv1a(pts, (size_t)len * sizeof(float)));
+  auto it = p->tabs.find(key);
+  if (it == p->tabs.end()) {
+    std::vector<float> nodes, tris;
+    if (ramp_bvh_build(pts, len / 9, nodes, tris) != 0) {
+      set_err("BVH build failed");
+      return RAMP_E_INVALID;
+    }
+    void *pn, *pt;
+    int rc = upload(nodes.data(), nodes.size() * sizeof(float), &pn, p->allocs);
+    if (rc) return rc;
+    rc = upload(tris.data(), tris.size() * sizeof(float), &pt, p->allocs);
+    if (rc) return rc;
+    it = p->tabs.emplace(key, std::make_pair(pn, pt)).first;
+  }
+  *nodes_dev = (const float4*)it->second.first;
+  *tris_dev = (const float4*)it->second.second;
+  return RAMP_OK;
+}
+
+/* Convert one caller descriptor into its device form. */
+static int make_comp(RampPlan* p, const RampComp& c, CompDev& d) {
+  memset(&d, 0, sizeof(d));
+  d.geom = c.geom; d.scat = c.scat; d.idx = c.idx; d.restore = c.restore;
+  memcpy(d.pos, c.pos, sizeof(d.pos));
+  rot_matrix(c.rot, d.R);
+  d.rotated = (c.rot[0] != 0.0f || c.rot[1] != 0.0f || c.rot[2] != 0.0f);
+  memcpy(d.gp, c.gp, sizeof(d.gp));
+  memcpy(d.sp, c.sp, sizeof(d.sp));
+  memcpy(d.gi, c.gi, sizeof(d.gi));
+  memcpy(d.si, c.si, sizeof(d.si));
+  for (int k = 0; k < RAMP_NTAB; ++k) {
+    d.tab_len[k] = c.table_len[k];
+    if (c.geom == RAMP_G_MESH && k == 0) continue;   /* the BVH replaces the raw points */
+    int rc = get_table(p, c.table[k], c.table_len[k], &d.tab[k]);
+    if (rc) return rc;
+  }
+  d.tally = c.tally;
+  d.tally_err = c.tally_err;
+  d.tally_len = c.tally_len;
+  if (c.geom == RAMP_G_MESH) {
+    int rc = get_bvh(p, c.table[0], c.table_len[0], &d.bvh_nodes, &d.bvh_tris);
+    if (rc) return rc;
+  }
+  return RAMP_OK;
+}
+
+static int check_state(const RampState* st, int64_t n) {
+  if (!st || !st->soa || !st->iidx) { set_err("state pointers are NULL"); return RAMP_E_INVALID; }
+  if (st->stride < n) { set_err("state stride %lld < n %lld", (long long)st->stride, (long long)n); return RAMP_E_INVALID; }
+  return RAMP_OK;
+}
+
+static PlainArgs plain_args(RampPlan* p, const RampState* st, int64_t n, const RampRng* rng) {
+  PlainArgs a;
+  a.soa = st->soa;
+  a.iidx = st->iidx;
+  a.stride = st->stride;
+  a.n = n;
+  a.rng.mode = rng ? rng->mode : 0;
+  a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.tid_base = rng ? rng->tid_base : 0u;
+  a.st = p->status;
+  return a;
+}
+
+extern "C" {
+
+int ramp_version(void) { return RAMP_ABI_VERSION; }
+
+int ramp_last_error(char* buf, int len) {
+  if (!buf || len <= 0) return RAMP_E_INVALID;
+  snprintf(buf, (size_t)len, "%s", g_err.c_str());
+  return RAMP_OK;
+}
+
+int ramp_plan_destroy(RampPlan* p) {
+  if (!p) return RAMP_OK;
+  for (void* a : p->allocs) cudaFree(a);
+  if (p->batch.comps_dev) cudaFree(p->batch.comps_dev);
+  if (p->batch.vars_dev) cudaFree(p->batch.vars_dev);
+  if (p->batch.tasks_dev) cudaFree(p->batch.tasks_dev);
+  delete p;
+  return RAMP_OK;
+}
+
+int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comps,
+                     const RampBlock* blocks, int n_blocks, RampPlan** out) {
+  if (!out || !source || (n_comps > 0 && !comps) || n_comps < 0 || n_blocks < 0 ||
+      (n_blocks > 0 && !blocks)) {
+    set_err("ramp_plan_create: invalid arguments");
+    return RAMP_E_INVALID;
+  }
+  *out = nullptr;
+  RampPlan* p = new RampPlan();
+  int rc = make_src(*source, p->src);
+  if (rc) { delete p; return rc; }
+  for (int b = 0; b < n_blocks; ++b) {
+    const RampBlock& B = blocks[b];
+    if (B.first < 0 || B.count < 0 || B.first + B.count > n_comps || (!B.linear && B.multi < 0)) {
+      set_err("block %d covers components outside [0, %d)", b, n_comps);
+      delete p;
+      return RAMP_E_INVALID;
+    }
+  }
+  p->comps_in.assign(comps, comps + n_comps);
+  p->blocks.assign(blocks, blocks + n_blocks);
+  p->comps.resize((size_t)n_comps);
+  for (int j = 0; j < n_comps; ++j) {
+    rc = validate_comp(comps[j], j);
+    if (!rc) rc = make_comp(p, comps[j], p->comps[j]);
+    if (rc) { ramp_plan_destroy(p); return rc; }
+  }
+  void* d;
+  rc = upload(p->comps.data(), p->comps.size() * sizeof(CompDev), &d, p->allocs);
+  if (rc) { ramp_plan_destroy(p); return rc; }
+  p->comps_dev = (CompDev*)d;
+  rc = upload(p->blocks.data(), p->blocks.size() * sizeof(RampBlock), &d, p->allocs);
+  if (rc) { ramp_plan_destroy(p); return rc; }
+  p->blocks_dev = (RampBlock*)d;
+  StatusDev zero;
+  memset(&zero, 0, sizeof(zero));
+  rc = upload(&zero, sizeof(zero), &d, p->allocs);
+  if (rc) { ramp_plan_destroy(p); return rc; }
+  p->status = (StatusDev*)d;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (p->sm_count <= 0) p->sm_count = 1;
+  *out = p;
+  return RAMP_OK;
+}
+
+int ramp_plan_status(RampPlan* p, uint32_t* flags, uint64_t* oob) {
+  if (!p) { set_err("NULL plan"); return RAMP_E_INVALID; }
+  StatusDev h;
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(&h, p->status, sizeof(h), cudaMemcpyDeviceToHost));
+  CK(cudaMemset(p->status, 0, sizeof(StatusDev)));
+  if (flags) *flags = h.flags;
+  if (oob) *oob = h.oob;
+  return RAMP_OK;
+}
+
+int ramp_generate(RampPlan* p, const RampState* st, int64_t n, int32_t num_sim, int32_t seed,
+                  const RampRng* rng, void* stream) {
+  if (!p) { set_err("NULL plan"); return RAMP_E_INVALID; }
+  int rc = check_state(st, n);
+  if (rc) return rc;
+  CK(launch_generate(p->src, plain_args(p, st, n, rng), num_sim, seed, (cudaStream_t)stream));
+  return RAMP_OK;
+}
+
+int ramp_run_block(RampPlan* p, int block, const RampState* st, int64_t n, const RampRng* rng,
+                   void* stream) {
+  if (!p || block < 0 || block >= (int)p->blocks.size()) {
+    set_err("ramp_run_block: bad plan or block index");
+    return RAMP_E_INVALID;
+  }
+  int rc = check_state(st, n);
+  if (rc) return rc;
+  const RampBlock& B = p->blocks[block];
+  PlainArgs a = plain_args(p, st, n, rng);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (B.linear) {
+    for (int j = B.first; j < B.first + B.count; ++j) CK(launch_linear_comp(p->comps[j], a, s));
+  } else {
+    CK(launch_nonlinear_block(p->comps_dev, B.first, B.count, B.multi, a, s));
+  }
+  return RAMP_OK;
+}
+
+int ramp_trace_plain(RampPlan* p, const RampState* st, int64_t n, int32_t num_sim, int32_t seed,
+                     const RampRng* rng, void* stream) {
+  int rc = ramp_generate(p, st, n, num_sim, seed, rng, stream);
+  if (rc) return rc;
+  for (int b = 0; b < (int)p->blocks.size(); ++b) {
+    rc = ramp_run_block(p, b, st, n, rng, stream);
+    if (rc) return rc;
+  }
+  return RAMP_OK;
+}
+
+static void tune_defaults(RampPlan* p, const RampTune* tune, int& block, int& grid,
+                          int64_t& task) {
+  block = (tune && tune->block > 0) ? tune->block : 256;
+  if (block % 32 || block > 1024) block = 256;
+  int bps = (tune && tune->blocks_per_sm > 0) ? tune->blocks_per_sm
+                                              : fused_max_blocks_per_sm(block, (int)p->comps.size());
+  grid = p->sm_count * bps;
+  task = (tune && tune->chunk > 0) ? tune->chunk : (int64_t)block * 8;
+}
+
+int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, const RampRng* rng,
+                     float* sb_carry, uint32_t* iidx_carry, const RampTune* tune, void* stream) {
+  if ((sb_carry == nullptr) != (iidx_carry == nullptr)) {
+    set_err("ramp_trace_fused: give both carry buffers or neither");
+    return RAMP_E_INVALID;
+  }
+  if (!p || n < 0) { set_err("ramp_trace_fused: bad arguments"); return RAMP_E_INVALID; }
+  if ((int)p->comps.size() > RAMP_MAX_COMPS) {
+    set_err("fused path supports at most %d components", RAMP_MAX_COMPS);
+    return RAMP_E_RANGE;
+  }
+  if (n == 0) return RAMP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  int block, grid;
+  int64_t task;
+  tune_defaults(p, tune, block, grid, task);
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.variants = nullptr;
+  a.tasks = nullptr;
+  a.task_size = task;
+  a.n_tasks = (n + task - 1) / task;
+  a.single.src = p->src;
+  a.single.n = n;
+  a.single.num_sim = num_sim;
+  a.single.seed = seed;
+  a.single.comps = p->comps_dev;
+  a.blocks = p->blocks_dev;
+  a.n_blocks = (int32_t)p->blocks.size();
+  a.n_comps = (int32_t)p->comps.size();
+  a.rng.mode = rng ? rng->mode : 0;
+  a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.tid_base = rng ? rng->tid_base : 0u;
+  a.carry_sb = sb_carry;
+  a.carry_iidx = iidx_carry;
+  a.st = p->status;
+  int64_t g = a.n_tasks < grid ? a.n_tasks : grid;
+  CK(cudaMemsetAsync(&p->status->workq, 0, sizeof(unsigned long long), s));
+  CK(launch_fused(a, block, (int)g, s));
+  return RAMP_OK;
+}
+
+int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
+                       const RampRng* rng, const RampTune* tune, void* stream) {
+  if (!p || !variants || n_variants <= 0) {
+    set_err("ramp_trace_batched: bad arguments");
+    return RAMP_E_INVALID;
+  }
+  const int nc = (int)p->comps.size();
+  if (nc > RAMP_MAX_COMPS) {
+    set_err("fused path supports at most %d components", RAMP_MAX_COMPS);
+    return RAMP_E_RANGE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int block, grid;
+  int64_t task;
+  tune_defaults(p, tune, block, grid, task);
+  BatchCache& B = p->batch;
+  /* descriptors: re-upload only when they change */
+  std::vector<CompDev> comps((size_t)n_variants * nc);
+  for (int v = 0; v < n_variants; ++v) {
+    if (!variants[v].comps || variants[v].n < 0) {
+      set_err("variant %d: missing components", v);
+      return RAMP_E_INVALID;
+    }
+    for (int j = 0; j < nc; ++j) {
+      const RampComp& c = variants[v].comps[j];
+      if (c.geom != p->comps_in[j].geom || c.scat != p->comps_in[j].scat) {
+        set_err("variant %d component %d: kinds differ from the plan", v, j);
+        return RAMP_E_INVALID;
+      }
+      int rc = validate_comp(c, j);
+      if (!rc) rc = make_comp(p, c, comps[(size_t)v * nc + j]);
+      if (rc) return rc;
+    }
+  }
+  size_t cbytes = comps.size() * sizeof(CompDev);
+  if (B.comps_cap < comps.size()) {
+    if (B.comps_dev) cudaFree(B.comps_dev);
+    CK(cudaMalloc(&B.comps_dev, cbytes));
+    B.comps_cap = comps.size();
+    B.comps_host.clear();
+  }
+  if (B.comps_host.size() != comps.size() ||
+      memcmp(B.comps_host.data(), comps.data(), cbytes) != 0) {
+    CK(cudaMemcpy(B.comps_dev, comps.data(), cbytes, cudaMemcpyHostToDevice));
+    B.comps_host = comps;
+  }
+  std::vector<VariantDev> vars((size_t)n_variants);
+  std::vector<TaskDev> tasks;
+  for (int v = 0; v < n_variants; ++v) {
+    int rc = make_src(variants[v].source, vars[v].src);
+    if (rc) return rc;
+    vars[v].n = variants[v].n;
+    vars[v].num_sim = variants[v].num_sim;
+    vars[v].seed = variants[v].seed;
+    vars[v].comps = B.comps_dev + (size_t)v * nc;
+    for (int64_t st0 = 0; st0 < variants[v].n; st0 += task) {
+      TaskDev t;
+      t.variant = v;
+      t.start = st0;
+      int64_t rem = variants[v].n - st0;
+      t.count = (int32_t)(rem < task ? rem : task);
+      tasks.push_back(t);
+    }
+  }
+  if (tasks.empty()) return RAMP_OK;
+  if (B.vars_cap < vars.size()) {
+    if (B.vars_dev) cudaFree(B.vars_dev);
+    CK(cudaMalloc(&B.vars_dev, vars.size() * sizeof(VariantDev)));
+    B.vars_cap = vars.size();
+    B.vars_host.clear();
+  }
+  if (B.vars_host.size() != vars.size() ||
+      memcmp(B.vars_host.data(), vars.data(), vars.size() * sizeof(VariantDev)) != 0) {
+    CK(cudaMemcpy(B.vars_dev, vars.data(), vars.size() * sizeof(VariantDev),
+                  cudaMemcpyHostToDevice));
+    B.vars_host = vars;
+  }
+  if (B.tasks_cap < tasks.size()) {
+    if (B.tasks_dev) cudaFree(B.tasks_dev);
+    CK(cudaMalloc(&B.tasks_dev, tasks.size() * sizeof(TaskDev)));
+    B.tasks_cap = tasks.size();
+    B.tasks_host.clear();
+  }
+  if (B.tasks_host.size() != tasks.size() ||
+      memcmp(B.tasks_host.data(), tasks.data(), tasks.size() * sizeof(TaskDev)) != 0) {
+    CK(cudaMemcpy(B.tasks_dev, tasks.data(), tasks.size() * sizeof(TaskDev),
+                  cudaMemcpyHostToDevice));
+    B.tasks_host = tasks;
+  }
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.variants = B.vars_dev;
+  a.tasks = B.tasks_dev;
+  a.n_tasks = (int64_t)tasks.size();
+  a.task_size = task;
+  a.blocks = p->blocks_dev;
+  a.n_blocks = (int32_t)p->blocks.size();
+  a.n_comps = nc;
+  a.rng.mode = rng ? rng->mode : 1;
+  a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.tid_base = 0u;   /* variants key by their own index */
+  a.st = p->status;
+  int64_t g = a.n_tasks < grid ? a.n_tasks : grid;
+  CK(cudaMemsetAsync(&p->status->workq, 0, sizeof(unsigned long long), s));
+  CK(launch_fused(a, block, (int)g, s));
+  return RAMP_OK;
+}
+
+int ramp_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out, int64_t n,
+                        void* stream) {
+  if (!c0 || !tid || !out || n < 0) { set_err("bad arguments"); return RAMP_E_INVALID; }
+  CK(launch_debug_threefry(c0, tid, out, n, (cudaStream_t)stream));
+  return RAMP_OK;
+}
+
+int ramp_debug_math(int fn, const float* a, const float* b, float* out, int64_t n,
+                    void* stream) {
+  if (!a || !out || n < 0) { set_err("bad arguments"); return RAMP_E_INVALID; }
+  CK(launch_debug_math(fn, a, b, out, n, (cudaStream_t)stream));
+  return RAMP_OK;
+}
+
+int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out, void* stream) {
+  if (!out || n_threads < 0 || iters < 0) { set_err("bad arguments"); return RAMP_E_INVALID; }
+  CK(launch_debug_rng_peak(n_threads, iters, out, (cudaStream_t)stream));
+  return RAMP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,850 @@
+/*
+ * device.cuh — the per-neutron chain as device functions over a neutron
+ * held in registers.  Shared by the plain per-component kernels
+ * (plain.cu) and the fused persistent kernel (fused.cu).
+ *
+ * Every function restates one reference OpenCL kernel (cited) with the
+ * same sequence of FP32 operations, so that with -fmad=false and the
+ * shared rmath.h library the results are bit-identical to the CPU oracle.
+ * Differences in structure, not in arithmetic: the frame transform uses a
+ * rotation matrix precomputed on the host (the reference recomputes the
+ * same nine products per work-item), a linear component's five kernels
+ * (transform, intersect, terminate, scatter, untransform) run back to back
+ * on registers, and the intersection record lives in registers (at the
+ * start of every linear component it always holds the reset value).
+ */
+#ifndef RAMP_DEVICE_CUH
+#define RAMP_DEVICE_CUH
+
+#include <stdint.h>
+#include "rmath.h"
+#include "rconst.h"
+#include "plan.h"
+
+#define DI __device__ __forceinline__
+
+/* ------------------------------------------------------------------ */
+/* neutron record in registers (NOTES:3-14)                            */
+/* ------------------------------------------------------------------ */
+struct Nt {
+  float x, y, z, vx, vy, vz, px, py, pz, p, t, sb, sc, sd, se, die;
+  uint32_t wr;   /* lanes sc/sd/se/die written since the last store */
+};
+#define WR_SC 1u
+#define WR_SD 2u
+#define WR_SE 4u
+#define WR_DIE 8u
+
+struct Is {
+  float x1, y1, z1, t1, x2, y2, z2, t2;
+};
+
+DI void is_reset(Is& s) {
+  s.x1 = 0.0f; s.y1 = 0.0f; s.z1 = 0.0f; s.t1 = RC_T_RESET;
+  s.x2 = 0.0f; s.y2 = 0.0f; s.z2 = 0.0f; s.t2 = RC_T_RESET;
+}
+DI void set_die(Nt& n, float v) { n.die = v; n.wr |= WR_DIE; }
+DI void set_sc(Nt& n, uint32_t idx) { n.sc = (float)idx; n.wr |= WR_SC; }
+
+/* ------------------------------------------------------------------ */
+/* float3 helpers (OpenCL built-ins, left-to-right dot)                 */
+/* ------------------------------------------------------------------ */
+struct V3 { float x, y, z; };
+DI V3 v3(float x, float y, float z) { V3 r; r.x = x; r.y = y; r.z = z; return r; }
+DI V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+DI V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+DI V3 mul(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+DI float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+DI float len3(V3 a) { return sqrtf(dot(a, a)); }
+DI V3 normalize(V3 a) {
+  float d = dot(a, a);
+  if (d == 0.0f) return a;
+  float inv = 1.0f / sqrtf(d);
+  return v3(a.x * inv, a.y * inv, a.z * inv);
+}
+DI V3 cross(V3 a, V3 b) {
+  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+DI bool all_eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+DI V3 npos(const Nt& n) { return v3(n.x, n.y, n.z); }
+DI V3 nvel(const Nt& n) { return v3(n.vx, n.vy, n.vz); }
+DI V3 npol(const Nt& n) { return v3(n.px, n.py, n.pz); }
+DI void set_pos(Nt& n, V3 v) { n.x = v.x; n.y = v.y; n.z = v.z; }
+DI void set_vel(Nt& n, V3 v) { n.vx = v.x; n.vy = v.y; n.vz = v.z; }
+DI void set_pol(Nt& n, V3 v) { n.px = v.x; n.py = v.y; n.pz = v.z; }
+DI V3 ip1(const Is& s) { return v3(s.x1, s.y1, s.z1); }
+DI V3 ip2(const Is& s) { return v3(s.x2, s.y2, s.z2); }
+
+/* ------------------------------------------------------------------ */
+/* Threefry-4x32-20 (Salmon et al., SC'11), written for the GPU: the key */
+/* schedule is built once per neutron and the constant key and counter  */
+/* words fold into immediates.                                           */
+/* ------------------------------------------------------------------ */
+DI uint32_t rotl(uint32_t x, int r) { return __funnelshift_l(x, x, r); }
+
+#define TF_E(a, b) x0 += x1; x1 = rotl(x1, a) ^ x0; x2 += x3; x3 = rotl(x3, b) ^ x2;
+#define TF_O(a, b) x0 += x3; x3 = rotl(x3, a) ^ x0; x2 += x1; x1 = rotl(x1, b) ^ x2;
+#define TF_INJ(s, k0, k1, k2, k3) x0 += k0; x1 += k1; x2 += k2; x3 += k3 + (s);
+
+DI void tf20(uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t& x3, uint32_t K0, uint32_t K1,
+             uint32_t K2, uint32_t K3, uint32_t K4) {
+  x0 += K0; x1 += K1; x2 += K2; x3 += K3;
+  TF_E(10, 26) TF_O(11, 21) TF_E(13, 27) TF_O(23, 5) TF_INJ(1u, K1, K2, K3, K4)
+  TF_E(6, 20) TF_O(17, 11) TF_E(25, 10) TF_O(18, 20) TF_INJ(2u, K2, K3, K4, K0)
+  TF_E(10, 26) TF_O(11, 21) TF_E(13, 27) TF_O(23, 5) TF_INJ(3u, K3, K4, K0, K1)
+  TF_E(6, 20) TF_O(17, 11) TF_E(25, 10) TF_O(18, 20) TF_INJ(4u, K4, K0, K1, K2)
+  TF_E(10, 26) TF_O(11, 21) TF_E(13, 27) TF_O(23, 5) TF_INJ(5u, K0, K1, K2, K3)
+}
+
+#define TF_C1 0xf00dcafeu
+#define TF_C2 0xdeadbeefu
+#define TF_C3 0xbeeff00du
+#define TF_K1 0xdecafbadu
+#define TF_K2 0xfacebeadu
+#define TF_K3 0x12345678u
+#define TF_PARITY 0x1BD11BDAu
+
+/* word x of threefry4x32({c0,C1,C2,C3}, {tid,K1,K2,K3}) (rand.h:7-16) */
+DI uint32_t tf_ref_x(uint32_t c0, uint32_t tid, uint32_t k4) {
+  uint32_t x0 = c0, x1 = TF_C1, x2 = TF_C2, x3 = TF_C3;
+  tf20(x0, x1, x2, x3, tid, TF_K1, TF_K2, TF_K3, k4);
+  return x0;
+}
+
+/* u01fixedpt_closed_closed_32_24 (Random123 u01fixedpt.h:137-140) */
+DI float u01cc(uint32_t i) {
+  return (float)((i & 0x7fffffc0u) + (i & 0x40u)) * (1.0f / 2147483648.0f);
+}
+
+struct Rng {
+  uint32_t tid, k1, k2, k4;   /* key words 0..2 and the parity word */
+  int mode;
+  uint32_t blk;               /* native mode: cached block index       */
+  uint32_t w0, w1, w2, w3;
+};
+
+DI void rng_init(Rng& r, int mode, uint32_t tid, uint32_t variant, uint32_t run_seed) {
+  r.mode = mode;
+  r.tid = tid;
+  if (mode == 0) {
+    r.k1 = TF_K1; r.k2 = TF_K2;
+  } else {
+    r.k1 = variant; r.k2 = run_seed;
+  }
+  r.k4 = TF_PARITY ^ tid ^ r.k1 ^ r.k2 ^ TF_K3;
+  r.blk = 0xffffffffu;
+  r.w0 = r.w1 = r.w2 = r.w3 = 0u;
+}
+
+/* rand() — mcramp/include/rand.h:4-21: counter word 0 is (uint)sb, sb is
+ * advanced by one.  Native mode reads word (sb & 3) of block sb >> 2. */
+DI float draw(Nt& n, Rng& r) {
+  uint32_t c = (uint32_t)n.sb;
+  uint32_t x;
+  if (r.mode == 0) {
+    x = tf_ref_x(c, r.tid, r.k4);
+  } else {
+    uint32_t b = c >> 2;
+    if (b != r.blk) {
+      uint32_t x0 = b, x1 = TF_C1, x2 = TF_C2, x3 = TF_C3;
+      tf20(x0, x1, x2, x3, r.tid, r.k1, r.k2, TF_K3, r.k4);
+      r.w0 = x0; r.w1 = x1; r.w2 = x2; r.w3 = x3;
+      r.blk = b;
+    }
+    uint32_t j = c & 3u;
+    x = (j == 0) ? r.w0 : (j == 1) ? r.w1 : (j == 2) ? r.w2 : r.w3;
+  }
+  n.sb += 1.0f;
+  return u01cc(x);
+}
+
+/* ------------------------------------------------------------------ */
+/* status                                                               */
+/* ------------------------------------------------------------------ */
+DI void raise_flag(StatusDev* st, unsigned int f) { atomicOr(&st->flags, f); }
+
+/* tally add with warp aggregation of lanes hitting the same bin */
+DI void tally_add(float* h, float* he, long long idx, float p) {
+  unsigned m = __activemask();
+  unsigned peers = __match_any_sync(m, idx);
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(peers) - 1;
+  float s = p, s2 = p * p;
+  if (__popc(peers) > 1) {
+    float a = 0.0f, a2 = 0.0f;
+    unsigned rest = peers;
+    while (rest) {
+      int src = __ffs(rest) - 1;
+      rest &= rest - 1;
+      float q = __shfl_sync(peers, p, src);
+      a += q;
+      a2 += q * q;
+    }
+    s = a; s2 = a2;
+  }
+  if (lane == leader) {
+    atomicAdd(h + idx, s);
+    if (he) atomicAdd(he + idx, s2);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* moderators                                                           */
+/* ------------------------------------------------------------------ */
+/* maxwell_energy_distn — cont_mod.cl:4-9 (pow(x,1.5) as x*sqrt(x)) */
+DI float maxwell(float E, float T) {
+  float rootE = sqrtf(E);
+  float overKT = 1.0f / (RC_K_B * T);
+  return 2.0f * rootE / sqrtf(RC_PI) * (overKT * sqrtf(overKT)) * rm_expf(-E * overKT);
+}
+
+/* generate_neutrons — flat_mod.cl:4-50 and cont_mod.cl:11-72 */
+DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t seed, Rng& r) {
+  n.x = n.y = n.z = n.vx = n.vy = n.vz = n.px = n.py = n.pz = 0.0f;
+  n.p = n.t = n.sc = n.sd = n.se = n.die = 0.0f;
+  n.wr = 0;
+  n.sb = (float)seed + old_sb;
+  const float E_min = s.p[5], E_max = s.p[6];
+  float E_range = (E_max - E_min);
+  float E_val = E_min + E_range * draw(n, r);
+  if (s.kind == RAMP_SRC_CONT) {
+    float E_J = RC_EV_J * E_val;
+    float M = s.p[8] * maxwell(E_J, s.p[7]) / s.dmax[0];
+    M += s.p[10] * maxwell(E_J, s.p[9]) / s.dmax[1];
+    M += s.p[12] * maxwell(E_J, s.p[11]) / s.dmax[2];
+    n.p = M / (float)num_sim;
+  } else {
+    n.p = 1.0f / (float)num_sim;
+  }
+  n.x = s.p[0] * (0.5f - draw(n, r));
+  n.y = s.p[1] * (0.5f - draw(n, r));
+  n.z = 0.0f;
+  float vel = RC_SE2V * sqrtf(E_val);
+  float Dx = s.p[2] * (0.5f - draw(n, r)) - n.x;
+  float Dy = s.p[3] * (0.5f - draw(n, r)) - n.y;
+  set_vel(n, mul(vel, normalize(v3(Dx, Dy, s.p[4]))));
+  float theta = 2 * RC_PI * draw(n, r);
+  float phi = rm_acosf(1 - 2 * draw(n, r));
+  float sp, cp, st, ct;
+  rm_sincosf(phi, &sp, &cp);
+  rm_sincosf(theta, &st, &ct);
+  n.px = sp * ct;
+  n.py = sp * st;
+  n.pz = cp;
+  n.die = 0.0f;
+}
+
+/* ------------------------------------------------------------------ */
+/* frame transform — frametransform.cl:4-42, geom.h:21-87               */
+/* pos/vel are always rotated (an identity matrix gives the same values */
+/* as the reference's explicit products), the spin only when the       */
+/* component is rotated.                                                 */
+/* ------------------------------------------------------------------ */
+DI V3 rot_fwd(const float* R, V3 v) {
+  return v3(dot(v3(R[0], R[1], R[2]), v), dot(v3(R[3], R[4], R[5]), v),
+            dot(v3(R[6], R[7], R[8]), v));
+}
+DI V3 rot_inv(const float* R, V3 v) {
+  return v3(dot(v3(R[0], R[3], R[6]), v), dot(v3(R[1], R[4], R[7]), v),
+            dot(v3(R[2], R[5], R[8]), v));
+}
+DI void transform(const CompDev& c, Nt& n) {
+  set_pos(n, sub(npos(n), v3(c.pos[0], c.pos[1], c.pos[2])));
+  set_pos(n, rot_inv(c.R, npos(n)));
+  set_vel(n, rot_inv(c.R, nvel(n)));
+  if (c.rotated) set_pol(n, rot_inv(c.R, npol(n)));
+}
+DI void untransform(const CompDev& c, Nt& n) {
+  set_pos(n, rot_fwd(c.R, npos(n)));
+  set_pos(n, add(npos(n), v3(c.pos[0], c.pos[1], c.pos[2])));
+  set_vel(n, rot_fwd(c.R, nvel(n)));
+  if (c.rotated) set_pol(n, rot_fwd(c.R, npol(n)));
+}
+
+/* rotate_about_axis — geom.h:1-19 */
+DI V3 rotate_about_axis(float angle, V3 a, V3 v) {
+  float s, c;
+  rm_sincosf(angle, &s, &c);
+  float Rxx = c + a.x * a.x * (1 - c);
+  float Rxy = a.x * a.y * (1 - c) - a.z * s;
+  float Rxz = a.x * a.z * (1 - c) + a.y * s;
+  float Ryx = a.y * a.x * (1 - c) + a.z * s;
+  float Ryy = c + a.y * a.y * (1 - c);
+  float Ryz = a.y * a.z * (1 - c) - a.x * s;
+  float Rzx = a.z * a.x * (1 - c) - a.y * s;
+  float Rzy = a.z * a.y * (1 - c) + a.x * s;
+  float Rzz = c + a.z * a.z * (1 - c);
+  return v3(Rxx * v.x + Rxy * v.y + Rxz * v.z, Ryx * v.x + Ryy * v.y + Ryz * v.z,
+            Rzx * v.x + Rzy * v.y + Rzz * v.z);
+}
+
+/* reflectivity_func — include/ref.h:3-53 (beta = 0 unless set) */
+DI float reflectivity(float q, float R0, float Qc, float alpha, float m, float W) {
+  float beta = 0.0f, arg;
+  if (W == 0.0f && alpha == 0.0f) {
+    m = m * 0.9853f + 0.1978f;
+    W = -0.0002f * m + 0.0022f;
+    alpha = 0.2304f * m + 5.0944f;
+    beta = -7.6251f * m + 68.1137f;
+    if (m <= 3) { alpha = m; beta = 0; }
+  }
+  arg = W > 0 ? (q - m * Qc) / W : 11;
+  if (arg > 10 || m <= 0 || Qc <= 0 || R0 <= 0) return 0.0f;
+  if (m < 1) { Qc *= m; m = 1; }
+  if (q <= Qc) return R0;
+  return R0 * 0.5f * (1 - rm_tanhf(arg)) * (1 - alpha * (q - Qc) + beta * (q - Qc) * (q - Qc));
+}
+
+/* ------------------------------------------------------------------ */
+/* geometry kernels: return true when they store iidx = comp_idx        */
+/* ------------------------------------------------------------------ */
+/* plane.cl:3-52 */
+DI bool g_plane(const CompDev& c, const Nt& n, Is& s) {
+  const float width = c.gp[0], height = c.gp[1];
+  V3 vel = nvel(n), pos = npos(n);
+  float t = 0.0f, x = 0.0f, y = 0.0f;
+  if (c.gi[0] == 0) {
+    t = (-pos.z) / vel.z; x = pos.x + t * vel.x; y = pos.y + t * vel.y;
+  } else if (c.gi[0] == 1) {
+    t = (-pos.x) / vel.x; x = pos.z + t * vel.z; y = pos.y + t * vel.y;
+  }
+  if ((fabsf(x) < width / 2.0f) && (fabsf(y) < height / 2.0f) && t < s.t1 && t < s.t2 &&
+      t > 0.0f && dot(vel, v3(0.0f, 0.0f, 1.0f)) > 0.f) {
+    V3 h = add(pos, mul(t, vel));
+    s.x1 = h.x; s.y1 = h.y; s.z1 = h.z;
+    s.x2 = h.x; s.y2 = h.y; s.z2 = h.z;
+    s.t1 = t; s.t2 = t;
+    return true;
+  }
+  return false;
+}
+
+/* cylinder_ext.cl:3-53 and banana.cl:3-55 */
+template <bool BANANA>
+DI bool g_cyl(const CompDev& c, const Nt& n, Is& s) {
+  const float radius = c.gp[0], height = c.gp[1];
+  float ppx = n.x, ppz = n.z, pvx = n.vx, pvz = n.vz;
+  float a = pvx * pvx + pvz * pvz;
+  float b = 2.0f * (ppx * pvx + ppz * pvz);
+  float cc = (ppx * ppx + ppz * ppz) - radius * radius;
+  float quotient = b * b - 4.0f * a * cc;
+  float sq = sqrtf(quotient);
+  float t1 = (-b - sq) / (2.f * a);
+  float t2 = (-b + sq) / (2.f * a);
+  float yt2 = n.y + t2 * n.vy;
+  bool window = true;
+  if (BANANA) {
+    /* (mintheta < theta2) < maxtheta, banana.cl:38 */
+    const float mintheta = c.gp[2], maxtheta = c.gp[3];
+    if (maxtheta > 1.0f) {
+      window = true;
+    } else if (!(maxtheta > 0.0f)) {
+      window = false;
+    } else {
+      float hx = ppx + t2 * pvx, hz = ppz + t2 * pvz;
+      float d2 = hx * hx + hz * hz;
+      float nz = hz;
+      if (d2 != 0.0f) { float inv = 1.0f / sqrtf(d2); nz = hz * inv; hx = hx * inv; }
+      float theta2 = rm_acosf(hx * 0.0f + nz * 1.0f);
+      window = (float)(mintheta < theta2) < maxtheta;
+    }
+  }
+  if ((quotient > 0.0f) && ((-height / 2.0f) < yt2) && (yt2 < (height / 2)) && window) {
+    bool ok = BANANA ? (t2 < s.t1 && t1 < 0.0f && t2 > 0.0f)
+                     : (t1 < s.t1 && t1 > 0.0f && t2 > 0.0f);
+    if (ok) {
+      V3 p1 = add(npos(n), mul(t1, nvel(n)));
+      V3 p2 = add(npos(n), mul(t2, nvel(n)));
+      s.x1 = p1.x; s.y1 = p1.y; s.z1 = p1.z; s.t1 = t1;
+      s.x2 = p2.x; s.y2 = p2.y; s.z2 = p2.z; s.t2 = t2;
+      return true;
+    }
+  }
+  return false;
+}
+
+/* sphere.cl:3-42 and sphere_int.cl:3-41 */
+template <bool INTERIOR>
+DI bool g_sphere(const CompDev& c, const Nt& n, Is& s) {
+  V3 pos = npos(n), vel = nvel(n);
+  float r = c.gp[0];
+  float a = dot(vel, vel);
+  float b = 2.0f * (dot(vel, pos));
+  float cc = dot(pos, pos) - r * r;
+  float quotient = b * b - 4.0f * a * cc;
+  if (quotient > 0.0f) {
+    float sq = sqrtf(quotient);
+    float d1 = (-b - sq) / (2.f * a);
+    float d2 = (-b + sq) / (2.f * a);
+    if (!INTERIOR) {
+      if (d1 < s.t1 && d1 > 0.f) {
+        V3 p1 = add(pos, mul(d1, vel)), p2 = add(pos, mul(d2, vel));
+        s.x1 = p1.x; s.y1 = p1.y; s.z1 = p1.z; s.t1 = d1;
+        s.x2 = p2.x; s.y2 = p2.y; s.z2 = p2.z; s.t2 = d2;
+        return true;
+      }
+    } else {
+      if (d1 < 0.0f && d2 < s.t1) {
+        V3 p2 = add(pos, mul(d2, vel));
+        s.x1 = p2.x; s.y1 = p2.y; s.z1 = p2.z; s.t1 = d2;
+        s.x2 = p2.x; s.y2 = p2.y; s.z2 = p2.z; s.t2 = d2;
+        return true;
+      }
+    }
+  }
+  return false;
+}
+
+/* box.cl:3-53 */
+DI bool g_box(const CompDev& c, const Nt& n, Is& s) {
+  V3 pos = npos(n), vel = nvel(n);
+  V3 A = v3(-c.gp[0] / 2.0f, -c.gp[1] / 2.0f, -c.gp[2] / 2.0f);
+  V3 B = v3(c.gp[0] / 2.0f, c.gp[1] / 2.0f, c.gp[2] / 2.0f);
+  V3 dA = sub(A, pos), dB = sub(B, pos);
+  float t1 = dA.x / vel.x, t2 = dB.x / vel.x, t3 = dA.y / vel.y;
+  float t4 = dB.y / vel.y, t5 = dA.z / vel.z, t6 = dB.z / vel.z;
+  float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
+  float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
+  if (tmax < 0.0f) return false;
+  if (tmin > tmax) return false;
+  V3 p1 = add(pos, mul(tmin, vel)), p2 = add(pos, mul(tmax, vel));
+  s.x1 = p1.x; s.y1 = p1.y; s.z1 = p1.z; s.t1 = tmin;
+  s.x2 = p2.x; s.y2 = p2.y; s.z2 = p2.z; s.t2 = tmax;
+  return true;
+}
+
+/* arm.cl:3-21 */
+DI bool g_arm(Is& s) {
+  s.x2 = 1.0f; s.y2 = 1.0f; s.z2 = 1.0f;
+  return true;
+}
+
+#include "mesh.cuh"
+
+/* dispatch; a mesh paired with SAttenuate leaves its chord sum in sd */
+DI bool intersect(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
+  switch (c.geom) {
+    case RAMP_G_PLANE: return g_plane(c, n, s);
+    case RAMP_G_CYL_EXT: return g_cyl<false>(c, n, s);
+    case RAMP_G_BANANA: return g_cyl<true>(c, n, s);
+    case RAMP_G_SPHERE: return g_sphere<false>(c, n, s);
+    case RAMP_G_SPHERE_INT: return g_sphere<true>(c, n, s);
+    case RAMP_G_BOX: return g_box(c, n, s);
+    case RAMP_G_ARM: return g_arm(s);
+    case RAMP_G_MESH: return g_mesh(c, n, s, st);
+    default: return false;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* scattering kernels                                                   */
+/* ------------------------------------------------------------------ */
+DI void s_finish(const CompDev& c, Nt& n, Is& s, uint32_t& ii) {
+  ii = 0;
+  set_sc(n, c.idx);
+  is_reset(s);
+}
+
+/* guide.cl:9-149 */
+DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
+  const float w1 = c.sp[0], h1 = c.sp[1], w2 = c.sp[2], h2 = c.sp[3], l = c.sp[4];
+  const float R0 = c.sp[5], Qc = c.sp[6], alpha = c.sp[7], m = c.sp[8], W = c.sp[9];
+  const uint32_t max_bounces = (uint32_t)c.si[0];
+  set_pos(n, ip2(s));
+  n.t += s.t2;
+  const float ww = 0.5f * (w2 - w1), hh = 0.5f * (h2 - h1);
+  const float whalf = 0.5f * w1, hhalf = 0.5f * h1;
+  uint32_t i = 0;
+  int guard = 0;
+  while (i < max_bounces) {
+    if (++guard > RC_GUIDE_HARD_CAP) {
+      set_die(n, 1.0f);
+      raise_flag(st, RAMP_F_GUIDE_CAP);
+      break;
+    }
+    float av = l * n.vx, bv = ww * n.vz, ah = l * n.vy, bh = hh * n.vz;
+    float vdotn_v1 = bv + av, vdotn_v2 = bv - av, vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
+    float cv1 = -whalf * l - n.z * ww, cv2 = n.x * l;
+    float ch1 = -hhalf * l - n.z * hh, ch2 = n.y * l;
+    float t1 = (l - n.z) / n.vz, t2;
+    i = 0;
+    if (vdotn_v1 < 0.0f && (t2 = (cv1 - cv2) / vdotn_v1) < t1) { t1 = t2; i = 1; }
+    if (vdotn_v2 < 0.0f && (t2 = (cv1 + cv2) / vdotn_v2) < t1) { t1 = t2; i = 2; }
+    if (vdotn_h1 < 0.0f && (t2 = (ch1 - ch2) / vdotn_h1) < t1) { t1 = t2; i = 3; }
+    if (vdotn_h2 < 0.0f && (t2 = (ch1 + ch2) / vdotn_h2) < t1) { t1 = t2; i = 4; }
+    if (i == 0) break;
+    n.x = n.x + t1 * n.vx; n.y = n.y + t1 * n.vy; n.z = n.z + t1 * n.vz;
+    n.t += t1;
+    float nlen2, q, d, vdn;
+    bool vert = (i <= 2);
+    float wv = vert ? ww : hh;
+    vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1 : vdotn_h2;
+    nlen2 = l * l + wv * wv;
+    q = RC_V2K * (-2.0f) * vdn / sqrtf(nlen2);
+    d = 2.0f * vdn / nlen2;
+    if (i == 1) n.vx = n.vx - d * l;
+    else if (i == 2) n.vx = n.vx + d * l;
+    else if (i == 3) n.vy = n.vy - d * l;
+    else n.vy = n.vy + d * l;
+    n.vz = n.vz - d * wv;
+    float refl = reflectivity(q, R0, Qc, alpha, m, W);
+    n.p *= refl;
+    if (refl < 1e-12f || refl > 1.0f) n.p = 0.0f;
+    i++;
+  }
+  if (i >= max_bounces) set_die(n, 1.0f);
+  s_finish(c, n, s, ii);
+}
+
+/* chopper.cl:4-59 */
+DI void s_chopper(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
+  const float slit_width = c.sp[0], radius = c.sp[1], freq = c.sp[2], phase = c.sp[3];
+  const float jitter = c.sp[4];
+  const uint32_t n_slits = (uint32_t)c.si[0];
+  set_pos(n, ip2(s));
+  n.t += s.t2;
+  float Tg = 2.0f * RC_PI / (float)n_slits;
+  float pha_error = jitter * 2.0f * (draw(n, r) - 0.5f);
+  float thi_chop = freq * (n.t - fabsf(phase)) + pha_error;
+  float thi_neut = rm_atan2f(n.x, n.y + radius);
+  float thi_diff = fabsf(thi_chop - thi_neut);
+  float ang_diff = fmodf(thi_diff, Tg);
+  if (fabsf(ang_diff - Tg) < ang_diff) ang_diff = fabsf(ang_diff - Tg);
+  float width = rm_atan2f(slit_width, n.y + radius);
+  if (ang_diff > width / 2.0f) set_die(n, 1.0f);
+  s_finish(c, n, s, ii);
+}
+
+/* sample_distn — isotropic.cl:5-73 */
+DI void sample_distn(Nt& n, Rng& r, const float* __restrict__ q, const float* __restrict__ w,
+                     const float* __restrict__ pw_cdf, const float* __restrict__ pq_cdf,
+                     uint32_t qsamples, uint32_t wsamples, float& omega, float& Q) {
+  float u = draw(n, r);
+  float v = draw(n, r);
+  float mindiff = 1.f;
+  uint32_t w_index = 0;
+  omega = 0.0f; Q = 0.0f;
+  for (uint32_t i = 0; i < wsamples; i++) {
+    float pc = __ldg(pw_cdf + i);
+    if (pc == 1.f) break;
+    if (fabsf(pc - v) < mindiff) {
+      mindiff = fabsf(pc - v);
+      float lo = (i > 0 ? __ldg(w + i - 1) : 0.0f);
+      omega = lo + (draw(n, r)) * (__ldg(w + i) - lo);
+      w_index = i;
+    }
+  }
+  mindiff = 1.f;
+  const float* row = pq_cdf + (size_t)w_index * qsamples;
+  for (uint32_t i = 0; i < qsamples; i++) {
+    float pc = __ldg(row + i);
+    if (pc == 1.f) break;
+    if (fabsf(pc - u) < mindiff) {
+      mindiff = fabsf(pc - u);
+      float lo = (i > 0 ? __ldg(q + i - 1) : 0.0f);
+      Q = lo + (draw(n, r)) * (__ldg(q + i) - lo);
+    }
+  }
+}
+
+/* isotropic.cl:75-322 */
+DI void s_isotropic(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
+  const float temperature = c.sp[0];
+  const uint32_t transmit = (uint32_t)c.si[0];
+  V3 path;
+  if (all_eq(ip1(s), ip2(s))) path = sub(ip2(s), npos(n));
+  else path = sub(ip2(s), ip1(s));
+  float ki = RC_V2K * len3(nvel(n));
+  V3 normvel = normalize(nvel(n));
+  float ss0 = c.sp[3], ss1 = c.sp[6], ss2 = c.sp[9];
+  float sigma_s = (ss0 + ss1 + ss2) / (2.f * ki * ki);
+  float sigma_a = (c.sp[2] + c.sp[5] + c.sp[8]) * 2200.f / len3(nvel(n));
+  float sigma_tot = sigma_a + sigma_s;
+  float mu = (c.sp[1] + c.sp[4] + c.sp[7]) * sigma_tot * 100.f;
+  float p_trans = rm_expf(-mu * len3(path));
+  if (draw(n, r) < p_trans) {
+    n.p *= p_trans;
+    set_pos(n, add(ip2(s), mul(0.0001f, normalize(path))));
+    n.t += s.t2;
+    if (transmit == 0) set_die(n, 1.0f);
+    s_finish(c, n, s, ii);
+    return;
+  }
+  n.p *= (1 - p_trans) * sigma_s / sigma_tot;
+  float eta = draw(n, r);
+  float path_length = (-1.f / mu) * rm_logf(1 - eta * (1 - rm_expf(-mu * len3(path))));
+  float u = draw(n, r);
+  u *= sigma_s;
+  uint32_t flag = 0;
+  float b1 = ss0 / (2.f * ki * ki), b2 = (ss0 + ss1) / (2.f * ki * ki);
+  if (u < b1) flag = 1;
+  else if (u > b1 && u < b2) flag = 2;
+  else if (u > b2) flag = 3;
+  float omega = 0.0f, Q = 0.0f;
+  if (flag >= 1) {
+    int ch = (int)flag - 1;
+    sample_distn(n, r, c.tab[4 * ch], c.tab[4 * ch + 1], c.tab[4 * ch + 2], c.tab[4 * ch + 3],
+                 (uint32_t)c.si[1 + 2 * ch], (uint32_t)c.si[2 + 2 * ch], omega, Q);
+  }
+  if (ki * ki < (RC_E2KS * omega)) {
+    set_die(n, 1.0f);
+    ii = 0;
+    is_reset(s);
+    return;
+  }
+  float kf;
+  if (draw(n, r) > 0.5f * rm_expf(-omega / (RC_KB * temperature))) {
+    kf = sqrtf(ki * ki - RC_E2KS * omega);
+    n.se = omega;
+  } else {
+    kf = sqrtf(ki * ki + RC_E2KS * omega);
+    n.se = -omega;
+  }
+  n.wr |= WR_SE;
+  float arg = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+  if (fabsf(arg) > 1) {
+    set_die(n, 1.0f);
+    ii = 0;
+    is_reset(s);
+    return;
+  }
+  float theta = rm_acosf(arg);
+  V3 oldvel = nvel(n);
+  float zz = -(n.vx + n.vy) / (n.vz);
+  V3 perp = normalize(v3(1.f, 1.f, zz));
+  float alpha = 2 * RC_PI * draw(n, r);
+  perp = rotate_about_axis(alpha, normvel, perp);
+  normvel = rotate_about_axis(theta, perp, normvel);
+  float TOFs = path_length / len3(nvel(n));
+  n.sd = Q;
+  n.wr |= WR_SD;
+  if (all_eq(ip1(s), ip2(s))) {
+    set_pos(n, mul(path_length, path));
+    n.t += TOFs;
+  } else {
+    set_pos(n, add(ip1(s), mul(path_length, path)));
+    n.t += s.t1 + TOFs;
+  }
+  set_vel(n, v3(normvel.x * kf * RC_K2V, normvel.y * kf * RC_K2V, normvel.z * kf * RC_K2V));
+  V3 dv = sub(oldvel, nvel(n));
+  V3 q_norm = normalize(v3(dv.x * RC_V2K, dv.y * RC_V2K, dv.z * RC_V2K));
+  if (flag == 2) {
+    const float k = -1.0f / 3.0f;
+    set_pol(n, v3(n.px * k, n.py * k, n.pz * k));
+  } else if (flag == 3) {
+    float dp = dot(npol(n), q_norm);
+    set_pol(n, v3(-q_norm.x * dp, -q_norm.y * dp, -q_norm.z * dp));
+  }
+  s_finish(c, n, s, ii);
+}
+
+/* powderN.cl:5-156 */
+DI void s_powdern(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st) {
+  const float* __restrict__ ssv2 = c.tab[0];
+  const float* __restrict__ qv = c.tab[1];
+  const float sigma_abs_v = c.sp[0], d_phi = c.sp[1];
+  const uint32_t num_lines = (uint32_t)c.si[0];
+  const uint32_t transmit = (uint32_t)c.si[1];
+  V3 path;
+  if (all_eq(ip1(s), ip2(s))) path = sub(ip2(s), npos(n));
+  else path = sub(ip2(s), ip1(s));
+  float full_path_length = len3(path);
+  float vel = len3(nvel(n));
+  float sigma_abs = sigma_abs_v * 2200.0f / vel;
+  float vv = vel * vel * RC_V2K * RC_V2K;
+  float sum_sigma_scat = 0.0f;
+  for (uint32_t j = 0; j < num_lines; j++) sum_sigma_scat += __ldg(ssv2 + j) / vv;
+  float p_inter = 1 - rm_expf(-(sum_sigma_scat + sigma_abs) * full_path_length);
+  if (draw(n, r) > p_inter) {
+    n.p *= 1 - p_inter;
+    set_pos(n, add(ip2(s), mul(0.0001f, normalize(path))));
+    n.t += s.t2;
+    if (transmit == 0) set_die(n, 1.0f);
+    s_finish(c, n, s, ii);
+    return;
+  }
+  uint32_t attempts = 0;
+  float arg = 0.0f, q_chosen = 0.0f;
+  while (true) {
+    float u = draw(n, r);
+    float v = 0.0f;
+    uint32_t j = 0;
+    while (v < u && j < num_lines) {
+      q_chosen = __ldg(qv + j);
+      v += (__ldg(ssv2 + j) / vv) / sum_sigma_scat;
+      j++;
+    }
+    arg = q_chosen * RC_K2V / (2.0f * vel);
+    if (arg < 1.0f) break;
+    bool give_up = (arg > 1.0f && attempts > 2 * num_lines);
+    if (give_up || attempts > RC_POWDER_HARD_CAP) {
+      if (!give_up) raise_flag(st, RAMP_F_POWDER_CAP);
+      set_die(n, 1.0f);
+      ii = 0;
+      is_reset(s);
+      return;
+    }
+    attempts++;
+  }
+  float twotheta = 2.0f * rm_asinf(arg);
+  float pen_depth = -rm_logf(1.0f - draw(n, r) * (1.0f - p_inter)) / (sigma_abs + sum_sigma_scat);
+  V3 beam_para = normalize(nvel(n));
+  V3 beam_perp = cross(beam_para, v3(0.0f, 1.0f, 0.0f));
+  if (len3(beam_perp) < 1e-3f) beam_perp = normalize(cross(beam_para, v3(1.0f, 0.0f, 0.0f)));
+  else beam_perp = normalize(beam_perp);
+  float phi;
+  if (d_phi != 0.0f) {
+    phi = (2.0f * draw(n, r) - 1.0f) * (d_phi * RC_PI / 180.0f);
+    if (draw(n, r) > 0.5f) phi += RC_PI;
+    phi += RC_PI / 2.0f;
+  } else {
+    phi = 2.0f * RC_PI * draw(n, r);
+  }
+  beam_perp = rotate_about_axis(phi, beam_para, beam_perp);
+  beam_para = rotate_about_axis(twotheta, beam_perp, beam_para);
+  if (all_eq(ip1(s), ip2(s))) {
+    set_pos(n, add(npos(n), mul(pen_depth, path)));
+    n.t += len3(mul(pen_depth, path)) / len3(nvel(n));
+  } else {
+    set_pos(n, add(ip1(s), mul(pen_depth, path)));
+    n.t += s.t2 - s.t1;
+  }
+  set_vel(n, mul(vel, normalize(beam_para)));
+  n.p *= (1 - rm_expf(-(sum_sigma_scat + sigma_abs) * pen_depth)) * sum_sigma_scat /
+         (sum_sigma_scat + sigma_abs);
+  s_finish(c, n, s, ii);
+}
+
+/* detector1D.cl:20-77 */
+DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
+  const float min_var = c.sp[0], step_var = c.sp[1], max_var = c.sp[2];
+  const uint32_t var = (uint32_t)c.si[0], restore = (uint32_t)c.si[1];
+  float var_val = 0.0f;
+  if (var == 0) { float L = len3(nvel(n)); var_val = RC_VS2E * (L * L); }
+  else if (var == 1) var_val = rm_degrees(rm_atan2f(s.x2, s.z2));
+  else if (var == 2) var_val = (1.0e6f) * (n.t + s.t2);
+  else if (var == 3) var_val = 2 * RC_PI / (RC_V2K * len3(nvel(n)));
+  if (min_var <= var_val && var_val <= max_var) {
+    uint32_t idx = (uint32_t)floorf((var_val - min_var) / step_var);
+    if ((long long)idx < c.tally_len) tally_add(c.tally, c.tally_err, idx, n.p);
+    else atomicAdd(&st->oob, 1ull);
+  }
+  if (restore == 0) {
+    set_pos(n, ip2(s));
+    n.t += s.t2;
+    set_die(n, 1.f);
+  }
+  s_finish(c, n, s, ii);
+}
+
+/* axis variables, detector2D.cl:48-145 */
+DI float det2d_val(uint32_t var, int axis, const Nt& n, const Is& s) {
+  float X2 = s.x2, Y2 = s.y2, Z2 = s.z2;
+  switch (var) {
+    case 0: return X2;
+    case 1: return Y2;
+    case 2: return rm_degrees(rm_atan2f(X2, Z2));
+    case 3: return rm_degrees(rm_atan2f(Y2, sqrtf(X2 * X2 + Z2 * Z2)));
+    case 4: return rm_sign(Y2) * rm_degrees(rm_acosf(X2 / sqrtf(X2 * X2 + Y2 * Y2)));
+    case 5: return (1.0e6f) * (n.t + s.t2);
+    case 6: return rm_degrees(rm_atan2f(n.vx, axis == 1 ? Y2 : n.vz));
+    case 7: return rm_degrees(rm_atan2f(n.vy, axis == 1 ? Y2 : n.vz));
+    case 8: return 2 * RC_PI / (RC_V2K * len3(nvel(n)));
+    case 9: { float L = len3(nvel(n)); return RC_VS2E * (L * L); }
+    case 10: return rm_sign(X2) * rm_degrees(rm_atan2f(sqrtf(X2 * X2 + Y2 * Y2), Z2));
+    default: return 0.0f;
+  }
+}
+
+DI int find_idx(float val, float b0, float b1, float b2) {
+  if (b0 <= val && val <= b2) return (int)roundf((val - b0) / b1);
+  return -1;
+}
+
+/* detector2D.cl:31-186 */
+DI void s_det2d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
+  int a1 = find_idx(det2d_val((uint32_t)c.si[0], 1, n, s), c.sp[0], c.sp[1], c.sp[2]);
+  int a2 = find_idx(det2d_val((uint32_t)c.si[1], 2, n, s), c.sp[3], c.sp[4], c.sp[5]);
+  if (!((a1 == -1) || (a2 == -1))) {
+    long long flat = (long long)a1 * c.si[3] + a2;
+    if (flat >= 0 && flat < c.tally_len) tally_add(c.tally, c.tally_err, flat, n.p);
+    else atomicAdd(&st->oob, 1ull);
+  }
+  if (c.si[4] == 0) {
+    set_pos(n, ip2(s));
+    n.t += s.t2;
+    set_die(n, 1.f);
+  }
+  s_finish(c, n, s, ii);
+}
+
+/* SAttenuate: weight exp(-mu L) over the mesh chord sum held in sd */
+DI void s_attenuate(const CompDev& c, Nt& n, Is& s, uint32_t& ii) {
+  float chord_len = n.sd * len3(nvel(n));
+  n.p *= rm_expf(-c.sp[0] * chord_len);
+  set_pos(n, ip2(s));
+  n.t += s.t2;
+  s_finish(c, n, s, ii);
+}
+
+DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st) {
+  switch (c.scat) {
+    case RAMP_S_ARM: ii = c.idx; is_reset(s); break;
+    case RAMP_S_GUIDE: s_guide(c, n, s, ii, st); break;
+    case RAMP_S_CHOPPER: s_chopper(c, n, s, ii, r); break;
+    case RAMP_S_ISOTROPIC: s_isotropic(c, n, s, ii, r); break;
+    case RAMP_S_POWDERN: s_powdern(c, n, s, ii, r, st); break;
+    case RAMP_S_DET1D: s_det1d(c, n, s, ii, st); break;
+    case RAMP_S_DET2D: s_det2d(c, n, s, ii, st); break;
+    case RAMP_S_COUNTER:
+      if (c.tally) atomicAdd(c.tally, n.p);
+      n.se = 1.0f; n.wr |= WR_SE;
+      s_finish(c, n, s, ii);
+      break;
+    case RAMP_S_BEAMSTOP: set_die(n, 1.0f); s_finish(c, n, s, ii); break;
+    case RAMP_S_ATTENUATE: s_attenuate(c, n, s, ii); break;
+    default: break;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* one component of a linear block (mcramp.py:124-157): transform,      */
+/* intersect, terminate, scatter, untransform on a live neutron.  The   */
+/* intersection starts at its reset value.                               */
+/* ------------------------------------------------------------------ */
+DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st) {
+  transform(c, n);
+  Is s;
+  is_reset(s);
+  if (intersect(c, n, s, st)) ii = c.idx;
+  /* terminate.cl:16-18 */
+  if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
+  if (ii == c.idx && !(n.die > 0.f)) scatter(c, n, s, ii, r, st);
+  if (!(n.die > 0.f)) untransform(c, n);
+}
+
+/* one non-linear block (mcramp.py:167-217): "multi" rounds of all
+ * geometries then all scatters; no termination step. */
+DI void block_nonlinear(const CompDev* comps, int first, int count, int multi, Nt& n,
+                        uint32_t& ii, Rng& r, StatusDev* st) {
+  Is s;
+  is_reset(s);
+  for (int e = 0; e < multi; ++e) {
+    for (int j = first; j < first + count; ++j) {
+      if (n.die > 0.f) break;
+      const CompDev& c = comps[j];
+      transform(c, n);
+      if (intersect(c, n, s, st)) ii = c.idx;
+      untransform(c, n);
+    }
+    for (int j = first; j < first + count; ++j) {
+      if (n.die > 0.f) break;
+      const CompDev& c = comps[j];
+      transform(c, n);
+      if (ii == c.idx) scatter(c, n, s, ii, r, st);
+      if (!(n.die > 0.f)) untransform(c, n);
+    }
+  }
+}
+
+#endif /* RAMP_DEVICE_CUH */

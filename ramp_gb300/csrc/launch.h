@@ -1,0 +1,50 @@
+/*
+ * launch.h — kernel launchers shared between the translation units of
+ * libramp_cuda.so (host side).
+ */
+#ifndef RAMP_LAUNCH_H
+#define RAMP_LAUNCH_H
+
+#include <cuda_runtime.h>
+#include "plan.h"
+
+struct PlainArgs {
+  float* soa;
+  uint32_t* iidx;
+  int64_t stride;
+  int64_t n;
+  RngDev rng;
+  StatusDev* st;
+};
+
+cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_sim,
+                            int32_t seed, cudaStream_t s);
+cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_t s);
+cudaError_t launch_nonlinear_block(const CompDev* comps_dev, int first, int count, int multi,
+                                   const PlainArgs& a, cudaStream_t s);
+
+struct FusedArgs {
+  const VariantDev* variants;   /* device; NULL: one variant, "single"  */
+  const TaskDev* tasks;         /* device; NULL: tasks of task_size     */
+  int64_t n_tasks;
+  int64_t task_size;
+  VariantDev single;
+  const RampBlock* blocks;      /* device */
+  int32_t n_blocks;
+  int32_t n_comps;
+  RngDev rng;
+  float* carry_sb;              /* optional, single variant */
+  uint32_t* carry_iidx;
+  StatusDev* st;
+};
+
+cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s);
+int fused_max_blocks_per_sm(int block, int n_comps);
+
+cudaError_t launch_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out,
+                                  int64_t n, cudaStream_t s);
+cudaError_t launch_debug_rng_peak(int64_t n, int32_t iters, uint32_t* out, cudaStream_t s);
+cudaError_t launch_debug_math(int fn, const float* a, const float* b, float* out, int64_t n,
+                              cudaStream_t s);
+
+#endif

@@ -1,0 +1,247 @@
+/*
+ * plain.cu — the plain path: neutron state as a structure of arrays in HBM
+ * (lane l of neutron i at soa[l*stride + i]) and one kernel per reference
+ * call site:
+ *   k_generate      gen_prg (flat_mod.cl:4, cont_mod.cl:11)
+ *   k_linear<S>     one component of a linear block: the reference's five
+ *                   launches transform, intersect, terminate, scatter,
+ *                   untransform (mcramp.py:124-157) fused into one pass
+ *   k_nonlinear     one non-linear block, all its events (mcramp.py:167-217)
+ * Each thread owns one neutron per grid-stride step; loads and stores of a
+ * lane are contiguous across a warp (128-byte transactions).  Dead
+ * neutrons cost one 4-byte read of the die lane; live ones read and write
+ * only the lanes their component touches (the S template parameter fixes
+ * that set at compile time).
+ */
+#include "device.cuh"
+#include "launch.h"
+
+#define PLAIN_BLOCK 256
+
+#define LANES_APPLY(OP, n, S, st, i)                                                      \
+  OP(n.x, RAMP_X) OP(n.y, RAMP_Y) OP(n.z, RAMP_Z) OP(n.vx, RAMP_VX) OP(n.vy, RAMP_VY)      \
+  OP(n.vz, RAMP_VZ) OP(n.px, RAMP_PX) OP(n.py, RAMP_PY) OP(n.pz, RAMP_PZ) OP(n.p, RAMP_P) \
+  OP(n.t, RAMP_TOF) OP(n.sb, RAMP_MC) OP(n.sc, RAMP_PREVCOMP) OP(n.sd, RAMP_SD)           \
+  OP(n.se, RAMP_SE) OP(n.die, RAMP_DIE)
+#define LD_(f, L) f = S[(L) * st + i];
+#define ST_(f, L) S[(L) * st + i] = f;
+#define LOAD_ALL(n, S, st, i) LANES_APPLY(LD_, n, S, st, i)
+#define STORE_ALL(n, S, st, i) LANES_APPLY(ST_, n, S, st, i)
+#define PLAIN_MAX_GRID (152 * 64)
+
+/* scatter dispatch with the kind fixed at compile time when SK >= 0 */
+template <int SK>
+DI void scatter_k(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st) {
+  switch (SK >= 0 ? SK : c.scat) {
+    case RAMP_S_ARM: ii = c.idx; is_reset(s); break;
+    case RAMP_S_GUIDE: s_guide(c, n, s, ii, st); break;
+    case RAMP_S_CHOPPER: s_chopper(c, n, s, ii, r); break;
+    case RAMP_S_ISOTROPIC: s_isotropic(c, n, s, ii, r); break;
+    case RAMP_S_POWDERN: s_powdern(c, n, s, ii, r, st); break;
+    case RAMP_S_DET1D: s_det1d(c, n, s, ii, st); break;
+    case RAMP_S_DET2D: s_det2d(c, n, s, ii, st); break;
+    case RAMP_S_COUNTER:
+      if (c.tally) atomicAdd(c.tally, n.p);
+      n.se = 1.0f; n.wr |= WR_SE;
+      s_finish(c, n, s, ii);
+      break;
+    case RAMP_S_BEAMSTOP: set_die(n, 1.0f); s_finish(c, n, s, ii); break;
+    case RAMP_S_ATTENUATE: s_attenuate(c, n, s, ii); break;
+    default: break;
+  }
+}
+
+template <int SK>
+DI void comp_linear_k(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st) {
+  transform(c, n);
+  Is s;
+  is_reset(s);
+  if (intersect(c, n, s, st)) ii = c.idx;
+  if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
+  if (ii == c.idx && !(n.die > 0.f)) scatter_k<SK>(c, n, s, ii, r, st);
+  if (!(n.die > 0.f)) untransform(c, n);
+}
+
+__global__ void __launch_bounds__(PLAIN_BLOCK)
+k_generate(const __grid_constant__ SrcDev src, const PlainArgs a, int32_t num_sim, int32_t seed) {
+  const int64_t st = a.stride;
+  float* __restrict__ S = a.soa;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float old_sb = S[RAMP_MC * st + i];
+    Nt n;
+    Rng r;
+    rng_init(r, a.rng.mode, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    generate(src, n, old_sb, num_sim, seed, r);
+    STORE_ALL(n, S, st, i);
+  }
+}
+
+template <int SK>
+__global__ void __launch_bounds__(PLAIN_BLOCK)
+k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
+  constexpr bool RD_P = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
+                        SK == RAMP_S_DET1D || SK == RAMP_S_DET2D || SK == RAMP_S_COUNTER ||
+                        SK == RAMP_S_ATTENUATE;
+  constexpr bool RD_T = SK == RAMP_S_GUIDE || SK == RAMP_S_CHOPPER || SK == RAMP_S_ISOTROPIC ||
+                        SK == RAMP_S_POWDERN || SK == RAMP_S_DET1D || SK == RAMP_S_DET2D ||
+                        SK == RAMP_S_ATTENUATE;
+  constexpr bool RD_SB = SK == RAMP_S_CHOPPER || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN;
+  constexpr bool MOD_VEL = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN;
+  constexpr bool USE_POL = SK == RAMP_S_ISOTROPIC;
+  const int64_t st = a.stride;
+  float* __restrict__ S = a.soa;
+  const bool pol = USE_POL || c.rotated;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float die = S[RAMP_DIE * st + i];
+    if (die > 0.f) continue;
+    Nt n;
+    n.wr = 0;
+    n.die = die;
+    n.x = S[RAMP_X * st + i];   n.y = S[RAMP_Y * st + i];   n.z = S[RAMP_Z * st + i];
+    n.vx = S[RAMP_VX * st + i]; n.vy = S[RAMP_VY * st + i]; n.vz = S[RAMP_VZ * st + i];
+    n.px = n.py = n.pz = 0.0f;
+    if (pol) { n.px = S[RAMP_PX * st + i]; n.py = S[RAMP_PY * st + i]; n.pz = S[RAMP_PZ * st + i]; }
+    n.p = RD_P ? S[RAMP_P * st + i] : 0.0f;
+    n.t = RD_T ? S[RAMP_TOF * st + i] : 0.0f;
+    n.sb = RD_SB ? S[RAMP_MC * st + i] : 0.0f;
+    n.sc = n.sd = n.se = 0.0f;
+    const uint32_t ii0 = a.iidx[i];
+    uint32_t ii = ii0;
+    Rng r;
+    rng_init(r, a.rng.mode, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    comp_linear_k<SK>(c, n, ii, r, a.st);
+    S[RAMP_X * st + i] = n.x; S[RAMP_Y * st + i] = n.y; S[RAMP_Z * st + i] = n.z;
+    if (MOD_VEL || c.rotated) {
+      S[RAMP_VX * st + i] = n.vx; S[RAMP_VY * st + i] = n.vy; S[RAMP_VZ * st + i] = n.vz;
+    }
+    if (pol) { S[RAMP_PX * st + i] = n.px; S[RAMP_PY * st + i] = n.py; S[RAMP_PZ * st + i] = n.pz; }
+    if (RD_P) S[RAMP_P * st + i] = n.p;
+    if (RD_T) S[RAMP_TOF * st + i] = n.t;
+    if (RD_SB) S[RAMP_MC * st + i] = n.sb;
+    if (n.wr & WR_SC) S[RAMP_PREVCOMP * st + i] = n.sc;
+    if (n.wr & WR_SD) S[RAMP_SD * st + i] = n.sd;
+    if (n.wr & WR_SE) S[RAMP_SE * st + i] = n.se;
+    if (n.wr & WR_DIE) S[RAMP_DIE * st + i] = n.die;
+    if (ii != ii0) a.iidx[i] = ii;
+  }
+}
+
+__global__ void __launch_bounds__(PLAIN_BLOCK)
+k_nonlinear(const CompDev* __restrict__ comps, int first, int count, int multi, const PlainArgs a) {
+  const int64_t st = a.stride;
+  float* __restrict__ S = a.soa;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float die = S[RAMP_DIE * st + i];
+    if (die > 0.f) continue;
+    Nt n;
+    LOAD_ALL(n, S, st, i);
+    n.wr = 0;
+    uint32_t ii = a.iidx[i];
+    Rng r;
+    rng_init(r, a.rng.mode, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    block_nonlinear(comps, first, count, multi, n, ii, r, a.st);
+    STORE_ALL(n, S, st, i);
+    a.iidx[i] = ii;
+  }
+}
+
+static int plain_grid(int64_t n) {
+  int64_t g = (n + PLAIN_BLOCK - 1) / PLAIN_BLOCK;
+  if (g > PLAIN_MAX_GRID) g = PLAIN_MAX_GRID;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_sim, int32_t seed,
+                            cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  k_generate<<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(src, a, num_sim, seed);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  int g = plain_grid(a.n);
+  switch (c.scat) {
+#define CASE(K) case K: k_linear<K><<<g, PLAIN_BLOCK, 0, s>>>(c, a); break;
+    CASE(RAMP_S_ARM) CASE(RAMP_S_GUIDE) CASE(RAMP_S_CHOPPER) CASE(RAMP_S_ISOTROPIC)
+    CASE(RAMP_S_POWDERN) CASE(RAMP_S_DET1D) CASE(RAMP_S_DET2D) CASE(RAMP_S_COUNTER)
+    CASE(RAMP_S_BEAMSTOP) CASE(RAMP_S_ATTENUATE)
+#undef CASE
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nonlinear_block(const CompDev* comps_dev, int first, int count, int multi,
+                                   const PlainArgs& a, cudaStream_t s) {
+  if (a.n <= 0 || multi <= 0 || count <= 0) return cudaSuccess;
+  k_nonlinear<<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(comps_dev, first, count, multi, a);
+  return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------ */
+/* debug kernels used by the parity tests                               */
+/* ------------------------------------------------------------------ */
+__global__ void k_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t t = tid[i];
+  out[i] = tf_ref_x(c0[i], t, TF_PARITY ^ t ^ TF_K1 ^ TF_K2 ^ TF_K3);
+}
+
+__global__ void k_debug_math(int fn, const float* a, const float* b, float* out, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float x = a[i], y = b ? b[i] : 0.0f, r = 0.0f;
+  switch (fn) {
+    case 0: r = rm_expf(x); break;
+    case 1: r = rm_logf(x); break;
+    case 2: r = rm_sinf(x); break;
+    case 3: r = rm_cosf(x); break;
+    case 4: r = rm_atan2f(x, y); break;
+    case 5: r = rm_asinf(x); break;
+    case 6: r = rm_acosf(x); break;
+    case 7: r = rm_tanhf(x); break;
+    case 8: r = rm_expm1f(x); break;
+    case 9: r = reflectivity(x, 0.99f, 0.0219f, 3.0f, 2.0f, 0.003f); break;
+    default: break;
+  }
+  out[i] = r;
+}
+
+__global__ void __launch_bounds__(256) k_debug_rng_peak(int32_t iters, uint32_t* out, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t tid = (uint32_t)i;
+  uint32_t k4 = TF_PARITY ^ tid ^ TF_K1 ^ TF_K2 ^ TF_K3;
+  uint32_t a = tid, b = tid ^ 0x9e3779b9u;
+  for (int k = 0; k < iters; ++k) {
+    a = tf_ref_x(a, tid, k4);
+    b = tf_ref_x(b, tid, k4);
+  }
+  out[i] = a ^ b;
+}
+
+cudaError_t launch_debug_rng_peak(int64_t n, int32_t iters, uint32_t* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_debug_rng_peak<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(iters, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out,
+                                  int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_debug_threefry<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c0, tid, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_debug_math(int fn, const float* a, const float* b, float* out, int64_t n,
+                              cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_debug_math<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fn, a, b, out, n);
+  return cudaGetLastError();
+}

@@ -1,0 +1,78 @@
+/*
+ * plan.h — device-side descriptors shared by the plain, fused and ABI
+ * translation units of libramp_cuda.so.
+ */
+#ifndef RAMP_PLAN_H
+#define RAMP_PLAN_H
+
+#include <stdint.h>
+#include "../../include/ramp.h"
+
+/* Per-component descriptor as the kernels read it: the RampComp slots plus
+ * the frame rotation matrix, precomputed on the host with the same float
+ * operations as mcramp/include/geom.h:21-53 evaluates per work-item, and
+ * device copies of the tables. */
+struct alignas(16) CompDev {
+  int32_t geom, scat;
+  uint32_t idx, restore;
+  float pos[3];
+  float R[9];                  /* r00 r01 r02 r10 r11 r12 r20 r21 r22     */
+  int32_t rotated;             /* any Euler angle non-zero                */
+  float gp[RAMP_NGP];
+  float sp[RAMP_NSP];
+  int32_t gi[RAMP_NGI];
+  int32_t si[RAMP_NSI];
+  const float* tab[RAMP_NTAB]; /* device tables                           */
+  int64_t tab_len[RAMP_NTAB];
+  float* tally;
+  float* tally_err;
+  int64_t tally_len;
+  const float4* bvh_nodes;     /* mesh: 2 float4 per node                 */
+  const float4* bvh_tris;      /* mesh: 3 float4 per triangle (v0,e1,e2)  */
+  int32_t bvh_root_leaf;
+  int32_t pad;
+};
+
+struct SrcDev {
+  int32_t kind;
+  int32_t pad;
+  float p[16];
+  float dmax[3];               /* maxwell(k_B T_i, T_i) (cont_mod.cl:25-27) */
+  float pad2;
+};
+
+struct RngDev {
+  int32_t mode;
+  uint32_t run_seed;
+  uint32_t tid_base;
+  uint32_t pad;
+};
+
+/* Device status block owned by a plan. */
+struct StatusDev {
+  unsigned int flags;
+  unsigned int pad;
+  unsigned long long oob;
+  unsigned long long workq;    /* work-queue head of the persistent kernel */
+  unsigned long long pad2;
+};
+
+#define RAMP_MAX_COMPS 64
+
+/* one task of the persistent batched kernel: neutrons [start, start+count)
+ * of variant v */
+struct TaskDev {
+  int32_t variant;
+  int32_t count;
+  int64_t start;
+};
+
+struct VariantDev {
+  SrcDev src;
+  int64_t n;
+  int32_t num_sim;
+  int32_t seed;
+  const CompDev* comps;        /* n_comps descriptors in device memory    */
+};
+
+#endif /* RAMP_PLAN_H */

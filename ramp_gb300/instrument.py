@@ -1,0 +1,433 @@
+"""Instrument facade and instrument-definition-file (IDF) parser.
+
+Mirrors mcramp/mcramp.py (Instrument 254-455, ExecutionBlock 35-251,
+frame_rotate 457-476): the same JSON grammar ($expr$ substitution evaluated
+with eval, // comments, "disable", "relative", "restore_neutron",
+"visualise", block "linear"/"multi"), the same component index assignment
+(the first index is 1 and every component, the source included, takes one),
+the same chunking (chunk = max_mem_alloc / 256 neutrons, a
+random.randint(0, 4096) seed per chunk, weights 1/N_chunk) and the same
+results API (data, save, plot).  Execution goes through libramp_cuda.so:
+``path="plain"`` launches one kernel per component (the reference's call
+structure), ``path="fused"`` runs the whole chain in one persistent kernel.
+There is no CPU fallback: without a CUDA device or without the library,
+execute() raises.
+"""
+import importlib
+import json
+import logging
+import os
+import re
+import warnings
+from collections import OrderedDict
+
+import numpy as np
+import torch
+
+from . import _abi
+from .scat.sprim import _device
+
+log = logging.getLogger("ramp_gb300")
+
+
+def build_kernel(filename, ctx=None):
+    """mcramp.build_kernel (mcramp.py:13-17) compiles a user OpenCL kernel;
+    there is no OpenCL runtime here.  User plugins subclass GPrim/SPrim and
+    reuse the built-in kernels through their descriptor slots."""
+    raise NotImplementedError("OpenCL kernels are not supported; ramp_gb300 runs built-in "
+                              "CUDA kernels selected by the plugin's descriptor kind")
+
+
+def frame_rotate(vec, rot):
+    """Rotate vec by Euler angles rot = [x, y, z] (mcramp.py:457-476)."""
+    x_a, y_a, z_a = rot[0], rot[1], rot[2]
+    r00 = np.cos(y_a) * np.cos(z_a)
+    r01 = -np.cos(x_a) * np.sin(z_a) + np.sin(x_a) * np.sin(y_a) * np.cos(z_a)
+    r02 = np.sin(x_a) * np.sin(z_a) + np.cos(x_a) * np.sin(y_a) * np.cos(z_a)
+    r10 = np.cos(y_a) * np.sin(z_a)
+    r11 = np.cos(x_a) * np.cos(z_a) + np.sin(x_a) * np.sin(y_a) * np.sin(z_a)
+    r12 = -np.sin(x_a) * np.cos(z_a) + np.cos(x_a) * np.sin(y_a) * np.sin(z_a)
+    r20 = -np.sin(y_a)
+    r21 = np.sin(x_a) * np.cos(y_a)
+    r22 = np.cos(x_a) * np.cos(y_a)
+    return [np.dot([r00, r01, r02], vec), np.dot([r10, r11, r12], vec),
+            np.dot([r20, r21, r22], vec)]
+
+
+def _resolve(name):
+    """Plugin class lookup (mcramp.py:80-92): built-ins first, then a module
+    of the same name on sys.path (user plugins)."""
+    pkg = importlib.import_module(__package__)
+    try:
+        return getattr(pkg, name)
+    except AttributeError:
+        return getattr(importlib.import_module(name), name)
+
+
+class KernelRef:
+    def __init__(self, block, comp, pos, rot, vis):
+        self.block = block
+        self.comp = comp
+        self.pos = pos
+        self.rot = rot
+        self.vis = vis
+        self.comp_name = self.comp["name"]
+
+
+class ExecutionBlock:
+    def __init__(self, source, components, parent, linear, max_events):
+        self.source = source
+        self.max_events = max_events
+        self.linear = linear
+        self.components = components
+        self.parent = parent
+
+    @staticmethod
+    def fromJSON(block, parent, linear, events, idx):
+        comps = OrderedDict()
+        source = None
+        for (name, comp) in block.items():
+            if name == "linear" or name == "multi":
+                continue
+            if "disable" in comp and comp["disable"]:
+                continue
+            if "source" in comp:
+                mk = _resolve(comp['moderator_kernel']['name'])
+                args = {k: v for (k, v) in comp['moderator_kernel'].items() if not k == 'name'}
+                args['ctx'] = parent.device
+                source = mk(**args)
+            else:
+                pos = comp['position'] if 'position' in comp else [0, 0, 0]
+                rot = comp['rotation'] if 'rotation' in comp else [0, 0, 0]
+                vis = comp['visualise'] if 'visualise' in comp else True
+                restore_neutron = comp['restore_neutron'] if 'restore_neutron' in comp else False
+                if 'relative' in comp:
+                    rcomp = comps[comp['relative']]
+                    rpos, rrot = rcomp["pos"], rcomp["rot"]
+                    pos = frame_rotate(pos, [rrot[0], rrot[1], rrot[2]])
+                    pos = np.add(pos, [rpos[0], rpos[1], rpos[2]])
+                    rot = np.add(rot, [rrot[0], rrot[1], rrot[2]])
+                gk = _resolve(comp['geom_kernel']['name'])
+                gargs = {k: v for (k, v) in comp['geom_kernel'].items() if not k == 'name'}
+                gargs['idx'] = parent.idx
+                gargs['ctx'] = parent.device
+                sk = _resolve(comp['scat_kernel']['name'])
+                sargs = {k: v for (k, v) in comp['scat_kernel'].items() if not k == 'name'}
+                sargs['idx'] = parent.idx
+                sargs['ctx'] = parent.device
+                sargs['inst'] = parent
+                sargs['block'] = idx
+                comps[name] = {
+                    "name": name,
+                    "geom_kernel": gk(**gargs),
+                    "scat_kernel": sk(**sargs),
+                    "restore_neutron": np.uint32(1) if restore_neutron else np.uint32(0),
+                    "pos": np.array((pos[0], pos[1], pos[2]), dtype=np.float32),
+                    "rot": np.array((rot[0], rot[1], rot[2]), dtype=np.float32),
+                    "vis": vis,
+                    "idx": int(parent.idx),
+                }
+                parent.kernel_refs.append(KernelRef(idx, comps[name], pos, rot, vis))
+            parent.idx += 1
+        return ExecutionBlock(source, comps, parent, linear, events)
+
+
+class Instrument:
+    """An instrument built from an IDF (mcramp.py:254-455).
+
+    Parameters
+    ----------
+    fn : str
+        Instrument definition file name.
+    ctx : torch.device, str, int or None
+        Device for tallies and neutron state (the reference takes an OpenCL
+        context here).  None selects cuda:0 when available.
+    queue : torch.cuda.Stream or None
+        Stream the kernels are launched on (None: the current stream).
+    **kwargs
+        Values for the $...$ variables of the IDF.
+    """
+
+    def __init__(self, fn, ctx=None, queue=None, **kwargs):
+        self.ctx = ctx
+        self.queue = queue
+        self.device = _device(ctx)
+        self.kernel_refs = []
+        self.idx = 1
+        self.fn = fn
+        self.blocks = self._fromJSON(fn, ctx, queue, **kwargs)
+        self._plan = None
+        self._keep = []
+        self.state = None
+        self.iidx = None
+        self.last_chunk = 0
+        self.oob_drops = 0
+        self.status_flags = 0
+
+    # ------------------------------------------------------------------
+    # IDF
+    # ------------------------------------------------------------------
+    def _substitute_params(self, json_str, **kwargs):
+        # as the reference (mcramp.py:328-355): a token that contains another
+        # variable name as a substring is substituted textually
+        pattern = r"(?:\$)(.*?)(?:\$)"
+        tokens = re.findall(pattern, json_str)
+        for t in tokens:
+            subbed_t = t
+            for key, value in kwargs.items():
+                subbed_t = subbed_t.replace("{}".format(key), str(value))
+            json_str = json_str.replace("${}$".format(t), str(eval(subbed_t)))
+        split_str = json_str.split("\n")
+        for line_num, line in enumerate(split_str):
+            if '//' in line:
+                split_str[line_num] = line.split("//", 1)[0]
+        return '\n'.join(split_str)
+
+    def _fromJSON(self, fn, ctx, queue, **kwargs):
+        with open(fn, 'r') as f:
+            json_str = self._substitute_params(f.read(), **kwargs)
+        inst = json.loads(json_str, object_pairs_hook=OrderedDict)
+        blocks = []
+        for i, block in enumerate(inst.values()):
+            if "linear" in block:
+                linear = block["linear"]
+                events = block["multi"] if (not linear and "multi" in block) else 1
+            else:
+                linear = True
+                events = 1
+            blocks.append(ExecutionBlock.fromJSON(block, self, linear, events, i))
+        return blocks
+
+    @property
+    def source(self):
+        for block in self.blocks:
+            if block.source is not None:
+                return block.source
+        raise ValueError("instrument has no source component")
+
+    # ------------------------------------------------------------------
+    # descriptors
+    # ------------------------------------------------------------------
+    def components(self):
+        """(name, component dict) for every non-source component in order."""
+        out = []
+        for block in self.blocks:
+            for name, comp in block.components.items():
+                out.append((name, comp))
+        return out
+
+    def descriptors(self, keep=None):
+        """POD descriptors (RampSource, RampComp array, RampBlock array) of
+        this instrument; host tables are kept alive in ``keep``."""
+        keep = self._keep if keep is None else keep
+        src = self.source.descriptor()
+        comps = []
+        blocks = []
+        for block in self.blocks:
+            first = len(comps)
+            for name, comp in block.components.items():
+                c = _abi.RampComp()
+                c.idx = comp["idx"]
+                c.restore = int(comp["restore_neutron"])
+                for k in range(3):
+                    c.pos[k] = comp["pos"][k]
+                    c.rot[k] = comp["rot"][k]
+                comp["geom_kernel"].fill(c, keep)
+                comp["scat_kernel"].fill(c, keep)
+                if c.geom == 0 or c.scat == 0:
+                    raise TypeError("component %s: plugin classes must set a kind" % name)
+                comps.append(c)
+            b = _abi.RampBlock()
+            b.first = first
+            b.count = len(comps) - first
+            b.linear = 1 if block.linear else 0
+            b.multi = int(block.max_events)
+            blocks.append(b)
+        carr = (_abi.RampComp * max(1, len(comps)))(*comps)
+        barr = (_abi.RampBlock * max(1, len(blocks)))(*blocks)
+        return src, carr, len(comps), barr, len(blocks)
+
+    def tallies(self):
+        out = []
+        for _, comp in self.components():
+            out.extend(comp["scat_kernel"].tallies())
+        return out
+
+    def reset_tallies(self):
+        """Zero every detector (the reference never resets them)."""
+        for t in self.tallies():
+            t.zero_()
+
+    # ------------------------------------------------------------------
+    # execution
+    # ------------------------------------------------------------------
+    def _lib(self):
+        if self.device.type != "cuda":
+            raise RuntimeError("Instrument.execute needs a CUDA device (ctx=%s)" % self.device)
+        return _abi.load()
+
+    def plan(self):
+        if self._plan is None:
+            lib = self._lib()
+            with torch.cuda.device(self.device):
+                src, carr, nc, barr, nb = self.descriptors()
+                h = _abi.ctypes.c_void_p()
+                _abi.check(lib, lib.ramp_plan_create(_abi.ctypes.byref(src), carr, nc, barr, nb,
+                                                     _abi.ctypes.byref(h)), "ramp_plan_create")
+                self._plan = h
+                self._lib_handle = lib
+        return self._plan
+
+    def __del__(self):
+        try:
+            if self._plan is not None:
+                self._lib_handle.ramp_plan_destroy(self._plan)
+                self._plan = None
+        except Exception:
+            pass
+
+    def max_mem_alloc_size(self):
+        """Stand-in for CL_DEVICE_MAX_MEM_ALLOC_SIZE: a quarter of the
+        device memory, the value NVIDIA's OpenCL driver reports."""
+        return torch.cuda.get_device_properties(self.device).total_memory // 4
+
+    def chunk_size(self, buf_max_mod=None):
+        m = self.max_mem_alloc_size()
+        return int(m / 8 / 32 / buf_max_mod) if buf_max_mod is not None else int(m / 8 / 32)
+
+    def _stream_ptr(self):
+        s = self.queue if self.queue is not None else torch.cuda.current_stream(self.device)
+        return _abi.ctypes.c_void_p(s.cuda_stream)
+
+    def _alloc_state(self, n):
+        stride = (n + 31) // 32 * 32
+        self.state = torch.zeros((_abi.NLANES, stride), dtype=torch.float32, device=self.device)
+        self.iidx = torch.zeros(stride, dtype=torch.int32, device=self.device)
+        st = _abi.RampState()
+        st.soa = self.state.data_ptr()
+        st.iidx = self.iidx.data_ptr()
+        st.stride = stride
+        return st
+
+    def execute(self, N, buf_max_mod=None, debug=False, trace=False, path="plain",
+                rng="reference", run_seed=0, tune=None, chunk=None, shard=None):
+        """Trace N neutron histories (mcramp.py:403-455).
+
+        path : "plain" (one kernel per component) or "fused" (one
+               persistent kernel for the whole chain).
+        rng  : "reference" reproduces the reference's per-draw Threefry
+               stream; "native" uses all four words of each block.
+        chunk: override the chunk size (default max_mem_alloc / 256).
+        shard: (rank, world) — trace only this rank's contiguous slice of
+               every chunk, keyed by global index and weighted by the full
+               chunk size, so the sum of all ranks' tallies equals a
+               single-device run (the histogram sum is the caller's
+               exchange step, e.g. torch.distributed.all_reduce).
+        """
+        lib = self._lib()
+        plan = self.plan()
+        N = int(N)
+        buf_max = int(chunk) if chunk else self.chunk_size(buf_max_mod)
+        rngd = _abi.RampRng()
+        rngd.mode = {"reference": 0, "native": 1}[rng]
+        rngd.run_seed = int(run_seed) & 0xffffffff
+        tuned = None
+        if tune is not None:
+            tuned = _abi.RampTune(*[int(tune.get(k, 0)) for k in
+                                    ("block", "blocks_per_sm", "chunk", "privatize")])
+        if trace:
+            warnings.warn("trace=True (visualisation lines) is not supported; ignored")
+        rank, world = shard if shard is not None else (0, 1)
+        if not (0 <= rank < world):
+            raise ValueError("shard must be (rank, world) with 0 <= rank < world")
+
+        def part(torun):
+            lo = torun * rank // world
+            hi = torun * (rank + 1) // world
+            return lo, hi - lo
+
+        first = part(min(N, buf_max))[1] if world > 1 else min(N, buf_max)
+        if world > 1 and N > buf_max:
+            first = max(part(buf_max)[1], part(N % buf_max or buf_max)[1])
+        src = self.source
+        with torch.cuda.device(self.device):
+            stream = self._stream_ptr()
+            if path == "plain":
+                st = self._alloc_state(first)
+            elif path == "fused":
+                carry = None
+                if N > buf_max:
+                    # per index: final RNG counter (float) and index buffer (uint32)
+                    carry = torch.zeros((2, first), dtype=torch.float32, device=self.device)
+            else:
+                raise ValueError("path must be 'plain' or 'fused'")
+            remaining = N
+            while remaining > 0:
+                torun = buf_max if remaining > buf_max else remaining
+                remaining -= torun
+                seed = src.next_seed()
+                lo, nloc = part(torun)
+                rngd.tid_base = lo
+                if path == "plain":
+                    rc = lib.ramp_trace_plain(plan, _abi.ctypes.byref(st), nloc, torun, seed,
+                                              _abi.ctypes.byref(rngd), stream)
+                    _abi.check(lib, rc, "ramp_trace_plain")
+                    if debug:
+                        torch.cuda.synchronize(self.device)
+                        alive = self.state[:, :nloc][_abi.LANE["die"]] == 0
+                        print("Neutron output after chunk (alive records):")
+                        print(self.state[:, :nloc][:, alive].T.cpu().numpy())
+                else:
+                    sbp = iip = None
+                    if carry is not None:
+                        sbp = _abi.ctypes.c_void_p(carry[0].data_ptr())
+                        iip = _abi.ctypes.c_void_p(carry[1].data_ptr())
+                    rc = lib.ramp_trace_fused(plan, nloc, torun, seed, _abi.ctypes.byref(rngd),
+                                              sbp, iip,
+                                              _abi.ctypes.byref(tuned) if tuned else None,
+                                              stream)
+                    _abi.check(lib, rc, "ramp_trace_fused")
+                self.last_chunk = nloc
+            self._check_status(lib, plan)
+
+    def _check_status(self, lib, plan):
+        flags = _abi.ctypes.c_uint32()
+        oob = _abi.ctypes.c_uint64()
+        _abi.check(lib, lib.ramp_plan_status(plan, _abi.ctypes.byref(flags),
+                                             _abi.ctypes.byref(oob)), "ramp_plan_status")
+        self.oob_drops += oob.value
+        self.status_flags |= flags.value
+        if flags.value & (_abi.F_GUIDE_CAP | _abi.F_POWDER_CAP | _abi.F_BVH_STACK):
+            warnings.warn("device status flags 0x%x: a bounded loop hit its cap and the "
+                          "affected neutrons were terminated" % flags.value)
+        if oob.value:
+            log.debug("%d tally writes fell outside their buffers and were dropped", oob.value)
+
+    def neutron_state(self):
+        """Final records of the last chunk as an array [n, 16] (the
+        reference's float16 layout) and the index buffer."""
+        if self.state is None:
+            raise RuntimeError("no plain-path state (run execute(path='plain') first)")
+        n = self.last_chunk
+        return (self.state[:, :n].T.contiguous().cpu().numpy(),
+                self.iidx[:n].cpu().numpy().view(np.uint32))
+
+    # ------------------------------------------------------------------
+    # results
+    # ------------------------------------------------------------------
+    def data(self):
+        """name -> data of every component (mcramp.py:281-293)."""
+        return {d.comp_name: d.comp["scat_kernel"].data(self.queue) for d in self.kernel_refs}
+
+    def plot(self):
+        from matplotlib.pyplot import show
+        for d in self.kernel_refs:
+            d.comp["scat_kernel"].plot(self.queue)
+        show()
+
+    def save(self):
+        for d in self.kernel_refs:
+            d.comp["scat_kernel"].save(self.queue)
+
+    def visualise(self, *args, **kwargs):
+        raise NotImplementedError("instrument visualisation is not part of ramp_gb300")

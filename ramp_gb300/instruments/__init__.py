@@ -1,0 +1,107 @@
+"""Synthetic instrument definition files (the reference's JSON format) for
+the benchmark and parity workloads, and generators for their inputs.
+
+* small_chain.json  — flat-spectrum moderator, 30x30 mm slit, vanadium-like
+  incoherent cylinder (r 5 mm, h 40 mm), banana detector r 2.5 m with a
+  500 x 500 (2theta 5-135 deg, TOF 0-20 ms) histogram.
+* let_like.json     — LET-like direct-geometry chopper spectrometer:
+  Maxwellian moderator at 40 K, four m=2 supermirror guide segments, five
+  disk choppers phased for $Ei$, optional slit ($use_slit$, $slit_w$),
+  powder sample with 40 lines, banana detector r 3.5 m with a 720 x 1000
+  (2theta -40..140 deg, TOF 0-50 ms) histogram.
+* mesh_imaging.json — near-parallel flat beam through a seeded perturbed
+  torus mesh (GMesh + SAttenuate, mu 0.5 /cm) rotated by $angle$, onto a
+  1024 x 1024 pixel detector.
+All inputs are seeded synthetic stand-ins; nothing is read from elsewhere.
+"""
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GENERATED = os.path.join(HERE, "_generated")
+
+
+def path(name):
+    return os.path.join(HERE, name)
+
+
+def write_flat_sqw(fn, sigma_abs=5.08, sigma_inc=5.08, rho=0.0723, nq=201, qmax=15.0,
+                   nw=5, wmax=0.05):
+    """A McStas Isotropic_Sqw file with S(q, w) flat in q and peaked at w=0
+    (a vanadium-like incoherent scatterer).  The header keeps the
+    reference loader's field names; its scattering cross-section is read
+    from the ``sigma_coh`` field (isotropic.py:200)."""
+    q = np.linspace(0.0, qmax, nq)
+    w = np.linspace(-wmax, wmax, nw)
+    s = np.exp(-0.5 * (w / (wmax / 2.0)) ** 2)
+    with open(fn, "w") as f:
+        f.write("# Format: Sqw data file for Isotropic_Sqw (synthetic, vanadium-like)\n")
+        f.write("# V_rho %.6f\n" % rho)
+        f.write("# sigma_abs %.4f\n" % sigma_abs)
+        f.write("# sigma_coh %.4f\n" % sigma_inc)
+        f.write("# sigma_inc 0.0\n")
+        f.write("# q vector\n")
+        f.write(" ".join("%.6f" % v for v in q) + "\n")
+        f.write("# w vector\n")
+        f.write(" ".join("%.6f" % v for v in w) + "\n")
+        f.write("# S(q,w) matrix, one row per q\n")
+        for _ in q:
+            f.write(" ".join("%.6e" % v for v in s) + "\n")
+    return fn
+
+
+def powder_lines(n=40, seed=7):
+    """d-spacings uniform in [0.8, 4] AA and |F|^2 log-uniform over three
+    decades, numpy seed 7."""
+    rng = np.random.default_rng(seed)
+    d = np.sort(rng.uniform(0.8, 4.0, n))
+    f2 = 10.0 ** rng.uniform(-1.0, 2.0, n)
+    return d, f2
+
+
+def torus_triangles(R=0.020, r=0.008, nu=448, nv=224, noise=0.0002, seed=5):
+    """A closed torus mesh (axis along y) with Gaussian vertex noise:
+    2*nu*nv triangles (200,704 for the defaults), float32 [n, 9]."""
+    rng = np.random.default_rng(seed)
+    u = np.arange(nu) * (2 * np.pi / nu)
+    v = np.arange(nv) * (2 * np.pi / nv)
+    U, V = np.meshgrid(u, v, indexing="ij")
+    X = (R + r * np.cos(V)) * np.cos(U)
+    Z = (R + r * np.cos(V)) * np.sin(U)
+    Y = r * np.sin(V)
+    P = np.stack([X, Y, Z], axis=-1) + rng.normal(0.0, noise, (nu, nv, 3))
+    i0, j0 = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    i1, j1 = (i0 + 1) % nu, (j0 + 1) % nv
+    a, b, c, d = P[i0, j0], P[i1, j0], P[i1, j1], P[i0, j1]
+    # counter-clockwise seen from outside: outward normals, as STL expects
+    t1 = np.concatenate([a, c, b], axis=-1).reshape(-1, 9)
+    t2 = np.concatenate([a, d, c], axis=-1).reshape(-1, 9)
+    return np.concatenate([t1, t2]).astype(np.float32)
+
+
+def ensure_inputs():
+    """Write the generated inputs (Sqw file, torus STL) if missing."""
+    from ..geom.mesh import write_stl
+    os.makedirs(GENERATED, exist_ok=True)
+    sqw = os.path.join(GENERATED, "vanadium_inc.sqw")
+    if not os.path.exists(sqw):
+        write_flat_sqw(sqw)
+    stl = os.path.join(GENERATED, "torus.stl")
+    if not os.path.exists(stl):
+        write_stl(stl, torus_triangles())
+    return {"sqw": sqw, "stl": stl}
+
+
+def let_like_kwargs(Ei=3.7, use_slit=0, slit_w=0.03):
+    return dict(Ei=Ei, use_slit=use_slit, slit_w=slit_w)
+
+
+def small_chain_kwargs():
+    # $...$ values are substituted as text and evaluated (mcramp.py:333-338),
+    # so a file name is passed as a Python string literal
+    return dict(sqw_file=repr(ensure_inputs()["sqw"]))
+
+
+def mesh_imaging_kwargs(angle=0.0):
+    return dict(stl_file=repr(ensure_inputs()["stl"]), angle=angle)

@@ -1,0 +1,3 @@
+"""Moderator plugins (mcramp/moderator/*)."""
+from .flat_mod import MFlat
+from .cont_mod import MCont

@@ -1,0 +1,209 @@
+"""Parity of the CUDA paths with the CPU oracle (the reference's kernels
+restated over its own record layout and sequencing).
+
+Per-neutron final records (all 16 lanes) and the index buffer must be
+bit-identical (NaN equal to NaN, +0 equal to -0): both sides run the same
+FP32 operations with the same math library and one rounding per operation.
+Histograms may differ only by the order of float atomic additions:
+|gpu - cpu| <= 1e-5 |cpu| + 1e-6 max|cpu| per bin.
+"""
+import os
+import random
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import ramp_gb300 as m
+from ramp_gb300 import _abi, instruments as I
+from ramp_gb300.batch import BatchedInstrument
+
+pytestmark = pytest.mark.gpu
+
+GOLD_DIR = os.path.join(os.path.dirname(__file__), "golden")
+GOLD = np.load(os.path.join(GOLD_DIR, "ref_pins.npz"))
+RTOL, ATOL_FRAC = 1e-5, 1e-6
+
+
+def records_equal(a, b):
+    eq = (a == b) | (np.isnan(a) & np.isnan(b))
+    if not eq.all():
+        bad = np.argwhere(~eq)
+        i, l = bad[0]
+        raise AssertionError("%d mismatching values; first at neutron %d lane %d: gpu %r cpu %r\n"
+                             "gpu %r\ncpu %r" % (len(bad), i, l, a[i, l], b[i, l], a[i], b[i]))
+
+
+def tallies_close(g_inst, c_inst):
+    for tg, tc in zip(g_inst.tallies(), c_inst.tallies()):
+        g = tg.cpu().numpy().astype(np.float64)
+        c = tc.numpy().astype(np.float64)
+        atol = ATOL_FRAC * max(np.abs(c).max(), 1e-30)
+        assert np.allclose(g, c, rtol=RTOL, atol=atol), \
+            "tally mismatch: max abs diff %g (scale %g)" % (np.abs(g - c).max(), np.abs(c).max())
+        assert np.array_equal(g != 0, c != 0) or np.abs(g - c).max() <= atol
+
+
+def pair(fn, kw, N, path="plain", rng="reference", chunk=None, seed=1234):
+    gi = m.Instrument(fn, "cuda", **kw)
+    random.seed(seed)
+    gi.execute(N, path=path, rng=rng, chunk=chunk)
+    torch.cuda.synchronize()
+    ci = m.Instrument(fn, "cpu", **kw)
+    random.seed(seed)
+    r = oracle.run(ci, N, chunk=chunk, rng_mode={"reference": 0, "native": 1}[rng])
+    return gi, ci, r
+
+
+def check_plain(fn, kw, N, **k):
+    gi, ci, r = pair(fn, kw, N, **k)
+    recs, iidx = gi.neutron_state()
+    records_equal(recs, r.neutrons)
+    assert np.array_equal(iidx, r.iidx)
+    tallies_close(gi, ci)
+    assert gi.oob_drops == r.oob
+    return gi, ci, r
+
+
+# ---------------------------------------------------------------- RNG / math
+def test_device_threefry_matches_reference_golden(cuda_lib):
+    c0 = torch.tensor(GOLD["threefry_ctr0"].view(np.int32), device="cuda")
+    tid = torch.tensor(GOLD["threefry_tid"].view(np.int32), device="cuda")
+    out = torch.empty_like(c0)
+    assert cuda_lib.ramp_debug_threefry(c0.data_ptr(), tid.data_ptr(), out.data_ptr(),
+                                        c0.numel(), None) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), GOLD["threefry_x"])
+
+
+@pytest.mark.parametrize("fn", range(10))
+def test_device_math_bit_identical_to_host(cuda_lib, fn):
+    r = np.random.default_rng(fn)
+    a = np.concatenate([r.uniform(-20, 20, 50000), r.standard_normal(50000),
+                        np.exp(r.uniform(-30, 30, 50000)), r.uniform(-1, 1, 50000),
+                        [0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan]]).astype(np.float32)
+    if fn == 9:
+        a = np.abs(r.uniform(0, 0.2, 200007)).astype(np.float32)
+    b = np.roll(a, 7)
+    host = oracle.math(fn, a, b)
+    da, db = torch.tensor(a, device="cuda"), torch.tensor(b, device="cuda")
+    out = torch.empty_like(da)
+    assert cuda_lib.ramp_debug_math(fn, da.data_ptr(), db.data_ptr(), out.data_ptr(),
+                                    da.numel(), None) == 0
+    torch.cuda.synchronize()
+    dev = out.cpu().numpy()
+    same = (dev.view(np.uint32) == host.view(np.uint32)) | (np.isnan(dev) & np.isnan(host))
+    assert same.all(), "fn %d: %d differ" % (fn, (~same).sum())
+
+
+# ---------------------------------------------------------------- plain path
+def test_small_chain_plain_matches_oracle(cuda_lib):
+    check_plain(I.path("small_chain.json"), I.small_chain_kwargs(), 300_000)
+
+
+def test_let_like_plain_matches_oracle(cuda_lib):
+    check_plain(I.path("let_like.json"), I.let_like_kwargs(), 1_000_000)
+
+
+def test_let_like_with_slit_and_other_ei(cuda_lib):
+    check_plain(I.path("let_like.json"), I.let_like_kwargs(Ei=12.0, use_slit=1, slit_w=0.02),
+                400_000)
+
+
+def test_mesh_imaging_bvh_matches_brute_force_oracle(cuda_lib):
+    check_plain(I.path("mesh_imaging.json"), I.mesh_imaging_kwargs(angle=0.37), 20_000)
+
+
+@pytest.mark.parametrize("name", ["nonlinear_env.json", "rotated_chain.json",
+                                  "guides_monitors.json"])
+def test_feature_chains_match_oracle(cuda_lib, name):
+    check_plain(os.path.join(GOLD_DIR, name), I.small_chain_kwargs(), 200_000)
+
+
+@pytest.mark.parametrize("N", [1, 37, 1000, 4099])
+def test_ragged_sizes(cuda_lib, N):
+    check_plain(I.path("small_chain.json"), I.small_chain_kwargs(), N)
+
+
+def test_multi_chunk_reference_keying(cuda_lib):
+    """Three chunks (the last one short): counters carry over between chunks
+    (flat_mod.cl:19) and weights are 1/N_chunk."""
+    check_plain(I.path("small_chain.json"), I.small_chain_kwargs(), 250_001, chunk=100_000)
+
+
+def test_native_keying_matches_oracle(cuda_lib):
+    check_plain(I.path("let_like.json"), I.let_like_kwargs(), 500_000, rng="native")
+
+
+# ---------------------------------------------------------------- fused path
+@pytest.mark.parametrize("fn,kw,N", [
+    ("small_chain.json", "small", 300_000),
+    ("let_like.json", "let", 1_000_000),
+    ("mesh_imaging.json", "mesh", 20_000)])
+def test_fused_matches_oracle(cuda_lib, fn, kw, N):
+    kws = {"small": I.small_chain_kwargs(), "let": I.let_like_kwargs(),
+           "mesh": I.mesh_imaging_kwargs(0.37)}[kw]
+    gi, ci, r = pair(I.path(fn), kws, N, path="fused")
+    tallies_close(gi, ci)
+    assert gi.oob_drops == r.oob
+
+
+@pytest.mark.parametrize("name", ["nonlinear_env.json", "rotated_chain.json",
+                                  "guides_monitors.json"])
+def test_fused_feature_chains(cuda_lib, name):
+    gi, ci, r = pair(os.path.join(GOLD_DIR, name), I.small_chain_kwargs(), 200_000,
+                     path="fused")
+    tallies_close(gi, ci)
+
+
+def test_fused_multi_chunk_carry(cuda_lib):
+    gi, ci, r = pair(I.path("small_chain.json"), I.small_chain_kwargs(), 250_001, path="fused",
+                     chunk=100_000)
+    tallies_close(gi, ci)
+
+
+def test_fused_native_keying(cuda_lib):
+    gi, ci, r = pair(I.path("let_like.json"), I.let_like_kwargs(), 500_000, path="fused",
+                     rng="native")
+    tallies_close(gi, ci)
+
+
+def test_fused_equals_plain_at_1e7(cuda_lib):
+    """Size-independent property at full size: the fused and plain paths
+    trace the same histories, so their tallies agree to reordering error."""
+    kw = I.let_like_kwargs()
+    a = m.Instrument(I.path("let_like.json"), "cuda", **kw)
+    b = m.Instrument(I.path("let_like.json"), "cuda", **kw)
+    random.seed(7)
+    a.execute(10_000_000, path="plain")
+    random.seed(7)
+    b.execute(10_000_000, path="fused")
+    for ta, tb in zip(a.tallies(), b.tallies()):
+        x, y = ta.cpu().double(), tb.cpu().double()
+        assert torch.allclose(x, y, rtol=RTOL, atol=ATOL_FRAC * float(x.abs().max()))
+
+
+# ---------------------------------------------------------------- batching
+def test_batched_variants_match_single_runs(cuda_lib):
+    """Variants with different Ei, slit width and neutron count in one
+    launch; each equals its own oracle run with the same seed and keying."""
+    variants = [I.let_like_kwargs(Ei=3.7, use_slit=1, slit_w=0.03),
+                I.let_like_kwargs(Ei=8.0, use_slit=1, slit_w=0.015),
+                I.let_like_kwargs(Ei=2.5, use_slit=1, slit_w=0.04)]
+    counts = [300_000, 123_457, 200_003]
+    for mode, rng in ((0, "reference"), (1, "native")):
+        B = BatchedInstrument(I.path("let_like.json"), variants, ctx="cuda")
+        B.execute(counts, rng=rng, seeds=[11, 2222, 4000])
+        torch.cuda.synchronize()
+        for v, (kw, n, seed) in enumerate(zip(variants, counts, [11, 2222, 4000])):
+            ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
+            oracle.run(ci, n, rng_mode=mode, variant=v, seeds=[seed])
+            tallies_close(B.instruments[v], ci)
+
+
+# ---------------------------------------------------------------- status
+def test_guide_bounce_cap_and_oob_counts(cuda_lib):
+    gi, ci, r = check_plain(os.path.join(GOLD_DIR, "guides_monitors.json"),
+                            I.small_chain_kwargs(), 100_000)
+    assert r.oob > 0 and gi.oob_drops == r.oob
