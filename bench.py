@@ -52,15 +52,17 @@ def args_():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=N_HIST)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
 
 
-def workload_config(n, world):
+def workload_config(n, world, path="fused persistent kernel (plain per-component path "
+                                   "reported beside)"):
     return {"workload": "LET-like chain (MCont 40 K, 4 m=2 guides, 5 choppers at Ei 3.7 meV, "
                         "40-line powder, 720x1000 banana histogram)",
             "histories_per_step_per_gpu": n, "global_histories_per_step": n * world,
             "rng": "reference keying (Threefry-4x32-20, one block per draw)",
-            "path": "fused persistent kernel (plain per-component path reported beside)",
+            "path": path,
             "l2": "flushed between steps (256 MiB write)", "parallelism": "dp%d" % world}
 
 
@@ -96,7 +98,8 @@ def run_reference(a):
             "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
             "ms_per_step": 1000.0 * statistics.mean(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference", "config": workload_config(CPU_SAMPLE, 1),
+            "impl": "reference",
+            "config": workload_config(CPU_SAMPLE, 1, "CPU restatement, reference sequencing"),
             "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0,
@@ -250,9 +253,9 @@ def main():
     inst._check_status(lib, inst.plan())
 
     # ---- end to end through the public API ----
-    e2e_steps = max(2, a.steps // 2)
+    e2e_steps = 0 if a.no_e2e else max(2, a.steps // 2)
     e2e_ms, h2d, d2h = [], 0, 0
-    for k in range(e2e_steps + 1):
+    for k in range(e2e_steps + 1 if e2e_steps else 0):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ei = m.Instrument(fn, dev, **kw)
@@ -267,7 +270,7 @@ def main():
         h2d = sum(x.nbytes for x in keep) + _abi.ctypes.sizeof(carr) + _abi.ctypes.sizeof(barr)
         d2h = sum(t.numel() * t.element_size() for t in ei.tallies())
         del ei, d
-    e2e = world * n / (statistics.mean(e2e_ms) / 1000.0)
+    e2e = world * n / (statistics.mean(e2e_ms) / 1000.0) if e2e_ms else None
 
     if rank != 0:
         return

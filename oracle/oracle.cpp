@@ -216,7 +216,12 @@ struct Ctx {
   std::atomic<uint32_t>* flags;
 };
 
+/* Tally addition.  The GPU's float atomics flush subnormal operands to
+ * zero (the reference's CAS-loop add leaves this to the OpenCL device), so
+ * terms are flushed the same way here. */
+inline float ftz(float x) { return fabsf(x) < 1.17549435e-38f ? copysignf(0.0f, x) : x; }
 inline void atomic_add_f(float* addr, float v) {
+  v = ftz(v);
 #pragma omp atomic
   *addr += v;
 }
@@ -482,31 +487,50 @@ void g_arm(float* n, float* s, uint32_t* iidx, const RampComp& k) {
   *iidx = k.idx;
 }
 
-/* Chord time through a closed mesh from its crossings (t, sign: -1 entering,
- * +1 exiting): sorted by t, each entry is paired with the next exit and
- * repeated entries or exits (a ray through an edge shared by two faces can
- * be accepted by both) are ignored.  The ray is taken to start outside.
- * Shared with the GPU kernel's semantics; the reference has no chord sum. */
-const int MESH_MAX_HITS = 16;
-float chord_from_hits(float* t, int* sg, int nh) {
-  for (int a = 1; a < nh; ++a) {
-    float tv = t[a]; int sv = sg[a]; int b = a - 1;
-    while (b >= 0 && (t[b] > tv || (t[b] == tv && sg[b] > sv))) { t[b + 1] = t[b]; sg[b + 1] = sg[b]; --b; }
-    t[b + 1] = tv; sg[b + 1] = sv;
+/* Watertight ray/triangle crossing (Woop, Benthin, Wald: "Watertight
+ * Ray/Triangle Intersection", JCGT 2(1), 2013) used for SAttenuate's chord:
+ * edge functions of a shared edge are exact negations of each other, so a
+ * ray through an edge crosses exactly one of its two faces; exact zeros are
+ * re-evaluated in double.  Returns the ray parameter t (NaN: no crossing).
+ * kx, ky, kz and Sx, Sy, Sz are the per-ray shear of the method. */
+struct Shear { int kx, ky, kz; float Sx, Sy, Sz; };
+Shear make_shear(V3 d) {
+  float ad[3] = {fabsf(d.x), fabsf(d.y), fabsf(d.z)};
+  float dd[3] = {d.x, d.y, d.z};
+  Shear S;
+  S.kz = (ad[0] > ad[1]) ? ((ad[0] > ad[2]) ? 0 : 2) : ((ad[1] > ad[2]) ? 1 : 2);
+  S.kx = (S.kz + 1) % 3; S.ky = (S.kx + 1) % 3;
+  if (dd[S.kz] < 0.0f) { int t = S.kx; S.kx = S.ky; S.ky = t; }
+  S.Sx = dd[S.kx] / dd[S.kz]; S.Sy = dd[S.ky] / dd[S.kz]; S.Sz = 1.0f / dd[S.kz];
+  return S;
+}
+float watertight_t(const Shear& S, V3 org, V3 v0, V3 v1, V3 v2) {
+  float A[3] = {v0.x - org.x, v0.y - org.y, v0.z - org.z};
+  float B[3] = {v1.x - org.x, v1.y - org.y, v1.z - org.z};
+  float C[3] = {v2.x - org.x, v2.y - org.y, v2.z - org.z};
+  float Ax = A[S.kx] - S.Sx * A[S.kz], Ay = A[S.ky] - S.Sy * A[S.kz];
+  float Bx = B[S.kx] - S.Sx * B[S.kz], By = B[S.ky] - S.Sy * B[S.kz];
+  float Cx = C[S.kx] - S.Sx * C[S.kz], Cy = C[S.ky] - S.Sy * C[S.kz];
+  float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
   }
-  double chord = 0.0, t_in = 0.0;
-  bool inside = false;
-  for (int a = 0; a < nh; ++a) {
-    if (sg[a] < 0 && !inside) { inside = true; t_in = t[a]; }
-    else if (sg[a] > 0 && inside) { inside = false; chord += (double)t[a] - t_in; }
-  }
-  return (float)chord;
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return NAN;
+  float det = U + V + W;
+  if (det == 0.0f) return NAN;
+  float Az = S.Sz * A[S.kz], Bz = S.Sz * B[S.kz], Cz = S.Sz * C[S.kz];
+  float T = U * Az + V * Bz + W * Cz;
+  return T / det;
 }
 
 /* intersect — mcramp/geom/mesh.cl:3-129 (brute force over all triangles).
- * With an SAttenuate scatter the chord time through the mesh
- * (chord_from_hits) is kept in the record's lane sd. */
-void g_mesh(float* n, float* s, uint32_t* iidx, const RampComp& k) {
+ * With an SAttenuate scatter the chord time through the mesh is kept in the
+ * record's lane sd: the sum over watertight crossings with t > eps of +t
+ * (leaving, n.v > 0) or -t (entering), i.e. the winding-number weighted time
+ * inside the surface, clamped at 0. */
+void g_mesh(const Ctx&, float* n, float* s, uint32_t* iidx, const RampComp& k) {
   const float* pts = k.table[0];
   const uint32_t num_tri = (uint32_t)(k.table_len[0] / 9);
   const int interior = k.gi[0];
@@ -521,9 +545,9 @@ void g_mesh(float* n, float* s, uint32_t* iidx, const RampComp& k) {
   const float eps = 0.000000001f;
   uint32_t num_intersections = 0;
   float out[8] = {0.0f, 0.0f, 0.0f, 1e8f, 0.0f, 0.0f, 0.0f, 1e8f};
-  float ht[MESH_MAX_HITS];
-  int hs[MESH_MAX_HITS];
-  int nh = 0;
+  const bool want_chord = (k.scat == RAMP_S_ATTENUATE);
+  Shear S = make_shear(vel);
+  double chord = 0.0;
   for (uint32_t i = 0; i < num_tri; ++i) {
     const float* p = pts + 9 * (size_t)i;
     V3 v0 = v3(p[0], p[1], p[2]), v1 = v3(p[3], p[4], p[5]), v2 = v3(p[6], p[7], p[8]);
@@ -550,8 +574,16 @@ void g_mesh(float* n, float* s, uint32_t* iidx, const RampComp& k) {
       V3 hp = add(pos, mulv(vel, t));
       out[4] = hp.x; out[5] = hp.y; out[6] = hp.z; out[7] = t;
     }
-    if (t > eps && nv != 0) {
-      if (nh < MESH_MAX_HITS) { ht[nh] = t; hs[nh] = nv > 0 ? 1 : -1; ++nh; }
+  }
+  if (want_chord) {
+    for (uint32_t i = 0; i < num_tri; ++i) {
+      const float* p = pts + 9 * (size_t)i;
+      V3 v0 = v3(p[0], p[1], p[2]), v1 = v3(p[3], p[4], p[5]), v2 = v3(p[6], p[7], p[8]);
+      float tw = watertight_t(S, pos, v0, v1, v2);
+      if (!(tw > eps)) continue;
+      float nv = dot(cross(sub(v1, v0), sub(v2, v0)), vel);
+      if (nv > 0) chord += (double)tw;
+      else if (nv < 0) chord -= (double)tw;
     }
   }
   if ((interior == 1) && (num_intersections % 2 == 1)) {
@@ -562,7 +594,7 @@ void g_mesh(float* n, float* s, uint32_t* iidx, const RampComp& k) {
   if (out[3] < s[3]) {
     for (int j = 0; j < 8; ++j) s[j] = out[j];
     *iidx = k.idx;
-    if (k.scat == RAMP_S_ATTENUATE) n[SD] = chord_from_hits(ht, hs, nh);
+    if (want_chord) n[SD] = chord > 0.0 ? (float)chord : 0.0f;
   }
 }
 
@@ -580,7 +612,7 @@ void intersect(const Ctx& c, const RampComp& k) {
       case RAMP_G_SPHERE_INT: g_sphere_int(n, s, c.iidx + i, k); break;
       case RAMP_G_BOX: g_box(n, s, c.iidx + i, k); break;
       case RAMP_G_ARM: g_arm(n, s, c.iidx + i, k); break;
-      case RAMP_G_MESH: g_mesh(n, s, c.iidx + i, k); break;
+      case RAMP_G_MESH: g_mesh(c, n, s, c.iidx + i, k); break;
       default: break;
     }
   }

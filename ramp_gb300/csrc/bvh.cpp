@@ -147,8 +147,8 @@ int ramp_bvh_build(const float* pts, int64_t n_tri, std::vector<float>& nodes,
     const float* p = pts + 9 * (size_t)B.order[i];
     float* o = &tris[12 * (size_t)i];
     o[0] = p[0]; o[1] = p[1]; o[2] = p[2];
-    o[4] = p[3] - p[0]; o[5] = p[4] - p[1]; o[6] = p[5] - p[2];
-    o[8] = p[6] - p[0]; o[9] = p[7] - p[1]; o[10] = p[8] - p[2];
+    o[4] = p[3]; o[5] = p[4]; o[6] = p[5];
+    o[8] = p[6]; o[9] = p[7]; o[10] = p[8];
   }
   return 0;
 }

@@ -163,13 +163,23 @@ DI float draw(Nt& n, Rng& r) {
 /* ------------------------------------------------------------------ */
 DI void raise_flag(StatusDev* st, unsigned int f) { atomicOr(&st->flags, f); }
 
-/* tally add with warp aggregation of lanes hitting the same bin */
+/* tally add with warp aggregation of lanes hitting the same bin of the
+ * same histogram (lanes of one warp can reach this code for different
+ * components of the same kind, so the histogram address is part of the
+ * match key) */
+/* Float atomic addition on the GPU (red/atom.add.f32) flushes subnormal
+ * operands to zero; terms are flushed here before any aggregation so that
+ * a tally is the FTZ sum of its terms whatever the grouping (the oracle
+ * flushes the same way). */
+DI float ftz(float x) { return fabsf(x) < 1.17549435e-38f ? copysignf(0.0f, x) : x; }
+
 DI void tally_add(float* h, float* he, long long idx, float p) {
   unsigned m = __activemask();
-  unsigned peers = __match_any_sync(m, idx);
+  unsigned peers = __match_any_sync(m, idx) & __match_any_sync(m, (unsigned long long)h);
   int lane = threadIdx.x & 31;
   int leader = __ffs(peers) - 1;
-  float s = p, s2 = p * p;
+  p = ftz(p);
+  float s = p, s2 = ftz(p * p);
   if (__popc(peers) > 1) {
     float a = 0.0f, a2 = 0.0f;
     unsigned rest = peers;
@@ -178,7 +188,7 @@ DI void tally_add(float* h, float* he, long long idx, float p) {
       rest &= rest - 1;
       float q = __shfl_sync(peers, p, src);
       a += q;
-      a2 += q * q;
+      a2 += ftz(q * q);
     }
     s = a; s2 = a2;
   }

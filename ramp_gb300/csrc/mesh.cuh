@@ -2,45 +2,65 @@
  * mesh.cuh — GMesh intersection (mcramp/geom/mesh.cl:3-129) through a
  * bounding volume hierarchy.
  *
- * The reference tests every triangle for every ray.  Its result does not
- * depend on the order in which triangles are visited: the entering and
- * exiting records keep the smallest t (ties give identical records, the
- * point being pos + vel*t), the crossing count is a sum, and the chord
- * (for SAttenuate) is built from the sorted crossings.  So a traversal that
- * reaches every triangle the ray can hit returns the reference's record.
- * For SAttenuate the crossings (t, sign)
- * are collected, sorted, and each entry is paired with the next exit
- * (repeated entries or exits, which a ray through an edge shared by two
- * faces can produce, are ignored); the ray is taken to start outside.
- * Node boxes are inflated at build time
- * so that float rounding in the slab test never culls a triangle that the
- * Moller-Trumbore test accepts; without interior parity or chord sums,
- * nodes that start beyond both current records are pruned.
+ * The reference tests every triangle for every ray (Moller-Trumbore).  Its
+ * record does not depend on the order in which triangles are visited: the
+ * entering and exiting hits keep the smallest t (ties give identical
+ * records, the point being pos + vel*t) and the crossing count is a sum.
+ * So a traversal that reaches every triangle the ray can hit returns the
+ * reference's record.  Node boxes are inflated at build time so that float
+ * rounding in the slab test never culls a triangle the exact test accepts;
+ * without interior parity or a chord, nodes that start beyond both current
+ * records are pruned.
+ *
+ * For SAttenuate the chord is the sum over watertight crossings (Woop,
+ * Benthin, Wald, JCGT 2013) of +t leaving / -t entering, accumulated in
+ * double: exact for the few dozen crossings of one ray, so independent of
+ * the visiting order; clamped at 0.
  *
  * Node layout: 2 float4 per node, (min.xyz, a) (max.xyz, b); b >= 0: inner
  * node with children a and b; b < 0: leaf with triangles [a, a - b).
- * Triangle layout: 3 float4, v0, e1 = v1 - v0, e2 = v2 - v0 (host float
- * subtraction, the same values the reference computes per test).
+ * Triangle layout: 3 float4, the vertices v0, v1, v2; edges are formed as
+ * the reference forms them (v1 - v0, v2 - v0 in float).
  */
 #ifndef RAMP_MESH_CUH
 #define RAMP_MESH_CUH
 
 #define RAMP_BVH_STACK 64
-#define RAMP_MESH_MAX_HITS 16
 
-DI float chord_from_hits(float* t, int* sg, int nh) {
-  for (int a = 1; a < nh; ++a) {
-    float tv = t[a]; int sv = sg[a]; int b = a - 1;
-    while (b >= 0 && (t[b] > tv || (t[b] == tv && sg[b] > sv))) { t[b + 1] = t[b]; sg[b + 1] = sg[b]; --b; }
-    t[b + 1] = tv; sg[b + 1] = sv;
+struct Shear { int kx, ky, kz; float Sx, Sy, Sz; };
+
+DI float comp3(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+DI Shear make_shear(V3 d) {
+  float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  Shear S;
+  S.kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+  S.kx = (S.kz + 1) % 3; S.ky = (S.kx + 1) % 3;
+  if (comp3(d, S.kz) < 0.0f) { int t = S.kx; S.kx = S.ky; S.ky = t; }
+  S.Sx = comp3(d, S.kx) / comp3(d, S.kz);
+  S.Sy = comp3(d, S.ky) / comp3(d, S.kz);
+  S.Sz = 1.0f / comp3(d, S.kz);
+  return S;
+}
+
+/* watertight crossing parameter t, NaN when the ray misses the face */
+DI float watertight_t(const Shear& S, V3 org, V3 v0, V3 v1, V3 v2) {
+  V3 A = sub(v0, org), B = sub(v1, org), C = sub(v2, org);
+  float Akz = comp3(A, S.kz), Bkz = comp3(B, S.kz), Ckz = comp3(C, S.kz);
+  float Ax = comp3(A, S.kx) - S.Sx * Akz, Ay = comp3(A, S.ky) - S.Sy * Akz;
+  float Bx = comp3(B, S.kx) - S.Sx * Bkz, By = comp3(B, S.ky) - S.Sy * Bkz;
+  float Cx = comp3(C, S.kx) - S.Sx * Ckz, Cy = comp3(C, S.ky) - S.Sy * Ckz;
+  float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
   }
-  double chord = 0.0, t_in = 0.0;
-  bool inside = false;
-  for (int a = 0; a < nh; ++a) {
-    if (sg[a] < 0 && !inside) { inside = true; t_in = t[a]; }
-    else if (sg[a] > 0 && inside) { inside = false; chord += (double)t[a] - t_in; }
-  }
-  return (float)chord;
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return __int_as_float(0x7fc00000);
+  float det = U + V + W;
+  if (det == 0.0f) return __int_as_float(0x7fc00000);
+  float T = U * (S.Sz * Akz) + V * (S.Sz * Bkz) + W * (S.Sz * Ckz);
+  return T / det;
 }
 
 DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
@@ -59,9 +79,9 @@ DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
   uint32_t num_intersections = 0;
   float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, o3 = 1e8f, o4 = 0.0f, o5 = 0.0f, o6 = 0.0f, o7 = 1e8f;
   const bool want_chord = (c.scat == RAMP_S_ATTENUATE);
-  float ht[RAMP_MESH_MAX_HITS];
-  int hs[RAMP_MESH_MAX_HITS];
-  int nh = 0;
+  Shear S;
+  if (want_chord) S = make_shear(vel);
+  double chord = 0.0;
   const float ix = 1.0f / vel.x, iy = 1.0f / vel.y, iz = 1.0f / vel.z;
   const float4* __restrict__ nodes = c.bvh_nodes;
   const float4* __restrict__ tris = c.bvh_tris;
@@ -87,7 +107,16 @@ DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
     }
     for (int k = wa; k < wa - wb; ++k) {
       float4 q0 = __ldg(tris + 3 * k), q1 = __ldg(tris + 3 * k + 1), q2 = __ldg(tris + 3 * k + 2);
-      V3 v0 = v3(q0.x, q0.y, q0.z), e1 = v3(q1.x, q1.y, q1.z), e2 = v3(q2.x, q2.y, q2.z);
+      V3 v0 = v3(q0.x, q0.y, q0.z), v1 = v3(q1.x, q1.y, q1.z), v2 = v3(q2.x, q2.y, q2.z);
+      V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+      if (want_chord) {
+        float tw = watertight_t(S, pos, v0, v1, v2);
+        if (tw > eps) {
+          float nvw = dot(cross(e1, e2), vel);
+          if (nvw > 0) chord += (double)tw;
+          else if (nvw < 0) chord -= (double)tw;
+        }
+      }
       V3 h = cross(vel, e2);
       float aa = dot(e1, h);
       if (fabsf(aa) < eps) continue;
@@ -108,10 +137,6 @@ DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
       if ((t > eps) && (t < o7) && (nv > 0)) {
         o4 = pos.x + vel.x * t; o5 = pos.y + vel.y * t; o6 = pos.z + vel.z * t; o7 = t;
       }
-      if (want_chord && t > eps && nv != 0) {
-        if (nh < RAMP_MESH_MAX_HITS) { ht[nh] = t; hs[nh] = nv > 0 ? 1 : -1; ++nh; }
-        else raise_flag(st, RAMP_F_BVH_STACK);
-      }
     }
   }
   if ((c.gi[0] == 1) && (num_intersections % 2 == 1)) {
@@ -122,7 +147,7 @@ DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
   if (o3 < s.t1) {
     s.x1 = o0; s.y1 = o1; s.z1 = o2; s.t1 = o3;
     s.x2 = o4; s.y2 = o5; s.z2 = o6; s.t2 = o7;
-    if (want_chord) { n.sd = chord_from_hits(ht, hs, nh); n.wr |= WR_SD; }
+    if (want_chord) { n.sd = chord > 0.0 ? (float)chord : 0.0f; n.wr |= WR_SD; }
     return true;
   }
   return false;
