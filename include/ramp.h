@@ -243,6 +243,22 @@ int ramp_trace_batched(RampPlan* plan, const RampVariant* variants,
                        int n_variants, const RampRng* rng,
                        const RampTune* tune, void* stream);
 
+/* ramp_trace_batched without device allocation.  No counterpart in the
+ * reference.  For callers that may not allocate device memory while
+ * tracing (a fixed memory budget, an external pool that forbids
+ * allocation): the descriptor, variant and task tables and the status and
+ * work counters of the batched kernel live in one fixed file-scope device
+ * array (at most 256 variants, 4096 component descriptors and 65536 tasks,
+ * about 3.3 MB per GPU, held until exit) instead of plan-owned buffers.
+ * Every variant's tables must already be held by the plan.  The first call
+ * on a device resolves the array's address; make it before any stream
+ * capture.  Calls share the array, so calls whose kernels overlap on the
+ * GPU race; order them on one stream.  Sizes beyond the maximum return
+ * RAMP_E_RANGE.                                                           */
+int ramp_trace_batched_noalloc(RampPlan* plan, const RampVariant* variants,
+                               int n_variants, const RampRng* rng,
+                               const RampTune* tune, void* stream);
+
 /* Debug/test entry points: evaluate the device RNG and math on a vector
  * of inputs (used by the parity tests, not by the chain).                 */
 int ramp_debug_threefry(const uint32_t* ctr0_dev, const uint32_t* tid_dev,

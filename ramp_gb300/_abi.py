@@ -111,6 +111,9 @@ _SIGS = {
     "ramp_trace_batched": ([ctypes.c_void_p, ctypes.POINTER(RampVariant), ctypes.c_int,
                             ctypes.POINTER(RampRng), ctypes.POINTER(RampTune),
                             ctypes.c_void_p], ctypes.c_int),
+    "ramp_trace_batched_noalloc": ([ctypes.c_void_p, ctypes.POINTER(RampVariant), ctypes.c_int,
+                                    ctypes.POINTER(RampRng), ctypes.POINTER(RampTune),
+                                    ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_threefry": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_math": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -558,3 +559,205 @@ int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out, void* s
 }
 
 }  // extern "C"
+
+/* ======================================================================
+ * ramp_trace_batched_noalloc — the batched fused path for callers that
+ * must not allocate device memory while they trace (for example a host
+ * loop that runs under a strict device-memory budget or an external
+ * memory pool that forbids allocation, or a caller preparing work it will
+ * later record into a CUDA graph): it uses only memory that already exists.
+ *
+ * The per-call scratch of the batched kernel (the device copies of every
+ * variant's component descriptors, the variant table, the task list, and
+ * the status / work-queue counters) lives in the file-scope array below
+ * instead of plan-owned buffers that grow with cudaMalloc.  Its size is
+ * fixed: RAMP_NOALLOC_MAX_VARIANTS variants, RAMP_NOALLOC_MAX_DESCS
+ * component descriptors in total (variants x components) and
+ * RAMP_NOALLOC_MAX_TASKS tasks, about 3.3 MB, held by every GPU on which
+ * the library is loaded until the process exits.  Tables (S(q,w), powder
+ * lines, mesh BVHs) must be ones the plan already holds: a variant whose
+ * tables differ from every table the plan uploaded is rejected.
+ *
+ * The first call on a device looks up the device address of the array
+ * (cudaGetSymbolAddress, with that device current) and caches it; make that
+ * first call before any stream capture.  All calls share the array, which
+ * keeps the previous call's contents: each call overwrites the descriptors
+ * and clears the counters before its launch, so two calls whose kernels
+ * overlap on the GPU (different streams, no ordering) race and give wrong
+ * results; order such calls on one stream.
+ * ==================================================================== */
+#define RAMP_NOALLOC_MAX_VARIANTS 256
+#define RAMP_NOALLOC_MAX_DESCS 4096
+#define RAMP_NOALLOC_MAX_TASKS 65536
+
+struct NoallocLayout {
+  StatusDev status;
+  unsigned char pad[256 - sizeof(StatusDev)];
+  VariantDev variants[RAMP_NOALLOC_MAX_VARIANTS];
+  CompDev descs[RAMP_NOALLOC_MAX_DESCS];
+  TaskDev tasks[RAMP_NOALLOC_MAX_TASKS];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoallocLayout)];
+
+#define RAMP_NOALLOC_MAX_DEVICES 64
+static NoallocLayout* g_noalloc_dev[RAMP_NOALLOC_MAX_DEVICES];
+/* host staging of the descriptor, variant and task tables (pageable copies
+ * complete before cudaMemcpyAsync returns, so one buffer serves all calls) */
+static NoallocLayout g_noalloc_host;
+static std::mutex g_noalloc_mutex;
+
+/* table lookup that never uploads */
+static int lookup_table(RampPlan* p, const float* host, int64_t len, const float** dev) {
+  static const float zero = 0.0f;
+  if (len <= 0 || !host) { host = &zero; len = 1; }
+  TabKey key(0, len, fnv1a(host, (size_t)len * sizeof(float)));
+  auto it = p->tabs.find(key);
+  if (it == p->tabs.end()) return RAMP_E_INVALID;
+  *dev = (const float*)it->second.first;
+  return RAMP_OK;
+}
+
+static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d) {
+  memset(&d, 0, sizeof(d));
+  d.geom = c.geom; d.scat = c.scat; d.idx = c.idx; d.restore = c.restore;
+  memcpy(d.pos, c.pos, sizeof(d.pos));
+  rot_matrix(c.rot, d.R);
+  d.rotated = (c.rot[0] != 0.0f || c.rot[1] != 0.0f || c.rot[2] != 0.0f);
+  memcpy(d.gp, c.gp, sizeof(d.gp));
+  memcpy(d.sp, c.sp, sizeof(d.sp));
+  memcpy(d.gi, c.gi, sizeof(d.gi));
+  memcpy(d.si, c.si, sizeof(d.si));
+  for (int k = 0; k < RAMP_NTAB; ++k) {
+    d.tab_len[k] = c.table_len[k];
+    if (c.geom == RAMP_G_MESH && k == 0) continue;
+    if (lookup_table(p, c.table[k], c.table_len[k], &d.tab[k])) {
+      set_err("ramp_trace_batched_noalloc: table %d of a variant component is not held by "
+              "the plan (create the plan from a variant with the same tables)", k);
+      return RAMP_E_INVALID;
+    }
+  }
+  d.tally = c.tally;
+  d.tally_err = c.tally_err;
+  d.tally_len = c.tally_len;
+  if (c.geom == RAMP_G_MESH) {
+    TabKey key(1, c.table_len[0], fnv1a(c.table[0], (size_t)c.table_len[0] * sizeof(float)));
+    auto it = p->tabs.find(key);
+    if (it == p->tabs.end()) {
+      set_err("ramp_trace_batched_noalloc: mesh of a variant is not held by the plan");
+      return RAMP_E_INVALID;
+    }
+    d.bvh_nodes = (const float4*)it->second.first;
+    d.bvh_tris = (const float4*)it->second.second;
+  }
+  return RAMP_OK;
+}
+
+extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* variants, int n_variants,
+                                          const RampRng* rng, const RampTune* tune, void* stream) {
+  if (!p || !variants || n_variants <= 0) {
+    set_err("ramp_trace_batched_noalloc: bad arguments");
+    return RAMP_E_INVALID;
+  }
+  const int nc = (int)p->comps.size();
+  if (nc > RAMP_MAX_COMPS) {
+    set_err("ramp_trace_batched_noalloc: at most %d components", RAMP_MAX_COMPS);
+    return RAMP_E_RANGE;
+  }
+  if (n_variants > RAMP_NOALLOC_MAX_VARIANTS || (int64_t)n_variants * nc > RAMP_NOALLOC_MAX_DESCS) {
+    set_err("ramp_trace_batched_noalloc: %d variants x %d components exceed the fixed scratch "
+            "(at most %d variants and %d descriptors)", n_variants, nc,
+            RAMP_NOALLOC_MAX_VARIANTS, RAMP_NOALLOC_MAX_DESCS);
+    return RAMP_E_RANGE;
+  }
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= RAMP_NOALLOC_MAX_DEVICES) {
+    set_err("ramp_trace_batched_noalloc: device %d beyond %d", dev, RAMP_NOALLOC_MAX_DEVICES);
+    return RAMP_E_RANGE;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_dev[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) {
+      set_err("ramp_trace_batched_noalloc: cudaGetSymbolAddress failed: %s",
+              cudaGetErrorString(e));
+      return RAMP_E_CUDA;
+    }
+    g_noalloc_dev[dev] = (NoallocLayout*)ptr;
+  }
+  NoallocLayout* D = g_noalloc_dev[dev];
+  NoallocLayout& H = g_noalloc_host;
+  int block, grid;
+  int64_t task;
+  tune_defaults(p, tune, block, grid, task);
+  /* tasks: grow the task size until the list fits the fixed table */
+  int64_t n_tasks = 0;
+  for (;;) {
+    n_tasks = 0;
+    for (int v = 0; v < n_variants; ++v) n_tasks += (variants[v].n + task - 1) / task;
+    if (n_tasks <= RAMP_NOALLOC_MAX_TASKS) break;
+    task *= 2;
+    if (task > (int64_t)1 << 30) {
+      set_err("ramp_trace_batched_noalloc: too many histories for the task table");
+      return RAMP_E_RANGE;
+    }
+  }
+  int64_t t = 0;
+  for (int v = 0; v < n_variants; ++v) {
+    const RampVariant& V = variants[v];
+    if (!V.comps || V.n < 0) {
+      set_err("ramp_trace_batched_noalloc: variant %d: missing components", v);
+      return RAMP_E_INVALID;
+    }
+    for (int j = 0; j < nc; ++j) {
+      const RampComp& c = V.comps[j];
+      if (c.geom != p->comps_in[j].geom || c.scat != p->comps_in[j].scat) {
+        set_err("ramp_trace_batched_noalloc: variant %d component %d: kinds differ from the "
+                "plan", v, j);
+        return RAMP_E_INVALID;
+      }
+      int rc = validate_comp(c, j);
+      if (!rc) rc = lookup_comp(p, c, H.descs[(size_t)v * nc + j]);
+      if (rc) return rc;
+    }
+    int rc = make_src(V.source, H.variants[v].src);
+    if (rc) return rc;
+    H.variants[v].n = V.n;
+    H.variants[v].num_sim = V.num_sim;
+    H.variants[v].seed = V.seed;
+    H.variants[v].comps = D->descs + (size_t)v * nc;
+    for (int64_t s0 = 0; s0 < V.n; s0 += task) {
+      H.tasks[t].variant = v;
+      H.tasks[t].start = s0;
+      H.tasks[t].count = (int32_t)((V.n - s0) < task ? (V.n - s0) : task);
+      ++t;
+    }
+  }
+  if (n_tasks == 0) return RAMP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaMemcpyAsync(D->descs, H.descs, (size_t)n_variants * nc * sizeof(CompDev),
+                     cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(D->variants, H.variants, (size_t)n_variants * sizeof(VariantDev),
+                     cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(D->tasks, H.tasks, (size_t)n_tasks * sizeof(TaskDev),
+                     cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(&D->status, 0, sizeof(StatusDev), s));
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.variants = D->variants;
+  a.tasks = D->tasks;
+  a.n_tasks = n_tasks;
+  a.task_size = task;
+  a.blocks = p->blocks_dev;
+  a.n_blocks = (int32_t)p->blocks.size();
+  a.n_comps = nc;
+  a.rng.mode = rng ? rng->mode : 1;
+  a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.tid_base = 0u;
+  a.st = &D->status;
+  int64_t g = n_tasks < grid ? n_tasks : grid;
+  CK(launch_fused(a, block, (int)g, s));
+  return RAMP_OK;
+}
