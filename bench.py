@@ -53,6 +53,7 @@ def args_():
     p.add_argument("--n", type=int, default=N_HIST)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--tune", default=None, help='fused launch config, e.g. {"blocks_per_sm": 3}')
     return p.parse_args()
 
 
@@ -179,10 +180,13 @@ def main():
 
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
 
+    tune = json.loads(a.tune) if a.tune else None
+
     def timed(inst, path, steps, warmup):
         for w in range(warmup):
             random.seed(10 + w)
-            inst.execute(n * world if shard else n, path=path, shard=shard)
+            inst.execute(n * world if shard else n, path=path, shard=shard,
+                         tune=tune if path == "fused" else None)
         barrier()
         torch.cuda.synchronize()
         ms = []
@@ -191,7 +195,8 @@ def main():
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             random.seed(1000 + k)
             s.record()
-            inst.execute(n * world if shard else n, path=path, shard=shard)
+            inst.execute(n * world if shard else n, path=path, shard=shard,
+                         tune=tune if path == "fused" else None)
             e.record()
             e.synchronize()
             ms.append(s.elapsed_time(e))
@@ -229,9 +234,11 @@ def main():
         random.seed(1000 + len(plain_ms) - 1)
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         rngd = _abi.RampRng()
+        tuned = _abi.RampTune(*[int((tune or {}).get(k, 0)) for k in
+                                ("block", "blocks_per_sm", "chunk", "privatize")])
         s.record(stream)
         rc = lib.ramp_trace_fused(inst.plan(), plain.last_chunk, plain.last_chunk, seed_last,
-                                  _abi.ctypes.byref(rngd), None, None, None,
+                                  _abi.ctypes.byref(rngd), None, None, _abi.ctypes.byref(tuned),
                                   _abi.ctypes.c_void_p(stream.cuda_stream))
         e.record(stream)
         e.synchronize()
@@ -290,7 +297,7 @@ def main():
         "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": fused_total_ms / a.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(n, world),
+        "config": dict(workload_config(n, world), tune=tune),
         "plain_path": {"value": plain_value, "unit": "histories/s",
                        "ms_per_step": plain_total_ms / len(plain_ms)},
         "fused_over_plain": value / plain_value,

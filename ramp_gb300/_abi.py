@@ -85,7 +85,8 @@ def set_table(comp, slot, arr, keep):
 # library loading
 # --------------------------------------------------------------------------
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_build", "libramp_cuda.so")
+# RAMP_CUDA_LIB selects another build of the library (e.g. an experimental one)
+LIB_PATH = os.environ.get("RAMP_CUDA_LIB") or os.path.join(_HERE, "_build", "libramp_cuda.so")
 _lib = None
 
 _SIGS = {

@@ -98,6 +98,44 @@ static float maxwell_h(float E, float T) {
   return 2.0f * rootE / sqrtf(RC_PI) * (overKT * sqrtf(overKT)) * rm_expf(-E * overKT);
 }
 
+/* Guide constants that guide.cl:39-43 and ref.h:7-31 recompute for every
+ * neutron and bounce, evaluated once with the same float operations:
+ * aux[0] ww, [1] hh, [2] (-whalf)*l, [3] (-hhalf)*l, [4] l*l + ww*ww,
+ * [5] sqrt of [4], [6] l*l + hh*hh, [7] sqrt of [6]; reflectivity after the
+ * m-parametrisation: [8] m, [9] W, [10] alpha, [11] beta, [12] m*Qc,
+ * [13] Qc after the m < 1 rescaling, [14] R0*0.5, [15] 1 if R = 0 always. */
+static void guide_aux(const RampComp& c, float* aux) {
+  const float w1 = c.sp[0], h1 = c.sp[1], w2 = c.sp[2], h2 = c.sp[3], l = c.sp[4];
+  const float R0 = c.sp[5], Qc = c.sp[6];
+  float alpha = c.sp[7], m = c.sp[8], W = c.sp[9];
+  float ww = 0.5f * (w2 - w1), hh = 0.5f * (h2 - h1);
+  float whalf = 0.5f * w1, hhalf = 0.5f * h1;
+  aux[0] = ww;
+  aux[1] = hh;
+  aux[2] = -whalf * l;
+  aux[3] = -hhalf * l;
+  aux[4] = l * l + ww * ww;
+  aux[5] = sqrtf(aux[4]);
+  aux[6] = l * l + hh * hh;
+  aux[7] = sqrtf(aux[6]);
+  float beta = 0.0f;
+  if (W == 0.0f && alpha == 0.0f) {
+    m = m * 0.9853f + 0.1978f;
+    W = -0.0002f * m + 0.0022f;
+    alpha = 0.2304f * m + 5.0944f;
+    beta = -7.6251f * m + 68.1137f;
+    if (m <= 3) { alpha = m; beta = 0; }
+  }
+  aux[8] = m;
+  aux[9] = W;
+  aux[10] = alpha;
+  aux[11] = beta;
+  aux[12] = m * Qc;
+  aux[13] = (m < 1) ? Qc * m : Qc;
+  aux[14] = R0 * 0.5f;
+  aux[15] = (m <= 0 || Qc <= 0 || R0 <= 0) ? 1.0f : 0.0f;
+}
+
 static int make_src(const RampSource& s, SrcDev& d) {
   if (s.kind != RAMP_SRC_FLAT && s.kind != RAMP_SRC_CONT) {
     set_err("unknown source kind %d", s.kind);
@@ -226,6 +264,7 @@ static int make_comp(RampPlan* p, const RampComp& c, CompDev& d) {
   memcpy(d.sp, c.sp, sizeof(d.sp));
   memcpy(d.gi, c.gi, sizeof(d.gi));
   memcpy(d.si, c.si, sizeof(d.si));
+  if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;   /* the BVH replaces the raw points */
@@ -378,14 +417,31 @@ int ramp_trace_plain(RampPlan* p, const RampState* st, int64_t n, int32_t num_si
   return RAMP_OK;
 }
 
+/* persistent grid for the fused kernel: one CTA per span at most */
+static int fused_grid(int64_t n_spans, int grid) {
+  int64_t need = n_spans < 1 ? 1 : n_spans;
+  return (int)(need < grid ? need : grid);
+}
+
 static void tune_defaults(RampPlan* p, const RampTune* tune, int& block, int& grid,
                           int64_t& task) {
-  block = (tune && tune->block > 0) ? tune->block : 256;
-  if (block % 32 || block > 1024) block = 256;
+  block = 256;   /* the fused kernel is compiled for 256-thread CTAs */
+  fused_set_min_blocks((tune && tune->blocks_per_sm > 0) ? tune->blocks_per_sm : 3);
   int bps = (tune && tune->blocks_per_sm > 0) ? tune->blocks_per_sm
                                               : fused_max_blocks_per_sm(block, (int)p->comps.size());
   grid = p->sm_count * bps;
-  task = (tune && tune->chunk > 0) ? tune->chunk : (int64_t)block * 8;
+  task = (tune && tune->chunk > 0) ? tune->chunk : 0;   /* 0: auto_task() */
+}
+
+/* span size for n histories: about eight spans per resident CTA, in
+ * multiples of 1024 neutrons, between 1024 and 65536 */
+static int64_t auto_task(int64_t n, int grid, int64_t task) {
+  if (task > 0) return task;
+  int64_t t = n / ((int64_t)grid * 8);
+  t = (t + 1023) / 1024 * 1024;
+  if (t < 1024) t = 1024;
+  if (t > 65536) t = 65536;
+  return t;
 }
 
 int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, const RampRng* rng,
@@ -404,6 +460,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   int block, grid;
   int64_t task;
   tune_defaults(p, tune, block, grid, task);
+  task = auto_task(n, grid, task);
   FusedArgs a;
   memset(&a, 0, sizeof(a));
   a.variants = nullptr;
@@ -424,9 +481,8 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.carry_sb = sb_carry;
   a.carry_iidx = iidx_carry;
   a.st = p->status;
-  int64_t g = a.n_tasks < grid ? a.n_tasks : grid;
   CK(cudaMemsetAsync(&p->status->workq, 0, sizeof(unsigned long long), s));
-  CK(launch_fused(a, block, (int)g, s));
+  CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
   return RAMP_OK;
 }
 
@@ -445,6 +501,11 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   int block, grid;
   int64_t task;
   tune_defaults(p, tune, block, grid, task);
+  {
+    int64_t total = 0;
+    for (int v = 0; v < n_variants; ++v) total += variants[v].n > 0 ? variants[v].n : 0;
+    task = auto_task(total, grid, task);
+  }
   BatchCache& B = p->batch;
   /* descriptors: re-upload only when they change */
   std::vector<CompDev> comps((size_t)n_variants * nc);
@@ -532,9 +593,8 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;   /* variants key by their own index */
   a.st = p->status;
-  int64_t g = a.n_tasks < grid ? a.n_tasks : grid;
   CK(cudaMemsetAsync(&p->status->workq, 0, sizeof(unsigned long long), s));
-  CK(launch_fused(a, block, (int)g, s));
+  CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
   return RAMP_OK;
 }
 
@@ -628,6 +688,7 @@ static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d) {
   memcpy(d.sp, c.sp, sizeof(d.sp));
   memcpy(d.gi, c.gi, sizeof(d.gi));
   memcpy(d.si, c.si, sizeof(d.si));
+  if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;
@@ -692,6 +753,11 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   int block, grid;
   int64_t task;
   tune_defaults(p, tune, block, grid, task);
+  {
+    int64_t total = 0;
+    for (int v = 0; v < n_variants; ++v) total += variants[v].n > 0 ? variants[v].n : 0;
+    task = auto_task(total, grid, task);
+  }
   /* tasks: grow the task size until the list fits the fixed table */
   int64_t n_tasks = 0;
   for (;;) {
@@ -757,7 +823,6 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;
   a.st = &D->status;
-  int64_t g = n_tasks < grid ? n_tasks : grid;
-  CK(launch_fused(a, block, (int)g, s));
+  CK(launch_fused(a, block, fused_grid(n_tasks, grid), s));
   return RAMP_OK;
 }

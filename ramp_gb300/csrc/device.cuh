@@ -455,15 +455,24 @@ DI void s_finish(const CompDev& c, Nt& n, Is& s, uint32_t& ii) {
   is_reset(s);
 }
 
+/* reflectivity_func (ref.h:3-53) with the per-guide constants of
+ * guide_aux: the same operations on the same values as reflectivity() */
+DI float reflectivity_pre(float q, const float* aux, float R0) {
+  const float W = aux[9];
+  float arg = W > 0 ? (q - aux[12]) / W : 11;
+  if (arg > 10 || aux[15] != 0.0f) return 0.0f;
+  const float Qc = aux[13];
+  if (q <= Qc) return R0;
+  return aux[14] * (1 - rm_tanhf(arg)) * (1 - aux[10] * (q - Qc) + aux[11] * (q - Qc) * (q - Qc));
+}
+
 /* guide.cl:9-149 */
 DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
-  const float w1 = c.sp[0], h1 = c.sp[1], w2 = c.sp[2], h2 = c.sp[3], l = c.sp[4];
-  const float R0 = c.sp[5], Qc = c.sp[6], alpha = c.sp[7], m = c.sp[8], W = c.sp[9];
+  const float l = c.sp[4], R0 = c.sp[5];
   const uint32_t max_bounces = (uint32_t)c.si[0];
+  const float ww = c.aux[0], hh = c.aux[1], Av = c.aux[2], Ah = c.aux[3];
   set_pos(n, ip2(s));
   n.t += s.t2;
-  const float ww = 0.5f * (w2 - w1), hh = 0.5f * (h2 - h1);
-  const float whalf = 0.5f * w1, hhalf = 0.5f * h1;
   uint32_t i = 0;
   int guard = 0;
   while (i < max_bounces) {
@@ -474,8 +483,8 @@ DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
     }
     float av = l * n.vx, bv = ww * n.vz, ah = l * n.vy, bh = hh * n.vz;
     float vdotn_v1 = bv + av, vdotn_v2 = bv - av, vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
-    float cv1 = -whalf * l - n.z * ww, cv2 = n.x * l;
-    float ch1 = -hhalf * l - n.z * hh, ch2 = n.y * l;
+    float cv1 = Av - n.z * ww, cv2 = n.x * l;
+    float ch1 = Ah - n.z * hh, ch2 = n.y * l;
     float t1 = (l - n.z) / n.vz, t2;
     i = 0;
     if (vdotn_v1 < 0.0f && (t2 = (cv1 - cv2) / vdotn_v1) < t1) { t1 = t2; i = 1; }
@@ -485,19 +494,19 @@ DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
     if (i == 0) break;
     n.x = n.x + t1 * n.vx; n.y = n.y + t1 * n.vy; n.z = n.z + t1 * n.vz;
     n.t += t1;
-    float nlen2, q, d, vdn;
-    bool vert = (i <= 2);
-    float wv = vert ? ww : hh;
-    vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1 : vdotn_h2;
-    nlen2 = l * l + wv * wv;
-    q = RC_V2K * (-2.0f) * vdn / sqrtf(nlen2);
-    d = 2.0f * vdn / nlen2;
+    const bool vert = (i <= 2);
+    const float wv = vert ? ww : hh;
+    const float nlen2 = vert ? c.aux[4] : c.aux[6];
+    const float snlen = vert ? c.aux[5] : c.aux[7];
+    const float vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1 : vdotn_h2;
+    const float q = RC_V2K * (-2.0f) * vdn / snlen;
+    const float d = 2.0f * vdn / nlen2;
     if (i == 1) n.vx = n.vx - d * l;
     else if (i == 2) n.vx = n.vx + d * l;
     else if (i == 3) n.vy = n.vy - d * l;
     else n.vy = n.vy + d * l;
     n.vz = n.vz - d * wv;
-    float refl = reflectivity(q, R0, Qc, alpha, m, W);
+    float refl = reflectivity_pre(q, c.aux, R0);
     n.p *= refl;
     if (refl < 1e-12f || refl > 1.0f) n.p = 0.0f;
     i++;

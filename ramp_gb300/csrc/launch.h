@@ -40,6 +40,7 @@ struct FusedArgs {
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s);
 int fused_max_blocks_per_sm(int block, int n_comps);
+void fused_set_min_blocks(int minb);
 
 cudaError_t launch_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out,
                                   int64_t n, cudaStream_t s);

@@ -62,6 +62,7 @@ DI void comp_linear_k(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* 
   if (!(n.die > 0.f)) untransform(c, n);
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(PLAIN_BLOCK)
 k_generate(const __grid_constant__ SrcDev src, const PlainArgs a, int32_t num_sim, int32_t seed) {
   const int64_t st = a.stride;
@@ -71,13 +72,13 @@ k_generate(const __grid_constant__ SrcDev src, const PlainArgs a, int32_t num_si
     float old_sb = S[RAMP_MC * st + i];
     Nt n;
     Rng r;
-    rng_init(r, a.rng.mode, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
     generate(src, n, old_sb, num_sim, seed, r);
     STORE_ALL(n, S, st, i);
   }
 }
 
-template <int SK>
+template <int SK, int MODE>
 __global__ void __launch_bounds__(PLAIN_BLOCK)
 k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
   constexpr bool RD_P = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
@@ -110,7 +111,7 @@ k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
     const uint32_t ii0 = a.iidx[i];
     uint32_t ii = ii0;
     Rng r;
-    rng_init(r, a.rng.mode, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
     comp_linear_k<SK>(c, n, ii, r, a.st);
     S[RAMP_X * st + i] = n.x; S[RAMP_Y * st + i] = n.y; S[RAMP_Z * st + i] = n.z;
     if (MOD_VEL || c.rotated) {
@@ -158,7 +159,8 @@ static int plain_grid(int64_t n) {
 cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_sim, int32_t seed,
                             cudaStream_t s) {
   if (a.n <= 0) return cudaSuccess;
-  k_generate<<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(src, a, num_sim, seed);
+  if (a.rng.mode == 0) k_generate<0><<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(src, a, num_sim, seed);
+  else k_generate<1><<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(src, a, num_sim, seed);
   return cudaGetLastError();
 }
 
@@ -166,11 +168,18 @@ cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_
   if (a.n <= 0) return cudaSuccess;
   int g = plain_grid(a.n);
   switch (c.scat) {
-#define CASE(K) case K: k_linear<K><<<g, PLAIN_BLOCK, 0, s>>>(c, a); break;
-    CASE(RAMP_S_ARM) CASE(RAMP_S_GUIDE) CASE(RAMP_S_CHOPPER) CASE(RAMP_S_ISOTROPIC)
-    CASE(RAMP_S_POWDERN) CASE(RAMP_S_DET1D) CASE(RAMP_S_DET2D) CASE(RAMP_S_COUNTER)
+/* kinds that draw random numbers get one instantiation per keying mode */
+#define CASE(K) case K: k_linear<K, 0><<<g, PLAIN_BLOCK, 0, s>>>(c, a); break;
+#define CASE2(K)                                                        \
+  case K:                                                               \
+    if (a.rng.mode == 0) k_linear<K, 0><<<g, PLAIN_BLOCK, 0, s>>>(c, a); \
+    else k_linear<K, 1><<<g, PLAIN_BLOCK, 0, s>>>(c, a);                \
+    break;
+    CASE(RAMP_S_ARM) CASE(RAMP_S_GUIDE) CASE2(RAMP_S_CHOPPER) CASE2(RAMP_S_ISOTROPIC)
+    CASE2(RAMP_S_POWDERN) CASE(RAMP_S_DET1D) CASE(RAMP_S_DET2D) CASE(RAMP_S_COUNTER)
     CASE(RAMP_S_BEAMSTOP) CASE(RAMP_S_ATTENUATE)
 #undef CASE
+#undef CASE2
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

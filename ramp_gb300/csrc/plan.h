@@ -27,6 +27,8 @@ struct alignas(16) CompDev {
   float* tally;
   float* tally_err;
   int64_t tally_len;
+  float aux[16];               /* per-kind constants derived on the host
+                                  (guide: see guide_aux in abi.cu)         */
   const float4* bvh_nodes;     /* mesh: 2 float4 per node                 */
   const float4* bvh_tris;      /* mesh: 3 float4 per triangle (v0,e1,e2)  */
   int32_t bvh_root_leaf;
