@@ -53,7 +53,11 @@ def args_():
     p.add_argument("--n", type=int, default=N_HIST)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--tune", default=None, help='fused launch config, e.g. {"blocks_per_sm": 3}')
+    p.add_argument("--tune", default="auto",
+                   help='fused launch config: "auto" (autotuner) or JSON, e.g. {"blocks_per_sm": 3}')
+    p.add_argument("--config", type=int, default=2, choices=[2, 3, 5],
+                   help="2: LET-like chain (default); 3: batched scan of 256 variants; "
+                        "5: mesh imaging, 360 views")
     return p.parse_args()
 
 
@@ -149,11 +153,95 @@ class Clocks:
                 "samples": len(rows)}
 
 
+# ---------------------------------------------------------------- configs 3 and 5
+def batched_workload(config, seed=11):
+    """Variants of the batched workloads: (IDF, list of kwargs, counts)."""
+    import numpy as np
+    from ramp_gb300 import instruments as I
+    rng = np.random.default_rng(seed)
+    if config == 3:
+        ei = np.exp(rng.uniform(np.log(2.0), np.log(20.0), 256))
+        slit = rng.uniform(0.010, 0.040, 256)
+        counts = np.exp(rng.uniform(np.log(1e5), np.log(4e6), 256)).astype(np.int64)
+        kws = [I.let_like_kwargs(Ei=float(e), use_slit=1, slit_w=float(w))
+               for e, w in zip(ei, slit)]
+        return I.path("let_like.json"), kws, [int(c) for c in counts]
+    angles = np.arange(360) * np.pi / 180.0
+    kws = [I.mesh_imaging_kwargs(angle=float(t)) for t in angles]
+    return I.path("mesh_imaging.json"), kws, [3_000_000] * 360
+
+
+def run_batched_config(a):
+    """Batched fused path (one launch for all variants) against the plain
+    path run variant after variant, on the same histories."""
+    import torch
+    import ramp_gb300 as m
+    from ramp_gb300 import _abi, build
+    from ramp_gb300.batch import BatchedInstrument
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    fn, kws, counts = batched_workload(a.config)
+    total = sum(counts)
+    B = BatchedInstrument(fn, kws, ctx=dev)
+    tune = None if a.tune in (None, "auto") else json.loads(a.tune)
+    for w in range(a.warmup):
+        B.execute(counts, rng="reference", seeds=list(range(len(counts))), tune=tune)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    ms = []
+    for k in range(a.steps):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        B.execute(counts, rng="reference", seeds=[(k * 7919 + v) % 4097 for v in range(len(counts))],
+                  tune=tune)
+        e.record()
+        e.synchronize()
+        ms.append(s.elapsed_time(e))
+    clk = clocks.stop()
+    # plain path, variant after variant, on the first 32 variants (each has its
+    # own plan; mesh plans build their own BVH), scaled to all histories
+    nplain = min(32, len(kws))
+    plain_insts = [m.Instrument(fn, dev, **kw) for kw in kws[:nplain]]
+    for inst in plain_insts:
+        inst.plan()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    import random as _r
+    s.record()
+    for inst, n in zip(plain_insts, counts[:nplain]):
+        _r.seed(n)
+        inst.execute(n, path="plain")
+    e.record()
+    e.synchronize()
+    plain_ms = s.elapsed_time(e) * total / sum(counts[:nplain])
+    value = total * a.steps / (sum(ms) / 1000.0)
+    name = {3: "batched scan: 256 LET-like variants (Ei log-uniform 2-20 meV with matched "
+               "chopper phases, slit 10-40 mm, N log-uniform 1e5-4e6), 720x1000 histogram each",
+            5: "mesh imaging: 360 views x 3e6 rays through a 200,704-triangle noisy torus "
+               "(BVH, watertight chords, mu 0.5/cm), 1024x1024 detector per view"}[a.config]
+    line = {"metric": "neutron histories/s", "value": value, "unit": "histories/s", "n_gpus": 1,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": statistics.mean(ms),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": name, "variants": len(counts), "histories_per_step": total,
+                       "rng": "reference keying", "path": "batched fused (one launch)"},
+            "plain_path_sequential": {"value": total / (plain_ms / 1000.0), "ms_per_step": plain_ms,
+                                      "sample": "first %d variants, scaled by histories" % nplain},
+            "batched_over_plain": (total / (statistics.mean(ms) / 1000.0)) / (total / (plain_ms / 1000.0)),
+            "gpu_launches": a.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- GPU arm
 def main():
     a = args_()
     if a.impl == "reference":
         run_reference(a)
+        return
+    if a.config in (3, 5):
+        run_batched_config(a)
         return
     import torch
     import torch.distributed as dist
@@ -180,7 +268,10 @@ def main():
 
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
 
-    tune = json.loads(a.tune) if a.tune else None
+    tune = "auto" if a.tune == "auto" else (json.loads(a.tune) if a.tune else None)
+    if tune == "auto":
+        from ramp_gb300 import autotune
+        tune = autotune.tune(m.Instrument(fn, dev, **kw), rng="reference")
 
     def timed(inst, path, steps, warmup):
         for w in range(warmup):

@@ -217,10 +217,24 @@ static uint64_t fnv1a(const void* data, size_t bytes) {
   return h;
 }
 
-static int get_table(RampPlan* p, const float* host, int64_t len, const float** dev) {
+/* content hash of a host table; within one call a table met again at the
+ * same address is not re-hashed (memo, optional) */
+typedef std::map<std::pair<const void*, int64_t>, uint64_t> HashMemo;
+static uint64_t table_hash(const void* host, int64_t bytes, HashMemo* memo) {
+  if (memo) {
+    auto it = memo->find(std::make_pair(host, bytes));
+    if (it != memo->end()) return it->second;
+  }
+  uint64_t h = fnv1a(host, (size_t)bytes);
+  if (memo) (*memo)[std::make_pair(host, bytes)] = h;
+  return h;
+}
+
+static int get_table(RampPlan* p, const float* host, int64_t len, const float** dev,
+                     HashMemo* memo = nullptr) {
   static const float zero = 0.0f;
   if (len <= 0 || !host) { host = &zero; len = 1; }
-  TabKey key(0, len, fnv1a(host, (size_t)len * sizeof(float)));
+  TabKey key(0, len, table_hash(host, len * (int64_t)sizeof(float), memo));
   auto it = p->tabs.find(key);
   if (it != p->tabs.end()) { *dev = (const float*)it->second.first; return RAMP_OK; }
   void* d;
@@ -232,8 +246,8 @@ static int get_table(RampPlan* p, const float* host, int64_t len, const float** 
 }
 
 static int get_bvh(RampPlan* p, const float* pts, int64_t len, const float4** nodes_dev,
-                   const float4** tris_dev) {
-  TabKey key(1, len, fnv1a(pts, (size_t)len * sizeof(float)));
+                   const float4** tris_dev, HashMemo* memo = nullptr) {
+  TabKey key(1, len, table_hash(pts, len * (int64_t)sizeof(float), memo));
   auto it = p->tabs.find(key);
   if (it == p->tabs.end()) {
     std::vector<float> nodes, tris;
@@ -254,7 +268,7 @@ static int get_bvh(RampPlan* p, const float* pts, int64_t len, const float4** no
 }
 
 /* Convert one caller descriptor into its device form. */
-static int make_comp(RampPlan* p, const RampComp& c, CompDev& d) {
+static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo = nullptr) {
   memset(&d, 0, sizeof(d));
   d.geom = c.geom; d.scat = c.scat; d.idx = c.idx; d.restore = c.restore;
   memcpy(d.pos, c.pos, sizeof(d.pos));
@@ -268,14 +282,14 @@ static int make_comp(RampPlan* p, const RampComp& c, CompDev& d) {
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;   /* the BVH replaces the raw points */
-    int rc = get_table(p, c.table[k], c.table_len[k], &d.tab[k]);
+    int rc = get_table(p, c.table[k], c.table_len[k], &d.tab[k], memo);
     if (rc) return rc;
   }
   d.tally = c.tally;
   d.tally_err = c.tally_err;
   d.tally_len = c.tally_len;
   if (c.geom == RAMP_G_MESH) {
-    int rc = get_bvh(p, c.table[0], c.table_len[0], &d.bvh_nodes, &d.bvh_tris);
+    int rc = get_bvh(p, c.table[0], c.table_len[0], &d.bvh_nodes, &d.bvh_tris, memo);
     if (rc) return rc;
   }
   return RAMP_OK;
@@ -509,6 +523,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   BatchCache& B = p->batch;
   /* descriptors: re-upload only when they change */
   std::vector<CompDev> comps((size_t)n_variants * nc);
+  HashMemo memo;
   for (int v = 0; v < n_variants; ++v) {
     if (!variants[v].comps || variants[v].n < 0) {
       set_err("variant %d: missing components", v);
@@ -521,7 +536,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
         return RAMP_E_INVALID;
       }
       int rc = validate_comp(c, j);
-      if (!rc) rc = make_comp(p, c, comps[(size_t)v * nc + j]);
+      if (!rc) rc = make_comp(p, c, comps[(size_t)v * nc + j], &memo);
       if (rc) return rc;
     }
   }
@@ -668,17 +683,18 @@ static NoallocLayout g_noalloc_host;
 static std::mutex g_noalloc_mutex;
 
 /* table lookup that never uploads */
-static int lookup_table(RampPlan* p, const float* host, int64_t len, const float** dev) {
+static int lookup_table(RampPlan* p, const float* host, int64_t len, const float** dev,
+                        HashMemo* memo) {
   static const float zero = 0.0f;
   if (len <= 0 || !host) { host = &zero; len = 1; }
-  TabKey key(0, len, fnv1a(host, (size_t)len * sizeof(float)));
+  TabKey key(0, len, table_hash(host, len * (int64_t)sizeof(float), memo));
   auto it = p->tabs.find(key);
   if (it == p->tabs.end()) return RAMP_E_INVALID;
   *dev = (const float*)it->second.first;
   return RAMP_OK;
 }
 
-static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d) {
+static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo) {
   memset(&d, 0, sizeof(d));
   d.geom = c.geom; d.scat = c.scat; d.idx = c.idx; d.restore = c.restore;
   memcpy(d.pos, c.pos, sizeof(d.pos));
@@ -692,7 +708,7 @@ static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d) {
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;
-    if (lookup_table(p, c.table[k], c.table_len[k], &d.tab[k])) {
+    if (lookup_table(p, c.table[k], c.table_len[k], &d.tab[k], memo)) {
       set_err("ramp_trace_batched_noalloc: table %d of a variant component is not held by "
               "the plan (create the plan from a variant with the same tables)", k);
       return RAMP_E_INVALID;
@@ -702,7 +718,8 @@ static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d) {
   d.tally_err = c.tally_err;
   d.tally_len = c.tally_len;
   if (c.geom == RAMP_G_MESH) {
-    TabKey key(1, c.table_len[0], fnv1a(c.table[0], (size_t)c.table_len[0] * sizeof(float)));
+    TabKey key(1, c.table_len[0],
+               table_hash(c.table[0], c.table_len[0] * (int64_t)sizeof(float), memo));
     auto it = p->tabs.find(key);
     if (it == p->tabs.end()) {
       set_err("ramp_trace_batched_noalloc: mesh of a variant is not held by the plan");
@@ -771,6 +788,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
     }
   }
   int64_t t = 0;
+  HashMemo memo;
   for (int v = 0; v < n_variants; ++v) {
     const RampVariant& V = variants[v];
     if (!V.comps || V.n < 0) {
@@ -785,7 +803,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
         return RAMP_E_INVALID;
       }
       int rc = validate_comp(c, j);
-      if (!rc) rc = lookup_comp(p, c, H.descs[(size_t)v * nc + j]);
+      if (!rc) rc = lookup_comp(p, c, H.descs[(size_t)v * nc + j], &memo);
       if (rc) return rc;
     }
     int rc = make_src(V.source, H.variants[v].src);

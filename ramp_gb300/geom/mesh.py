@@ -7,6 +7,21 @@ from .gprim import GPrim
 from .. import _abi
 
 
+_STL_CACHE = {}
+
+
+def read_stl_cached(filename):
+    """read_stl with a per-process cache keyed by path and modification
+    time: components built from the same file share one (read-only) array."""
+    key = (os.path.abspath(filename), os.path.getmtime(filename))
+    pts = _STL_CACHE.get(key)
+    if pts is None:
+        pts = read_stl(filename)
+        pts.setflags(write=False)
+        _STL_CACHE[key] = pts
+    return pts
+
+
 def read_stl(filename):
     """Triangles of an STL file (binary or ASCII) as a float32 array
     [n_tri, 9] = v0, v1, v2, the layout numpy-stl's ``mesh.points`` gives
@@ -65,7 +80,7 @@ class GMesh(GPrim):
     def __init__(self, filename='', interior=False, idx=0, ctx=None, points=None):
         self.idx = np.uint32(idx)
         self.filename = filename
-        self.points = read_stl(filename) if points is None else \
+        self.points = read_stl_cached(filename) if points is None else \
             np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 9)
         allv = self.points.reshape(-1, 3)
         mn, mx = allv.min(axis=0), allv.max(axis=0)

@@ -317,6 +317,8 @@ class Instrument:
                persistent kernel for the whole chain).
         rng  : "reference" reproduces the reference's per-draw Threefry
                stream; "native" uses all four words of each block.
+        tune : fused launch configuration: a dict (blocks_per_sm, chunk) or
+               "auto" for the cached autotuner choice (ramp_gb300.autotune).
         chunk: override the chunk size (default max_mem_alloc / 256).
         shard: (rank, world) — trace only this rank's contiguous slice of
                every chunk, keyed by global index and weighted by the full
@@ -332,6 +334,12 @@ class Instrument:
         rngd.mode = {"reference": 0, "native": 1}[rng]
         rngd.run_seed = int(run_seed) & 0xffffffff
         tuned = None
+        if tune == "auto":
+            if path != "fused":
+                tune = None
+            else:
+                from . import autotune
+                tune = autotune.tune(self, rng=rng)
         if tune is not None:
             tuned = _abi.RampTune(*[int(tune.get(k, 0)) for k in
                                     ("block", "blocks_per_sm", "chunk", "privatize")])
