@@ -243,6 +243,48 @@ int ramp_trace_batched(RampPlan* plan, const RampVariant* variants,
                        int n_variants, const RampRng* rng,
                        const RampTune* tune, void* stream);
 
+/* ---- differentiation ---------------------------------------------------
+ * Parameters that enter neutron weights smoothly.  kind selects the
+ * descriptor value, comp the component (index into the plan's components;
+ * ignored for the source).  POWDER_SIGMA_ABS is the descriptor value
+ * sigma_abs * v = pack * sigma_abs / vc * 100 (powderN.py:65).           */
+#define RAMP_DP_GUIDE_R0          1
+#define RAMP_DP_GUIDE_QC          2
+#define RAMP_DP_GUIDE_ALPHA       3
+#define RAMP_DP_GUIDE_M           4
+#define RAMP_DP_GUIDE_W           5
+#define RAMP_DP_SOURCE_T          6   /* T1 = T2 = T3 of MCont            */
+#define RAMP_DP_POWDER_SIGMA_ABS  7
+#define RAMP_MAX_DIFF_PARAMS     32
+
+typedef struct RampDiffParam {
+  int32_t kind;
+  int32_t comp;
+} RampDiffParam;
+
+/* Set one parameter of a plan in place (no counterpart in the reference:
+ * there, changing a parameter means building a new Instrument).          */
+int ramp_plan_set_param(RampPlan* plan, int32_t kind, int32_t comp, float value);
+
+/* Gradient of a loss of one detector's histogram with respect to
+ * n_params parameters (no counterpart in the reference).  dL_dH is dL/dH
+ * per bin of component det_comp's histogram (device memory).  The chain is
+ * replayed for neutrons [0, n) with the chunk parameters of the forward
+ * run (num_sim, seed, rng): the counter-based RNG recomputes every
+ * neutron's state at every component boundary exactly.  Per neutron the
+ * kernel accumulates d log p / d theta (analytic local derivatives of the
+ * reflectivity, the Maxwellian weight and the powder attenuation, the
+ * powder depth reparameterised through its inverse CDF) and, at each tally
+ * by the loss detector, adds dL/dH_bin * p * d log p / d theta to grad
+ * (device, double, n_params entries, accumulated).  lr = 1 adds the
+ * likelihood-ratio terms of the powder's transmit/scatter branch (an
+ * unbiased estimator; lr = 0 is the pathwise derivative that central
+ * finite differences with common random numbers measure).               */
+int ramp_adjoint(RampPlan* plan, const RampDiffParam* params, int n_params,
+                 int det_comp, const float* dL_dH, int64_t n, int32_t num_sim,
+                 int32_t seed, const RampRng* rng, int lr, double* grad,
+                 void* stream);
+
 /* ramp_trace_batched without device allocation.  No counterpart in the
  * reference.  For callers that may not allocate device memory while
  * tracing (a fixed memory budget, an external pool that forbids

@@ -67,6 +67,14 @@ class RampVariant(ctypes.Structure):
                 ("seed", ctypes.c_int32)]
 
 
+class RampDiffParam(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("comp", ctypes.c_int32)]
+
+
+DP_GUIDE_R0, DP_GUIDE_QC, DP_GUIDE_ALPHA, DP_GUIDE_M, DP_GUIDE_W, DP_SOURCE_T, \
+    DP_POWDER_SIGMA_ABS = range(1, 8)
+
+
 class RampTune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("chunk", ctypes.c_int32), ("privatize", ctypes.c_int32)]
@@ -115,6 +123,12 @@ _SIGS = {
     "ramp_trace_batched_noalloc": ([ctypes.c_void_p, ctypes.POINTER(RampVariant), ctypes.c_int,
                                     ctypes.POINTER(RampRng), ctypes.POINTER(RampTune),
                                     ctypes.c_void_p], ctypes.c_int),
+    "ramp_plan_set_param": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_float],
+                            ctypes.c_int),
+    "ramp_adjoint": ([ctypes.c_void_p, ctypes.POINTER(RampDiffParam), ctypes.c_int, ctypes.c_int,
+                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                      ctypes.POINTER(RampRng), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
+                     ctypes.c_int),
     "ramp_debug_threefry": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_math": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libramp_cuda.so")
 
-CU_SOURCES = ["plain.cu", "fused.cu", "abi.cu"]
+CU_SOURCES = ["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
 CPP_SOURCES = ["bvh.cpp"]
 HEADERS = ["device.cuh", "mesh.cuh", "plan.h", "launch.h", "rmath.h", "rconst.h", "bvh.h",
            os.path.join("..", "..", "include", "ramp.h")]

@@ -58,6 +58,7 @@ struct BatchCache {
 typedef std::tuple<int, int64_t, uint64_t> TabKey;
 
 struct RampPlan {
+  RampSource src_in;
   SrcDev src;
   std::vector<RampComp> comps_in;    /* the caller's descriptors           */
   std::vector<CompDev> comps;        /* host copy of device descriptors    */
@@ -69,6 +70,8 @@ struct RampPlan {
   int sm_count = 0;
   BatchCache batch;
   std::map<TabKey, std::pair<void*, void*>> tabs;
+  std::vector<CompDev> adj_host;     /* descriptors of the last adjoint   */
+  CompDev* adj_dev = nullptr;
 };
 
 /* ---------------------------------------------------------------------- */
@@ -143,6 +146,7 @@ static int make_src(const RampSource& s, SrcDev& d) {
   }
   memset(&d, 0, sizeof(d));
   d.kind = s.kind;
+  d.dslot_T = -1;
   memcpy(d.p, s.p, sizeof(d.p));
   if (s.kind == RAMP_SRC_CONT) {
     d.dmax[0] = maxwell_h(RC_K_B * s.p[7], s.p[7]);
@@ -278,6 +282,7 @@ static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo 
   memcpy(d.sp, c.sp, sizeof(d.sp));
   memcpy(d.gi, c.gi, sizeof(d.gi));
   memcpy(d.si, c.si, sizeof(d.si));
+  for (int k = 0; k < 6; ++k) d.dslot[k] = -1;
   if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
@@ -343,6 +348,7 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
   }
   *out = nullptr;
   RampPlan* p = new RampPlan();
+  p->src_in = *source;
   int rc = make_src(*source, p->src);
   if (rc) { delete p; return rc; }
   for (int b = 0; b < n_blocks; ++b) {
@@ -613,6 +619,105 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   return RAMP_OK;
 }
 
+int ramp_plan_set_param(RampPlan* p, int32_t kind, int32_t comp, float value) {
+  if (!p) { set_err("NULL plan"); return RAMP_E_INVALID; }
+  if (kind == RAMP_DP_SOURCE_T) {
+    if (p->src_in.kind != RAMP_SRC_CONT) {
+      set_err("ramp_plan_set_param: the source has no temperature");
+      return RAMP_E_INVALID;
+    }
+    p->src_in.p[7] = p->src_in.p[9] = p->src_in.p[11] = value;
+    return make_src(p->src_in, p->src);
+  }
+  if (comp < 0 || comp >= (int)p->comps_in.size()) {
+    set_err("ramp_plan_set_param: component %d out of range", comp);
+    return RAMP_E_INVALID;
+  }
+  RampComp& c = p->comps_in[comp];
+  if (kind >= RAMP_DP_GUIDE_R0 && kind <= RAMP_DP_GUIDE_W) {
+    if (c.scat != RAMP_S_GUIDE) { set_err("component %d is not a guide", comp); return RAMP_E_INVALID; }
+    c.sp[5 + (kind - RAMP_DP_GUIDE_R0)] = value;
+  } else if (kind == RAMP_DP_POWDER_SIGMA_ABS) {
+    if (c.scat != RAMP_S_POWDERN) { set_err("component %d is not a powder", comp); return RAMP_E_INVALID; }
+    c.sp[0] = value;
+  } else {
+    set_err("ramp_plan_set_param: unknown parameter kind %d", kind);
+    return RAMP_E_INVALID;
+  }
+  int rc = make_comp(p, c, p->comps[comp]);
+  if (rc) return rc;
+  CK(cudaMemcpy(p->comps_dev + comp, &p->comps[comp], sizeof(CompDev), cudaMemcpyHostToDevice));
+  return RAMP_OK;
+}
+
+int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det_comp,
+                 const float* dL_dH, int64_t n, int32_t num_sim, int32_t seed,
+                 const RampRng* rng, int lr, double* grad, void* stream) {
+  if (!p || !params || n_params <= 0 || n_params > RAMP_MAX_DIFF_PARAMS || !dL_dH || !grad ||
+      n < 0) {
+    set_err("ramp_adjoint: bad arguments");
+    return RAMP_E_INVALID;
+  }
+  const int nc = (int)p->comps.size();
+  if (det_comp < 0 || det_comp >= nc ||
+      (p->comps[det_comp].scat != RAMP_S_DET2D && p->comps[det_comp].scat != RAMP_S_DET1D)) {
+    set_err("ramp_adjoint: component %d is not a histogram detector", det_comp);
+    return RAMP_E_INVALID;
+  }
+  if ((int)p->adj_host.size() != nc) {
+    p->adj_host.resize((size_t)nc);
+    void* d;
+    int rc = upload(p->comps.data(), (size_t)nc * sizeof(CompDev), &d, p->allocs);
+    if (rc) return rc;
+    p->adj_dev = (CompDev*)d;
+  }
+  std::vector<CompDev>& A = p->adj_host;
+  A = p->comps;
+  SrcDev src = p->src;
+  for (int k = 0; k < n_params; ++k) {
+    const RampDiffParam& q = params[k];
+    if (q.kind == RAMP_DP_SOURCE_T) {
+      if (src.kind != RAMP_SRC_CONT) { set_err("ramp_adjoint: source has no temperature"); return RAMP_E_INVALID; }
+      src.dslot_T = k;
+      continue;
+    }
+    if (q.comp < 0 || q.comp >= nc) { set_err("ramp_adjoint: parameter %d: bad component", k); return RAMP_E_INVALID; }
+    CompDev& c = A[q.comp];
+    if (q.kind >= RAMP_DP_GUIDE_R0 && q.kind <= RAMP_DP_GUIDE_W && c.scat == RAMP_S_GUIDE) {
+      c.dslot[q.kind - RAMP_DP_GUIDE_R0] = (int16_t)k;
+    } else if (q.kind == RAMP_DP_POWDER_SIGMA_ABS && c.scat == RAMP_S_POWDERN) {
+      c.dslot[0] = (int16_t)k;
+    } else {
+      set_err("ramp_adjoint: parameter %d (kind %d) does not match component %d", k, q.kind, q.comp);
+      return RAMP_E_INVALID;
+    }
+  }
+  A[det_comp].adj_det = 1;
+  A[det_comp].dLdH = dL_dH;
+  cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaMemcpyAsync(p->adj_dev, A.data(), (size_t)nc * sizeof(CompDev), cudaMemcpyHostToDevice, s));
+  AdjointArgs a;
+  memset(&a, 0, sizeof(a));
+  a.src = src;
+  a.comps = p->adj_dev;
+  a.blocks = p->blocks_dev;
+  a.n_blocks = (int32_t)p->blocks.size();
+  a.nslot = n_params;
+  a.n = n;
+  a.num_sim = num_sim;
+  a.seed = seed;
+  a.rng.mode = rng ? rng->mode : 0;
+  a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.tid_base = rng ? rng->tid_base : 0u;
+  a.grad = grad;
+  a.lr = lr;
+  a.st = p->status;
+  int64_t g = (n + 255) / 256;
+  int64_t cap = (int64_t)p->sm_count * 8;
+  CK(launch_adjoint(a, (int)(g < cap ? g : cap), s));
+  return RAMP_OK;
+}
+
 int ramp_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out, int64_t n,
                         void* stream) {
   if (!c0 || !tid || !out || n < 0) { set_err("bad arguments"); return RAMP_E_INVALID; }
@@ -704,6 +809,7 @@ static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* mem
   memcpy(d.sp, c.sp, sizeof(d.sp));
   memcpy(d.gi, c.gi, sizeof(d.gi));
   memcpy(d.si, c.si, sizeof(d.si));
+  for (int k = 0; k < 6; ++k) d.dslot[k] = -1;
   if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];

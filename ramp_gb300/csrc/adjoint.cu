@@ -1,0 +1,43 @@
+/*
+ * adjoint.cu — gradients of a detector-histogram loss with respect to
+ * weight parameters (ramp_adjoint).  Each thread replays one neutron from
+ * its counter-based RNG key through the same device functions as the
+ * forward paths, instantiated with an AdjDiff context that accumulates
+ * d log p / d theta and contributes dL/dH_bin * p * d log p / d theta at the
+ * loss detector.  The replay is the checkpoint: a neutron's state at every
+ * component boundary is recomputed exactly, nothing per neutron is stored.
+ */
+#include "device.cuh"
+#include "launch.h"
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    Nt n;
+    Rng r;
+    rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    AdjDiff dx;
+    dx.reset(a.nslot, a.grad, a.lr);
+    uint32_t ii = 0;
+    generate<AdjDiff>(a.src, n, 0.0f, a.num_sim, a.seed, r, &dx);
+    for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
+      const RampBlock B = a.blocks[b];
+      if (B.linear) {
+        for (int k = B.first; k < B.first + B.count; ++k) {
+          if (n.die > 0.f) break;
+          comp_linear<AdjDiff>(a.comps[k], n, ii, r, a.st, &dx);
+        }
+      } else {
+        block_nonlinear<AdjDiff>(a.comps, B.first, B.count, B.multi, n, ii, r, a.st, &dx);
+      }
+    }
+  }
+}
+
+cudaError_t launch_adjoint(const AdjointArgs& a, int grid, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  if (a.rng.mode == 0) k_adjoint<0><<<grid, 256, 0, s>>>(a);
+  else k_adjoint<1><<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}

@@ -199,6 +199,36 @@ DI void tally_add(float* h, float* he, long long idx, float p) {
 }
 
 /* ------------------------------------------------------------------ */
+/* adjoint context: the chain functions take a context type D; NoDiff    */
+/* compiles every derivative hook away (the forward kernels), AdjDiff    */
+/* accumulates d log p / d theta per neutron and, at the loss detector,  */
+/* adds dL/dH_bin * p * d log p / d theta to the gradient.               */
+/* ------------------------------------------------------------------ */
+struct NoDiff {
+  static constexpr bool on = false;
+};
+
+struct AdjDiff {
+  static constexpr bool on = true;
+  float dlog[RAMP_MAX_DIFF];
+  double* grad;      /* nslot accumulators, global                       */
+  int nslot;
+  int lr;            /* add likelihood-ratio terms of branch choices     */
+  DI void reset(int n, double* g, int lr_) {
+    nslot = n; grad = g; lr = lr_;
+    for (int k = 0; k < RAMP_MAX_DIFF; ++k) dlog[k] = 0.0f;
+  }
+  DI void add(int slot, float v) { if (slot >= 0) dlog[slot] += v; }
+  /* the neutron is tallied by the loss detector with weight p in a bin of
+   * adjoint g */
+  DI void tallied(float g, float p) {
+    float w = g * p;
+    if (w == 0.0f) return;
+    for (int k = 0; k < nslot; ++k) atomicAdd(grad + k, (double)w * (double)dlog[k]);
+  }
+};
+
+/* ------------------------------------------------------------------ */
 /* moderators                                                           */
 /* ------------------------------------------------------------------ */
 /* maxwell_energy_distn — cont_mod.cl:4-9 (pow(x,1.5) as x*sqrt(x)) */
@@ -209,7 +239,9 @@ DI float maxwell(float E, float T) {
 }
 
 /* generate_neutrons — flat_mod.cl:4-50 and cont_mod.cl:11-72 */
-DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t seed, Rng& r) {
+template <class D = NoDiff>
+DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t seed, Rng& r,
+                 D* dx = nullptr) {
   n.x = n.y = n.z = n.vx = n.vy = n.vz = n.px = n.py = n.pz = 0.0f;
   n.p = n.t = n.sc = n.sd = n.se = n.die = 0.0f;
   n.wr = 0;
@@ -223,6 +255,20 @@ DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t 
     M += s.p[10] * maxwell(E_J, s.p[9]) / s.dmax[1];
     M += s.p[12] * maxwell(E_J, s.p[11]) / s.dmax[2];
     n.p = M / (float)num_sim;
+    if constexpr (D::on) {
+      /* weight I M(E;T)/M(kT;T) = I sqrt(x) e^(1-x), x = E/kT, for the
+         common temperature T of the three terms: d log/dT = (x - 1/2)/T */
+      if (s.dslot_T >= 0 && M != 0.0f) {
+        float acc = 0.0f;
+        for (int q = 0; q < 3; ++q) {
+          const float T = s.p[7 + 2 * q], I = s.p[8 + 2 * q];
+          const float term = I * maxwell(E_J, T) / s.dmax[q];
+          const float x = E_J / (RC_K_B * T);
+          acc += term * (x - 0.5f) / T;
+        }
+        dx->add(s.dslot_T, acc / M);
+      }
+    }
   } else {
     n.p = 1.0f / (float)num_sim;
   }
@@ -466,8 +512,54 @@ DI float reflectivity_pre(float q, const float* aux, float R0) {
   return aux[14] * (1 - rm_tanhf(arg)) * (1 - aux[10] * (q - Qc) + aux[11] * (q - Qc) * (q - Qc));
 }
 
+/* d log R / d (R0, Qc, alpha, m, W) for a bounce with momentum q, R > 0
+ * (analytic derivative of reflectivity_func, ref.h:3-53) */
+template <class D>
+DI void guide_dlogR(const CompDev& c, float q, float R, D* dx) {
+  const float R0 = c.sp[5], Qc = c.sp[6], m0 = c.sp[8];
+  const float m = c.aux[8], W = c.aux[9], alpha = c.aux[10], beta = c.aux[11];
+  const float Qc2 = c.aux[13];
+  const bool param = (c.sp[9] == 0.0f && c.sp[7] == 0.0f);   /* m-parametrisation */
+  float dR[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  if (q <= Qc2) {
+    dR[0] = 1.0f;
+  } else {
+    const float arg = (q - c.aux[12]) / W;
+    const float th = rm_tanhf(arg);
+    const float T = 1.0f - th, dT = -(1.0f - th * th);
+    const float u = q - Qc2;
+    const float P = 1.0f - alpha * u + beta * u * u;
+    const float R0h = 0.5f * R0;
+    const float dPdQc2 = alpha - 2.0f * beta * u;
+    const float dQc2dQc = (m < 1.0f) ? m : 1.0f;
+    const float dQc2dm = (m < 1.0f) ? Qc : 0.0f;
+    const float dargdQc = -m / W, dargdm = -Qc / W, dargdW = -arg / W;
+    dR[0] = 0.5f * T * P;
+    dR[1] = R0h * (dT * dargdQc * P + T * dPdQc2 * dQc2dQc);
+    /* m and W, alpha, beta as the reflectivity sees them */
+    float dRdm = R0h * (dT * dargdm * P + T * dPdQc2 * dQc2dm);
+    float dRdW = R0h * dT * dargdW * P;
+    float dRdalpha = R0h * T * (-u);
+    float dRdbeta = R0h * T * u * u;
+    if (!param) {
+      dR[2] = dRdalpha;
+      dR[3] = dRdm;
+      dR[4] = dRdW;
+    } else {
+      /* m_eff = 0.9853 m + 0.1978; W, alpha, beta follow m_eff */
+      float dalpha_dm = (m <= 3.0f) ? 1.0f : 0.2304f;
+      float dbeta_dm = (m <= 3.0f) ? 0.0f : -7.6251f;
+      float total = dRdm + dRdW * (-0.0002f) + dRdalpha * dalpha_dm + dRdbeta * dbeta_dm;
+      dR[3] = total * 0.9853f;
+      (void)m0;
+    }
+  }
+  for (int k = 0; k < 5; ++k) dx->add(c.dslot[k], dR[k] / R);
+}
+
 /* guide.cl:9-149 */
-DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
+template <class D = NoDiff>
+DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* dx = nullptr) {
   const float l = c.sp[4], R0 = c.sp[5];
   const uint32_t max_bounces = (uint32_t)c.si[0];
   const float ww = c.aux[0], hh = c.aux[1], Av = c.aux[2], Ah = c.aux[3];
@@ -509,6 +601,9 @@ DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
     float refl = reflectivity_pre(q, c.aux, R0);
     n.p *= refl;
     if (refl < 1e-12f || refl > 1.0f) n.p = 0.0f;
+    if constexpr (D::on) {
+      if (n.p != 0.0f) guide_dlogR(c, q, refl, dx);
+    }
     i++;
   }
   if (i >= max_bounces) set_die(n, 1.0f);
@@ -658,7 +753,9 @@ DI void s_isotropic(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
 }
 
 /* powderN.cl:5-156 */
-DI void s_powdern(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st) {
+template <class D = NoDiff>
+DI void s_powdern(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st,
+                  D* dx = nullptr) {
   const float* __restrict__ ssv2 = c.tab[0];
   const float* __restrict__ qv = c.tab[1];
   const float sigma_abs_v = c.sp[0], d_phi = c.sp[1];
@@ -674,8 +771,15 @@ DI void s_powdern(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDe
   float sum_sigma_scat = 0.0f;
   for (uint32_t j = 0; j < num_lines; j++) sum_sigma_scat += __ldg(ssv2 + j) / vv;
   float p_inter = 1 - rm_expf(-(sum_sigma_scat + sigma_abs) * full_path_length);
+  /* d Sigma / d (sigma_abs * v), the descriptor value sp[0] */
+  const float dSig = 2200.0f / vel;
   if (draw(n, r) > p_inter) {
     n.p *= 1 - p_inter;
+    if constexpr (D::on) {
+      /* weight factor exp(-Sigma L); the branch has the same probability */
+      float g = -full_path_length * dSig;
+      dx->add(c.dslot[0], dx->lr ? 2.0f * g : g);
+    }
     set_pos(n, add(ip2(s), mul(0.0001f, normalize(path))));
     n.t += s.t2;
     if (transmit == 0) set_die(n, 1.0f);
@@ -706,7 +810,8 @@ DI void s_powdern(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDe
     attempts++;
   }
   float twotheta = 2.0f * rm_asinf(arg);
-  float pen_depth = -rm_logf(1.0f - draw(n, r) * (1.0f - p_inter)) / (sigma_abs + sum_sigma_scat);
+  const float u_depth = draw(n, r);
+  float pen_depth = -rm_logf(1.0f - u_depth * (1.0f - p_inter)) / (sigma_abs + sum_sigma_scat);
   V3 beam_para = normalize(nvel(n));
   V3 beam_perp = cross(beam_para, v3(0.0f, 1.0f, 0.0f));
   if (len3(beam_perp) < 1e-3f) beam_perp = normalize(cross(beam_para, v3(1.0f, 0.0f, 0.0f)));
@@ -731,11 +836,24 @@ DI void s_powdern(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDe
   set_vel(n, mul(vel, normalize(beam_para)));
   n.p *= (1 - rm_expf(-(sum_sigma_scat + sigma_abs) * pen_depth)) * sum_sigma_scat /
          (sum_sigma_scat + sigma_abs);
+  if constexpr (D::on) {
+    /* weight factor (1 - e^(-Sigma d)) Ss / Sigma with the depth d
+       reparameterised through its inverse CDF at fixed u:
+       d = -log(A)/Sigma, A = 1 - u (1 - e^(-Sigma L)) */
+    const float Sig = sum_sigma_scat + sigma_abs, L = full_path_length;
+    const float eL = rm_expf(-Sig * L), ed = rm_expf(-Sig * pen_depth);
+    const float A = 1.0f - u_depth * (1.0f - eL);
+    const float dd = u_depth * L * eL / (A * Sig) - pen_depth / Sig;
+    float g = (ed * (pen_depth + Sig * dd)) / (1.0f - ed) - 1.0f / Sig;
+    if (dx->lr) g += L * eL / (1.0f - eL);       /* scatter branch, probability 1 - e^(-Sigma L) */
+    dx->add(c.dslot[0], g * dSig);
+  }
   s_finish(c, n, s, ii);
 }
 
 /* detector1D.cl:20-77 */
-DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
+template <class D = NoDiff>
+DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* dx = nullptr) {
   const float min_var = c.sp[0], step_var = c.sp[1], max_var = c.sp[2];
   const uint32_t var = (uint32_t)c.si[0], restore = (uint32_t)c.si[1];
   float var_val = 0.0f;
@@ -745,8 +863,15 @@ DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
   else if (var == 3) var_val = 2 * RC_PI / (RC_V2K * len3(nvel(n)));
   if (min_var <= var_val && var_val <= max_var) {
     uint32_t idx = (uint32_t)floorf((var_val - min_var) / step_var);
-    if ((long long)idx < c.tally_len) tally_add(c.tally, c.tally_err, idx, n.p);
-    else atomicAdd(&st->oob, 1ull);
+    if ((long long)idx < c.tally_len) {
+      if constexpr (D::on) {
+        if (c.adj_det) dx->tallied(__ldg(c.dLdH + idx), ftz(n.p));
+      } else {
+        tally_add(c.tally, c.tally_err, idx, n.p);
+      }
+    } else if constexpr (!D::on) {
+      atomicAdd(&st->oob, 1ull);
+    }
   }
   if (restore == 0) {
     set_pos(n, ip2(s));
@@ -781,13 +906,21 @@ DI int find_idx(float val, float b0, float b1, float b2) {
 }
 
 /* detector2D.cl:31-186 */
-DI void s_det2d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st) {
+template <class D = NoDiff>
+DI void s_det2d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* dx = nullptr) {
   int a1 = find_idx(det2d_val((uint32_t)c.si[0], 1, n, s), c.sp[0], c.sp[1], c.sp[2]);
   int a2 = find_idx(det2d_val((uint32_t)c.si[1], 2, n, s), c.sp[3], c.sp[4], c.sp[5]);
   if (!((a1 == -1) || (a2 == -1))) {
     long long flat = (long long)a1 * c.si[3] + a2;
-    if (flat >= 0 && flat < c.tally_len) tally_add(c.tally, c.tally_err, flat, n.p);
-    else atomicAdd(&st->oob, 1ull);
+    if (flat >= 0 && flat < c.tally_len) {
+      if constexpr (D::on) {
+        if (c.adj_det) dx->tallied(__ldg(c.dLdH + flat), ftz(n.p));
+      } else {
+        tally_add(c.tally, c.tally_err, flat, n.p);
+      }
+    } else if constexpr (!D::on) {
+      atomicAdd(&st->oob, 1ull);
+    }
   }
   if (c.si[4] == 0) {
     set_pos(n, ip2(s));
@@ -806,17 +939,19 @@ DI void s_attenuate(const CompDev& c, Nt& n, Is& s, uint32_t& ii) {
   s_finish(c, n, s, ii);
 }
 
-DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st) {
+template <class D = NoDiff>
+DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st,
+                D* dx = nullptr) {
   switch (c.scat) {
     case RAMP_S_ARM: ii = c.idx; is_reset(s); break;
-    case RAMP_S_GUIDE: s_guide(c, n, s, ii, st); break;
+    case RAMP_S_GUIDE: s_guide<D>(c, n, s, ii, st, dx); break;
     case RAMP_S_CHOPPER: s_chopper(c, n, s, ii, r); break;
     case RAMP_S_ISOTROPIC: s_isotropic(c, n, s, ii, r); break;
-    case RAMP_S_POWDERN: s_powdern(c, n, s, ii, r, st); break;
-    case RAMP_S_DET1D: s_det1d(c, n, s, ii, st); break;
-    case RAMP_S_DET2D: s_det2d(c, n, s, ii, st); break;
+    case RAMP_S_POWDERN: s_powdern<D>(c, n, s, ii, r, st, dx); break;
+    case RAMP_S_DET1D: s_det1d<D>(c, n, s, ii, st, dx); break;
+    case RAMP_S_DET2D: s_det2d<D>(c, n, s, ii, st, dx); break;
     case RAMP_S_COUNTER:
-      if (c.tally) atomicAdd(c.tally, n.p);
+      if (!D::on && c.tally) atomicAdd(c.tally, n.p);
       n.se = 1.0f; n.wr |= WR_SE;
       s_finish(c, n, s, ii);
       break;
@@ -831,21 +966,24 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
 /* intersect, terminate, scatter, untransform on a live neutron.  The   */
 /* intersection starts at its reset value.                               */
 /* ------------------------------------------------------------------ */
-DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st) {
+template <class D = NoDiff>
+DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st,
+                    D* dx = nullptr) {
   transform(c, n);
   Is s;
   is_reset(s);
   if (intersect(c, n, s, st)) ii = c.idx;
   /* terminate.cl:16-18 */
   if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
-  if (ii == c.idx && !(n.die > 0.f)) scatter(c, n, s, ii, r, st);
+  if (ii == c.idx && !(n.die > 0.f)) scatter<D>(c, n, s, ii, r, st, dx);
   if (!(n.die > 0.f)) untransform(c, n);
 }
 
 /* one non-linear block (mcramp.py:167-217): "multi" rounds of all
  * geometries then all scatters; no termination step. */
+template <class D = NoDiff>
 DI void block_nonlinear(const CompDev* comps, int first, int count, int multi, Nt& n,
-                        uint32_t& ii, Rng& r, StatusDev* st) {
+                        uint32_t& ii, Rng& r, StatusDev* st, D* dx = nullptr) {
   Is s;
   is_reset(s);
   for (int e = 0; e < multi; ++e) {
@@ -860,7 +998,7 @@ DI void block_nonlinear(const CompDev* comps, int first, int count, int multi, N
       if (n.die > 0.f) break;
       const CompDev& c = comps[j];
       transform(c, n);
-      if (ii == c.idx) scatter(c, n, s, ii, r, st);
+      if (ii == c.idx) scatter<D>(c, n, s, ii, r, st, dx);
       if (!(n.die > 0.f)) untransform(c, n);
     }
   }

@@ -42,6 +42,23 @@ cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s
 int fused_max_blocks_per_sm(int block, int n_comps);
 void fused_set_min_blocks(int minb);
 
+struct AdjointArgs {
+  SrcDev src;
+  const CompDev* comps;         /* device, with the adjoint fields set     */
+  const RampBlock* blocks;      /* device */
+  int32_t n_blocks;
+  int32_t nslot;
+  int64_t n;
+  int32_t num_sim;
+  int32_t seed;
+  RngDev rng;
+  double* grad;
+  int32_t lr;
+  StatusDev* st;
+};
+
+cudaError_t launch_adjoint(const AdjointArgs& a, int grid, cudaStream_t s);
+
 cudaError_t launch_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out,
                                   int64_t n, cudaStream_t s);
 cudaError_t launch_debug_rng_peak(int64_t n, int32_t iters, uint32_t* out, cudaStream_t s);

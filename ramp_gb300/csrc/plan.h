@@ -29,6 +29,12 @@ struct alignas(16) CompDev {
   int64_t tally_len;
   float aux[16];               /* per-kind constants derived on the host
                                   (guide: see guide_aux in abi.cu)         */
+  int16_t dslot[6];            /* adjoint: gradient slot of each of this
+                                  component's differentiable parameters
+                                  (guide R0 Qc alpha m W; powder sigma_abs
+                                  in slot 0), -1 when not differentiated  */
+  int32_t adj_det;             /* adjoint: 1 for the loss detector        */
+  const float* dLdH;           /* adjoint: dL/dH of the loss detector     */
   const float4* bvh_nodes;     /* mesh: 2 float4 per node                 */
   const float4* bvh_tris;      /* mesh: 3 float4 per triangle (v0,e1,e2)  */
   int32_t bvh_root_leaf;
@@ -40,7 +46,9 @@ struct SrcDev {
   int32_t pad;
   float p[16];
   float dmax[3];               /* maxwell(k_B T_i, T_i) (cont_mod.cl:25-27) */
-  float pad2;
+  int32_t dslot_T;             /* adjoint: gradient slot of the common
+                                  moderator temperature, -1 when not
+                                  differentiated                          */
 };
 
 struct RngDev {
@@ -60,6 +68,7 @@ struct StatusDev {
 };
 
 #define RAMP_MAX_COMPS 64
+#define RAMP_MAX_DIFF 32   /* differentiable parameters per adjoint launch */
 
 /* one task of the persistent batched kernel: neutrons [start, start+count)
  * of variant v */
