@@ -55,9 +55,9 @@ def args_():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--tune", default="auto",
                    help='fused launch config: "auto" (autotuner) or JSON, e.g. {"blocks_per_sm": 3}')
-    p.add_argument("--config", type=int, default=2, choices=[2, 3, 5],
+    p.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
                    help="2: LET-like chain (default); 3: batched scan of 256 variants; "
-                        "5: mesh imaging, 360 views")
+                        "4: gradients of a histogram loss (grads/s); 5: mesh imaging, 360 views")
     return p.parse_args()
 
 
@@ -69,6 +69,14 @@ def workload_config(n, world, path="fused persistent kernel (plain per-component
             "rng": "reference keying (Threefry-4x32-20, one block per draw)",
             "path": path,
             "l2": "flushed between steps (256 MiB write)", "parallelism": "dp%d" % world}
+
+
+def peaks_file():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 # ---------------------------------------------------------------- CPU arm
@@ -234,7 +242,144 @@ def run_batched_config(a):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- config 4
+def run_gradients(a, n=10_000_000):
+    """grads/s: forward histogram + loss + adjoint gradient of 22 parameters
+    (4 guides x R0, Qc, alpha, m, W; moderator T; powder sigma_abs) on the
+    LET-like chain at 1e7 histories; the gradient is also compared with
+    central finite differences (common random numbers, step 1e-3)."""
+    import numpy as np
+    import torch
+    import ramp_gb300 as m
+    from ramp_gb300 import build, instruments as I
+    from ramp_gb300.diff import DiffChain, LET_LIKE_PARAMS, histogram
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    inst = m.Instrument(I.path("let_like.json"), dev, **I.let_like_kwargs())
+    chain = DiffChain(inst, LET_LIKE_PARAMS, detector="detector")
+    theta0 = chain.values()
+    r = np.random.default_rng(23)
+    chain.set(theta0 * (1.0 + 0.05 * torch.tensor(r.standard_normal(len(theta0)))))
+    Ht = chain.forward(n, seed=999).double().clone()
+
+    def step(seed):
+        th = theta0.clone().requires_grad_()
+        L = ((histogram(chain, th, n, seed).double() - Ht) ** 2).sum()
+        L.backward()
+        return th.grad
+
+    for w in range(a.warmup):
+        step(10 + w)
+    torch.cuda.synchronize()
+    ms = []
+    for k in range(a.steps):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        g = step(100 + k)
+        e.record()
+        e.synchronize()
+        ms.append(s.elapsed_time(e))
+    g = step(1)
+    fd = torch.zeros_like(g)
+    with torch.no_grad():
+        for k in range(len(theta0)):
+            h = 1e-3 * float(theta0[k])
+            tp, tm = theta0.clone(), theta0.clone()
+            tp[k] += h
+            tm[k] -= h
+            Lp = ((histogram(chain, tp, n, 1).double() - Ht) ** 2).sum()
+            Lm = ((histogram(chain, tm, n, 1).double() - Ht) ** 2).sum()
+            fd[k] = (Lp - Lm) / (2 * h)
+    rel = ((g - fd).abs() / fd.abs().clamp_min(1e-300)).tolist()
+    table = {nm: {"adjoint": float(x), "fd": float(y), "rel_err": float(z)}
+             for nm, x, y, z in zip(chain.names, g.tolist(), fd.tolist(), rel)}
+    line = {"metric": "grads/s", "value": 1000.0 / statistics.mean(ms), "unit": "grads/s",
+            "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": statistics.mean(ms),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "LET-like chain, 1e7 histories, loss sum (H - H*)^2 over the "
+                                   "720x1000 detector, 22 parameters, fused forward + adjoint",
+                       "histories": n},
+            "histories_per_s_forward_and_adjoint": n / (statistics.mean(ms) / 1000.0),
+            "gradient_vs_central_fd": table}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- GPU arm
+def plain_alive_counts(lib, inst, n, seed, dev):
+    """Histories alive at the entry of each component of a plain-path
+    chunk: the chain is re-planned with one linear block per component and
+    stepped block by block (ramp_generate, ramp_run_block), counting live
+    records in between.  Returns (alive per component, components per
+    block entry)."""
+    import torch
+    from ramp_gb300 import _abi
+    ct = _abi.ctypes
+    keep = []
+    src, carr, nc, barr, nb = inst.descriptors(keep)
+    blocks = []
+    for k in range(nb):
+        b = barr[k]
+        if b.linear:
+            blocks += [_abi.RampBlock(j, 1, 1, b.multi) for j in range(b.first, b.first + b.count)]
+        else:
+            blocks.append(_abi.RampBlock(b.first, b.count, 0, b.multi))
+    barr2 = (_abi.RampBlock * len(blocks))(*blocks)
+    plan = ct.c_void_p()
+    _abi.check(lib, lib.ramp_plan_create(ct.byref(src), carr, nc, barr2, len(blocks),
+                                         ct.byref(plan)), "ramp_plan_create")
+    try:
+        st = inst._alloc_state(n)
+        rng = _abi.RampRng()
+        stream = ct.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        _abi.check(lib, lib.ramp_generate(plan, ct.byref(st), n, n, seed, ct.byref(rng), stream),
+                   "ramp_generate")
+        die = inst.state[_abi.LANE["die"], :n]
+        alive, width = [], []
+        for b in range(len(blocks)):
+            alive.append(int((die == 0).sum()))
+            width.append(blocks[b].count)
+            _abi.check(lib, lib.ramp_run_block(plan, b, ct.byref(st), n, ct.byref(rng), stream),
+                       "ramp_run_block")
+        torch.cuda.synchronize(dev)
+    finally:
+        lib.ramp_plan_destroy(plan)
+    return alive, width
+
+
+def graph_small_n(inst_factory, tune, dev, sizes=(100_000, 1_000_000), reps=20):
+    """ms per execute() at small N, eager against a CUDA-graph replay of the
+    same trace (ramp_gb300.graph), for both paths."""
+    import torch
+    out = {}
+    for path in ("plain", "fused"):
+        for n in sizes:
+            inst = inst_factory()
+            tn = tune if path == "fused" else None
+            for _ in range(3):
+                inst.execute(n, path=path, tune=tn)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                inst.execute(n, path=path, tune=tn)
+            torch.cuda.synchronize(dev)
+            eager = 1000.0 * (time.perf_counter() - t0) / reps
+            g = inst.capture(n, path=path, tune=tn, state=7)
+            for _ in range(3):
+                g.replay()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                g.replay()
+            torch.cuda.synchronize(dev)
+            graph = 1000.0 * (time.perf_counter() - t0) / reps
+            g.check()
+            out["%s_%d" % (path, n)] = {"eager_ms": eager, "graph_ms": graph,
+                                        "graph_histories_per_s": n / (graph / 1000.0)}
+    return out
+
+
 def main():
     a = args_()
     if a.impl == "reference":
@@ -242,6 +387,9 @@ def main():
         return
     if a.config in (3, 5):
         run_batched_config(a)
+        return
+    if a.config == 4:
+        run_gradients(a)
         return
     import torch
     import torch.distributed as dist
@@ -350,6 +498,23 @@ def main():
     peak_ops = peak_draws_s * THREEFRY_OPS
     inst._check_status(lib, inst.plan())
 
+    # ---- plain path against HBM: 56 B per generated record, 112 B per
+    # record alive at a component's entry, 4 B (die flag) per dead one ----
+    random.seed(1000 + len(plain_ms) - 1)
+    alive, width = plain_alive_counts(lib, plain, n, plain.source.next_seed(), dev)
+    plain_bytes = 56.0 * n + sum(w * (a_ * 112.0 + (n - a_) * 4.0) for a_, w in zip(alive, width))
+    plain_step_s = plain_total_ms / len(plain_ms) / 1000.0
+    hbm_peak = peaks_file().get("hbm_gbs")
+    plain_roof = {"bound": "hbm", "achieved": plain_bytes / plain_step_s / 1e9,
+                  "peak": hbm_peak, "unit": "GB/s",
+                  "frac": (plain_bytes / plain_step_s / 1e9 / hbm_peak) if hbm_peak else None,
+                  "algorithmic_bytes_per_step": plain_bytes,
+                  "alive_at_component_entry": alive,
+                  "peak_source": "measured (copy bandwidth)" if hbm_peak else None}
+
+    # ---- CUDA graphs at small N ----
+    graphs = graph_small_n(lambda: m.Instrument(fn, dev, **kw), tune, dev)
+
     # ---- end to end through the public API ----
     e2e_steps = 0 if a.no_e2e else max(2, a.steps // 2)
     e2e_ms, h2d, d2h = [], 0, 0
@@ -378,11 +543,7 @@ def main():
         cpu = {"value": v, "unit": "histories/s", "cores": threads, "kind": "port",
                "sample": "%d LET-like histories, CPU restatement of the reference kernels "
                          "(reference sequencing), OpenMP, best of 1 after 1 warm-up" % CPU_SAMPLE}
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
-    except OSError:
-        pass
+    peaks = peaks_file()
     line = {
         "metric": "neutron histories/s", "value": value, "unit": "histories/s",
         "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
@@ -390,7 +551,8 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": dict(workload_config(n, world), tune=tune),
         "plain_path": {"value": plain_value, "unit": "histories/s",
-                       "ms_per_step": plain_total_ms / len(plain_ms)},
+                       "ms_per_step": plain_total_ms / len(plain_ms), "roofline": plain_roof},
+        "graph_small_n": graphs,
         "fused_over_plain": value / plain_value,
         "roofline": {"bound": "issue", "achieved": achieved_ops / 1e9, "peak": peak_ops / 1e9,
                      "unit": "Gop/s", "frac": achieved_ops / peak_ops, "traffic": None,

@@ -160,6 +160,10 @@ typedef struct RampRng {
                           sharded chunk keys its neutrons exactly as a
                           single-device run would                         */
   uint32_t reserved;
+  const int32_t* seed_dev;  /* optional (device): when set, the chunk seed
+                          is read here when the kernel runs instead of the
+                          seed argument — what lets a CUDA graph replay
+                          draw a new seed each time (ramp_seed_advance)   */
 } RampRng;
 
 /* One variant of a batched fused launch: its own components (same kinds
@@ -300,6 +304,12 @@ int ramp_adjoint(RampPlan* plan, const RampDiffParam* params, int n_params,
 int ramp_trace_batched_noalloc(RampPlan* plan, const RampVariant* variants,
                                int n_variants, const RampRng* rng,
                                const RampTune* tune, void* stream);
+
+/* Draw the next chunk seed on the device: seed_dev[0] receives a value in
+ * [0, 4096] (the range of the per-chunk randint(0, 4096) seed,
+ * flat_mod.py:32) from a 64-bit LCG whose state is seed_dev[2..3].  For
+ * CUDA graphs: captured after a trace, every replay traces a new chunk.  */
+int ramp_seed_advance(int32_t* seed_dev, void* stream);
 
 /* Debug/test entry points: evaluate the device RNG and math on a vector
  * of inputs (used by the parity tests, not by the chain).                 */

@@ -58,7 +58,8 @@ class RampState(ctypes.Structure):
 
 class RampRng(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("run_seed", ctypes.c_uint32),
-                ("tid_base", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("tid_base", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("seed_dev", ctypes.c_void_p)]
 
 
 class RampVariant(ctypes.Structure):
@@ -129,6 +130,7 @@ _SIGS = {
                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                       ctypes.POINTER(RampRng), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
                      ctypes.c_int),
+    "ramp_seed_advance": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_threefry": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_math": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

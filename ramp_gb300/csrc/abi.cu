@@ -315,6 +315,7 @@ static PlainArgs plain_args(RampPlan* p, const RampState* st, int64_t n, const R
   a.rng.mode = rng ? rng->mode : 0;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = rng ? rng->tid_base : 0u;
+  a.rng.seed_dev = rng ? rng->seed_dev : nullptr;
   a.st = p->status;
   return a;
 }
@@ -498,6 +499,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.rng.mode = rng ? rng->mode : 0;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = rng ? rng->tid_base : 0u;
+  a.rng.seed_dev = rng ? rng->seed_dev : nullptr;
   a.carry_sb = sb_carry;
   a.carry_iidx = iidx_carry;
   a.st = p->status;
@@ -709,12 +711,19 @@ int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det
   a.rng.mode = rng ? rng->mode : 0;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = rng ? rng->tid_base : 0u;
+  a.rng.seed_dev = rng ? rng->seed_dev : nullptr;
   a.grad = grad;
   a.lr = lr;
   a.st = p->status;
   int64_t g = (n + 255) / 256;
   int64_t cap = (int64_t)p->sm_count * 8;
   CK(launch_adjoint(a, (int)(g < cap ? g : cap), s));
+  return RAMP_OK;
+}
+
+int ramp_seed_advance(int32_t* seed_dev, void* stream) {
+  if (!seed_dev) { set_err("ramp_seed_advance: NULL seed"); return RAMP_E_INVALID; }
+  CK(launch_seed_advance(seed_dev, (cudaStream_t)stream));
   return RAMP_OK;
 }
 

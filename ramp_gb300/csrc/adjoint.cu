@@ -20,7 +20,8 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
     AdjDiff dx;
     dx.reset(a.nslot, a.grad, a.lr);
     uint32_t ii = 0;
-    generate<AdjDiff>(a.src, n, 0.0f, a.num_sim, a.seed, r, &dx);
+    generate<AdjDiff>(a.src, n, 0.0f, a.num_sim, a.rng.seed_dev ? *a.rng.seed_dev : a.seed, r,
+                      &dx);
     for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
       const RampBlock B = a.blocks[b];
       if (B.linear) {

@@ -53,7 +53,8 @@ k_fused(const FusedArgs a) {
       V = &a.single;
     }
     const CompDev* __restrict__ comps = V->comps;
-    const int32_t num_sim = V->num_sim, seed = V->seed;
+    const int32_t num_sim = V->num_sim;
+    const int32_t seed = (a.rng.seed_dev && !a.tasks) ? *a.rng.seed_dev : V->seed;
     for (int j = lane; j < count; j += 32) {
       const int64_t i = start + j;
       Nt n;
@@ -84,48 +85,41 @@ static int g_fused_minb = 3;
 void fused_set_min_blocks(int minb) { g_fused_minb = minb < 1 ? 1 : (minb > 4 ? 4 : minb); }
 
 template <int MINB>
-static cudaError_t launch_mb(const FusedArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-  if (a.rng.mode == 0) {
-    cudaFuncSetAttribute(k_fused<MINB, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(RAMP_MAX_COMPS * sizeof(CompDev)));
-    k_fused<MINB, 0><<<grid, block, smem, s>>>(a);
-  } else {
-    cudaFuncSetAttribute(k_fused<MINB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(RAMP_MAX_COMPS * sizeof(CompDev)));
-    k_fused<MINB, 1><<<grid, block, smem, s>>>(a);
-  }
+static cudaError_t launch_mb(const FusedArgs& a, int block, int grid, cudaStream_t s) {
+  if (a.rng.mode == 0) k_fused<MINB, 0><<<grid, block, 0, s>>>(a);
+  else k_fused<MINB, 1><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s) {
   if (a.n_tasks <= 0) return cudaSuccess;
   if (a.n_blocks > FUSED_MAX_BLOCKS || a.n_comps > RAMP_MAX_COMPS) return cudaErrorInvalidValue;
-  size_t smem = (size_t)a.n_comps * sizeof(CompDev);
   switch (g_fused_minb) {
-    case 1: return launch_mb<1>(a, block, grid, smem, s);
-    case 2: return launch_mb<2>(a, block, grid, smem, s);
-    case 4: return launch_mb<4>(a, block, grid, smem, s);
-    default: return launch_mb<3>(a, block, grid, smem, s);
+    case 1: return launch_mb<1>(a, block, grid, s);
+    case 2: return launch_mb<2>(a, block, grid, s);
+    case 4: return launch_mb<4>(a, block, grid, s);
+    default: return launch_mb<3>(a, block, grid, s);
   }
 }
 
 template <int MINB>
-static int occ(int block, size_t smem) {
+static int occ(int block) {
+  static int cached = 0;
+  if (cached > 0) return cached;
   int nb = 0;
-  cudaFuncSetAttribute(k_fused<MINB, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(RAMP_MAX_COMPS * sizeof(CompDev)));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<MINB, 0>, block, smem) !=
-      cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<MINB, 0>, block, 0) !=
+      cudaSuccess || nb <= 0)
     return 1;
-  return nb > 0 ? nb : 1;
+  cached = nb;
+  return nb;
 }
 
 int fused_max_blocks_per_sm(int block, int n_comps) {
-  size_t smem = (size_t)n_comps * sizeof(CompDev);
+  (void)n_comps;
   switch (g_fused_minb) {
-    case 1: return occ<1>(block, smem);
-    case 2: return occ<2>(block, smem);
-    case 4: return occ<4>(block, smem);
-    default: return occ<3>(block, smem);
+    case 1: return occ<1>(block);
+    case 2: return occ<2>(block);
+    case 4: return occ<4>(block);
+    default: return occ<3>(block);
   }
 }

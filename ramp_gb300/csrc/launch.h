@@ -59,6 +59,7 @@ struct AdjointArgs {
 
 cudaError_t launch_adjoint(const AdjointArgs& a, int grid, cudaStream_t s);
 
+cudaError_t launch_seed_advance(int32_t* seed_dev, cudaStream_t s);
 cudaError_t launch_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out,
                                   int64_t n, cudaStream_t s);
 cudaError_t launch_debug_rng_peak(int64_t n, int32_t iters, uint32_t* out, cudaStream_t s);

@@ -73,7 +73,7 @@ k_generate(const __grid_constant__ SrcDev src, const PlainArgs a, int32_t num_si
     Nt n;
     Rng r;
     rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
-    generate(src, n, old_sb, num_sim, seed, r);
+    generate(src, n, old_sb, num_sim, a.rng.seed_dev ? *a.rng.seed_dev : seed, r);
     STORE_ALL(n, S, st, i);
   }
 }
@@ -238,6 +238,19 @@ __global__ void __launch_bounds__(256) k_debug_rng_peak(int32_t iters, uint32_t*
 cudaError_t launch_debug_rng_peak(int64_t n, int32_t iters, uint32_t* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_debug_rng_peak<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(iters, out, n);
+  return cudaGetLastError();
+}
+
+/* next chunk seed in [0, 4096] from a 64-bit LCG (Knuth's MMIX constants) */
+__global__ void k_seed_advance(int32_t* seed_dev) {
+  unsigned long long* st = reinterpret_cast<unsigned long long*>(seed_dev + 2);
+  unsigned long long x = *st * 6364136223846793005ull + 1442695040888963407ull;
+  *st = x;
+  seed_dev[0] = (int32_t)((x >> 33) % 4097ull);
+}
+
+cudaError_t launch_seed_advance(int32_t* seed_dev, cudaStream_t s) {
+  k_seed_advance<<<1, 1, 0, s>>>(seed_dev);
   return cudaGetLastError();
 }
 

@@ -56,6 +56,7 @@ struct RngDev {
   uint32_t run_seed;
   uint32_t tid_base;
   uint32_t pad;
+  const int32_t* seed_dev;   /* when set, the chunk seed is read here */
 };
 
 /* Device status block owned by a plan. */

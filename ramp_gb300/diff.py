@@ -92,6 +92,7 @@ class DiffChain:
             _abi.check(lib, lib.ramp_plan_set_param(plan, kind, j, float(np.float32(v * scale))),
                        "ramp_plan_set_param")
         self._theta = theta
+        self.inst._param_epoch = getattr(self.inst, "_param_epoch", 0) + 1
 
     def forward(self, n, seed, rng="reference"):
         """The detector histogram (flat, float32, device) of n histories at
@@ -99,7 +100,7 @@ class DiffChain:
         lib = self.inst._lib()
         plan = self.inst.plan()
         self.inst.reset_tallies()
-        rngd = _abi.RampRng({"reference": 0, "native": 1}[rng], 0, 0, 0)
+        rngd = _abi.RampRng({"reference": 0, "native": 1}[rng], 0, 0, 0, None)
         with torch.cuda.device(self.inst.device):
             stream = self.inst._stream_ptr()
             _abi.check(lib, lib.ramp_trace_fused(plan, int(n), int(n), int(seed),

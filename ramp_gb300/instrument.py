@@ -398,6 +398,14 @@ class Instrument:
                 self.last_chunk = nloc
             self._check_status(lib, plan)
 
+    def capture(self, N, path="fused", rng="reference", run_seed=0, tune=None, chunk=None,
+                state=None):
+        """``execute(N, ...)`` captured as a CUDA graph whose replays draw
+        their chunk seeds on the device (ramp_gb300.graph.capture)."""
+        from .graph import capture
+        return capture(self, N, path=path, rng=rng, run_seed=run_seed, tune=tune, chunk=chunk,
+                       state=state)
+
     def _check_status(self, lib, plan):
         flags = _abi.ctypes.c_uint32()
         oob = _abi.ctypes.c_uint64()
