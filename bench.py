@@ -307,47 +307,6 @@ def run_gradients(a, n=10_000_000):
 
 
 # ---------------------------------------------------------------- GPU arm
-def plain_alive_counts(lib, inst, n, seed, dev):
-    """Histories alive at the entry of each component of a plain-path
-    chunk: the chain is re-planned with one linear block per component and
-    stepped block by block (ramp_generate, ramp_run_block), counting live
-    records in between.  Returns (alive per component, components per
-    block entry)."""
-    import torch
-    from ramp_gb300 import _abi
-    ct = _abi.ctypes
-    keep = []
-    src, carr, nc, barr, nb = inst.descriptors(keep)
-    blocks = []
-    for k in range(nb):
-        b = barr[k]
-        if b.linear:
-            blocks += [_abi.RampBlock(j, 1, 1, b.multi) for j in range(b.first, b.first + b.count)]
-        else:
-            blocks.append(_abi.RampBlock(b.first, b.count, 0, b.multi))
-    barr2 = (_abi.RampBlock * len(blocks))(*blocks)
-    plan = ct.c_void_p()
-    _abi.check(lib, lib.ramp_plan_create(ct.byref(src), carr, nc, barr2, len(blocks),
-                                         ct.byref(plan)), "ramp_plan_create")
-    try:
-        st = inst._alloc_state(n)
-        rng = _abi.RampRng()
-        stream = ct.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
-        _abi.check(lib, lib.ramp_generate(plan, ct.byref(st), n, n, seed, ct.byref(rng), stream),
-                   "ramp_generate")
-        die = inst.state[_abi.LANE["die"], :n]
-        alive, width = [], []
-        for b in range(len(blocks)):
-            alive.append(int((die == 0).sum()))
-            width.append(blocks[b].count)
-            _abi.check(lib, lib.ramp_run_block(plan, b, ct.byref(st), n, ct.byref(rng), stream),
-                       "ramp_run_block")
-        torch.cuda.synchronize(dev)
-    finally:
-        lib.ramp_plan_destroy(plan)
-    return alive, width
-
-
 def graph_small_n(inst_factory, tune, dev, sizes=(100_000, 1_000_000), reps=20):
     """ms per execute() at small N, eager against a CUDA-graph replay of the
     same trace (ramp_gb300.graph), for both paths."""
@@ -473,8 +432,7 @@ def main():
         random.seed(1000 + len(plain_ms) - 1)
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         rngd = _abi.RampRng()
-        tuned = _abi.RampTune(*[int((tune or {}).get(k, 0)) for k in
-                                ("block", "blocks_per_sm", "chunk", "privatize")])
+        tuned = _abi.tune_struct(tune or {})
         s.record(stream)
         rc = lib.ramp_trace_fused(inst.plan(), plain.last_chunk, plain.last_chunk, seed_last,
                                   _abi.ctypes.byref(rngd), None, None, _abi.ctypes.byref(tuned),
@@ -501,8 +459,9 @@ def main():
     # ---- plain path against HBM: 56 B per generated record, 112 B per
     # record alive at a component's entry, 4 B (die flag) per dead one ----
     random.seed(1000 + len(plain_ms) - 1)
-    alive, width = plain_alive_counts(lib, plain, n, plain.source.next_seed(), dev)
-    plain_bytes = 56.0 * n + sum(w * (a_ * 112.0 + (n - a_) * 4.0) for a_, w in zip(alive, width))
+    from ramp_gb300.autotune import survival
+    alive = survival(plain, n, "reference", plain.source.next_seed())
+    plain_bytes = 56.0 * n + sum(a_ * 112.0 + (n - a_) * 4.0 for a_ in alive if a_ is not None)
     plain_step_s = plain_total_ms / len(plain_ms) / 1000.0
     hbm_peak = peaks_file().get("hbm_gbs")
     plain_roof = {"bound": "hbm", "achieved": plain_bytes / plain_step_s / 1e9,

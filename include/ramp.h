@@ -183,6 +183,10 @@ typedef struct RampTune {
   int32_t blocks_per_sm;        /* persistent CTAs per SM                */
   int32_t chunk;                /* neutrons claimed per work-queue grab  */
   int32_t privatize;            /* 1: shared-memory tally privatisation  */
+  int32_t split;                /* fused path: compact the survivors into
+                                   full warps before this component (0:
+                                   off; must not fall inside a non-linear
+                                   block)                                */
 } RampTune;
 
 typedef struct RampPlan RampPlan;
@@ -204,7 +208,8 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps,
 int ramp_plan_destroy(RampPlan* plan);
 
 /* Read and clear the plan's device status flags (RAMP_F_*) and the count
- * of tally writes that fell outside their buffers.  Synchronises.         */
+ * of nonzero-weight tally writes that fell outside their buffers (a write
+ * of weight zero loses nothing and is not counted).  Synchronises.       */
 int ramp_plan_status(RampPlan* plan, uint32_t* flags, uint64_t* oob_drops);
 
 /* Moderator pass over neutrons [0, n): replaces gen_prg
@@ -234,7 +239,10 @@ int ramp_trace_plain(RampPlan* plan, const RampState* st, int64_t n,
  * execute()) hold per index the final RNG counter and index-buffer value
  * of the previous chunk and receive this chunk's; they are what makes
  * multi-chunk runs reproduce the reference keying (flat_mod.cl:19) with
- * nothing else of the neutron state in memory.                           */
+ * nothing else of the neutron state in memory.  Without carry buffers only
+ * the tallies are observable, and a neutron whose weight becomes exactly
+ * zero is retired at once (every later weight factor multiplies it and
+ * every tally adds p or p^2, so it could only add zeros).               */
 int ramp_trace_fused(RampPlan* plan, int64_t n, int32_t num_sim,
                      int32_t seed, const RampRng* rng, float* sb_carry,
                      uint32_t* iidx_carry, const RampTune* tune,

@@ -975,7 +975,7 @@ void s_det1d(const Ctx& c, int64_t, float* n, float* s, uint32_t* iidx, const Ra
     if ((int64_t)idx < nb && k.tally) {
       atomic_add_f(&k.tally[idx], n[P]);
       atomic_add_f(&k.tally_err[idx], n[P] * n[P]);
-    } else {
+    } else if (n[P] != 0.0f) {
       c.oob->fetch_add(1);
     }
   }
@@ -1030,7 +1030,7 @@ void s_det2d(const Ctx& c, int64_t, float* n, float* s, uint32_t* iidx, const Ra
     if (flat >= 0 && flat < k.tally_len && k.tally) {
       atomic_add_f(&k.tally[flat], n[P]);
       atomic_add_f(&k.tally_err[flat], n[P] * n[P]);
-    } else {
+    } else if (n[P] != 0.0f) {
       c.oob->fetch_add(1);
     }
   }

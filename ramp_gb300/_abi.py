@@ -78,7 +78,19 @@ DP_GUIDE_R0, DP_GUIDE_QC, DP_GUIDE_ALPHA, DP_GUIDE_M, DP_GUIDE_W, DP_SOURCE_T, \
 
 class RampTune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("chunk", ctypes.c_int32), ("privatize", ctypes.c_int32)]
+                ("chunk", ctypes.c_int32), ("privatize", ctypes.c_int32),
+                ("split", ctypes.c_int32)]
+
+
+TUNE_KEYS = ("block", "blocks_per_sm", "chunk", "privatize", "split")
+
+
+def tune_struct(tune):
+    """RampTune from a dict of launch settings (missing keys: 0 = default)."""
+    unknown = set(tune) - set(TUNE_KEYS)
+    if unknown:
+        raise ValueError("unknown launch settings: %s" % sorted(unknown))
+    return RampTune(*[int(tune.get(k, 0)) for k in TUNE_KEYS])
 
 
 def set_table(comp, slot, arr, keep):

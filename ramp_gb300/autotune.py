@@ -3,8 +3,11 @@
 The fused kernel's result does not depend on its launch configuration (the
 RNG is counter-based and keyed by neutron index), so the configuration can
 be chosen purely for speed.  ``tune(inst)`` times short fused runs of the
-instrument over the candidates (register cap = minimum CTAs per SM, and
-the span of neutrons a task covers) and keeps the fastest; results are
+instrument over the candidates (register cap = minimum CTAs per SM, the
+span of neutrons a task covers, and whether survivors are compacted into
+full warps before the first component that less than half of the
+histories reach — found by a plain-path pilot, ``survival``) and keeps the
+fastest; results are
 cached in a JSON file keyed by GPU name, the instrument's component
 structure and the keying mode.  Tuning uses fixed seeds and restores the
 instrument's tallies afterwards: it leaves no trace in the results or in
@@ -21,7 +24,7 @@ import torch
 
 from . import _abi
 
-CANDIDATES = [dict(blocks_per_sm=b, chunk=c) for b in (2, 3, 4) for c in (0, 4096, 16384)]
+CANDIDATES = [dict(blocks_per_sm=b, chunk=c) for b in (3, 4) for c in (0, 4096)]
 
 
 def cache_path():
@@ -55,8 +58,76 @@ def _save(cache):
     os.replace(tmp, p)
 
 
+def survival(inst, n=1_000_000, rng="reference", seed=17):
+    """Histories alive at the entry of each component, out of n traced on
+    the plain path with the chain re-planned as one block per linear
+    component (ramp_generate, then ramp_run_block block by block, counting
+    live records in between).  Entry i belongs to component i; components
+    inside a non-linear block after its first get None.  Adds the pilot's
+    histories to the instrument's tallies (callers restore them)."""
+    ct = ctypes
+    lib = inst._lib()
+    keep = []
+    src, carr, nc, barr, nb = inst.descriptors(keep)
+    blocks, first_of = [], []
+    for k in range(nb):
+        b = barr[k]
+        if b.linear:
+            for j in range(b.first, b.first + b.count):
+                blocks.append(_abi.RampBlock(j, 1, 1, b.multi))
+                first_of.append(j)
+        else:
+            blocks.append(_abi.RampBlock(b.first, b.count, 0, b.multi))
+            first_of.append(b.first)
+    barr2 = (_abi.RampBlock * max(1, len(blocks)))(*blocks)
+    plan = ct.c_void_p()
+    _abi.check(lib, lib.ramp_plan_create(ct.byref(src), carr, nc, barr2, len(blocks),
+                                         ct.byref(plan)), "ramp_plan_create")
+    alive = [None] * nc
+    try:
+        dev = inst.device
+        stride = (n + 31) // 32 * 32
+        soa = torch.zeros((_abi.NLANES, stride), dtype=torch.float32, device=dev)
+        iidx = torch.zeros(stride, dtype=torch.int32, device=dev)
+        st = _abi.RampState()
+        st.soa, st.iidx, st.stride = soa.data_ptr(), iidx.data_ptr(), stride
+        rngd = _abi.RampRng({"reference": 0, "native": 1}[rng], 0, 0, 0)
+        with torch.cuda.device(dev):
+            stream = ct.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+            _abi.check(lib, lib.ramp_generate(plan, ct.byref(st), n, n, seed, ct.byref(rngd),
+                                              stream), "ramp_generate")
+            die = soa[_abi.LANE["die"], :n]
+            for b in range(len(blocks)):
+                alive[first_of[b]] = int((die == 0).sum())
+                _abi.check(lib, lib.ramp_run_block(plan, b, ct.byref(st), n, ct.byref(rngd),
+                                                   stream), "ramp_run_block")
+            torch.cuda.synchronize(dev)
+            flags, oob = ct.c_uint32(), ct.c_uint64()
+            lib.ramp_plan_status(plan, ct.byref(flags), ct.byref(oob))
+    finally:
+        lib.ramp_plan_destroy(plan)
+    return alive
+
+
+def split_point(inst, alive, threshold=0.5):
+    """First component at whose entry fewer than ``threshold`` of the
+    histories are alive (a valid compaction point), or 0."""
+    _, _, nc, barr, nb = inst.descriptors([])
+    inside = set()
+    for k in range(nb):
+        if not barr[k].linear:
+            inside.update(range(barr[k].first + 1, barr[k].first + barr[k].count))
+    n0 = alive[0] if alive and alive[0] else 0
+    for k in range(1, nc):
+        if k in inside or alive[k] is None:
+            continue
+        if n0 and alive[k] < threshold * n0:
+            return k
+    return 0
+
+
 def _time_config(lib, plan, n, rng, cfg, stream, reps=2):
-    tune = _abi.RampTune(0, int(cfg.get("blocks_per_sm", 0)), int(cfg.get("chunk", 0)), 0)
+    tune = _abi.tune_struct(cfg)
     best = None
     for r in range(reps + 1):
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -85,9 +156,13 @@ def tune(inst, n_probe=2_000_000, rng="reference", candidates=None, force=False)
     saved = [t.clone() for t in inst.tallies()]
     rngd = _abi.RampRng({"reference": 0, "native": 1}[rng], 0, 0, 0)
     results = []
+    split = 0
+    if candidates is None:
+        split = split_point(inst, survival(inst, min(n_probe, 1_000_000), rng))
+        candidates = [dict(c, split=k) for c in CANDIDATES for k in ((0, split) if split else (0,))]
     with torch.cuda.device(inst.device):
         stream = torch.cuda.current_stream(inst.device)
-        for cfg in (candidates or CANDIDATES):
+        for cfg in candidates:
             results.append((_time_config(lib, plan, n_probe, rngd, cfg, stream), cfg))
         torch.cuda.synchronize(inst.device)
         for t, s in zip(inst.tallies(), saved):
@@ -95,7 +170,7 @@ def tune(inst, n_probe=2_000_000, rng="reference", candidates=None, force=False)
         inst._check_status(lib, plan)
     results.sort(key=lambda x: x[0])
     best = results[0][1]
-    cache[key] = {"config": best, "ms": results[0][0], "n_probe": n_probe,
+    cache[key] = {"config": best, "ms": results[0][0], "n_probe": n_probe, "split_candidate": split,
                   "all": [[ms, c] for ms, c in results]}
     _save(cache)
     return dict(best)

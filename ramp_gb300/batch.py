@@ -66,8 +66,7 @@ class BatchedInstrument:
         rngd.run_seed = int(run_seed) & 0xffffffff
         tuned = None
         if tune is not None:
-            tuned = _abi.RampTune(*[int(tune.get(k, 0)) for k in
-                                    ("block", "blocks_per_sm", "chunk", "privatize")])
+            tuned = _abi.tune_struct(tune)
         with torch.cuda.device(self.device):
             stream = base._stream_ptr()
             rc = lib.ramp_trace_batched(plan, variants, nv, ctypes.byref(rngd),

@@ -19,9 +19,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libramp_cuda.so")
 
-CU_SOURCES = ["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
+CU_SOURCES = ["plain.cu", "fused.cu", "fused_3r.cu", "fused_3n.cu", "fused_4r.cu", "fused_4n.cu",
+              "adjoint.cu", "abi.cu"]
 CPP_SOURCES = ["bvh.cpp"]
-HEADERS = ["device.cuh", "mesh.cuh", "plan.h", "launch.h", "rmath.h", "rconst.h", "bvh.h",
+HEADERS = ["device.cuh", "fused_kernel.cuh", "mesh.cuh", "plan.h", "launch.h", "rmath.h", "rconst.h", "bvh.h",
            os.path.join("..", "..", "include", "ramp.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

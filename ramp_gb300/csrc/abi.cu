@@ -454,6 +454,25 @@ static void tune_defaults(RampPlan* p, const RampTune* tune, int& block, int& gr
   task = (tune && tune->chunk > 0) ? tune->chunk : 0;   /* 0: auto_task() */
 }
 
+/* survivor-compaction point of a fused launch (RampTune.split): a
+ * component index in [0, n_comps) not strictly inside a non-linear block */
+static int tune_split(const RampPlan* p, const RampTune* tune, int32_t* out) {
+  *out = 0;
+  if (!tune || tune->split <= 0) return RAMP_OK;
+  const int k = tune->split;
+  if (k >= (int)p->comps.size()) {
+    set_err("RampTune.split %d: the chain has %d components", k, (int)p->comps.size());
+    return RAMP_E_INVALID;
+  }
+  for (const RampBlock& B : p->blocks)
+    if (!B.linear && B.first < k && k < B.first + B.count) {
+      set_err("RampTune.split %d falls inside a non-linear block", k);
+      return RAMP_E_INVALID;
+    }
+  *out = k;
+  return RAMP_OK;
+}
+
 /* span size for n histories: about eight spans per resident CTA, in
  * multiples of 1024 neutrons, between 1024 and 65536 */
 static int64_t auto_task(int64_t n, int grid, int64_t task) {
@@ -503,6 +522,8 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.carry_sb = sb_carry;
   a.carry_iidx = iidx_carry;
   a.st = p->status;
+  int rc = tune_split(p, tune, &a.split);
+  if (rc) return rc;
   CK(cudaMemsetAsync(&p->status->workq, 0, sizeof(unsigned long long), s));
   CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
   return RAMP_OK;
@@ -616,6 +637,8 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;   /* variants key by their own index */
   a.st = p->status;
+  int rc = tune_split(p, tune, &a.split);
+  if (rc) return rc;
   CK(cudaMemsetAsync(&p->status->workq, 0, sizeof(unsigned long long), s));
   CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
   return RAMP_OK;
@@ -956,6 +979,8 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;
   a.st = &D->status;
+  int rc = tune_split(p, tune, &a.split);
+  if (rc) return rc;
   CK(launch_fused(a, block, fused_grid(n_tasks, grid), s));
   return RAMP_OK;
 }

@@ -22,12 +22,14 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
     uint32_t ii = 0;
     generate<AdjDiff>(a.src, n, 0.0f, a.num_sim, a.rng.seed_dev ? *a.rng.seed_dev : a.seed, r,
                       &dx);
+    /* a zero-weight neutron contributes dL/dH * p * dlog p = 0: retired */
+    if (n.p == 0.0f) n.die = 1.0f;
     for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
       const RampBlock B = a.blocks[b];
       if (B.linear) {
         for (int k = B.first; k < B.first + B.count; ++k) {
           if (n.die > 0.f) break;
-          comp_linear<AdjDiff>(a.comps[k], n, ii, r, a.st, &dx);
+          comp_linear<AdjDiff>(a.comps[k], n, ii, r, a.st, &dx, true);
         }
       } else {
         block_nonlinear<AdjDiff>(a.comps, B.first, B.count, B.multi, n, ii, r, a.st, &dx);

@@ -559,7 +559,8 @@ DI void guide_dlogR(const CompDev& c, float q, float R, D* dx) {
 
 /* guide.cl:9-149 */
 template <class D = NoDiff>
-DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* dx = nullptr) {
+DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* dx = nullptr,
+                const bool zx = false) {
   const float l = c.sp[4], R0 = c.sp[5];
   const uint32_t max_bounces = (uint32_t)c.si[0];
   const float ww = c.aux[0], hh = c.aux[1], Av = c.aux[2], Ah = c.aux[3];
@@ -601,6 +602,10 @@ DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
     float refl = reflectivity_pre(q, c.aux, R0);
     n.p *= refl;
     if (refl < 1e-12f || refl > 1.0f) n.p = 0.0f;
+    if (zx && n.p == 0.0f) {   /* retire: it can only add zeros from here */
+      set_die(n, 1.0f);
+      return;
+    }
     if constexpr (D::on) {
       if (n.p != 0.0f) guide_dlogR(c, q, refl, dx);
     }
@@ -870,7 +875,7 @@ DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
         tally_add(c.tally, c.tally_err, idx, n.p);
       }
     } else if constexpr (!D::on) {
-      atomicAdd(&st->oob, 1ull);
+      if (n.p != 0.0f) atomicAdd(&st->oob, 1ull);   /* a nonzero weight was lost */
     }
   }
   if (restore == 0) {
@@ -919,7 +924,7 @@ DI void s_det2d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
         tally_add(c.tally, c.tally_err, flat, n.p);
       }
     } else if constexpr (!D::on) {
-      atomicAdd(&st->oob, 1ull);
+      if (n.p != 0.0f) atomicAdd(&st->oob, 1ull);   /* a nonzero weight was lost */
     }
   }
   if (c.si[4] == 0) {
@@ -941,10 +946,10 @@ DI void s_attenuate(const CompDev& c, Nt& n, Is& s, uint32_t& ii) {
 
 template <class D = NoDiff>
 DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st,
-                D* dx = nullptr) {
+                D* dx = nullptr, const bool zx = false) {
   switch (c.scat) {
     case RAMP_S_ARM: ii = c.idx; is_reset(s); break;
-    case RAMP_S_GUIDE: s_guide<D>(c, n, s, ii, st, dx); break;
+    case RAMP_S_GUIDE: s_guide<D>(c, n, s, ii, st, dx, zx); break;
     case RAMP_S_CHOPPER: s_chopper(c, n, s, ii, r); break;
     case RAMP_S_ISOTROPIC: s_isotropic(c, n, s, ii, r); break;
     case RAMP_S_POWDERN: s_powdern<D>(c, n, s, ii, r, st, dx); break;
@@ -968,14 +973,18 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
 /* ------------------------------------------------------------------ */
 template <class D = NoDiff>
 DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st,
-                    D* dx = nullptr) {
+                    D* dx = nullptr, const bool zx = false) {
   transform(c, n);
   Is s;
   is_reset(s);
   if (intersect(c, n, s, st)) ii = c.idx;
   /* terminate.cl:16-18 */
   if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
-  if (ii == c.idx && !(n.die > 0.f)) scatter<D>(c, n, s, ii, r, st, dx);
+  if (ii == c.idx && !(n.die > 0.f)) scatter<D>(c, n, s, ii, r, st, dx, zx);
+  if (zx && n.p == 0.0f) {
+    set_die(n, 1.0f);
+    return;
+  }
   if (!(n.die > 0.f)) untransform(c, n);
 }
 

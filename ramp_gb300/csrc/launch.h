@@ -36,6 +36,8 @@ struct FusedArgs {
   float* carry_sb;              /* optional, single variant */
   uint32_t* carry_iidx;
   StatusDev* st;
+  int32_t split;                /* survivor compaction before this component; 0: off */
+  int32_t pad;
 };
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s);

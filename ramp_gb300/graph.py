@@ -113,8 +113,7 @@ def capture(inst, N, path="fused", rng="reference", run_seed=0, tune=None, chunk
             from . import autotune
             tune = autotune.tune(inst, rng=rng)
     if tune is not None:
-        tuned = _abi.RampTune(*[int(tune.get(k, 0)) for k in
-                                ("block", "blocks_per_sm", "chunk", "privatize")])
+        tuned = _abi.tune_struct(tune)
     dev = inst.device
     first = min(N, buf_max)
     with torch.cuda.device(dev):

@@ -341,8 +341,7 @@ class Instrument:
                 from . import autotune
                 tune = autotune.tune(self, rng=rng)
         if tune is not None:
-            tuned = _abi.RampTune(*[int(tune.get(k, 0)) for k in
-                                    ("block", "blocks_per_sm", "chunk", "privatize")])
+            tuned = _abi.tune_struct(tune)
         if trace:
             warnings.warn("trace=True (visualisation lines) is not supported; ignored")
         rank, world = shard if shard is not None else (0, 1)

@@ -74,7 +74,9 @@ def test_likelihood_ratio_terms_only_touch_branching_parameters(problem):
     g1, _ = adjoint_grad(chain, theta0, Ht, seed=5, lr=True)
     k = chain.names.index("sample.sigma_abs")
     others = [j for j in range(len(g0)) if j != k]
-    assert torch.allclose(g0[others], g1[others], rtol=1e-9, atol=0)
+    # the same per-neutron terms summed by double atomics in another order
+    assert torch.allclose(g0[others], g1[others], rtol=1e-9,
+                          atol=1e-12 * float(g0.abs().max()))
     assert g0[k] != g1[k]
 
 

@@ -69,10 +69,10 @@ class _Host:
         return self._t
 
 
-def pair(fn, kw, N, path="plain", rng="reference", chunk=None, seed=1234):
+def pair(fn, kw, N, path="plain", rng="reference", chunk=None, seed=1234, tune=None):
     gi = m.Instrument(fn, "cuda", **kw)
     random.seed(seed)
-    gi.execute(N, path=path, rng=rng, chunk=chunk)
+    gi.execute(N, path=path, rng=rng, chunk=chunk, tune=tune)
     torch.cuda.synchronize()
     ci = m.Instrument(fn, "cpu", **kw)
     random.seed(seed)
@@ -223,6 +223,74 @@ def test_batched_variants_match_single_runs(cuda_lib):
             ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
             oracle.run(ci, n, rng_mode=mode, variant=v, seeds=[seed])
             tallies_close(B.instruments[v], ci)
+
+
+# ------------------------------------------------- survivor compaction
+@pytest.mark.parametrize("fn,kw,N,split,rng", [
+    ("small_chain.json", "small", 300_000, 1, "reference"),
+    ("small_chain.json", "small", 300_000, 2, "native"),
+    ("let_like.json", "let", 1_000_000, 2, "reference"),
+    ("let_like.json", "let", 1_000_000, 5, "native"),
+    ("mesh_imaging.json", "mesh", 20_000, 1, "reference")])
+def test_fused_split_matches_oracle(cuda_lib, fn, kw, N, split, rng):
+    """Compacting survivors into full warps changes only the order in
+    which neutrons are traced."""
+    kws = {"small": I.small_chain_kwargs(), "let": I.let_like_kwargs(),
+           "mesh": I.mesh_imaging_kwargs(0.37)}[kw]
+    gi, ci, r = pair(I.path(fn), kws, N, path="fused", rng=rng, tune={"split": split})
+    tallies_close(gi, ci)
+    assert gi.oob_drops == r.oob
+
+
+@pytest.mark.parametrize("split", [1, 4])
+def test_fused_split_at_nonlinear_block_boundaries(cuda_lib, split):
+    gi, ci, r = pair(os.path.join(GOLD_DIR, "nonlinear_env.json"), I.small_chain_kwargs(),
+                     200_000, path="fused", tune={"split": split})
+    tallies_close(gi, ci)
+
+
+def test_fused_split_inside_nonlinear_block_is_refused(cuda_lib):
+    gi = m.Instrument(os.path.join(GOLD_DIR, "nonlinear_env.json"), "cuda",
+                      **I.small_chain_kwargs())
+    with pytest.raises(RuntimeError, match="non-linear block"):
+        gi.execute(1000, path="fused", tune={"split": 2})
+    with pytest.raises(RuntimeError, match="components"):
+        gi.execute(1000, path="fused", tune={"split": 99})
+
+
+def test_fused_split_with_multi_chunk_carry(cuda_lib):
+    """Carry buffers are written when each neutron finishes, parked or not."""
+    gi, ci, r = pair(I.path("let_like.json"), I.let_like_kwargs(), 250_001, path="fused",
+                     chunk=100_000, tune={"split": 2})
+    tallies_close(gi, ci)
+
+
+def test_batched_split_matches_single_runs(cuda_lib):
+    """Parked survivors of different variants share a warp in stage B."""
+    variants = [I.let_like_kwargs(Ei=3.7), I.let_like_kwargs(Ei=8.0), I.let_like_kwargs(Ei=2.5)]
+    counts = [300_000, 123_457, 200_003]
+    B = BatchedInstrument(I.path("let_like.json"), variants, ctx="cuda")
+    B.execute(counts, rng="native", seeds=[11, 2222, 4000], tune={"split": 2, "chunk": 4096})
+    torch.cuda.synchronize()
+    for v, (kw, n, seed) in enumerate(zip(variants, counts, [11, 2222, 4000])):
+        ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
+        oracle.run(ci, n, rng_mode=1, variant=v, seeds=[seed])
+        tallies_close(B.instruments[v], ci)
+
+
+def test_autotune_survival_and_split_point(cuda_lib, tmp_path, monkeypatch):
+    from ramp_gb300 import autotune
+    monkeypatch.setenv("RAMP_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    inst = m.Instrument(I.path("let_like.json"), "cuda", **I.let_like_kwargs())
+    alive = autotune.survival(inst, 200_000)
+    assert alive[0] == 200_000 and all(a >= b for a, b in zip(alive, alive[1:]))
+    # the first chopper passes a few per cent: compaction goes before the second
+    assert autotune.split_point(inst, alive) == 2
+    before = [t.clone() for t in inst.tallies()]
+    cfg = autotune.tune(inst, n_probe=200_000)
+    assert set(cfg) <= set(("blocks_per_sm", "chunk", "split"))
+    for t, b in zip(inst.tallies(), before):
+        assert torch.equal(t, b)
 
 
 # ---------------------------------------------------------------- status
