@@ -183,10 +183,14 @@ typedef struct RampTune {
   int32_t blocks_per_sm;        /* persistent CTAs per SM                */
   int32_t chunk;                /* neutrons claimed per work-queue grab  */
   int32_t privatize;            /* 1: shared-memory tally privatisation  */
-  int32_t split;                /* fused path: compact the survivors into
-                                   full warps before this component (0:
-                                   off; must not fall inside a non-linear
-                                   block)                                */
+  int32_t split;                /* fused path: split the chain before this
+                                   component (0: off; not inside a
+                                   non-linear block).  Stage A appends the
+                                   neutrons alive there to a survivor
+                                   buffer in HBM (about 72 B per history of the
+                                   launch, owned by the plan) and stage B
+                                   traces them 32 to a warp.  Ignored by
+                                   ramp_trace_batched_noalloc.           */
 } RampTune;
 
 typedef struct RampPlan RampPlan;
@@ -206,6 +210,11 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps,
                      int n_comps, const RampBlock* blocks, int n_blocks,
                      RampPlan** out);
 int ramp_plan_destroy(RampPlan* plan);
+
+/* Allocate the plan's survivor buffer for split fused launches
+ * (RampTune.split) of up to n histories now, e.g. before capturing them
+ * in a CUDA graph (a split launch otherwise grows it on first use).    */
+int ramp_plan_reserve(RampPlan* plan, int64_t n);
 
 /* Read and clear the plan's device status flags (RAMP_F_*) and the count
  * of nonzero-weight tally writes that fell outside their buffers (a write

@@ -143,6 +143,7 @@ _SIGS = {
                       ctypes.POINTER(RampRng), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
                      ctypes.c_int),
     "ramp_seed_advance": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "ramp_plan_reserve": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
     "ramp_debug_threefry": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_math": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

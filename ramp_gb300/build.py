@@ -19,8 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libramp_cuda.so")
 
-CU_SOURCES = ["plain.cu", "fused.cu", "fused_3r.cu", "fused_3n.cu", "fused_4r.cu", "fused_4n.cu",
-              "adjoint.cu", "abi.cu"]
+CU_SOURCES = (["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
+              + ["fused_%d%s%s.cu" % (mb, m, b) for mb in (3, 4) for m in "rn" for b in "sb"])
 CPP_SOURCES = ["bvh.cpp"]
 HEADERS = ["device.cuh", "fused_kernel.cuh", "mesh.cuh", "plan.h", "launch.h", "rmath.h", "rconst.h", "bvh.h",
            os.path.join("..", "..", "include", "ramp.h")]

@@ -72,6 +72,8 @@ struct RampPlan {
   std::map<TabKey, std::pair<void*, void*>> tabs;
   std::vector<CompDev> adj_host;     /* descriptors of the last adjoint   */
   CompDev* adj_dev = nullptr;
+  uint32_t* surv = nullptr;          /* survivor buffer of split launches */
+  int64_t surv_cap = 0;              /* slots (128 per work item) */
 };
 
 /* ---------------------------------------------------------------------- */
@@ -336,6 +338,7 @@ int ramp_plan_destroy(RampPlan* p) {
   if (p->batch.comps_dev) cudaFree(p->batch.comps_dev);
   if (p->batch.vars_dev) cudaFree(p->batch.vars_dev);
   if (p->batch.tasks_dev) cudaFree(p->batch.tasks_dev);
+  if (p->surv) cudaFree(p->surv);
   delete p;
   return RAMP_OK;
 }
@@ -473,6 +476,43 @@ static int tune_split(const RampPlan* p, const RampTune* tune, int32_t* out) {
   return RAMP_OK;
 }
 
+/* survivor buffer for split launches covering up to n_items work items
+ * of 128 neutrons: SURV_WORDS words per slot plus one count per item
+ * (grows, never shrinks) */
+static int ensure_surv(RampPlan* p, int64_t n_items) {
+  const int64_t slots = n_items * 128;
+  if (slots <= p->surv_cap) return RAMP_OK;
+  if (p->surv) { cudaFree(p->surv); p->surv = nullptr; p->surv_cap = 0; }
+  void* d = nullptr;
+  const size_t bytes = ((size_t)slots * SURV_WORDS + (size_t)n_items) * sizeof(uint32_t);
+  cudaError_t e = cudaMalloc(&d, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_err("survivor buffer for %lld histories: %s", (long long)slots, cudaGetErrorString(e));
+    return RAMP_E_NOMEM;
+  }
+  p->surv = (uint32_t*)d;
+  p->surv_cap = slots;
+  return RAMP_OK;
+}
+
+/* wire a split launch of n_items work items to the survivor buffer */
+static int attach_surv(RampPlan* p, FusedArgs& a, int64_t n_items, cudaStream_t s) {
+  int rc = ensure_surv(p, n_items);
+  if (rc) return rc;
+  a.surv = p->surv;
+  a.surv_cap = p->surv_cap;
+  a.surv_cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS;
+  a.surv_items = n_items;
+  CK(cudaMemsetAsync(a.surv_cnt, 0, (size_t)n_items * sizeof(uint32_t), s));
+  return RAMP_OK;
+}
+
+int ramp_plan_reserve(RampPlan* p, int64_t n) {
+  if (!p || n < 0) { set_err("ramp_plan_reserve: bad arguments"); return RAMP_E_INVALID; }
+  return ensure_surv(p, (n + 127) / 128);
+}
+
 /* span size for n histories: about eight spans per resident CTA, in
  * multiples of 1024 neutrons, between 1024 and 65536 */
 static int64_t auto_task(int64_t n, int grid, int64_t task) {
@@ -524,7 +564,11 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.st = p->status;
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
-  CK(cudaMemsetAsync(&p->status->workq, 0, sizeof(unsigned long long), s));
+  if (a.split > 0) {
+    rc = attach_surv(p, a, (n + 127) / 128, s);
+    if (rc) return rc;
+  }
+  CK(cudaMemsetAsync(&p->status->workq, 0, 3 * sizeof(unsigned long long), s));
   CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
   return RAMP_OK;
 }
@@ -639,7 +683,11 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.st = p->status;
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
-  CK(cudaMemsetAsync(&p->status->workq, 0, sizeof(unsigned long long), s));
+  if (a.split > 0) {
+    rc = attach_surv(p, a, a.n_tasks * ((task + 127) / 128), s);
+    if (rc) return rc;
+  }
+  CK(cudaMemsetAsync(&p->status->workq, 0, 3 * sizeof(unsigned long long), s));
   CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
   return RAMP_OK;
 }
@@ -979,8 +1027,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;
   a.st = &D->status;
-  int rc = tune_split(p, tune, &a.split);
-  if (rc) return rc;
+  /* no survivor split here: it would need a buffer sized by the call */
   CK(launch_fused(a, block, fused_grid(n_tasks, grid), s));
   return RAMP_OK;
 }

@@ -1,0 +1,5 @@
+/* fused kernel instantiations: register cap 3 CTAs per SM, native keying,
+ * batched variants (one translation unit each, so they compile in parallel) */
+#include "fused_kernel.cuh"
+
+template cudaError_t launch_fk<3, 1, true>(const FusedArgs&, int, int, cudaStream_t);

@@ -1,0 +1,6 @@
+/* fused kernel instantiations: register cap 3 CTAs per SM, native keying,
+ * one instrument (one translation unit each, so they compile in parallel) */
+#include "fused_kernel.cuh"
+
+template cudaError_t launch_fk<3, 1, false>(const FusedArgs&, int, int, cudaStream_t);
+template int occ_mm<3, 1>(int);

@@ -1,0 +1,6 @@
+/* fused kernel instantiations: register cap 4 CTAs per SM, reference keying,
+ * one instrument (one translation unit each, so they compile in parallel) */
+#include "fused_kernel.cuh"
+
+template cudaError_t launch_fk<4, 0, false>(const FusedArgs&, int, int, cudaStream_t);
+template int occ_mm<4, 0>(int);

@@ -38,7 +38,12 @@ struct FusedArgs {
   StatusDev* st;
   int32_t split;                /* survivor compaction before this component; 0: off */
   int32_t pad;
+  uint32_t* surv;               /* split: SURV_WORDS x surv_cap survivor records */
+  int64_t surv_cap;             /* slots: 128 per work item */
+  uint32_t* surv_cnt;           /* survivors per work item */
+  int64_t surv_items;
 };
+#define SURV_WORDS 18           /* 15 record lanes (die is 0), iidx, index, variant */
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s);
 int fused_max_blocks_per_sm(int block, int n_comps);

@@ -65,6 +65,8 @@ struct StatusDev {
   unsigned int pad;
   unsigned long long oob;
   unsigned long long workq;    /* work-queue head of the persistent kernel */
+  unsigned long long surv;     /* survivors appended by a split launch's stage A */
+  unsigned long long workq_b;  /* work-queue head of its stage B */
   unsigned long long pad2;
 };
 
