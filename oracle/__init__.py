@@ -89,12 +89,16 @@ class Result:
 
 
 def run(inst, N, chunk=None, rng_mode=0, run_seed=0, variant=0, threads=0, seeds=None,
-        tid_base=0, num_sim=None):
+        tid_base=0, num_sim=None, shard=None):
     """Trace N histories of ``inst`` (an Instrument built with ctx="cpu")
     through the CPU restatement; tallies accumulate into the instrument's
     host tallies.  Returns the final chunk's records.  ``tid_base`` and
     ``num_sim`` describe a shard: records [0, N) are neutrons
-    [tid_base, tid_base+N) of a chunk of ``num_sim`` histories."""
+    [tid_base, tid_base+N) of a chunk of ``num_sim`` histories.
+    ``shard=(rank, world)`` traces rank's part of every chunk of an
+    N-history run: the slice [lo, hi) of the first chunk's index range,
+    clipped to each chunk's size (the same global indices every chunk,
+    so carried RNG counters stay with their index)."""
     import torch  # noqa: F401  (tallies are torch CPU tensors)
     for t in inst.tallies():
         if t.device.type != "cpu":
@@ -104,6 +108,11 @@ def run(inst, N, chunk=None, rng_mode=0, run_seed=0, variant=0, threads=0, seeds
     N = int(N)
     buf_max = int(chunk) if chunk else N
     first = min(N, buf_max)
+    s_lo, s_hi = 0, first
+    if shard is not None:
+        rank, world = shard
+        s_lo, s_hi = first * rank // world, first * (rank + 1) // world
+        first = max(1, s_hi - s_lo)
     neutrons = np.zeros((first, 16), dtype=np.float32)
     isect = np.zeros((first, 8), dtype=np.float32)
     iidx = np.zeros(first, dtype=np.uint32)
@@ -120,15 +129,22 @@ def run(inst, N, chunk=None, rng_mode=0, run_seed=0, variant=0, threads=0, seeds
         remaining -= torun
         seed = inst.source.next_seed() if seeds is None else int(seeds[k])
         k += 1
+        nrec, nsim = torun, int(num_sim) if num_sim else torun
+        if shard is not None:
+            nrec, nsim = max(0, min(s_hi, torun) - s_lo), torun
+            rng.tid_base = s_lo
+            if nrec == 0:
+                last = 0
+                continue
         rc = lib().oracle_execute_chunk(ctypes.addressof(src), ctypes.addressof(carr), nc,
                                         ctypes.addressof(barr), nb, neutrons.ctypes.data,
-                                        isect.ctypes.data, iidx.ctypes.data, torun,
-                                        int(num_sim) if num_sim else torun, seed,
+                                        isect.ctypes.data, iidx.ctypes.data, nrec,
+                                        nsim, seed,
                                         ctypes.addressof(rng), int(variant), 0, int(threads),
                                         ctypes.addressof(flags), ctypes.addressof(oob))
         if rc != 0:
             raise RuntimeError("oracle_execute_chunk failed (%d)" % rc)
         tot_flags |= flags.value
         tot_oob += oob.value
-        last = torun
+        last = nrec
     return Result(neutrons[:last], isect[:last], iidx[:last], tot_flags, tot_oob)

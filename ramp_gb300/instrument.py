@@ -25,6 +25,7 @@ import numpy as np
 import torch
 
 from . import _abi
+from .shard import chunk_slices
 from .scat.sprim import _device
 
 log = logging.getLogger("ramp_gb300")
@@ -345,17 +346,8 @@ class Instrument:
         if trace:
             warnings.warn("trace=True (visualisation lines) is not supported; ignored")
         rank, world = shard if shard is not None else (0, 1)
-        if not (0 <= rank < world):
-            raise ValueError("shard must be (rank, world) with 0 <= rank < world")
-
-        def part(torun):
-            lo = torun * rank // world
-            hi = torun * (rank + 1) // world
-            return lo, hi - lo
-
-        first = part(min(N, buf_max))[1] if world > 1 else min(N, buf_max)
-        if world > 1 and N > buf_max:
-            first = max(part(buf_max)[1], part(N % buf_max or buf_max)[1])
+        slices = chunk_slices(N, buf_max, rank, world)
+        first = max(1, max(nloc for _, _, nloc in slices))
         src = self.source
         with torch.cuda.device(self.device):
             stream = self._stream_ptr()
@@ -368,13 +360,12 @@ class Instrument:
                     carry = torch.zeros((2, first), dtype=torch.float32, device=self.device)
             else:
                 raise ValueError("path must be 'plain' or 'fused'")
-            remaining = N
-            while remaining > 0:
-                torun = buf_max if remaining > buf_max else remaining
-                remaining -= torun
-                seed = src.next_seed()
-                lo, nloc = part(torun)
+            for torun, lo, nloc in slices:
+                seed = src.next_seed()          # every rank draws every chunk's seed
                 rngd.tid_base = lo
+                self.last_chunk = nloc
+                if nloc == 0:
+                    continue
                 if path == "plain":
                     rc = lib.ramp_trace_plain(plan, _abi.ctypes.byref(st), nloc, torun, seed,
                                               _abi.ctypes.byref(rngd), stream)

@@ -14,7 +14,7 @@ import ramp_gb300 as m
 from ramp_gb300 import instruments as I
 from ramp_gb300.graph import lcg_seeds
 
-from test_gpu_parity import _Host, records_equal, tallies_close
+from helpers import _Host, records_equal, tallies_close
 
 pytestmark = pytest.mark.gpu
 

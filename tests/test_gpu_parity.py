@@ -21,52 +21,12 @@ import ramp_gb300 as m
 from ramp_gb300 import _abi, instruments as I
 from ramp_gb300.batch import BatchedInstrument
 
+from helpers import U32, _Host, records_equal, tallies_close  # noqa: F401
+
 pytestmark = pytest.mark.gpu
 
 GOLD_DIR = os.path.join(os.path.dirname(__file__), "golden")
 GOLD = np.load(os.path.join(GOLD_DIR, "ref_pins.npz"))
-
-
-def records_equal(a, b):
-    eq = (a == b) | (np.isnan(a) & np.isnan(b))
-    if not eq.all():
-        bad = np.argwhere(~eq)
-        i, l = bad[0]
-        raise AssertionError("%d mismatching values; first at neutron %d lane %d: gpu %r cpu %r\n"
-                             "gpu %r\ncpu %r" % (len(bad), i, l, a[i, l], b[i, l], a[i], b[i]))
-
-
-U32 = 2.0 ** -24
-
-
-def tallies_close(g_inst, c_inst):
-    tg_all, tc_all = g_inst.tallies(), c_inst.tallies()
-    for k, (tg, tc) in enumerate(zip(tg_all, tc_all)):
-        g = tg.cpu().numpy().astype(np.float64)
-        c = tc.numpy().astype(np.float64)
-        # n_eff from the (sum p, sum p^2) pair this tally belongs to
-        if k % 2 == 0 and k + 1 < len(tc_all) and tc_all[k + 1].numel() == tc.numel():
-            H, E = c, tc_all[k + 1].numpy().astype(np.float64)
-        elif k % 2 == 1 and tc_all[k - 1].numel() == tc.numel():
-            H, E = tc_all[k - 1].numpy().astype(np.float64), c
-        else:
-            H, E = c, None
-        n_eff = np.where(E > 0, H * H / np.where(E > 0, E, 1), 1.0) if E is not None else \
-            np.full_like(c, 1e6)
-        tol = 2 * (n_eff + 1) * U32 * np.abs(c) + 1e-12 * max(np.abs(c).max(), 1e-30)
-        bad = np.abs(g - c) > tol
-        assert not bad.any(), "tally %d: %d bins differ, worst %g vs tol %g" % (
-            k, bad.sum(), np.abs(g - c)[bad].max(), tol[bad][np.argmax(np.abs(g - c)[bad])])
-        assert np.array_equal(g != 0, c != 0)
-
-
-class _Host:
-    """Host view of another instrument's tallies (for GPU-vs-GPU checks)."""
-    def __init__(self, inst):
-        self._t = [t.cpu() for t in inst.tallies()]
-
-    def tallies(self):
-        return self._t
 
 
 def pair(fn, kw, N, path="plain", rng="reference", chunk=None, seed=1234, tune=None):
@@ -291,6 +251,32 @@ def test_autotune_survival_and_split_point(cuda_lib, tmp_path, monkeypatch):
     assert set(cfg) <= set(("blocks_per_sm", "chunk", "split"))
     for t, b in zip(inst.tallies(), before):
         assert torch.equal(t, b)
+
+
+# ---------------------------------------------------------------- shards
+@pytest.mark.parametrize("path", ["plain", "fused"])
+def test_shards_sum_to_single_run(cuda_lib, path):
+    """Two shards traced one after the other on this GPU (no collective):
+    their tallies sum to the oracle's single run, including a short last
+    chunk whose slice is clipped for the higher rank."""
+    kw = I.let_like_kwargs()
+    N, chunk = 250_001, 100_000
+    parts = []
+    for rank in range(2):
+        gi = m.Instrument(I.path("let_like.json"), "cuda", **kw)
+        random.seed(77)
+        gi.execute(N, path=path, chunk=chunk, shard=(rank, 2))
+        parts.append([t.double().cpu() for t in gi.tallies()])
+    torch.cuda.synchronize()
+
+    class Summed:
+        def tallies(self):
+            return [(a + b).float() for a, b in zip(*parts)]
+
+    ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
+    random.seed(77)
+    oracle.run(ci, N, chunk=chunk)
+    tallies_close(Summed(), ci)
 
 
 # ---------------------------------------------------------------- status
