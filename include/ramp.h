@@ -191,6 +191,11 @@ typedef struct RampTune {
                                    launch, owned by the plan) and stage B
                                    traces them 32 to a warp.  Ignored by
                                    ramp_trace_batched_noalloc.           */
+  int32_t streams;              /* ramp_trace_batched: 1 = one launch over
+                                   a task list; otherwise each variant is
+                                   a launch of its own on up to this many
+                                   concurrent streams (0: 8).  A split
+                                   launch is always one launch.          */
 } RampTune;
 
 typedef struct RampPlan RampPlan;

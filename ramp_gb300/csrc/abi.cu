@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
@@ -51,6 +52,18 @@ struct BatchCache {
   size_t tasks_cap = 0;
   std::vector<VariantDev> vars_host;
   std::vector<TaskDev> tasks_host;
+  unsigned long long* counters = nullptr;   /* per-variant work queues */
+  size_t counters_cap = 0;
+};
+
+/* streams of the concurrent per-variant launches of ramp_trace_batched */
+#define RAMP_BATCH_STREAMS 8
+struct StreamSet {
+  bool ready = false;
+  int device = -1;
+  cudaStream_t st[RAMP_BATCH_STREAMS];
+  cudaEvent_t fork;
+  cudaEvent_t join[RAMP_BATCH_STREAMS];
 };
 
 /* device copies of host tables, keyed by (kind, length, content hash) so
@@ -74,6 +87,7 @@ struct RampPlan {
   CompDev* adj_dev = nullptr;
   uint32_t* surv = nullptr;          /* survivor buffer of split launches */
   int64_t surv_cap = 0;              /* slots (128 per work item) */
+  StreamSet streams;
 };
 
 /* ---------------------------------------------------------------------- */
@@ -339,6 +353,14 @@ int ramp_plan_destroy(RampPlan* p) {
   if (p->batch.vars_dev) cudaFree(p->batch.vars_dev);
   if (p->batch.tasks_dev) cudaFree(p->batch.tasks_dev);
   if (p->surv) cudaFree(p->surv);
+  if (p->batch.counters) cudaFree(p->batch.counters);
+  if (p->streams.ready) {
+    for (int k = 0; k < RAMP_BATCH_STREAMS; ++k) {
+      cudaStreamDestroy(p->streams.st[k]);
+      cudaEventDestroy(p->streams.join[k]);
+    }
+    cudaEventDestroy(p->streams.fork);
+  }
   delete p;
   return RAMP_OK;
 }
@@ -562,6 +584,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.carry_sb = sb_carry;
   a.carry_iidx = iidx_carry;
   a.st = p->status;
+  a.workq = &p->status->workq;
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
   if (a.split > 0) {
@@ -570,6 +593,63 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   }
   CK(cudaMemsetAsync(&p->status->workq, 0, 3 * sizeof(unsigned long long), s));
   CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
+  return RAMP_OK;
+}
+
+/* ramp_trace_batched as concurrent single-variant launches: each variant
+ * is a launch of the single-instrument kernel (its descriptors are kernel
+ * parameters, read through the uniform datapath) with its own work-queue
+ * counter, spread longest-first over RAMP_BATCH_STREAMS streams that fork
+ * from and join back into the caller's stream (event record/wait only, so
+ * the whole call can be captured in a CUDA graph).  Kernels of different
+ * streams fill each other's tails. */
+static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<VariantDev>& vars,
+                           int block, int grid, const RampTune* tune, cudaStream_t s) {
+  BatchCache& B = p->batch;
+  const size_t nv = vars.size();
+  if (B.counters_cap < nv) {
+    if (B.counters) cudaFree(B.counters);
+    B.counters = nullptr;
+    B.counters_cap = 0;
+    CK(cudaMalloc(&B.counters, nv * sizeof(unsigned long long)));
+    B.counters_cap = nv;
+  }
+  StreamSet& S = p->streams;
+  if (!S.ready) {
+    for (int k = 0; k < RAMP_BATCH_STREAMS; ++k) {
+      CK(cudaStreamCreateWithFlags(&S.st[k], cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&S.join[k], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming));
+    S.ready = true;
+  }
+  const int ns = (tune && tune->streams > 1 && tune->streams < RAMP_BATCH_STREAMS)
+                     ? tune->streams : RAMP_BATCH_STREAMS;
+  CK(cudaMemsetAsync(B.counters, 0, nv * sizeof(unsigned long long), s));
+  CK(cudaEventRecord(S.fork, s));
+  for (int k = 0; k < ns; ++k) CK(cudaStreamWaitEvent(S.st[k], S.fork, 0));
+  std::vector<int> order(nv);
+  for (size_t v = 0; v < nv; ++v) order[v] = (int)v;
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return vars[x].n > vars[y].n; });
+  std::vector<int64_t> load(ns, 0);
+  for (int v : order) {
+    if (vars[v].n <= 0) continue;
+    int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[k] += vars[v].n;
+    FusedArgs a = base;
+    a.variants = nullptr;
+    a.tasks = nullptr;
+    a.single = vars[v];
+    a.var_key = v;
+    a.workq = B.counters + v;
+    a.task_size = auto_task(vars[v].n, grid, (tune && tune->chunk > 0) ? tune->chunk : 0);
+    a.n_tasks = (vars[v].n + a.task_size - 1) / a.task_size;
+    CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), S.st[k]));
+  }
+  for (int k = 0; k < ns; ++k) {
+    CK(cudaEventRecord(S.join[k], S.st[k]));
+    CK(cudaStreamWaitEvent(s, S.join[k], 0));
+  }
   return RAMP_OK;
 }
 
@@ -627,6 +707,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   }
   std::vector<VariantDev> vars((size_t)n_variants);
   std::vector<TaskDev> tasks;
+  const bool use_streams = !(tune && (tune->streams == 1 || tune->split > 0));
   for (int v = 0; v < n_variants; ++v) {
     int rc = make_src(variants[v].source, vars[v].src);
     if (rc) return rc;
@@ -634,6 +715,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     vars[v].num_sim = variants[v].num_sim;
     vars[v].seed = variants[v].seed;
     vars[v].comps = B.comps_dev + (size_t)v * nc;
+    if (use_streams) continue;
     for (int64_t st0 = 0; st0 < variants[v].n; st0 += task) {
       TaskDev t;
       t.variant = v;
@@ -642,6 +724,18 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
       t.count = (int32_t)(rem < task ? rem : task);
       tasks.push_back(t);
     }
+  }
+  if (use_streams) {
+    FusedArgs a;
+    memset(&a, 0, sizeof(a));
+    a.blocks = p->blocks_dev;
+    a.n_blocks = (int32_t)p->blocks.size();
+    a.n_comps = nc;
+    a.rng.mode = rng ? rng->mode : 1;
+    a.rng.run_seed = rng ? rng->run_seed : 0u;
+    a.rng.tid_base = 0u;   /* variants key by their own index */
+    a.st = p->status;
+    return batched_streams(p, a, vars, block, grid, tune, s);
   }
   if (tasks.empty()) return RAMP_OK;
   if (B.vars_cap < vars.size()) {
@@ -681,6 +775,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;   /* variants key by their own index */
   a.st = p->status;
+  a.workq = &p->status->workq;
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
   if (a.split > 0) {
@@ -1027,6 +1122,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;
   a.st = &D->status;
+  a.workq = &D->status.workq;
   /* no survivor split here: it would need a buffer sized by the call */
   CK(launch_fused(a, block, fused_grid(n_tasks, grid), s));
   return RAMP_OK;

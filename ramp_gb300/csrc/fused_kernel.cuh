@@ -129,7 +129,7 @@ k_fused(const FusedArgs a) {
     const int KE = PHASE == 1 ? a.split : a.n_comps;
     for (;;) {
       unsigned long long t = 0;
-      if (lane == 0) t = atomicAdd(&a.st->workq, 1ull);
+      if (lane == 0) t = atomicAdd(a.workq, 1ull);
       t = __shfl_sync(FULL_MASK, t, 0);
       int var;
       int64_t start, count;
@@ -147,7 +147,7 @@ k_fused(const FusedArgs a) {
         if (count > FUSED_WARP_TASK) count = FUSED_WARP_TASK;
         V = a.variants + var;
       } else {
-        var = 0;
+        var = a.var_key;
         start = (int64_t)t * FUSED_WARP_TASK;
         if (start >= a.single.n) break;
         count = a.single.n - start;

@@ -42,6 +42,9 @@ struct FusedArgs {
   int64_t surv_cap;             /* slots: 128 per work item */
   uint32_t* surv_cnt;           /* survivors per work item */
   int64_t surv_items;
+  unsigned long long* workq;    /* work-queue counter of this launch */
+  int32_t var_key;              /* single variant: its index in the RNG key */
+  int32_t pad2;
 };
 #define SURV_WORDS 18           /* 15 record lanes (die is 0), iidx, index, variant */
 

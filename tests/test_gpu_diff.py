@@ -74,10 +74,12 @@ def test_likelihood_ratio_terms_only_touch_branching_parameters(problem):
     g1, _ = adjoint_grad(chain, theta0, Ht, seed=5, lr=True)
     k = chain.names.index("sample.sigma_abs")
     others = [j for j in range(len(g0)) if j != k]
-    # the same per-neutron terms summed by double atomics in another order
-    assert torch.allclose(g0[others], g1[others], rtol=1e-9,
-                          atol=1e-12 * float(g0.abs().max()))
-    assert g0[k] != g1[k]
+    # the same per-neutron terms against a forward histogram (hence dL/dH)
+    # that differs only by the order of its float additions
+    d = (g0[others] - g1[others]).abs()
+    tol = 1e-5 * g0[others].abs() + 1e-6 * float(g0.abs().max())
+    assert bool((d <= tol).all()), "max |diff| %g" % float(d.max())
+    assert abs(float(g1[k] - g0[k])) > 1e-3 * abs(float(g0[k]))
 
 
 def test_adjoint_is_deterministic_in_value(problem):

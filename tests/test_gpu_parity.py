@@ -168,16 +168,19 @@ def test_fused_equals_plain_at_1e7(cuda_lib):
 
 
 # ---------------------------------------------------------------- batching
-def test_batched_variants_match_single_runs(cuda_lib):
-    """Variants with different Ei, slit width and neutron count in one
-    launch; each equals its own oracle run with the same seed and keying."""
+@pytest.mark.parametrize("tune", [None, {"streams": 1}, {"streams": 2, "blocks_per_sm": 4}])
+def test_batched_variants_match_single_runs(cuda_lib, tune):
+    """Variants with different Ei, slit width and neutron count, traced as
+    concurrent per-variant launches (default), as one launch over a task
+    list (streams 1), or on two streams; each equals its own oracle run
+    with the same seed and keying."""
     variants = [I.let_like_kwargs(Ei=3.7, use_slit=1, slit_w=0.03),
                 I.let_like_kwargs(Ei=8.0, use_slit=1, slit_w=0.015),
                 I.let_like_kwargs(Ei=2.5, use_slit=1, slit_w=0.04)]
     counts = [300_000, 123_457, 200_003]
     for mode, rng in ((0, "reference"), (1, "native")):
         B = BatchedInstrument(I.path("let_like.json"), variants, ctx="cuda")
-        B.execute(counts, rng=rng, seeds=[11, 2222, 4000])
+        B.execute(counts, rng=rng, seeds=[11, 2222, 4000], tune=tune)
         torch.cuda.synchronize()
         for v, (kw, n, seed) in enumerate(zip(variants, counts, [11, 2222, 4000])):
             ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
