@@ -194,7 +194,7 @@ typedef struct RampTune {
   int32_t streams;              /* ramp_trace_batched: 1 = one launch over
                                    a task list; otherwise each variant is
                                    a launch of its own on up to this many
-                                   concurrent streams (0: 8).  A split
+                                   concurrent streams (0: 16).  A split
                                    launch is always one launch.          */
 } RampTune;
 

@@ -16,7 +16,7 @@ EXT(3, 1)
 EXT(4, 0)
 EXT(4, 1)
 
-static int g_fused_minb = 3;
+static int g_fused_minb = 4;
 
 /* register cap: 3 or 4 CTAs of 256 threads per SM (at 2 the kernel is
  * never faster on GB300) */
