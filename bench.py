@@ -234,11 +234,13 @@ def run_batched_config(a):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": name, "variants": len(counts), "histories_per_step": total,
-                       "rng": "reference keying", "path": "batched fused (one launch)"},
+                       "rng": "reference keying",
+                       "path": "batched fused: one single-instrument launch per variant on "
+                               "16 concurrent streams forked from the caller's stream"},
             "plain_path_sequential": {"value": total / (plain_ms / 1000.0), "ms_per_step": plain_ms,
                                       "sample": "first %d variants, scaled by histories" % nplain},
             "batched_over_plain": (total / (statistics.mean(ms) / 1000.0)) / (total / (plain_ms / 1000.0)),
-            "gpu_launches": a.steps, "clocks": clk}
+            "gpu_launches": a.steps * sum(1 for c in counts if c > 0), "clocks": clk}
     print(json.dumps(line), flush=True)
 
 
@@ -272,6 +274,8 @@ def run_gradients(a, n=10_000_000):
     for w in range(a.warmup):
         step(10 + w)
     torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
     ms = []
     for k in range(a.steps):
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -280,6 +284,7 @@ def run_gradients(a, n=10_000_000):
         e.record()
         e.synchronize()
         ms.append(s.elapsed_time(e))
+    clk = clocks.stop()
     g = step(1)
     fd = torch.zeros_like(g)
     with torch.no_grad():
@@ -302,6 +307,7 @@ def run_gradients(a, n=10_000_000):
                                    "720x1000 detector, 22 parameters, fused forward + adjoint",
                        "histories": n},
             "histories_per_s_forward_and_adjoint": n / (statistics.mean(ms) / 1000.0),
+            "gpu_launches": a.steps * 2, "clocks": clk,
             "gradient_vs_central_fd": table}
     print(json.dumps(line), flush=True)
 
@@ -524,7 +530,7 @@ def main():
         "e2e": {"value": e2e, "unit": "histories/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "includes": "Instrument(...) parse + plan/table upload, execute, data() readback"},
-        "gpu_launches": a.steps,
+        "gpu_launches": a.steps * (2 if int((tune or {}).get("split", 0)) > 0 else 1),
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
