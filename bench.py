@@ -480,6 +480,23 @@ def main():
     # ---- CUDA graphs at small N ----
     graphs = graph_small_n(lambda: m.Instrument(fn, dev, **kw), tune, dev)
 
+    # ---- the same chain fed by the tabulated ISIS moderator (MISIS) ----
+    mi = m.Instrument(I.path("let_like_misis.json"), dev, **I.let_like_misis_kwargs())
+    misis_ms = []
+    for k in range(4):
+        random.seed(2000 + k)
+        s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        mi.execute(n, path="fused", tune=tune)
+        e0.record()
+        e0.synchronize()
+        if k > 0:
+            misis_ms.append(s0.elapsed_time(e0))
+    misis = {"value": n / (statistics.mean(misis_ms) / 1000.0), "unit": "histories/s",
+             "ms_per_step": statistics.mean(misis_ms),
+             "workload": "LET-like chain with the MISIS moderator (synthetic 60 x 100 "
+                         "time-energy spectrum), %d histories, fused" % n}
+
     # ---- end to end through the public API ----
     e2e_steps = 0 if a.no_e2e else max(2, a.steps // 2)
     e2e_ms, h2d, d2h = [], 0, 0
@@ -518,6 +535,7 @@ def main():
         "plain_path": {"value": plain_value, "unit": "histories/s",
                        "ms_per_step": plain_total_ms / len(plain_ms), "roofline": plain_roof},
         "graph_small_n": graphs,
+        "let_like_misis": misis,
         "fused_over_plain": value / plain_value,
         "roofline": {"bound": "issue", "achieved": achieved_ops / 1e9, "peak": peak_ops / 1e9,
                      "unit": "Gop/s", "frac": achieved_ops / peak_ops, "traffic": None,

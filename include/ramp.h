@@ -62,7 +62,8 @@ enum RampLane {
 /* ---- component kinds --------------------------------------------------- */
 enum RampSourceKind {
   RAMP_SRC_FLAT = 1,   /* MFlat  moderator/flat_mod.py:10, flat_mod.cl:4  */
-  RAMP_SRC_CONT = 2    /* MCont  moderator/cont_mod.py:10, cont_mod.cl:11 */
+  RAMP_SRC_CONT = 2,   /* MCont  moderator/cont_mod.py:10, cont_mod.cl:11 */
+  RAMP_SRC_ISIS = 3    /* MISIS  moderator/isis_mod.py:10, isis_mod.cl:15 */
 };
 
 enum RampGeomKind {
@@ -99,11 +100,17 @@ enum RampScatKind {
 
 /* One moderator (the component with "source": true, mcramp.py:58-63).
  * p[]: mod_dim.x, mod_dim.y, target_dim.x, target_dim.y, target_dist,
- *      E_min, E_max, T1, I1, T2, I2, T3, I3, str_area               */
+ *      E_min, E_max, T1, I1, T2, I2, T3, I3, str_area, total
+ * MISIS tables (host arrays, copied at plan creation): table[0] the flux
+ * CDF over (energy row, time bin), (n_e - 1) * n_t values; table[1] the
+ * n_t time bins (s); table[2] the n_e energy bin edges (meV); table[3] the
+ * n_e cumulative flux at the energy edges (isis_mod.py:85-165).          */
 typedef struct RampSource {
   int32_t kind;
   int32_t reserved;
   float p[16];
+  const float* table[4];
+  int64_t table_len[4];
 } RampSource;
 
 /* One non-source component (mcramp.py:65-108): a geometry kernel and a

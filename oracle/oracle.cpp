@@ -305,6 +305,79 @@ void gen_cont(const Ctx& c, const RampSource& s, int32_t num_sim, int32_t seed) 
   }
 }
 
+/* find_closest_in_cdf — mcramp/moderator/isis_mod.cl:4-13, a linear scan;
+ * entries past the table read as 0 (the reference passes n_t * n_e, one
+ * energy row more than the flux table holds) */
+inline float isis_at(const float* t, int64_t len, int64_t i) {
+  return (i >= 0 && i < len) ? t[i] : 0.0f;
+}
+inline int isis_cdf(const float* t, int64_t len, int64_t scan, float val) {
+  for (int64_t i = 0; i < scan; i++)
+    if ((isis_at(t, len, i) - val) > 0.0f) return (int)(i - 1);
+  return 0;
+}
+
+/* generate_neutrons — mcramp/moderator/isis_mod.cl:15-104 */
+void gen_isis(const Ctx& c, const RampSource& s, int32_t num_sim, int32_t seed) {
+  const float mdx = s.p[0], mdy = s.p[1], tdx = s.p[2], tdy = s.p[3];
+  const float target_dist = s.p[4], str_area = s.p[13], total = s.p[14];
+  const float* flux = s.table[0];
+  const float* tb = s.table[1];
+  const float* eb = s.table[2];
+  const float* ei = s.table[3];
+  const int64_t nflux = s.table_len[0];
+  const int nt = (int)s.table_len[1], ne = (int)s.table_len[2];
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < c.n; ++i) {
+    float* n = c.neutrons + 16 * i;
+    uint32_t tid = c.tid_base + (uint32_t)i;
+    float old_sb = n[SB];
+    for (int k = 0; k < 16; ++k) n[k] = 0.0f;
+    n[SB] = (float)seed + old_sb;
+    float deviate = total * o_rand(n, tid, c.kg);
+    int idx = isis_cdf(flux, nflux, (int64_t)nt * ne, deviate);
+    int Epnt = isis_cdf(ei, ne, ne, deviate);
+    int Tpnt = (int)fmodf((float)idx, (float)nt);
+    if (Tpnt >= nt - 1) Tpnt -= 1;
+    float time_val = isis_at(tb, nt, Tpnt);
+    float time_range = isis_at(tb, nt, Tpnt + 1) - isis_at(tb, nt, Tpnt);
+    float time_spread = isis_at(flux, nflux, (int64_t)Epnt * nt + Tpnt + 1) -
+                        isis_at(flux, nflux, (int64_t)Epnt * nt + Tpnt);
+    float R = deviate - isis_at(flux, nflux, (int64_t)Epnt * nt + Tpnt);
+    R /= time_spread;
+    time_val += time_range * R;
+    float ener_spread = isis_at(ei, ne, Epnt + 1) - isis_at(ei, ne, Epnt);
+    int i0 = (Epnt > 3) ? Epnt - 3 : 0;
+    int i1 = ((ne - Epnt - 1) > 3) ? Epnt + 3 : (ne - 1);
+    deviate = isis_at(ei, ne, Epnt) + ener_spread * o_rand(n, tid, c.kg);
+    float accumulator = 0.0f;
+    for (int a = i0; a <= i1; a++) {
+      float Pj = 1.0f;
+      for (int b = i0; b <= i1; b++)
+        if (b != a) Pj *= (deviate - isis_at(ei, ne, b)) / (isis_at(ei, ne, a) - isis_at(ei, ne, b));
+      Pj *= isis_at(eb, ne, a);
+      accumulator += Pj;
+    }
+    float ener_val = accumulator;
+    n[0] = mdx * (0.5f - o_rand(n, tid, c.kg));
+    n[1] = mdy * (0.5f - o_rand(n, tid, c.kg));
+    n[2] = 0.0f;
+    float vel = RC_SE2V * sqrtf(ener_val);
+    float Dx = tdx * (0.5f - o_rand(n, tid, c.kg)) - n[0];
+    float Dy = tdy * (0.5f - o_rand(n, tid, c.kg)) - n[1];
+    set_vel(n, mul(vel, normalize(v3(Dx, Dy, target_dist))));
+    float theta = 2 * RC_PI * o_rand(n, tid, c.kg);
+    float phi = rm_acosf(1 - 2 * o_rand(n, tid, c.kg));
+    n[6] = rm_sinf(phi) * rm_cosf(theta);
+    n[7] = rm_sinf(phi) * rm_sinf(theta);
+    n[8] = rm_cosf(phi);
+    n[P] = str_area * total * 6.2415093e+12f / (float)num_sim;
+    n[TOF] = time_val;
+    n[DIE] = 0.0f;
+    reset_isect(c.isect + 8 * i);
+  }
+}
+
 /* ---------------- frame transform & termination ------------------------- */
 /* transform — mcramp/scat/frametransform.cl:4-23 */
 void transform(const Ctx& c, const RampComp& k) {
@@ -1109,6 +1182,7 @@ int oracle_execute_chunk(const RampSource* src, const RampComp* comps, int n_com
   c.oob = &oob; c.flags = &flags;
   if (src->kind == RAMP_SRC_FLAT) gen_flat(c, *src, num_sim, seed);
   else if (src->kind == RAMP_SRC_CONT) gen_cont(c, *src, num_sim, seed);
+  else if (src->kind == RAMP_SRC_ISIS) gen_isis(c, *src, num_sim, seed);
   else return RAMP_E_UNSUPPORTED;
   for (int b = 0; b < n_blocks; ++b) {
     const RampBlock& B = blocks[b];

@@ -3,7 +3,7 @@ Monte-Carlo ray-tracing chain behind RAMP's instrument-definition format and
 plugin classes (mcramp).  ``import ramp_gb300 as mcramp`` gives the names an
 mcramp script uses: Instrument, frame_rotate, build_kernel and the plugin
 classes."""
-from .moderator import MFlat, MCont
+from .moderator import MFlat, MCont, MISIS
 from .geom import (GPrim, GPlane, GCylinderExt, GBanana, GSphere, GSphereInt, GBox, GArm,
                    GMesh)
 from .scat import (SPrim, SArm, SBeamstop, SGuide, SChopper, SIsotropic, SPowderN,

@@ -15,7 +15,7 @@ LANE = dict(x=0, y=1, z=2, vx=3, vy=4, vz=5, px=6, py=7, pz=8, p=9, tof=10,
             mc=11, prevcomp=12, sd=13, se=14, die=15)
 
 # kinds (RampSourceKind / RampGeomKind / RampScatKind)
-SRC_FLAT, SRC_CONT = 1, 2
+SRC_FLAT, SRC_CONT, SRC_ISIS = 1, 2, 3
 G_PLANE, G_CYL_EXT, G_BANANA, G_SPHERE, G_SPHERE_INT, G_BOX, G_ARM, G_MESH = range(1, 9)
 (S_ARM, S_GUIDE, S_CHOPPER, S_ISOTROPIC, S_POWDERN, S_DET1D, S_DET2D, S_COUNTER,
  S_BEAMSTOP, S_ATTENUATE) = range(1, 11)
@@ -32,7 +32,9 @@ F_GUIDE_CAP, F_POWDER_CAP, F_TALLY_OOB, F_BVH_STACK, F_WORKQ = 1, 2, 4, 8, 16
 
 class RampSource(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("p", ctypes.c_float * 16)]
+                ("p", ctypes.c_float * 16),
+                ("table", ctypes.POINTER(ctypes.c_float) * 4),
+                ("table_len", ctypes.c_int64 * 4)]
 
 
 class RampComp(ctypes.Structure):

@@ -3,6 +3,7 @@
  * creation (descriptor validation, frame matrices, table and BVH upload),
  * the plain and fused launchers, status readback and error messages.
  */
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -155,23 +156,6 @@ static void guide_aux(const RampComp& c, float* aux) {
   aux[15] = (m <= 0 || Qc <= 0 || R0 <= 0) ? 1.0f : 0.0f;
 }
 
-static int make_src(const RampSource& s, SrcDev& d) {
-  if (s.kind != RAMP_SRC_FLAT && s.kind != RAMP_SRC_CONT) {
-    set_err("unknown source kind %d", s.kind);
-    return RAMP_E_UNSUPPORTED;
-  }
-  memset(&d, 0, sizeof(d));
-  d.kind = s.kind;
-  d.dslot_T = -1;
-  memcpy(d.p, s.p, sizeof(d.p));
-  if (s.kind == RAMP_SRC_CONT) {
-    d.dmax[0] = maxwell_h(RC_K_B * s.p[7], s.p[7]);
-    d.dmax[1] = maxwell_h(RC_K_B * s.p[9], s.p[9]);
-    d.dmax[2] = maxwell_h(RC_K_B * s.p[11], s.p[11]);
-  }
-  return RAMP_OK;
-}
-
 static int upload(const void* host, size_t bytes, void** dev, std::vector<void*>& owner) {
   void* p = nullptr;
   CK(cudaMalloc(&p, bytes > 0 ? bytes : 16));
@@ -262,6 +246,56 @@ static int get_table(RampPlan* p, const float* host, int64_t len, const float** 
   if (rc) return rc;
   p->tabs[key] = std::make_pair(d, (void*)nullptr);
   *dev = (const float*)d;
+  return RAMP_OK;
+}
+
+static int lookup_table(RampPlan* p, const float* host, int64_t len, const float** dev,
+                        HashMemo* memo);
+
+/* device source descriptor; MISIS tables are uploaded (or, for callers
+ * that may not allocate, looked up among the plan's tables) */
+static int make_src(RampPlan* p, const RampSource& s, SrcDev& d, bool may_upload = true,
+                    HashMemo* memo = nullptr) {
+  if (s.kind != RAMP_SRC_FLAT && s.kind != RAMP_SRC_CONT && s.kind != RAMP_SRC_ISIS) {
+    set_err("unknown source kind %d", s.kind);
+    return RAMP_E_UNSUPPORTED;
+  }
+  memset(&d, 0, sizeof(d));
+  d.kind = s.kind;
+  d.dslot_T = -1;
+  memcpy(d.p, s.p, sizeof(d.p));
+  if (s.kind == RAMP_SRC_CONT) {
+    d.dmax[0] = maxwell_h(RC_K_B * s.p[7], s.p[7]);
+    d.dmax[1] = maxwell_h(RC_K_B * s.p[9], s.p[9]);
+    d.dmax[2] = maxwell_h(RC_K_B * s.p[11], s.p[11]);
+  }
+  if (s.kind == RAMP_SRC_ISIS) {
+    const int64_t nt = s.table_len[1], ne = s.table_len[2];
+    if (nt < 2 || ne < 2 || s.table_len[0] != (ne - 1) * nt || s.table_len[3] != ne ||
+        !s.table[0] || !s.table[1] || !s.table[2] || !s.table[3] || nt * ne > INT32_MAX) {
+      set_err("MISIS: tables must hold (n_e-1)*n_t flux values, n_t times, n_e energies and "
+              "n_e cumulative values, n_t, n_e >= 2");
+      return RAMP_E_INVALID;
+    }
+    /* the device searches the two cumulative tables by bisection, which
+       equals the reference's linear scan on non-decreasing tables */
+    for (int k : {0, 3})
+      for (int64_t i = 1; i < s.table_len[k]; ++i)
+        if (!(s.table[k][i] >= s.table[k][i - 1])) {
+          set_err("MISIS: cumulative table %d decreases at %lld", k, (long long)i);
+          return RAMP_E_INVALID;
+        }
+    for (int k = 0; k < 4; ++k) {
+      int rc = may_upload ? get_table(p, s.table[k], s.table_len[k], &d.tab[k], memo)
+                          : lookup_table(p, s.table[k], s.table_len[k], &d.tab[k], memo);
+      if (rc) {
+        if (!may_upload) set_err("MISIS tables are not in the plan");
+        return rc;
+      }
+    }
+    d.n_t = (int32_t)nt;
+    d.n_e = (int32_t)ne;
+  }
   return RAMP_OK;
 }
 
@@ -375,7 +409,7 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
   *out = nullptr;
   RampPlan* p = new RampPlan();
   p->src_in = *source;
-  int rc = make_src(*source, p->src);
+  int rc = make_src(p, *source, p->src);
   if (rc) { delete p; return rc; }
   for (int b = 0; b < n_blocks; ++b) {
     const RampBlock& B = blocks[b];
@@ -711,7 +745,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   std::vector<TaskDev> tasks;
   const bool use_streams = !(tune && (tune->streams == 1 || tune->split > 0));
   for (int v = 0; v < n_variants; ++v) {
-    int rc = make_src(variants[v].source, vars[v].src);
+    int rc = make_src(p, variants[v].source, vars[v].src, true, &memo);
     if (rc) return rc;
     vars[v].n = variants[v].n;
     vars[v].num_sim = variants[v].num_sim;
@@ -797,7 +831,7 @@ int ramp_plan_set_param(RampPlan* p, int32_t kind, int32_t comp, float value) {
       return RAMP_E_INVALID;
     }
     p->src_in.p[7] = p->src_in.p[9] = p->src_in.p[11] = value;
-    return make_src(p->src_in, p->src);
+    return make_src(p, p->src_in, p->src);
   }
   if (comp < 0 || comp >= (int)p->comps_in.size()) {
     set_err("ramp_plan_set_param: component %d out of range", comp);
@@ -1089,7 +1123,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
       if (!rc) rc = lookup_comp(p, c, H.descs[(size_t)v * nc + j], &memo);
       if (rc) return rc;
     }
-    int rc = make_src(V.source, H.variants[v].src);
+    int rc = make_src(p, V.source, H.variants[v].src, false, &memo);
     if (rc) return rc;
     H.variants[v].n = V.n;
     H.variants[v].num_sim = V.num_sim;

@@ -238,7 +238,89 @@ DI float maxwell(float E, float T) {
   return 2.0f * rootE / sqrtf(RC_PI) * (overKT * sqrtf(overKT)) * rm_expf(-E * overKT);
 }
 
-/* generate_neutrons — flat_mod.cl:4-50 and cont_mod.cl:11-72 */
+/* MISIS table read: entries outside the table read as 0 (the reference
+ * reads past both ends for a deviate below the first flux value or above
+ * the last, isis_mod.cl:27-38) */
+DI float isis_at(const float* __restrict__ t, int64_t len, int64_t i) {
+  return (i >= 0 && i < len) ? __ldg(t + i) : 0.0f;
+}
+
+/* find_closest_in_cdf (isis_mod.cl:4-13): the index before the first entry
+ * above val, 0 when none is; by bisection (the table is non-decreasing and
+ * val >= 0, so entries past its end, read as 0, never qualify) */
+DI int isis_cdf(const float* __restrict__ t, int len, float val) {
+  int lo = 0, hi = len;               /* first index with t[i] - val > 0 */
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((__ldg(t + mid) - val) > 0.0f) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo < len ? lo - 1 : 0;
+}
+
+/* energy and time of an MISIS history (isis_mod.cl:31-70); returns the
+ * energy in meV, the emission time in t0 */
+DI float isis_sample(const SrcDev& s, Nt& n, Rng& r, float& t0) {
+  const float* __restrict__ flux = s.tab[0];
+  const float* __restrict__ tb = s.tab[1];
+  const float* __restrict__ eb = s.tab[2];
+  const float* __restrict__ ei = s.tab[3];
+  const int nt = s.n_t, ne = s.n_e;
+  const int64_t nflux = (int64_t)(ne - 1) * nt;
+  float deviate = s.p[14] * draw(n, r);
+  const int idx = isis_cdf(flux, (int)nflux, deviate);
+  const int Epnt = isis_cdf(ei, ne, deviate);
+  int Tpnt = (int)fmodf((float)idx, (float)nt);
+  if (Tpnt >= nt - 1) Tpnt -= 1;
+  float time_val = isis_at(tb, nt, Tpnt);
+  const float time_range = isis_at(tb, nt, Tpnt + 1) - isis_at(tb, nt, Tpnt);
+  const int64_t row = (int64_t)Epnt * nt;
+  const float time_spread = isis_at(flux, nflux, row + Tpnt + 1) - isis_at(flux, nflux, row + Tpnt);
+  float R = deviate - isis_at(flux, nflux, row + Tpnt);
+  R /= time_spread;
+  time_val += time_range * R;
+  const float ener_spread = isis_at(ei, ne, Epnt + 1) - isis_at(ei, ne, Epnt);
+  const int i0 = (Epnt > 3) ? Epnt - 3 : 0;
+  const int i1 = ((ne - Epnt - 1) > 3) ? Epnt + 3 : (ne - 1);
+  deviate = isis_at(ei, ne, Epnt) + ener_spread * draw(n, r);
+  float acc = 0.0f;                     /* Lagrange interpolation of the edge */
+  for (int i = i0; i <= i1; i++) {
+    float Pj = 1.0f;
+    const float ei_i = isis_at(ei, ne, i);
+    for (int j = i0; j <= i1; j++)
+      if (j != i) Pj *= (deviate - isis_at(ei, ne, j)) / (ei_i - isis_at(ei, ne, j));
+    Pj *= isis_at(eb, ne, i);
+    acc += Pj;
+  }
+  t0 = time_val;
+  return acc;
+}
+
+/* MCont weight sum_i I_i M(E; T_i) / M(k_B T_i; T_i) / N (cont_mod.cl:22-31) */
+template <class D>
+DI float cont_weight(const SrcDev& s, float E_val, int32_t num_sim, D* dx) {
+  float E_J = RC_EV_J * E_val;
+  float M = s.p[8] * maxwell(E_J, s.p[7]) / s.dmax[0];
+  M += s.p[10] * maxwell(E_J, s.p[9]) / s.dmax[1];
+  M += s.p[12] * maxwell(E_J, s.p[11]) / s.dmax[2];
+  if constexpr (D::on) {
+    /* weight I M(E;T)/M(kT;T) = I sqrt(x) e^(1-x), x = E/kT, for the
+       common temperature T of the three terms: d log/dT = (x - 1/2)/T */
+    if (s.dslot_T >= 0 && M != 0.0f) {
+      float acc = 0.0f;
+      for (int q = 0; q < 3; ++q) {
+        const float T = s.p[7 + 2 * q], I = s.p[8 + 2 * q];
+        const float term = I * maxwell(E_J, T) / s.dmax[q];
+        const float x = E_J / (RC_K_B * T);
+        acc += term * (x - 0.5f) / T;
+      }
+      dx->add(s.dslot_T, acc / M);
+    }
+  }
+  return M / (float)num_sim;
+}
+
+/* generate_neutrons — flat_mod.cl:4-50, cont_mod.cl:11-72, isis_mod.cl:15-104 */
 template <class D = NoDiff>
 DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t seed, Rng& r,
                  D* dx = nullptr) {
@@ -246,31 +328,16 @@ DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t 
   n.p = n.t = n.sc = n.sd = n.se = n.die = 0.0f;
   n.wr = 0;
   n.sb = (float)seed + old_sb;
-  const float E_min = s.p[5], E_max = s.p[6];
-  float E_range = (E_max - E_min);
-  float E_val = E_min + E_range * draw(n, r);
-  if (s.kind == RAMP_SRC_CONT) {
-    float E_J = RC_EV_J * E_val;
-    float M = s.p[8] * maxwell(E_J, s.p[7]) / s.dmax[0];
-    M += s.p[10] * maxwell(E_J, s.p[9]) / s.dmax[1];
-    M += s.p[12] * maxwell(E_J, s.p[11]) / s.dmax[2];
-    n.p = M / (float)num_sim;
-    if constexpr (D::on) {
-      /* weight I M(E;T)/M(kT;T) = I sqrt(x) e^(1-x), x = E/kT, for the
-         common temperature T of the three terms: d log/dT = (x - 1/2)/T */
-      if (s.dslot_T >= 0 && M != 0.0f) {
-        float acc = 0.0f;
-        for (int q = 0; q < 3; ++q) {
-          const float T = s.p[7 + 2 * q], I = s.p[8 + 2 * q];
-          const float term = I * maxwell(E_J, T) / s.dmax[q];
-          const float x = E_J / (RC_K_B * T);
-          acc += term * (x - 0.5f) / T;
-        }
-        dx->add(s.dslot_T, acc / M);
-      }
-    }
+  float E_val, t0 = 0.0f;
+  if (s.kind == RAMP_SRC_ISIS) {
+    E_val = isis_sample(s, n, r, t0);
+    n.p = s.p[13] * s.p[14] * 6.2415093e+12f / (float)num_sim;
   } else {
-    n.p = 1.0f / (float)num_sim;
+    const float E_min = s.p[5], E_max = s.p[6];
+    float E_range = (E_max - E_min);
+    E_val = E_min + E_range * draw(n, r);
+    n.p = (s.kind == RAMP_SRC_CONT) ? cont_weight<D>(s, E_val, num_sim, dx)
+                                    : 1.0f / (float)num_sim;
   }
   n.x = s.p[0] * (0.5f - draw(n, r));
   n.y = s.p[1] * (0.5f - draw(n, r));
@@ -287,6 +354,7 @@ DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t 
   n.px = sp * ct;
   n.py = sp * st;
   n.pz = cp;
+  n.t = t0;
   n.die = 0.0f;
 }
 

@@ -49,6 +49,9 @@ struct SrcDev {
   int32_t dslot_T;             /* adjoint: gradient slot of the common
                                   moderator temperature, -1 when not
                                   differentiated                          */
+  const float* tab[4];         /* MISIS: flux CDF, time bins, energy edges,
+                                  cumulative flux at the edges (device)   */
+  int32_t n_t, n_e;            /* MISIS: time bins, energy edges          */
 };
 
 struct RngDev {

@@ -9,6 +9,9 @@ the benchmark and parity workloads, and generators for their inputs.
   disk choppers phased for $Ei$, optional slit ($use_slit$, $slit_w$),
   powder sample with 40 lines, banana detector r 3.5 m with a 720 x 1000
   (2theta -40..140 deg, TOF 0-50 ms) histogram.
+* let_like_misis.json — the LET-like chain fed by the tabulated ISIS
+  moderator (MISIS) from a seeded synthetic spectrum file in the McStas/MCNP
+  tally format ($spec_file$).
 * mesh_imaging.json — near-parallel flat beam through a seeded perturbed
   torus mesh (GMesh + SAttenuate, mu 0.5 /cm) rotated by $angle$, onto a
   1024 x 1024 pixel detector.
@@ -80,8 +83,39 @@ def torus_triangles(R=0.020, r=0.008, nu=448, nv=224, noise=0.0002, seed=5):
     return np.concatenate([t1, t2]).astype(np.float32)
 
 
+def write_isis_spectrum(fn, n_e=60, n_t=100, seed=3, time_offset=150.0):
+    """A synthetic moderator spectrum in the McStas/MCNP tally text format the
+    reference's MISIS reads: per energy bin (edges in MeV, log-spaced from
+    1e-11 to 1e-7), a time histogram of ``t value (error)`` lines (t in
+    units of 10 ns, log-spaced 1..1e6) and a total line.  Intensities are a
+    Maxwellian-like energy shape times a pulse in time with seeded noise;
+    the first energy bin is empty."""
+    r = np.random.default_rng(seed)
+    edges = np.logspace(-11, -7, n_e + 1)
+    t = np.logspace(0, 6, n_t)
+    E = 0.5 * (edges[:-1] + edges[1:]) * 1e9                   # meV
+    shape_e = (E / 3.0) * np.exp(-E / 3.0) + 0.05 * np.exp(-E / 40.0)
+    tau = 2e2 + 2e3 / np.sqrt(E + 0.1)                          # pulse width, 10 ns units
+    out = ["1tally 5 nps %d" % 200000, "c synthetic spectrum, seed %d" % seed,
+           "c TimeOffset %g" % time_offset]
+    for k in range(n_e):
+        out += [" surface 9999", "segment:  0", "user bin total",
+                "energy bin: %.6e to %.6e" % (edges[k], edges[k + 1]), "cosine:   1", " time "]
+        pulse = (t / tau[k]) * np.exp(-t / tau[k])
+        vals = 1e-8 * shape_e[k] * pulse * (1.0 + 0.1 * r.standard_normal(n_t)).clip(0.0)
+        if k == 0:
+            vals[:] = 0.0
+        for ti, v in zip(t, vals):
+            out.append("%.6e %.6e (%.6e) " % (ti, v, 0.1 * v))
+        out.append("  total      %.6e (%.6e)" % (vals.sum(), 0.1 * vals.sum()))
+    out.append("1end")
+    with open(fn, "w") as f:
+        f.write("\n".join(out) + "\n")
+
+
 def ensure_inputs():
-    """Write the generated inputs (Sqw file, torus STL) if missing."""
+    """Write the generated inputs (Sqw file, torus STL, moderator spectrum)
+    if missing."""
     from ..geom.mesh import write_stl
     os.makedirs(GENERATED, exist_ok=True)
     sqw = os.path.join(GENERATED, "vanadium_inc.sqw")
@@ -90,11 +124,19 @@ def ensure_inputs():
     stl = os.path.join(GENERATED, "torus.stl")
     if not os.path.exists(stl):
         write_stl(stl, torus_triangles())
-    return {"sqw": sqw, "stl": stl}
+    spec = os.path.join(GENERATED, "isis_spectrum.mcstas")
+    if not os.path.exists(spec):
+        write_isis_spectrum(spec)
+    return {"sqw": sqw, "stl": stl, "spectrum": spec}
 
 
 def let_like_kwargs(Ei=3.7, use_slit=0, slit_w=0.03):
     return dict(Ei=Ei, use_slit=use_slit, slit_w=slit_w)
+
+
+def let_like_misis_kwargs(Ei=3.7, use_slit=0, slit_w=0.03):
+    return dict(Ei=Ei, use_slit=use_slit, slit_w=slit_w,
+                spec_file=repr(ensure_inputs()["spectrum"]))
 
 
 def small_chain_kwargs():

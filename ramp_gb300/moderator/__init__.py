@@ -1,3 +1,4 @@
 """Moderator plugins (mcramp/moderator/*)."""
 from .flat_mod import MFlat
 from .cont_mod import MCont
+from .isis_mod import MISIS

@@ -39,7 +39,7 @@ def test_version_and_error_string(lib):
 
 def test_struct_sizes_match_header_layout():
     assert ctypes.sizeof(_abi.RampComp) == 464
-    assert ctypes.sizeof(_abi.RampSource) == 72
+    assert ctypes.sizeof(_abi.RampSource) == 136
     assert ctypes.sizeof(_abi.RampRng) == 24
     assert ctypes.sizeof(_abi.RampState) == 24
 

@@ -121,6 +121,29 @@ def test_native_keying_matches_oracle(cuda_lib):
     check_plain(I.path("let_like.json"), I.let_like_kwargs(), 500_000, rng="native")
 
 
+def test_misis_chain_plain_matches_oracle(cuda_lib):
+    """The tabulated ISIS moderator: bisection on the device, the
+    reference's linear scan in the oracle; records bit-identical."""
+    check_plain(I.path("let_like_misis.json"), I.let_like_misis_kwargs(), 300_000)
+
+
+def test_misis_chain_fused_and_native(cuda_lib):
+    gi, ci, r = pair(I.path("let_like_misis.json"), I.let_like_misis_kwargs(), 400_000,
+                     path="fused")
+    tallies_close(gi, ci)
+    check_plain(I.path("let_like_misis.json"), I.let_like_misis_kwargs(), 100_000, rng="native")
+
+
+def test_misis_rejects_decreasing_tables(cuda_lib):
+    inst = m.Instrument(I.path("let_like_misis.json"), "cuda", **I.let_like_misis_kwargs())
+    inst.source.spectrum = dict(inst.source.spectrum)
+    flux = inst.source.spectrum["flux"].copy()
+    flux[5] = flux[4] - 1.0
+    inst.source.spectrum["flux"] = flux
+    with pytest.raises(RuntimeError, match="decreases"):
+        inst.execute(1000)
+
+
 # ---------------------------------------------------------------- fused path
 @pytest.mark.parametrize("fn,kw,N", [
     ("small_chain.json", "small", 300_000),
