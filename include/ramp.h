@@ -87,8 +87,10 @@ enum RampScatKind {
   RAMP_S_DET2D     = 7,   /* SDetector2D  scat/detector2D.cl:31         */
   RAMP_S_COUNTER   = 8,   /* SCounter     scat/counter.cl:18            */
   RAMP_S_BEAMSTOP  = 9,   /* SBeamstop    scat/beamstop.cl:3            */
-  RAMP_S_ATTENUATE = 10   /* SAttenuate   no reference counterpart: Beer-
+  RAMP_S_ATTENUATE = 10,  /* SAttenuate   no reference counterpart: Beer-
                              Lambert weight over the summed mesh chords */
+  RAMP_S_MONO      = 11,  /* SMonochromator scat/monochromator.cl:22    */
+  RAMP_S_POWDER1   = 12   /* SPowder1     scat/powder1.cl:5             */
 };
 
 /* ---- descriptors ------------------------------------------------------- */

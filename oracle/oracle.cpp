@@ -1128,6 +1128,162 @@ void s_attenuate(const Ctx&, int64_t, float* n, float* s, uint32_t* iidx, const 
   finish(n, s, iidx, k);
 }
 
+/* randnorm — mcramp/scat/monochromator.cl:10-20 (Box-Muller, cosine) */
+inline float o_randnorm(float* n, uint32_t tid, const Keying& kg) {
+  float u1 = o_rand(n, tid, kg);
+  float u2 = o_rand(n, tid, kg);
+  return sqrtf(-2.0f * rm_logf(u1)) * rm_cosf(2.0f * RC_PI * u2);
+}
+
+/* GAUSS(x, 0, rms) — mcramp/scat/monochromator.cl:5-8 */
+inline float o_gauss(float x, float rms) {
+  float d = x - 0.0f;
+  return rm_expf(-d * d / (2.0f * rms * rms)) / (sqrtf(2.0f * RC_PI) * rms);
+}
+
+/* monochromator — mcramp/scat/monochromator.cl:22-195.
+ * sp: slab_width, slab_height, gap, mosaic_h, mosaic_v, r0, d_spacing,
+ * radius_vertical, radius_horizontal; si: n_horizontal, n_vertical;
+ * table[0], table[1]: Gauss-Legendre nodes and weights */
+void s_mono(const Ctx& c, int64_t i, float* n, float* s, uint32_t* iidx, const RampComp& k) {
+  uint32_t tid = c.tid_base + (uint32_t)i;
+  const float slab_width = k.sp[0], slab_height = k.sp[1], gap = k.sp[2];
+  const float mosaic_h = k.sp[3], mosaic_v = k.sp[4], r0 = k.sp[5], d_spacing = k.sp[6];
+  const float radius_vertical = k.sp[7], radius_horizontal = k.sp[8];
+  const uint32_t n_h = (uint32_t)k.si[0], n_v = (uint32_t)k.si[1];
+  const float* gx = k.table[0];
+  const float* gw = k.table[1];
+  const uint32_t glen = (uint32_t)k.table_len[0];
+  set_pos(n, ipos2(s));
+  n[TOF] += s[7];
+  float mos_rms_y = RC_MIN2RAD * mosaic_h / sqrtf(8.0f * rm_logf(2.0f));
+  float mos_rms_z = RC_MIN2RAD * mosaic_v / sqrtf(8.0f * rm_logf(2.0f));
+  float mos_rms_max = mos_rms_y > mos_rms_z ? mos_rms_y : mos_rms_z;
+  float Q = 2.0f * RC_PI / d_spacing;
+  float zmax = (((float)n_h * (slab_width + gap)) - gap) / 2.0f;
+  float zmin = -zmax;
+  float ymax = (((float)n_v * (slab_height + gap)) - gap) / 2.0f;
+  float ymin = -ymax;
+  if (n[2] > zmin && n[2] < zmax && n[1] > ymin && n[1] < ymax) {
+    float col = ceilf((n[2] - zmin) / (slab_width + gap));
+    float row = ceilf((n[1] - ymin) / (slab_height + gap));
+    float tilt_h = radius_horizontal > 0.0f
+        ? rm_asinf((col - (float)(n_h + 1) / 2.0f) * (slab_width + gap) / radius_horizontal)
+        : 0.0f;
+    float tilt_v = radius_vertical > 0.0f
+        ? -rm_asinf((row - (float)(n_v + 1) / 2.0f) * (slab_height + gap) / radius_vertical)
+        : 0.0f;
+    float center_z = zmin + (col - 0.5f) * (slab_width + gap) - gap / 2.0f;
+    float center_y = ymin + (row - 0.5f) * (slab_height + gap) - gap / 2.0f;
+    V3 slab_pos = v3(0.0f, center_y, center_z);
+    float slab_rot[3] = {0.0f, tilt_h, tilt_v};
+    set_vel(n, frame_derotate(nvel(n), slab_rot));
+    set_pos(n, sub(npos(n), slab_pos));
+    set_pos(n, frame_derotate(npos(n), slab_rot));
+    if (fabsf(n[2]) <= slab_width / 2.0f && fabsf(n[1]) <= slab_height / 2.0f) {
+      V3 ki = mul(RC_V2K, nvel(n));
+      float ratio = -2.0f * ki.x / Q;
+      float Q_order = floorf(ratio + 0.5f);
+      if (Q_order == 0.0f) Q_order = ratio < 0.0f ? -1.0f : 1.0f;
+      if (Q_order < 0.0f) Q_order = -Q_order;
+      V3 ku = normalize(ki);
+      if (Q_order > 2.0f * length(ki) / Q) Q_order -= 1.0f;
+      float q0 = Q_order * Q;
+      float q0x = ratio < 0.0f ? -q0 : q0;
+      float theta = rm_asinf(q0 / (2.0f * length(ki)));
+      float delta = rm_asinf(fabsf(ku.x)) - theta;
+      float l12 = sqrtf(ki.y * ki.y + ki.z * ki.z);
+      float p_reflect = fabsf(r0) *
+          rm_expf(-ki.z * ki.z / (l12 * l12) * delta * delta / (2.0f * mos_rms_y * mos_rms_y)) *
+          rm_expf(-ki.y * ki.y / (l12 * l12) * delta * delta / (2.0f * mos_rms_z * mos_rms_z));
+      if (o_rand(n, tid, c.kg) <= p_reflect) {
+        float cos_2theta = rm_cosf(2.0f * theta);
+        float k_sin_2theta = length(ki) * rm_sinf(2.0f * theta);
+        V3 b = normalize(cross(ki, v3(q0x, 0.0f, 0.0f)));
+        b = mul(k_sin_2theta, b);
+        V3 a = cross(b, ku);
+        float total = 0.0f;
+        float mos_sample = mos_rms_max / rm_cosf(theta);
+        V3 c1 = mul(cos_2theta - 1.0f, ki);
+        float w = 0.0f;
+        V3 q;
+        for (uint32_t it = 0; it < 100; it++) {
+          w = 5.0f * mos_sample;
+          float cos_phi = rm_cosf(w), sin_phi = rm_sinf(w);
+          q = add(add(c1, mul(cos_phi, a)), mul(sin_phi, b));
+          q.y = q.y / mos_rms_z;
+          q.z = q.z / mos_rms_y;
+          if (q.z * q.z + q.y * q.y < (25.0f / (2.0f / 3.0f)) * (q.x * q.x)) break;
+          mos_sample *= (2.0f / 3.0f);
+        }
+        for (uint32_t g = 0; g < glen; g++) {
+          float phi = w * gx[g];
+          float cos_phi = rm_cosf(phi), sin_phi = rm_sinf(phi);
+          q = add(add(c1, mul(cos_phi, a)), mul(sin_phi, b));
+          p_reflect = o_gauss(q.z / q.x, mos_rms_y) * o_gauss(q.y / q.x, mos_rms_z);
+          total += gw[g] * p_reflect;
+        }
+        total *= w;
+        float phi = mos_sample * o_randnorm(n, tid, c.kg);
+        float cos_phi = rm_cosf(phi), sin_phi = rm_sinf(phi);
+        q = add(add(c1, mul(cos_phi, a)), mul(sin_phi, b));
+        p_reflect = o_gauss(q.z / q.x, mos_rms_y) * o_gauss(q.y / q.x, mos_rms_z);
+        set_vel(n, mul(RC_K2V, add(ki, q)));
+        p_reflect /= total * o_gauss(phi, mos_sample);
+        if (p_reflect > 1.0f) p_reflect = 1.0f;
+        n[P] *= p_reflect;
+      }
+    }
+    set_pos(n, frame_rotate(npos(n), slab_rot));
+    set_pos(n, add(npos(n), slab_pos));
+    set_vel(n, frame_rotate(nvel(n), slab_rot));
+  }
+  finish(n, s, iidx, k);
+}
+
+/* powder1 — mcramp/scat/powder1.cl:5-100.  sp: sigma_scat*v^2,
+ * sigma_abs*v, q, d_phi */
+void s_powder1(const Ctx& c, int64_t i, float* n, float* s, uint32_t* iidx, const RampComp& k) {
+  uint32_t tid = c.tid_base + (uint32_t)i;
+  const float sigma_scat_v2 = k.sp[0], sigma_abs_v = k.sp[1], q = k.sp[2], d_phi = k.sp[3];
+  n[TOF] += s[3];
+  V3 path = sub(ipos2(s), ipos1(s));
+  float full_path_length = length(path);
+  float vel = length(nvel(n));
+  float sigma_scat = sigma_scat_v2 / (vel * vel * RC_V2K * RC_V2K);
+  float sigma_abs = sigma_abs_v * 2200.0f / vel;
+  float p_scat = sigma_scat / (sigma_abs + sigma_scat);
+  float p_inter = 1 - rm_expf(-(sigma_scat + sigma_abs) * full_path_length);
+  float arg = q * RC_K2V / (2.0f * vel);
+  if (arg > 1.0f) {
+    finish(n, s, iidx, k);
+    return;
+  }
+  float twotheta = 2.0f * rm_asinf(arg);
+  n[P] *= p_scat;
+  float pen_depth = -rm_logf(1.0f - o_rand(n, tid, c.kg) * (1.0f - p_inter)) /
+                    (sigma_abs + sigma_scat);
+  V3 beam_para = normalize(nvel(n));
+  V3 beam_perp = cross(beam_para, v3(0.0f, 1.0f, 0.0f));
+  if (length(beam_perp) < 1e-3f) beam_perp = normalize(cross(beam_para, v3(1.0f, 0.0f, 0.0f)));
+  else beam_perp = normalize(beam_perp);
+  float phi;
+  if (d_phi != 0.0f) {
+    phi = (2.0f * o_rand(n, tid, c.kg) - 1.0f) * (d_phi * RC_PI / 180.0f);
+    if (o_rand(n, tid, c.kg) > 0.5f) phi += RC_PI;
+    phi += RC_PI / 2.0f;
+  } else {
+    phi = 2.0f * RC_PI * o_rand(n, tid, c.kg);
+  }
+  beam_perp = rotate_about_axis(phi, beam_para, beam_perp);
+  beam_para = rotate_about_axis(twotheta, beam_perp, beam_para);
+  set_pos(n, add(ipos1(s), mul(pen_depth, path)));
+  set_vel(n, mul(vel, normalize(beam_para)));
+  n[TOF] += s[7] - s[3];
+  n[P] *= full_path_length * sigma_scat * rm_expf(-(sigma_scat + sigma_abs) * full_path_length);
+  finish(n, s, iidx, k);
+}
+
 void scatter(const Ctx& c, const RampComp& k) {
 #pragma omp parallel for schedule(dynamic, 4096)
   for (int64_t i = 0; i < c.n; ++i) {
@@ -1147,6 +1303,8 @@ void scatter(const Ctx& c, const RampComp& k) {
       case RAMP_S_COUNTER: s_counter(c, i, n, s, ii, k); break;
       case RAMP_S_BEAMSTOP: s_beamstop(c, i, n, s, ii, k); break;
       case RAMP_S_ATTENUATE: s_attenuate(c, i, n, s, ii, k); break;
+      case RAMP_S_MONO: s_mono(c, i, n, s, ii, k); break;
+      case RAMP_S_POWDER1: s_powder1(c, i, n, s, ii, k); break;
       default: break;
     }
   }

@@ -170,7 +170,7 @@ static int validate_comp(const RampComp& c, int j) {
     set_err("component %d: unknown geometry kind %d", j, c.geom);
     return RAMP_E_UNSUPPORTED;
   }
-  if (c.scat < RAMP_S_ARM || c.scat > RAMP_S_ATTENUATE) {
+  if (c.scat < RAMP_S_ARM || c.scat > RAMP_S_POWDER1) {
     set_err("component %d: unknown scatter kind %d", j, c.scat);
     return RAMP_E_UNSUPPORTED;
   }

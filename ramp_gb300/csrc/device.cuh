@@ -924,6 +924,185 @@ DI void s_powdern(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDe
   s_finish(c, n, s, ii);
 }
 
+/* randnorm — monochromator.cl:10-20 (Box-Muller, cosine branch) */
+DI float randnorm(Nt& n, Rng& r) {
+  float u1 = draw(n, r);
+  float u2 = draw(n, r);
+  return sqrtf(-2.0f * rm_logf(u1)) * rm_cosf(2.0f * RC_PI * u2);
+}
+
+/* GAUSS(x, 0, rms) — monochromator.cl:5-8 */
+DI float gauss0(float x, float rms) {
+  float d = x - 0.0f;
+  return rm_expf(-d * d / (2.0f * rms * rms)) / (sqrtf(2.0f * RC_PI) * rms);
+}
+
+/* frame matrix of a rotation given by angles, as geom.h:21-53 builds it */
+DI void frame_matrix(float x_a, float y_a, float z_a, float* R) {
+  float sx, cx, sy, cy, sz, cz;
+  rm_sincosf(x_a, &sx, &cx);
+  rm_sincosf(y_a, &sy, &cy);
+  rm_sincosf(z_a, &sz, &cz);
+  R[0] = cy * cz;
+  R[1] = -cx * sz + sx * sy * cz;
+  R[2] = sx * sz + cx * sy * cz;
+  R[3] = cy * sz;
+  R[4] = cx * cz + sx * sy * sz;
+  R[5] = -sx * cz + cx * sy * sz;
+  R[6] = -sy;
+  R[7] = sx * cy;
+  R[8] = cx * cy;
+}
+
+/* SMonochromator — monochromator.cl:22-195: a mosaic crystal of
+ * n_horizontal x n_vertical slabs (optionally curved), Bragg reflection of
+ * the allowed order from the local yz plane with an anisotropic Gaussian
+ * mosaic; the outgoing direction is sampled around the Bragg cone and
+ * weighted by the mosaic over a 15-point Gauss-Legendre normalisation.
+ * sp: slab_width, slab_height, gap, mosaic_h, mosaic_v (arc min), r0,
+ * d_spacing, radius_vertical, radius_horizontal; si: n_horizontal,
+ * n_vertical; tab[0], tab[1]: Gauss-Legendre nodes and weights */
+DI void s_mono(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
+  const float slab_width = c.sp[0], slab_height = c.sp[1], gap = c.sp[2];
+  const float mosaic_h = c.sp[3], mosaic_v = c.sp[4], r0 = c.sp[5], d_spacing = c.sp[6];
+  const float radius_vertical = c.sp[7], radius_horizontal = c.sp[8];
+  const uint32_t n_h = (uint32_t)c.si[0], n_v = (uint32_t)c.si[1];
+  const float* __restrict__ gx = c.tab[0];
+  const float* __restrict__ gw = c.tab[1];
+  const uint32_t glen = (uint32_t)c.tab_len[0];
+  set_pos(n, ip2(s));
+  n.t += s.t2;
+  float mos_rms_y = RC_MIN2RAD * mosaic_h / sqrtf(8.0f * rm_logf(2.0f));
+  float mos_rms_z = RC_MIN2RAD * mosaic_v / sqrtf(8.0f * rm_logf(2.0f));
+  float mos_rms_max = mos_rms_y > mos_rms_z ? mos_rms_y : mos_rms_z;
+  float Q = 2.0f * RC_PI / d_spacing;
+  float zmax = (((float)n_h * (slab_width + gap)) - gap) / 2.0f;
+  float zmin = -zmax;
+  float ymax = (((float)n_v * (slab_height + gap)) - gap) / 2.0f;
+  float ymin = -ymax;
+  if (n.z > zmin && n.z < zmax && n.y > ymin && n.y < ymax) {
+    float col = ceilf((n.z - zmin) / (slab_width + gap));
+    float row = ceilf((n.y - ymin) / (slab_height + gap));
+    float tilt_h = radius_horizontal > 0.0f
+        ? rm_asinf((col - (float)(n_h + 1) / 2.0f) * (slab_width + gap) / radius_horizontal)
+        : 0.0f;
+    float tilt_v = radius_vertical > 0.0f
+        ? -rm_asinf((row - (float)(n_v + 1) / 2.0f) * (slab_height + gap) / radius_vertical)
+        : 0.0f;
+    float center_z = zmin + (col - 0.5f) * (slab_width + gap) - gap / 2.0f;
+    float center_y = ymin + (row - 0.5f) * (slab_height + gap) - gap / 2.0f;
+    V3 slab_pos = v3(0.0f, center_y, center_z);
+    float R[9];
+    frame_matrix(0.0f, tilt_h, tilt_v, R);
+    set_vel(n, rot_inv(R, nvel(n)));
+    set_pos(n, sub(npos(n), slab_pos));
+    set_pos(n, rot_inv(R, npos(n)));
+    if (fabsf(n.z) <= slab_width / 2.0f && fabsf(n.y) <= slab_height / 2.0f) {
+      V3 ki = mul(RC_V2K, nvel(n));
+      float ratio = -2.0f * ki.x / Q;
+      float Q_order = floorf(ratio + 0.5f);
+      if (Q_order == 0.0f) Q_order = ratio < 0.0f ? -1.0f : 1.0f;
+      if (Q_order < 0.0f) Q_order = -Q_order;
+      V3 ku = normalize(ki);
+      if (Q_order > 2.0f * len3(ki) / Q) Q_order -= 1.0f;
+      float q0 = Q_order * Q;
+      float q0x = ratio < 0.0f ? -q0 : q0;
+      float theta = rm_asinf(q0 / (2.0f * len3(ki)));
+      float delta = rm_asinf(fabsf(ku.x)) - theta;
+      float l12 = sqrtf(ki.y * ki.y + ki.z * ki.z);
+      float p_reflect = fabsf(r0) *
+          rm_expf(-ki.z * ki.z / (l12 * l12) * delta * delta / (2.0f * mos_rms_y * mos_rms_y)) *
+          rm_expf(-ki.y * ki.y / (l12 * l12) * delta * delta / (2.0f * mos_rms_z * mos_rms_z));
+      if (draw(n, r) <= p_reflect) {
+        float cos_2theta = rm_cosf(2.0f * theta);
+        float k_sin_2theta = len3(ki) * rm_sinf(2.0f * theta);
+        V3 b = normalize(cross(ki, v3(q0x, 0.0f, 0.0f)));
+        b = mul(k_sin_2theta, b);
+        V3 a = cross(b, ku);
+        float total = 0.0f;
+        float mos_sample = mos_rms_max / rm_cosf(theta);
+        V3 c1 = mul(cos_2theta - 1.0f, ki);
+        float w = 0.0f;
+        V3 q;
+        for (uint32_t it = 0; it < 100; it++) {
+          w = 5.0f * mos_sample;
+          float sin_phi, cos_phi;
+          rm_sincosf(w, &sin_phi, &cos_phi);
+          q = add(add(c1, mul(cos_phi, a)), mul(sin_phi, b));
+          q.y = q.y / mos_rms_z;
+          q.z = q.z / mos_rms_y;
+          if (q.z * q.z + q.y * q.y < (25.0f / (2.0f / 3.0f)) * (q.x * q.x)) break;
+          mos_sample *= (2.0f / 3.0f);
+        }
+        for (uint32_t g = 0; g < glen; g++) {
+          float phi = w * __ldg(gx + g);
+          float sin_phi, cos_phi;
+          rm_sincosf(phi, &sin_phi, &cos_phi);
+          q = add(add(c1, mul(cos_phi, a)), mul(sin_phi, b));
+          p_reflect = gauss0(q.z / q.x, mos_rms_y) * gauss0(q.y / q.x, mos_rms_z);
+          total += __ldg(gw + g) * p_reflect;
+        }
+        total *= w;
+        float phi = mos_sample * randnorm(n, r);
+        float sin_phi, cos_phi;
+        rm_sincosf(phi, &sin_phi, &cos_phi);
+        q = add(add(c1, mul(cos_phi, a)), mul(sin_phi, b));
+        p_reflect = gauss0(q.z / q.x, mos_rms_y) * gauss0(q.y / q.x, mos_rms_z);
+        set_vel(n, mul(RC_K2V, add(ki, q)));
+        p_reflect /= total * gauss0(phi, mos_sample);
+        if (p_reflect > 1.0f) p_reflect = 1.0f;
+        n.p *= p_reflect;
+      }
+    }
+    set_pos(n, rot_fwd(R, npos(n)));
+    set_pos(n, add(npos(n), slab_pos));
+    set_vel(n, rot_fwd(R, nvel(n)));
+  }
+  s_finish(c, n, s, ii);
+}
+
+/* SPowder1 — powder1.cl:5-100: one Bragg line; the neutron scatters onto
+ * the Debye-Scherrer cone at a depth drawn from the attenuation, with
+ * optional phi focusing.  sp: sigma_scat*v^2, sigma_abs*v, q, d_phi */
+DI void s_powder1(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
+  const float sigma_scat_v2 = c.sp[0], sigma_abs_v = c.sp[1], q = c.sp[2], d_phi = c.sp[3];
+  n.t += s.t1;
+  V3 path = sub(ip2(s), ip1(s));
+  float full_path_length = len3(path);
+  float vel = len3(nvel(n));
+  float sigma_scat = sigma_scat_v2 / (vel * vel * RC_V2K * RC_V2K);
+  float sigma_abs = sigma_abs_v * 2200.0f / vel;
+  float p_scat = sigma_scat / (sigma_abs + sigma_scat);
+  float p_inter = 1 - rm_expf(-(sigma_scat + sigma_abs) * full_path_length);
+  float arg = q * RC_K2V / (2.0f * vel);
+  if (arg > 1.0f) {
+    s_finish(c, n, s, ii);
+    return;
+  }
+  float twotheta = 2.0f * rm_asinf(arg);
+  n.p *= p_scat;
+  float pen_depth = -rm_logf(1.0f - draw(n, r) * (1.0f - p_inter)) / (sigma_abs + sigma_scat);
+  V3 beam_para = normalize(nvel(n));
+  V3 beam_perp = cross(beam_para, v3(0.0f, 1.0f, 0.0f));
+  if (len3(beam_perp) < 1e-3f) beam_perp = normalize(cross(beam_para, v3(1.0f, 0.0f, 0.0f)));
+  else beam_perp = normalize(beam_perp);
+  float phi;
+  if (d_phi != 0.0f) {
+    phi = (2.0f * draw(n, r) - 1.0f) * (d_phi * RC_PI / 180.0f);
+    if (draw(n, r) > 0.5f) phi += RC_PI;
+    phi += RC_PI / 2.0f;
+  } else {
+    phi = 2.0f * RC_PI * draw(n, r);
+  }
+  beam_perp = rotate_about_axis(phi, beam_para, beam_perp);
+  beam_para = rotate_about_axis(twotheta, beam_perp, beam_para);
+  set_pos(n, add(ip1(s), mul(pen_depth, path)));
+  set_vel(n, mul(vel, normalize(beam_para)));
+  n.t += s.t2 - s.t1;
+  n.p *= full_path_length * sigma_scat * rm_expf(-(sigma_scat + sigma_abs) * full_path_length);
+  s_finish(c, n, s, ii);
+}
+
 /* detector1D.cl:20-77 */
 template <class D = NoDiff>
 DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* dx = nullptr) {
@@ -1030,6 +1209,8 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
       break;
     case RAMP_S_BEAMSTOP: set_die(n, 1.0f); s_finish(c, n, s, ii); break;
     case RAMP_S_ATTENUATE: s_attenuate(c, n, s, ii); break;
+    case RAMP_S_MONO: s_mono(c, n, s, ii, r); break;
+    case RAMP_S_POWDER1: s_powder1(c, n, s, ii, r); break;
     default: break;
   }
 }

@@ -47,6 +47,8 @@ DI void scatter_k(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDe
       break;
     case RAMP_S_BEAMSTOP: set_die(n, 1.0f); s_finish(c, n, s, ii); break;
     case RAMP_S_ATTENUATE: s_attenuate(c, n, s, ii); break;
+    case RAMP_S_MONO: s_mono(c, n, s, ii, r); break;
+    case RAMP_S_POWDER1: s_powder1(c, n, s, ii, r); break;
     default: break;
   }
 }
@@ -83,12 +85,14 @@ __global__ void __launch_bounds__(PLAIN_BLOCK)
 k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
   constexpr bool RD_P = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
                         SK == RAMP_S_DET1D || SK == RAMP_S_DET2D || SK == RAMP_S_COUNTER ||
-                        SK == RAMP_S_ATTENUATE;
+                        SK == RAMP_S_ATTENUATE || SK == RAMP_S_MONO || SK == RAMP_S_POWDER1;
   constexpr bool RD_T = SK == RAMP_S_GUIDE || SK == RAMP_S_CHOPPER || SK == RAMP_S_ISOTROPIC ||
                         SK == RAMP_S_POWDERN || SK == RAMP_S_DET1D || SK == RAMP_S_DET2D ||
-                        SK == RAMP_S_ATTENUATE;
-  constexpr bool RD_SB = SK == RAMP_S_CHOPPER || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN;
-  constexpr bool MOD_VEL = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN;
+                        SK == RAMP_S_ATTENUATE || SK == RAMP_S_MONO || SK == RAMP_S_POWDER1;
+  constexpr bool RD_SB = SK == RAMP_S_CHOPPER || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
+                         SK == RAMP_S_MONO || SK == RAMP_S_POWDER1;
+  constexpr bool MOD_VEL = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
+                           SK == RAMP_S_MONO || SK == RAMP_S_POWDER1;
   constexpr bool USE_POL = SK == RAMP_S_ISOTROPIC;
   const int64_t st = a.stride;
   float* __restrict__ S = a.soa;
@@ -177,7 +181,7 @@ cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_
     break;
     CASE(RAMP_S_ARM) CASE(RAMP_S_GUIDE) CASE2(RAMP_S_CHOPPER) CASE2(RAMP_S_ISOTROPIC)
     CASE2(RAMP_S_POWDERN) CASE(RAMP_S_DET1D) CASE(RAMP_S_DET2D) CASE(RAMP_S_COUNTER)
-    CASE(RAMP_S_BEAMSTOP) CASE(RAMP_S_ATTENUATE)
+    CASE(RAMP_S_BEAMSTOP) CASE(RAMP_S_ATTENUATE) CASE2(RAMP_S_MONO) CASE2(RAMP_S_POWDER1)
 #undef CASE
 #undef CASE2
     default: return cudaErrorInvalidValue;

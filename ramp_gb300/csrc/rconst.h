@@ -17,6 +17,7 @@
 #define RC_E2KS    (1.0f / 2.072f)       /*                    consts.h:32 */
 #define RC_KB      (8.6173f * 10e-2f)    /* 0.86173            consts.h:36 */
 #define RC_EV_J    1.6021765e-22f        /* meV -> J      cont_mod.cl:20   */
+#define RC_MIN2RAD (RC_PI / (180.0f * 60.0f))  /* arc minute -> rad consts.h:20 */
 
 /* intersection record reset value (doc/writing/buffers.rst:50-80) */
 #define RC_T_RESET 100000.0f

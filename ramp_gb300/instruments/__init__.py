@@ -12,6 +12,9 @@ the benchmark and parity workloads, and generators for their inputs.
 * let_like_misis.json — the LET-like chain fed by the tabulated ISIS
   moderator (MISIS) from a seeded synthetic spectrum file in the McStas/MCNP
   tally format ($spec_file$).
+* powder_diffractometer.json — curved PG(002) mosaic monochromator at the
+  Bragg angle for $Ei$ ($mono_angle$), one-line powder sphere (SPowder1),
+  banana detector with a 1D 2theta histogram (-10..150 deg, 0.1 deg).
 * mesh_imaging.json — near-parallel flat beam through a seeded perturbed
   torus mesh (GMesh + SAttenuate, mu 0.5 /cm) rotated by $angle$, onto a
   1024 x 1024 pixel detector.
@@ -137,6 +140,13 @@ def let_like_kwargs(Ei=3.7, use_slit=0, slit_w=0.03):
 def let_like_misis_kwargs(Ei=3.7, use_slit=0, slit_w=0.03):
     return dict(Ei=Ei, use_slit=use_slit, slit_w=slit_w,
                 spec_file=repr(ensure_inputs()["spectrum"]))
+
+
+def powder_diffractometer_kwargs(Ei=14.7, d_mono=3.355):
+    """Incident energy (meV) and the monochromator Bragg angle for it
+    (rad): sin(theta) = lambda / 2d, lambda = 9.045 / sqrt(Ei) AA."""
+    lam = 9.04456 / np.sqrt(Ei)
+    return dict(Ei=Ei, mono_angle=float(np.arcsin(lam / (2.0 * d_mono))))
 
 
 def small_chain_kwargs():

@@ -10,3 +10,5 @@ from .detector1D import SDetector1D
 from .detector2D import SDetector2D
 from .counter import SCounter
 from .attenuate import SAttenuate
+from .monochromator import SMonochromator
+from .powder1 import SPowder1

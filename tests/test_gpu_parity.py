@@ -144,6 +144,22 @@ def test_misis_rejects_decreasing_tables(cuda_lib):
         inst.execute(1000)
 
 
+@pytest.mark.parametrize("rng", ["reference", "native"])
+def test_powder_diffractometer_plain_matches_oracle(cuda_lib, rng):
+    """Curved mosaic monochromator (slab tilts, Bragg orders, mosaic
+    quadrature, Box-Muller draw) and a one-line powder: records
+    bit-identical."""
+    check_plain(I.path("powder_diffractometer.json"), I.powder_diffractometer_kwargs(),
+                300_000, rng=rng)
+
+
+def test_powder_diffractometer_fused_matches_oracle(cuda_lib):
+    gi, ci, r = pair(I.path("powder_diffractometer.json"), I.powder_diffractometer_kwargs(),
+                     500_000, path="fused")
+    tallies_close(gi, ci)
+    assert gi.oob_drops == r.oob
+
+
 # ---------------------------------------------------------------- fused path
 @pytest.mark.parametrize("fn,kw,N", [
     ("small_chain.json", "small", 300_000),

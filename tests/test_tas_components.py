@@ -1,0 +1,55 @@
+"""SMonochromator and SPowder1: host preparation against the reference's
+own plugins (golden values made by tests/golden/make_tas_golden.py), and
+the oracle's powder diffractometer against the Bragg law."""
+import os
+import random
+
+import numpy as np
+
+import ramp_gb300 as m
+from ramp_gb300 import _abi, instruments as I
+from ramp_gb300.scat.monochromator import gauss_legendre_15
+
+GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "tas_host.npz"))
+
+
+def test_quadrature_tables_match_reference():
+    x, w = gauss_legendre_15()
+    assert np.array_equal(x, GOLD["gauss_x"].astype(np.float32))
+    assert np.array_equal(w, GOLD["gauss_w"].astype(np.float32))
+
+
+def test_powder1_constants_match_reference():
+    for case, want in zip(GOLD["powder1_cases"], GOLD["powder1"]):
+        d, pack, vc, sa, mult, dw, f2, dphi = case
+        p = m.SPowder1(d_spacing=d, pack=pack, vc=vc, sigma_abs=sa, multiplicity=int(mult),
+                       DW=dw, F2=f2, d_phi=dphi)
+        got = np.array([p.sigma_scat_v2, p.sigma_abs_v, p.q, p.d_phi], dtype=np.float32)
+        assert np.array_equal(got, want)
+
+
+def test_descriptor_slots():
+    inst = m.Instrument(I.path("powder_diffractometer.json"), "cpu",
+                        **I.powder_diffractometer_kwargs())
+    keep = []
+    _, carr, nc, _, _ = inst.descriptors(keep)
+    kinds = [carr[j].scat for j in range(nc)]
+    assert _abi.S_MONO in kinds and _abi.S_POWDER1 in kinds
+    j = kinds.index(_abi.S_MONO)
+    assert carr[j].table_len[0] == 15 and carr[j].si[0] == 4
+
+
+def test_oracle_diffraction_peak_at_bragg_angle():
+    """Ei 14.7 meV through the monochromator, d = 2.5 AA powder line: the
+    detector peak sits at 2 asin(lambda / 2d)."""
+    import oracle
+    kw = I.powder_diffractometer_kwargs(Ei=14.7)
+    inst = m.Instrument(I.path("powder_diffractometer.json"), "cpu", **kw)
+    random.seed(1)
+    oracle.run(inst, 200_000)
+    h = inst.tallies()[0].numpy()
+    assert h.sum() > 0
+    lam = 9.04456 / np.sqrt(14.7)
+    two_theta = 2 * np.degrees(np.arcsin(lam / (2 * 2.5)))
+    peak = -10.0 + 0.1 * (np.argmax(h) + 0.5)
+    assert abs(peak - two_theta) < 0.5
