@@ -90,7 +90,11 @@ enum RampScatKind {
   RAMP_S_ATTENUATE = 10,  /* SAttenuate   no reference counterpart: Beer-
                              Lambert weight over the summed mesh chords */
   RAMP_S_MONO      = 11,  /* SMonochromator scat/monochromator.cl:22    */
-  RAMP_S_POWDER1   = 12   /* SPowder1     scat/powder1.cl:5             */
+  RAMP_S_POWDER1   = 12,  /* SPowder1     scat/powder1.cl:5             */
+  RAMP_S_RESCAL    = 13   /* SRescal      scat/rescal.cl:5: writes one
+                             8-float event per neutron index into the
+                             buffer bound by ramp_plan_set_buffer; plain
+                             path, linear blocks only                   */
 };
 
 /* ---- descriptors ------------------------------------------------------- */
@@ -224,6 +228,11 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps,
                      int n_comps, const RampBlock* blocks, int n_blocks,
                      RampPlan** out);
 int ramp_plan_destroy(RampPlan* plan);
+
+/* Bind component comp's output buffer (device, len floats): the event
+ * list of an SRescal component (8 floats per neutron index of a chunk).
+ * Replaces the buffer the descriptor named at plan creation.            */
+int ramp_plan_set_buffer(RampPlan* plan, int32_t comp, float* buf, int64_t len);
 
 /* Allocate the plan's survivor buffer for split fused launches
  * (RampTune.split) of up to n histories now, e.g. before capturing them

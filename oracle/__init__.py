@@ -103,8 +103,6 @@ def run(inst, N, chunk=None, rng_mode=0, run_seed=0, variant=0, threads=0, seeds
     for t in inst.tallies():
         if t.device.type != "cpu":
             raise ValueError("the oracle needs an Instrument with ctx='cpu'")
-    keep = []
-    src, carr, nc, barr, nb = inst.descriptors(keep)
     N = int(N)
     buf_max = int(chunk) if chunk else N
     first = min(N, buf_max)
@@ -113,6 +111,11 @@ def run(inst, N, chunk=None, rng_mode=0, run_seed=0, variant=0, threads=0, seeds
         rank, world = shard
         s_lo, s_hi = first * rank // world, first * (rank + 1) // world
         first = max(1, s_hi - s_lo)
+    events = inst.event_components()
+    for _, sc in events:             # per-index event buffers (SRescal)
+        sc.prepare(first, torch.device("cpu"))
+    keep = []
+    src, carr, nc, barr, nb = inst.descriptors(keep)
     neutrons = np.zeros((first, 16), dtype=np.float32)
     isect = np.zeros((first, 8), dtype=np.float32)
     iidx = np.zeros(first, dtype=np.uint32)
@@ -136,6 +139,8 @@ def run(inst, N, chunk=None, rng_mode=0, run_seed=0, variant=0, threads=0, seeds
             if nrec == 0:
                 last = 0
                 continue
+        for _, sc in events:
+            sc.begin_chunk()
         rc = lib().oracle_execute_chunk(ctypes.addressof(src), ctypes.addressof(carr), nc,
                                         ctypes.addressof(barr), nb, neutrons.ctypes.data,
                                         isect.ctypes.data, iidx.ctypes.data, nrec,
@@ -147,4 +152,9 @@ def run(inst, N, chunk=None, rng_mode=0, run_seed=0, variant=0, threads=0, seeds
         tot_flags |= flags.value
         tot_oob += oob.value
         last = nrec
+        if events:
+            import torch as _t
+            se = _t.from_numpy(neutrons[:, 14].copy())
+            for _, sc in events:
+                sc.reduce(se, nrec)
     return Result(neutrons[:last], isect[:last], iidx[:last], tot_flags, tot_oob)

@@ -1284,6 +1284,45 @@ void s_powder1(const Ctx& c, int64_t i, float* n, float* s, uint32_t* iidx, cons
   finish(n, s, iidx, k);
 }
 
+/* rescal — mcramp/scat/rescal.cl:5-76; the event goes to k.tally[8 i..],
+ * ev.s345 (never written by the reference) as 0.  sp: target xyz, E0, dE,
+ * focus_r */
+void s_rescal(const Ctx& c, int64_t i, float* n, float* s, uint32_t* iidx, const RampComp& k) {
+  uint32_t tid = c.tid_base + (uint32_t)i;
+  V3 target = v3(k.sp[0], k.sp[1], k.sp[2]);
+  const float E0 = k.sp[3], dE = k.sp[4], focus_r = k.sp[5];
+  V3 path = sub(ipos2(s), ipos1(s));
+  set_pos(n, add(ipos1(s), mul(o_rand(n, tid, c.kg), path)));
+  V3 ki = mul(RC_V2K, nvel(n));
+  float l2 = length(target) * length(target);
+  float costhetamax = sqrtf(l2 / (focus_r * focus_r + l2));
+  float theta = rm_acosf(1.0f - o_rand(n, tid, c.kg) * (1.0f - costhetamax));
+  float phi = o_rand(n, tid, c.kg) * 2.0f * RC_PI;
+  V3 target_perp;
+  if (target.x == 0.0f && target.z == 0.0f) target_perp = v3(1.0f, 0.0f, 0.0f);
+  else target_perp = v3(-target.z, 0.0f, target.x);
+  V3 target_perp_perp = cross(target, target_perp);
+  V3 target_final = target;
+  target_final = rotate_about_axis(theta, target_perp_perp, target_final);
+  target_final = rotate_about_axis(phi, target, target_final);
+  target_final = normalize(target_final);
+  float Ef = E0 + dE * (1.0f - 2.0f * o_rand(n, tid, c.kg));
+  float vf = RC_SE2V * sqrtf(Ef);
+  set_vel(n, mul(vf, target_final));
+  V3 kf = mul(RC_V2K, nvel(n));
+  float lk = length(mul(RC_K2V, ki));
+  if (k.tally && 8 * i + 8 <= k.tally_len) {
+    float* ev = k.tally + 8 * i;
+    ev[0] = ki.x - kf.x; ev[1] = ki.y - kf.y; ev[2] = ki.z - kf.z;
+    ev[3] = 0.0f; ev[4] = 0.0f; ev[5] = 0.0f;
+    ev[6] = n[P];
+    ev[7] = RC_VS2E * (lk * lk) - Ef;
+  } else {
+    c.oob->fetch_add(1);
+  }
+  finish(n, s, iidx, k);
+}
+
 void scatter(const Ctx& c, const RampComp& k) {
 #pragma omp parallel for schedule(dynamic, 4096)
   for (int64_t i = 0; i < c.n; ++i) {
@@ -1305,6 +1344,7 @@ void scatter(const Ctx& c, const RampComp& k) {
       case RAMP_S_ATTENUATE: s_attenuate(c, i, n, s, ii, k); break;
       case RAMP_S_MONO: s_mono(c, i, n, s, ii, k); break;
       case RAMP_S_POWDER1: s_powder1(c, i, n, s, ii, k); break;
+      case RAMP_S_RESCAL: s_rescal(c, i, n, s, ii, k); break;
       default: break;
     }
   }

@@ -7,7 +7,8 @@ from .moderator import MFlat, MCont, MISIS
 from .geom import (GPrim, GPlane, GCylinderExt, GBanana, GSphere, GSphereInt, GBox, GArm,
                    GMesh)
 from .scat import (SPrim, SArm, SBeamstop, SGuide, SChopper, SIsotropic, SPowderN,
-                   SDetector1D, SDetector2D, SCounter, SAttenuate, SMonochromator, SPowder1)
+                   SDetector1D, SDetector2D, SCounter, SAttenuate, SMonochromator, SPowder1,
+                   SRescal)
 from .instrument import Instrument, ExecutionBlock, KernelRef, frame_rotate, build_kernel
 
 __version__ = "0.1.0"

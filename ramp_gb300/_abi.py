@@ -18,11 +18,12 @@ LANE = dict(x=0, y=1, z=2, vx=3, vy=4, vz=5, px=6, py=7, pz=8, p=9, tof=10,
 SRC_FLAT, SRC_CONT, SRC_ISIS = 1, 2, 3
 G_PLANE, G_CYL_EXT, G_BANANA, G_SPHERE, G_SPHERE_INT, G_BOX, G_ARM, G_MESH = range(1, 9)
 (S_ARM, S_GUIDE, S_CHOPPER, S_ISOTROPIC, S_POWDERN, S_DET1D, S_DET2D, S_COUNTER,
- S_BEAMSTOP, S_ATTENUATE, S_MONO, S_POWDER1) = range(1, 13)
+ S_BEAMSTOP, S_ATTENUATE, S_MONO, S_POWDER1, S_RESCAL) = range(1, 14)
 
 NGP, NSP, NGI, NSI, NTAB = 12, 24, 4, 12, 12
 
 RAMP_OK = 0
+E_INVALID, E_CUDA, E_NOMEM, E_DEVICE, E_UNSUPPORTED, E_RANGE = -1, -2, -3, -4, -5, -6
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "device status flag raised", -5: "unsupported component",
           -6: "size beyond documented maximum"}
@@ -146,6 +147,8 @@ _SIGS = {
                      ctypes.c_int),
     "ramp_seed_advance": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "ramp_plan_reserve": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
+    "ramp_plan_set_buffer": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64],
+                             ctypes.c_int),
     "ramp_debug_threefry": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_math": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

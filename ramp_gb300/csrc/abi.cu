@@ -89,7 +89,18 @@ struct RampPlan {
   uint32_t* surv = nullptr;          /* survivor buffer of split launches */
   int64_t surv_cap = 0;              /* slots (128 per work item) */
   StreamSet streams;
+  bool plain_only = false;           /* a component writes per-index output */
 };
+
+/* whole-chain kernels (fused, batched, adjoint) cannot write per-index
+ * component output */
+static int check_whole_chain(const RampPlan* p, const char* who) {
+  if (p->plain_only) {
+    set_err("%s: SRescal writes one event per neutron index; use the plain path", who);
+    return RAMP_E_UNSUPPORTED;
+  }
+  return RAMP_OK;
+}
 
 /* ---------------------------------------------------------------------- */
 /* host float helpers: the same operations the device uses                 */
@@ -170,7 +181,7 @@ static int validate_comp(const RampComp& c, int j) {
     set_err("component %d: unknown geometry kind %d", j, c.geom);
     return RAMP_E_UNSUPPORTED;
   }
-  if (c.scat < RAMP_S_ARM || c.scat > RAMP_S_POWDER1) {
+  if (c.scat < RAMP_S_ARM || c.scat > RAMP_S_RESCAL) {
     set_err("component %d: unknown scatter kind %d", j, c.scat);
     return RAMP_E_UNSUPPORTED;
   }
@@ -427,6 +438,15 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
     if (!rc) rc = make_comp(p, comps[j], p->comps[j]);
     if (rc) { ramp_plan_destroy(p); return rc; }
   }
+  for (const RampComp& c : p->comps_in)
+    if (c.scat == RAMP_S_RESCAL) p->plain_only = true;
+  for (const RampBlock& B : p->blocks)
+    for (int j = B.first; !B.linear && j < B.first + B.count; ++j)
+      if (p->comps_in[j].scat == RAMP_S_RESCAL) {
+        set_err("component %d: SRescal must sit in a linear block", j);
+        ramp_plan_destroy(p);
+        return RAMP_E_UNSUPPORTED;
+      }
   void* d;
   rc = upload(p->comps.data(), p->comps.size() * sizeof(CompDev), &d, p->allocs);
   if (rc) { ramp_plan_destroy(p); return rc; }
@@ -566,6 +586,19 @@ static int attach_surv(RampPlan* p, FusedArgs& a, int64_t n_items, cudaStream_t 
   return RAMP_OK;
 }
 
+int ramp_plan_set_buffer(RampPlan* p, int32_t comp, float* buf, int64_t len) {
+  if (!p || comp < 0 || comp >= (int)p->comps.size() || len < 0 || (len > 0 && !buf)) {
+    set_err("ramp_plan_set_buffer: bad arguments");
+    return RAMP_E_INVALID;
+  }
+  p->comps[comp].tally = buf;
+  p->comps[comp].tally_len = len;
+  p->comps_in[comp].tally = buf;
+  p->comps_in[comp].tally_len = len;
+  CK(cudaMemcpy(p->comps_dev + comp, &p->comps[comp], sizeof(CompDev), cudaMemcpyHostToDevice));
+  return RAMP_OK;
+}
+
 int ramp_plan_reserve(RampPlan* p, int64_t n) {
   if (!p || n < 0) { set_err("ramp_plan_reserve: bad arguments"); return RAMP_E_INVALID; }
   return ensure_surv(p, (n + 127) / 128);
@@ -589,6 +622,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
     return RAMP_E_INVALID;
   }
   if (!p || n < 0) { set_err("ramp_trace_fused: bad arguments"); return RAMP_E_INVALID; }
+  if (int rc0 = check_whole_chain(p, "ramp_trace_fused")) return rc0;
   if ((int)p->comps.size() > RAMP_MAX_COMPS) {
     set_err("fused path supports at most %d components", RAMP_MAX_COMPS);
     return RAMP_E_RANGE;
@@ -695,6 +729,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     set_err("ramp_trace_batched: bad arguments");
     return RAMP_E_INVALID;
   }
+  if (int rc0 = check_whole_chain(p, "ramp_trace_batched")) return rc0;
   const int nc = (int)p->comps.size();
   if (nc > RAMP_MAX_COMPS) {
     set_err("fused path supports at most %d components", RAMP_MAX_COMPS);
@@ -862,6 +897,7 @@ int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det
     set_err("ramp_adjoint: bad arguments");
     return RAMP_E_INVALID;
   }
+  if (int rc0 = check_whole_chain(p, "ramp_adjoint")) return rc0;
   const int nc = (int)p->comps.size();
   if (det_comp < 0 || det_comp >= nc ||
       (p->comps[det_comp].scat != RAMP_S_DET2D && p->comps[det_comp].scat != RAMP_S_DET1D)) {
@@ -1054,6 +1090,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
     set_err("ramp_trace_batched_noalloc: bad arguments");
     return RAMP_E_INVALID;
   }
+  if (int rc0 = check_whole_chain(p, "ramp_trace_batched_noalloc")) return rc0;
   const int nc = (int)p->comps.size();
   if (nc > RAMP_MAX_COMPS) {
     set_err("ramp_trace_batched_noalloc: at most %d components", RAMP_MAX_COMPS);

@@ -1103,6 +1103,39 @@ DI void s_powder1(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
   s_finish(c, n, s, ii);
 }
 
+/* SRescal — rescal.cl:5-76: picks a scattering point along the chord,
+ * sends the neutron into a cone of half-angle atan(focus_r / |target|)
+ * around target with final energy E0 +- dE, and records the event
+ * (ki - kf, weight, energy transfer) in ev[8] (ev[3..5] are 0).
+ * sp: target.x, target.y, target.z, E0, dE, focus_r */
+DI void s_rescal(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, float* ev) {
+  const V3 target = v3(c.sp[0], c.sp[1], c.sp[2]);
+  const float E0 = c.sp[3], dE = c.sp[4], focus_r = c.sp[5];
+  V3 path = sub(ip2(s), ip1(s));
+  set_pos(n, add(ip1(s), mul(draw(n, r), path)));
+  V3 ki = mul(RC_V2K, nvel(n));
+  float l2 = len3(target) * len3(target);
+  float costhetamax = sqrtf(l2 / (focus_r * focus_r + l2));
+  float theta = rm_acosf(1.0f - draw(n, r) * (1.0f - costhetamax));
+  float phi = draw(n, r) * 2.0f * RC_PI;
+  V3 target_perp = (target.x == 0.0f && target.z == 0.0f) ? v3(1.0f, 0.0f, 0.0f)
+                                                           : v3(-target.z, 0.0f, target.x);
+  V3 target_perp_perp = cross(target, target_perp);
+  V3 target_final = rotate_about_axis(theta, target_perp_perp, target);
+  target_final = rotate_about_axis(phi, target, target_final);
+  target_final = normalize(target_final);
+  float Ef = E0 + dE * (1.0f - 2.0f * draw(n, r));
+  float vf = RC_SE2V * sqrtf(Ef);
+  set_vel(n, mul(vf, target_final));
+  V3 kf = mul(RC_V2K, nvel(n));
+  float lk = len3(mul(RC_K2V, ki));
+  ev[0] = ki.x - kf.x; ev[1] = ki.y - kf.y; ev[2] = ki.z - kf.z;
+  ev[3] = 0.0f; ev[4] = 0.0f; ev[5] = 0.0f;
+  ev[6] = n.p;
+  ev[7] = RC_VS2E * (lk * lk) - Ef;
+  s_finish(c, n, s, ii);
+}
+
 /* detector1D.cl:20-77 */
 template <class D = NoDiff>
 DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* dx = nullptr) {

@@ -31,7 +31,12 @@
 
 /* scatter dispatch with the kind fixed at compile time when SK >= 0 */
 template <int SK>
-DI void scatter_k(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st) {
+DI void scatter_k(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st,
+                  float* ev = nullptr) {
+  if constexpr (SK == RAMP_S_RESCAL) {
+    s_rescal(c, n, s, ii, r, ev);
+    return;
+  }
   switch (SK >= 0 ? SK : c.scat) {
     case RAMP_S_ARM: ii = c.idx; is_reset(s); break;
     case RAMP_S_GUIDE: s_guide(c, n, s, ii, st); break;
@@ -54,13 +59,14 @@ DI void scatter_k(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDe
 }
 
 template <int SK>
-DI void comp_linear_k(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st) {
+DI void comp_linear_k(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st,
+                      float* ev = nullptr) {
   transform(c, n);
   Is s;
   is_reset(s);
   if (intersect(c, n, s, st)) ii = c.idx;
   if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
-  if (ii == c.idx && !(n.die > 0.f)) scatter_k<SK>(c, n, s, ii, r, st);
+  if (ii == c.idx && !(n.die > 0.f)) scatter_k<SK>(c, n, s, ii, r, st, ev);
   if (!(n.die > 0.f)) untransform(c, n);
 }
 
@@ -85,14 +91,15 @@ __global__ void __launch_bounds__(PLAIN_BLOCK)
 k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
   constexpr bool RD_P = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
                         SK == RAMP_S_DET1D || SK == RAMP_S_DET2D || SK == RAMP_S_COUNTER ||
-                        SK == RAMP_S_ATTENUATE || SK == RAMP_S_MONO || SK == RAMP_S_POWDER1;
+                        SK == RAMP_S_ATTENUATE || SK == RAMP_S_MONO || SK == RAMP_S_POWDER1 ||
+                        SK == RAMP_S_RESCAL;
   constexpr bool RD_T = SK == RAMP_S_GUIDE || SK == RAMP_S_CHOPPER || SK == RAMP_S_ISOTROPIC ||
                         SK == RAMP_S_POWDERN || SK == RAMP_S_DET1D || SK == RAMP_S_DET2D ||
                         SK == RAMP_S_ATTENUATE || SK == RAMP_S_MONO || SK == RAMP_S_POWDER1;
   constexpr bool RD_SB = SK == RAMP_S_CHOPPER || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
-                         SK == RAMP_S_MONO || SK == RAMP_S_POWDER1;
+                         SK == RAMP_S_MONO || SK == RAMP_S_POWDER1 || SK == RAMP_S_RESCAL;
   constexpr bool MOD_VEL = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
-                           SK == RAMP_S_MONO || SK == RAMP_S_POWDER1;
+                           SK == RAMP_S_MONO || SK == RAMP_S_POWDER1 || SK == RAMP_S_RESCAL;
   constexpr bool USE_POL = SK == RAMP_S_ISOTROPIC;
   const int64_t st = a.stride;
   float* __restrict__ S = a.soa;
@@ -116,7 +123,20 @@ k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
     uint32_t ii = ii0;
     Rng r;
     rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
-    comp_linear_k<SK>(c, n, ii, r, a.st);
+    float ev[8];
+    comp_linear_k<SK>(c, n, ii, r, a.st, ev);
+    if constexpr (SK == RAMP_S_RESCAL) {
+      /* the event of a neutron this component scattered (rescal.cl:67) */
+      if (n.wr & WR_SC) {
+        if (c.tally && 8 * i + 8 <= c.tally_len) {
+          float4* e = reinterpret_cast<float4*>(c.tally + 8 * i);
+          e[0] = make_float4(ev[0], ev[1], ev[2], ev[3]);
+          e[1] = make_float4(ev[4], ev[5], ev[6], ev[7]);
+        } else {
+          atomicAdd(&a.st->oob, 1ull);
+        }
+      }
+    }
     S[RAMP_X * st + i] = n.x; S[RAMP_Y * st + i] = n.y; S[RAMP_Z * st + i] = n.z;
     if (MOD_VEL || c.rotated) {
       S[RAMP_VX * st + i] = n.vx; S[RAMP_VY * st + i] = n.vy; S[RAMP_VZ * st + i] = n.vz;
@@ -182,6 +202,7 @@ cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_
     CASE(RAMP_S_ARM) CASE(RAMP_S_GUIDE) CASE2(RAMP_S_CHOPPER) CASE2(RAMP_S_ISOTROPIC)
     CASE2(RAMP_S_POWDERN) CASE(RAMP_S_DET1D) CASE(RAMP_S_DET2D) CASE(RAMP_S_COUNTER)
     CASE(RAMP_S_BEAMSTOP) CASE(RAMP_S_ATTENUATE) CASE2(RAMP_S_MONO) CASE2(RAMP_S_POWDER1)
+    CASE2(RAMP_S_RESCAL)
 #undef CASE
 #undef CASE2
     default: return cudaErrorInvalidValue;

@@ -327,6 +327,9 @@ class Instrument:
                single-device run (the histogram sum is the caller's
                exchange step, e.g. torch.distributed.all_reduce).
         """
+        events = self.event_components()
+        if events and path != "plain":
+            raise ValueError("SRescal records one event per neutron index: use path='plain'")
         lib = self._lib()
         plan = self.plan()
         N = int(N)
@@ -351,6 +354,10 @@ class Instrument:
         src = self.source
         with torch.cuda.device(self.device):
             stream = self._stream_ptr()
+            for j, sc in events:
+                buf = sc.prepare(first, self.device)
+                _abi.check(lib, lib.ramp_plan_set_buffer(plan, j, _abi.ctypes.c_void_p(buf.data_ptr()),
+                                                         buf.numel()), "ramp_plan_set_buffer")
             if path == "plain":
                 st = self._alloc_state(first)
             elif path == "fused":
@@ -367,9 +374,13 @@ class Instrument:
                 if nloc == 0:
                     continue
                 if path == "plain":
+                    for _, sc in events:
+                        sc.begin_chunk()
                     rc = lib.ramp_trace_plain(plan, _abi.ctypes.byref(st), nloc, torun, seed,
                                               _abi.ctypes.byref(rngd), stream)
                     _abi.check(lib, rc, "ramp_trace_plain")
+                    for _, sc in events:
+                        sc.reduce(self.state[_abi.LANE["se"]], nloc)
                     if debug:
                         torch.cuda.synchronize(self.device)
                         alive = self.state[:, :nloc][_abi.LANE["die"]] == 0
@@ -395,6 +406,18 @@ class Instrument:
         from .graph import capture
         return capture(self, N, path=path, rng=rng, run_seed=run_seed, tune=tune, chunk=chunk,
                        state=state)
+
+    def event_components(self):
+        """(descriptor index, plugin) of the components that record one
+        event per neutron index (SRescal)."""
+        out = []
+        j = 0
+        for block in self.blocks:
+            for name, comp in block.components.items():
+                if getattr(comp["scat_kernel"], "kind", None) == _abi.S_RESCAL:
+                    out.append((j, comp["scat_kernel"]))
+                j += 1
+        return out
 
     def _check_status(self, lib, plan):
         flags = _abi.ctypes.c_uint32()

@@ -15,6 +15,8 @@ the benchmark and parity workloads, and generators for their inputs.
 * powder_diffractometer.json — curved PG(002) mosaic monochromator at the
   Bragg angle for $Ei$ ($mono_angle$), one-line powder sphere (SPowder1),
   banana detector with a 1D 2theta histogram (-10..150 deg, 0.1 deg).
+* tas_like.json — triple-axis-like: PG(002) monochromator for $Ei$, SRescal
+  sample focusing onto a PG(002) analyser set for $Ef$, and a counter.
 * mesh_imaging.json — near-parallel flat beam through a seeded perturbed
   torus mesh (GMesh + SAttenuate, mu 0.5 /cm) rotated by $angle$, onto a
   1024 x 1024 pixel detector.
@@ -147,6 +149,17 @@ def powder_diffractometer_kwargs(Ei=14.7, d_mono=3.355):
     (rad): sin(theta) = lambda / 2d, lambda = 9.045 / sqrt(Ei) AA."""
     lam = 9.04456 / np.sqrt(Ei)
     return dict(Ei=Ei, mono_angle=float(np.arcsin(lam / (2.0 * d_mono))))
+
+
+def tas_like_kwargs(Ei=5.0, Ef=5.0, dE=0.2, sample_angle=0.6, d_mono=3.355):
+    """Bragg angles of monochromator and analyser for Ei and Ef (rad), the
+    sample's scattering angle and its focusing target (the analyser, 1 m
+    away in the sample frame)."""
+    def bragg(E):
+        return float(np.arcsin(9.04456 / np.sqrt(E) / (2.0 * d_mono)))
+    return dict(Ei=Ei, Ef=Ef, dE=dE, mono_angle=bragg(Ei), ana_angle=bragg(Ef),
+                sample_angle=sample_angle,
+                sample_target=[float(np.sin(sample_angle)), 0.0, float(np.cos(sample_angle))])
 
 
 def small_chain_kwargs():

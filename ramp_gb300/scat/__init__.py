@@ -12,3 +12,4 @@ from .counter import SCounter
 from .attenuate import SAttenuate
 from .monochromator import SMonochromator
 from .powder1 import SPowder1
+from .rescal import SRescal

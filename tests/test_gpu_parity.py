@@ -160,6 +160,27 @@ def test_powder_diffractometer_fused_matches_oracle(cuda_lib):
     assert gi.oob_drops == r.oob
 
 
+def test_tas_like_plain_matches_oracle_with_events(cuda_lib):
+    """Monochromator, SRescal with its per-index event list, analyser and
+    counter: records and the kept events bit-identical."""
+    gi, ci, r = check_plain(I.path("tas_like.json"), I.tas_like_kwargs(), 300_000)
+    g = dict(gi.components())["Sample"]["scat_kernel"].data()
+    c = dict(ci.components())["Sample"]["scat_kernel"].data()
+    assert len(g[0]) == len(c[0]) > 0
+    for a, b in zip(g, c):
+        assert np.array_equal(a, b)
+
+
+def test_rescal_plan_refuses_whole_chain_launches(cuda_lib):
+    inst = m.Instrument(I.path("tas_like.json"), "cuda", **I.tas_like_kwargs())
+    inst.execute(1000)
+    lib = inst._lib()
+    rngd = _abi.RampRng()
+    rc = lib.ramp_trace_fused(inst.plan(), 1000, 1000, 1, _abi.ctypes.byref(rngd), None, None,
+                              None, None)
+    assert rc == _abi.E_UNSUPPORTED
+
+
 # ---------------------------------------------------------------- fused path
 @pytest.mark.parametrize("fn,kw,N", [
     ("small_chain.json", "small", 300_000),

@@ -53,3 +53,26 @@ def test_oracle_diffraction_peak_at_bragg_angle():
     two_theta = 2 * np.degrees(np.arcsin(lam / (2 * 2.5)))
     peak = -10.0 + 0.1 * (np.argmax(h) + 0.5)
     assert abs(peak - two_theta) < 0.5
+
+
+def test_oracle_tas_events_follow_the_counter():
+    """SRescal keeps the events of the neutrons the final counter flagged;
+    with Ef = Ei the energy transfer centres on zero."""
+    import oracle
+    kw = I.tas_like_kwargs(Ei=5.0, Ef=5.0, dE=0.2)
+    inst = m.Instrument(I.path("tas_like.json"), "cpu", **kw)
+    random.seed(2)
+    r = oracle.run(inst, 200_000)
+    comps = dict(inst.components())
+    qx, qy, qz, dE, p = comps["Sample"]["scat_kernel"].data()
+    hits = int((r.neutrons[:, _abi.LANE["se"]] > 0).sum())
+    assert len(qx) == hits > 0
+    assert abs(float(np.average(dE, weights=p))) < 0.2
+    assert np.all(np.abs(dE) <= 1.1)       # |Ei - Ef| + dE spread of the source and Rescal
+
+
+def test_rescal_needs_the_plain_path():
+    inst = m.Instrument(I.path("tas_like.json"), "cpu", **I.tas_like_kwargs())
+    import pytest
+    with pytest.raises(ValueError, match="plain"):
+        inst.execute(1000, path="fused")
