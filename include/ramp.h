@@ -91,10 +91,14 @@ enum RampScatKind {
                              Lambert weight over the summed mesh chords */
   RAMP_S_MONO      = 11,  /* SMonochromator scat/monochromator.cl:22    */
   RAMP_S_POWDER1   = 12,  /* SPowder1     scat/powder1.cl:5             */
-  RAMP_S_RESCAL    = 13   /* SRescal      scat/rescal.cl:5: writes one
+  RAMP_S_RESCAL    = 13,  /* SRescal      scat/rescal.cl:5: writes one
                              8-float event per neutron index into the
                              buffer bound by ramp_plan_set_buffer; plain
                              path, linear blocks only                   */
+  RAMP_S_HOST      = 14   /* scattering done by the host between
+                             ramp_component_enter and _leave (SMCPLOut
+                             scat/mcpl_out.py:85, SMCPLIn mcpl_in.py:39);
+                             plain path, linear blocks only             */
 };
 
 /* ---- descriptors ------------------------------------------------------- */
@@ -228,6 +232,27 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps,
                      int n_comps, const RampBlock* blocks, int n_blocks,
                      RampPlan** out);
 int ramp_plan_destroy(RampPlan* plan);
+
+/* Run linear components [k0, k1) over neutrons [0, n) (each a k_linear
+ * pass): the pieces of a linear block around a host component.          */
+int ramp_run_components(RampPlan* plan, int32_t k0, int32_t k1, const RampState* st,
+                        int64_t n, const RampRng* rng, void* stream);
+
+/* The device halves of a host component's pass (mcramp.py:124-157):
+ * enter = frame transform, intersection, termination; leave = inverse
+ * transform.  The host acts on the state in between.                    */
+int ramp_component_enter(RampPlan* plan, int32_t comp, const RampState* st, int64_t n,
+                         const RampRng* rng, void* stream);
+int ramp_component_leave(RampPlan* plan, int32_t comp, const RampState* st, int64_t n,
+                         void* stream);
+
+/* Order-preserving compaction of neutrons [0, n) whose die lane is not
+ * exactly 1 (mcpl_out.py:103): row r of out holds the lanes set in the
+ * bit mask `lanes` (ascending lane order) of the r-th such neutron; *count
+ * (device) receives the number of rows.  out holds n rows at most;
+ * scratch holds ceil(n / 1024) int64.                                    */
+int ramp_gather_alive(const RampState* st, int64_t n, uint32_t lanes, float* out,
+                      int64_t* scratch, int64_t scratch_len, int64_t* count, void* stream);
 
 /* Bind component comp's output buffer (device, len floats): the event
  * list of an SRescal component (8 floats per neutron index of a chunk).

@@ -111,6 +111,8 @@ def run(inst, N, chunk=None, rng_mode=0, run_seed=0, variant=0, threads=0, seeds
         rank, world = shard
         s_lo, s_hi = first * rank // world, first * (rank + 1) // world
         first = max(1, s_hi - s_lo)
+    if inst.host_components():
+        raise NotImplementedError("the oracle has no host components (MCPL in/out)")
     events = inst.event_components()
     for _, sc in events:             # per-index event buffers (SRescal)
         sc.prepare(first, torch.device("cpu"))

@@ -8,7 +8,7 @@ from .geom import (GPrim, GPlane, GCylinderExt, GBanana, GSphere, GSphereInt, GB
                    GMesh)
 from .scat import (SPrim, SArm, SBeamstop, SGuide, SChopper, SIsotropic, SPowderN,
                    SDetector1D, SDetector2D, SCounter, SAttenuate, SMonochromator, SPowder1,
-                   SRescal)
+                   SRescal, SMCPLOut, SMCPLIn)
 from .instrument import Instrument, ExecutionBlock, KernelRef, frame_rotate, build_kernel
 
 __version__ = "0.1.0"

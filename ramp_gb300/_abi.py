@@ -18,7 +18,7 @@ LANE = dict(x=0, y=1, z=2, vx=3, vy=4, vz=5, px=6, py=7, pz=8, p=9, tof=10,
 SRC_FLAT, SRC_CONT, SRC_ISIS = 1, 2, 3
 G_PLANE, G_CYL_EXT, G_BANANA, G_SPHERE, G_SPHERE_INT, G_BOX, G_ARM, G_MESH = range(1, 9)
 (S_ARM, S_GUIDE, S_CHOPPER, S_ISOTROPIC, S_POWDERN, S_DET1D, S_DET2D, S_COUNTER,
- S_BEAMSTOP, S_ATTENUATE, S_MONO, S_POWDER1, S_RESCAL) = range(1, 14)
+ S_BEAMSTOP, S_ATTENUATE, S_MONO, S_POWDER1, S_RESCAL, S_HOST) = range(1, 15)
 
 NGP, NSP, NGI, NSI, NTAB = 12, 24, 4, 12, 12
 
@@ -149,6 +149,17 @@ _SIGS = {
     "ramp_plan_reserve": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
     "ramp_plan_set_buffer": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64],
                              ctypes.c_int),
+    "ramp_run_components": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                             ctypes.POINTER(RampState), ctypes.c_int64, ctypes.POINTER(RampRng),
+                             ctypes.c_void_p], ctypes.c_int),
+    "ramp_component_enter": ([ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(RampState),
+                              ctypes.c_int64, ctypes.POINTER(RampRng), ctypes.c_void_p],
+                             ctypes.c_int),
+    "ramp_component_leave": ([ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(RampState),
+                              ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
+    "ramp_gather_alive": ([ctypes.POINTER(RampState), ctypes.c_int64, ctypes.c_uint32,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                           ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_threefry": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_math": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

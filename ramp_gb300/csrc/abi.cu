@@ -96,7 +96,8 @@ struct RampPlan {
  * component output */
 static int check_whole_chain(const RampPlan* p, const char* who) {
   if (p->plain_only) {
-    set_err("%s: SRescal writes one event per neutron index; use the plain path", who);
+    set_err("%s: the chain has a component that needs the plain path (SRescal events, "
+            "host components)", who);
     return RAMP_E_UNSUPPORTED;
   }
   return RAMP_OK;
@@ -181,7 +182,7 @@ static int validate_comp(const RampComp& c, int j) {
     set_err("component %d: unknown geometry kind %d", j, c.geom);
     return RAMP_E_UNSUPPORTED;
   }
-  if (c.scat < RAMP_S_ARM || c.scat > RAMP_S_RESCAL) {
+  if (c.scat < RAMP_S_ARM || c.scat > RAMP_S_HOST) {
     set_err("component %d: unknown scatter kind %d", j, c.scat);
     return RAMP_E_UNSUPPORTED;
   }
@@ -439,11 +440,11 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
     if (rc) { ramp_plan_destroy(p); return rc; }
   }
   for (const RampComp& c : p->comps_in)
-    if (c.scat == RAMP_S_RESCAL) p->plain_only = true;
+    if (c.scat == RAMP_S_RESCAL || c.scat == RAMP_S_HOST) p->plain_only = true;
   for (const RampBlock& B : p->blocks)
     for (int j = B.first; !B.linear && j < B.first + B.count; ++j)
-      if (p->comps_in[j].scat == RAMP_S_RESCAL) {
-        set_err("component %d: SRescal must sit in a linear block", j);
+      if (p->comps_in[j].scat == RAMP_S_RESCAL || p->comps_in[j].scat == RAMP_S_HOST) {
+        set_err("component %d: SRescal and host components must sit in a linear block", j);
         ramp_plan_destroy(p);
         return RAMP_E_UNSUPPORTED;
       }
@@ -583,6 +584,76 @@ static int attach_surv(RampPlan* p, FusedArgs& a, int64_t n_items, cudaStream_t 
   a.surv_cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS;
   a.surv_items = n_items;
   CK(cudaMemsetAsync(a.surv_cnt, 0, (size_t)n_items * sizeof(uint32_t), s));
+  return RAMP_OK;
+}
+
+/* the linear block holding component k, or -1 */
+static int linear_block_of(const RampPlan* p, int k) {
+  for (size_t b = 0; b < p->blocks.size(); ++b) {
+    const RampBlock& B = p->blocks[b];
+    if (k >= B.first && k < B.first + B.count) return B.linear ? (int)b : -1;
+  }
+  return -1;
+}
+
+int ramp_run_components(RampPlan* p, int32_t k0, int32_t k1, const RampState* st, int64_t n,
+                        const RampRng* rng, void* stream) {
+  if (!p || k0 < 0 || k1 > (int)p->comps.size() || k0 > k1) {
+    set_err("ramp_run_components: bad range");
+    return RAMP_E_INVALID;
+  }
+  int rc = check_state(st, n);
+  if (rc) return rc;
+  PlainArgs a = plain_args(p, st, n, rng);
+  for (int k = k0; k < k1; ++k) {
+    if (linear_block_of(p, k) < 0) {
+      set_err("ramp_run_components: component %d is not in a linear block", k);
+      return RAMP_E_INVALID;
+    }
+    CK(launch_linear_comp(p->comps[k], a, (cudaStream_t)stream));
+  }
+  return RAMP_OK;
+}
+
+static int host_half(RampPlan* p, int32_t comp, const RampState* st, int64_t n,
+                     const RampRng* rng, int leave, void* stream) {
+  if (!p || comp < 0 || comp >= (int)p->comps.size() || linear_block_of(p, comp) < 0) {
+    set_err("ramp_component_%s: component %d is not in a linear block", leave ? "leave" : "enter",
+            comp);
+    return RAMP_E_INVALID;
+  }
+  int rc = check_state(st, n);
+  if (rc) return rc;
+  CK(launch_host_half(p->comps[comp], plain_args(p, st, n, rng), leave, (cudaStream_t)stream));
+  return RAMP_OK;
+}
+
+int ramp_component_enter(RampPlan* p, int32_t comp, const RampState* st, int64_t n,
+                         const RampRng* rng, void* stream) {
+  return host_half(p, comp, st, n, rng, 0, stream);
+}
+
+int ramp_component_leave(RampPlan* p, int32_t comp, const RampState* st, int64_t n,
+                         void* stream) {
+  return host_half(p, comp, st, n, nullptr, 1, stream);
+}
+
+int ramp_gather_alive(const RampState* st, int64_t n, uint32_t lanes, float* out,
+                      int64_t* scratch, int64_t scratch_len, int64_t* count, void* stream) {
+  int rc = check_state(st, n);
+  if (rc) return rc;
+  if (!out || !count || lanes == 0 || lanes >= (1u << RAMP_NLANES) ||
+      (n > 0 && (!scratch || scratch_len < (n + 1023) / 1024))) {
+    set_err("ramp_gather_alive: bad arguments (scratch needs ceil(n/1024) entries)");
+    return RAMP_E_INVALID;
+  }
+  PlainArgs a;
+  memset(&a, 0, sizeof(a));
+  a.soa = st->soa;
+  a.iidx = st->iidx;
+  a.stride = st->stride;
+  a.n = n;
+  CK(launch_gather_alive(a, lanes, out, scratch, count, (cudaStream_t)stream));
   return RAMP_OK;
 }
 

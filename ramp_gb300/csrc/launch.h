@@ -17,6 +17,9 @@ struct PlainArgs {
   StatusDev* st;
 };
 
+cudaError_t launch_host_half(const CompDev& c, const PlainArgs& a, int leave, cudaStream_t s);
+cudaError_t launch_gather_alive(const PlainArgs& a, uint32_t lanes, float* out, int64_t* scratch,
+                                int64_t* total, cudaStream_t s);
 cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_sim,
                             int32_t seed, cudaStream_t s);
 cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_t s);

@@ -180,6 +180,132 @@ static int plain_grid(int64_t n) {
   return (int)g;
 }
 
+/* A host component (MCPL output or input, scatter done on the host)
+ * splits its linear pass (mcramp.py:124-157) around the host action:
+ * k_enter transforms into the component frame, intersects and terminates;
+ * k_leave transforms back. */
+__global__ void __launch_bounds__(PLAIN_BLOCK)
+k_enter(const __grid_constant__ CompDev c, const PlainArgs a) {
+  const int64_t st = a.stride;
+  float* __restrict__ S = a.soa;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (S[RAMP_DIE * st + i] > 0.f) continue;
+    Nt n;
+    LOAD_ALL(n, S, st, i);
+    n.wr = 0;
+    uint32_t ii = a.iidx[i];
+    transform(c, n);
+    Is s;
+    is_reset(s);
+    if (intersect(c, n, s, a.st)) ii = c.idx;
+    if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
+    STORE_ALL(n, S, st, i);
+    a.iidx[i] = ii;
+  }
+}
+
+__global__ void __launch_bounds__(PLAIN_BLOCK)
+k_leave(const __grid_constant__ CompDev c, const PlainArgs a) {
+  const int64_t st = a.stride;
+  float* __restrict__ S = a.soa;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (S[RAMP_DIE * st + i] > 0.f) continue;
+    Nt n;
+    LOAD_ALL(n, S, st, i);
+    untransform(c, n);
+    STORE_ALL(n, S, st, i);
+  }
+}
+
+cudaError_t launch_host_half(const CompDev& c, const PlainArgs& a, int leave, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  if (leave) k_leave<<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(c, a);
+  else k_enter<<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(c, a);
+  return cudaGetLastError();
+}
+
+/* Order-preserving compaction of the records that are not dead (die lane
+ * not exactly 1, the test of mcpl_out.py:103) into rows of the selected
+ * lanes: per 1024-index tile a count, one scan of the tile counts, then
+ * each record goes to its tile offset plus its rank inside the tile
+ * (warp ballots).  The rows keep the index order. */
+#define GATHER_TILE 1024
+
+__global__ void __launch_bounds__(GATHER_TILE)
+k_alive_count(const float* __restrict__ die, int64_t n, int64_t* __restrict__ tile_count) {
+  __shared__ int warp_n[GATHER_TILE / 32];
+  const int64_t i = (int64_t)blockIdx.x * GATHER_TILE + threadIdx.x;
+  const bool keep = i < n && !(die[i] == 1.0f);
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  if ((threadIdx.x & 31) == 0) warp_n[threadIdx.x >> 5] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < GATHER_TILE / 32; ++w) t += warp_n[w];
+    tile_count[blockIdx.x] = t;
+  }
+}
+
+/* exclusive scan of the tile counts in place (one CTA; each thread sums a
+ * contiguous run, then the runs are scanned) and the total */
+__global__ void __launch_bounds__(1024)
+k_scan_tiles(int64_t* __restrict__ c, int64_t nt, int64_t* __restrict__ total) {
+  __shared__ int64_t part[1024];
+  const int64_t per = (nt + 1023) / 1024;
+  const int64_t b = threadIdx.x * per, e = (b + per < nt) ? b + per : nt;
+  int64_t sum = 0;
+  for (int64_t k = b; k < e; ++k) sum += c[k];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t run = 0;
+    for (int t = 0; t < 1024; ++t) { const int64_t v = part[t]; part[t] = run; run += v; }
+    *total = run;
+  }
+  __syncthreads();
+  int64_t run = part[threadIdx.x];
+  for (int64_t k = b; k < e; ++k) { const int64_t v = c[k]; c[k] = run; run += v; }
+}
+
+__global__ void __launch_bounds__(GATHER_TILE)
+k_alive_gather(const float* __restrict__ S, int64_t st, int64_t n,
+               const int64_t* __restrict__ tile_off, uint32_t lanes, int nl,
+               float* __restrict__ out) {
+  __shared__ int warp_off[GATHER_TILE / 32];
+  const int64_t i = (int64_t)blockIdx.x * GATHER_TILE + threadIdx.x;
+  const bool keep = i < n && !(S[RAMP_DIE * st + i] == 1.0f);
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) warp_off[w] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int k = 0; k < GATHER_TILE / 32; ++k) { const int v = warp_off[k]; warp_off[k] = run; run += v; }
+  }
+  __syncthreads();
+  if (!keep) return;
+  const int64_t row = tile_off[blockIdx.x] + warp_off[w] + __popc(m & ((1u << lane) - 1u));
+  float* o = out + row * nl;
+  int k = 0;
+  for (int l = 0; l < RAMP_NLANES; ++l)
+    if (lanes & (1u << l)) o[k++] = S[(int64_t)l * st + i];
+}
+
+cudaError_t launch_gather_alive(const PlainArgs& a, uint32_t lanes, float* out, int64_t* scratch,
+                                int64_t* total, cudaStream_t s) {
+  const int64_t nt = (a.n + GATHER_TILE - 1) / GATHER_TILE;
+  if (nt <= 0) return cudaMemsetAsync(total, 0, sizeof(int64_t), s);
+  int nl = __builtin_popcount(lanes);
+  k_alive_count<<<(unsigned)nt, GATHER_TILE, 0, s>>>(a.soa + (int64_t)RAMP_DIE * a.stride, a.n,
+                                                     scratch);
+  k_scan_tiles<<<1, 1024, 0, s>>>(scratch, nt, total);
+  k_alive_gather<<<(unsigned)nt, GATHER_TILE, 0, s>>>(a.soa, a.stride, a.n, scratch, lanes, nl,
+                                                      out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_sim, int32_t seed,
                             cudaStream_t s) {
   if (a.n <= 0) return cudaSuccess;

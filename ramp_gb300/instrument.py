@@ -328,8 +328,9 @@ class Instrument:
                exchange step, e.g. torch.distributed.all_reduce).
         """
         events = self.event_components()
-        if events and path != "plain":
-            raise ValueError("SRescal records one event per neutron index: use path='plain'")
+        hosts = self.host_components()
+        if (events or hosts) and path != "plain":
+            raise ValueError("SRescal and MCPL components act per neutron index: use path='plain'")
         lib = self._lib()
         plan = self.plan()
         N = int(N)
@@ -376,9 +377,13 @@ class Instrument:
                 if path == "plain":
                     for _, sc in events:
                         sc.begin_chunk()
-                    rc = lib.ramp_trace_plain(plan, _abi.ctypes.byref(st), nloc, torun, seed,
-                                              _abi.ctypes.byref(rngd), stream)
-                    _abi.check(lib, rc, "ramp_trace_plain")
+                    if hosts:
+                        self._trace_with_hosts(lib, plan, st, nloc, torun, seed, rngd, stream,
+                                               hosts)
+                    else:
+                        rc = lib.ramp_trace_plain(plan, _abi.ctypes.byref(st), nloc, torun, seed,
+                                                  _abi.ctypes.byref(rngd), stream)
+                        _abi.check(lib, rc, "ramp_trace_plain")
                     for _, sc in events:
                         sc.reduce(self.state[_abi.LANE["se"]], nloc)
                     if debug:
@@ -406,6 +411,51 @@ class Instrument:
         from .graph import capture
         return capture(self, N, path=path, rng=rng, run_seed=run_seed, tune=tune, chunk=chunk,
                        state=state)
+
+    def host_components(self):
+        """(descriptor index, plugin) of the components whose scattering runs
+        on the host (SMCPLOut, SMCPLIn)."""
+        out = []
+        j = 0
+        for block in self.blocks:
+            for name, comp in block.components.items():
+                if getattr(comp["scat_kernel"], "kind", None) == _abi.S_HOST:
+                    out.append((j, comp["scat_kernel"]))
+                j += 1
+        return out
+
+    def _trace_with_hosts(self, lib, plan, st, n, num_sim, seed, rngd, stream, hosts):
+        """One plain-path chunk with host components: the moderator, then
+        every block; a linear block holding host components runs in pieces
+        around each host action (mcramp.py:124-157)."""
+        ct = _abi.ctypes
+        _abi.check(lib, lib.ramp_generate(plan, ct.byref(st), n, num_sim, seed, ct.byref(rngd),
+                                          stream), "ramp_generate")
+        host_at = dict(hosts)
+        first = 0
+        for b, block in enumerate(self.blocks):
+            count = len(block.components)
+            inside = [j for j in range(first, first + count) if j in host_at]
+            if not inside:
+                _abi.check(lib, lib.ramp_run_block(plan, b, ct.byref(st), n, ct.byref(rngd),
+                                                   stream), "ramp_run_block")
+            else:
+                k = first
+                for j in inside:
+                    _abi.check(lib, lib.ramp_run_components(plan, k, j, ct.byref(st), n,
+                                                            ct.byref(rngd), stream),
+                               "ramp_run_components")
+                    _abi.check(lib, lib.ramp_component_enter(plan, j, ct.byref(st), n,
+                                                             ct.byref(rngd), stream),
+                               "ramp_component_enter")
+                    host_at[j].host_action(self, st, n)
+                    _abi.check(lib, lib.ramp_component_leave(plan, j, ct.byref(st), n, stream),
+                               "ramp_component_leave")
+                    k = j + 1
+                _abi.check(lib, lib.ramp_run_components(plan, k, first + count, ct.byref(st), n,
+                                                        ct.byref(rngd), stream),
+                           "ramp_run_components")
+            first += count
 
     def event_components(self):
         """(descriptor index, plugin) of the components that record one

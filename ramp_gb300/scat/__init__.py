@@ -13,3 +13,4 @@ from .attenuate import SAttenuate
 from .monochromator import SMonochromator
 from .powder1 import SPowder1
 from .rescal import SRescal
+from .mcpl_io import SMCPLOut, SMCPLIn
