@@ -90,7 +90,10 @@ struct RampPlan {
   int64_t surv_cap = 0;              /* slots (128 per work item) */
   StreamSet streams;
   bool plain_only = false;           /* a component writes per-index output */
+  bool ext = false;                  /* an extended kind: MISIS, SMonochromator, SPowder1 */
 };
+
+static bool ext_source(const RampSource& s) { return s.kind == RAMP_SRC_ISIS; }
 
 /* whole-chain kernels (fused, batched, adjoint) cannot write per-index
  * component output */
@@ -439,8 +442,11 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
     if (!rc) rc = make_comp(p, comps[j], p->comps[j]);
     if (rc) { ramp_plan_destroy(p); return rc; }
   }
-  for (const RampComp& c : p->comps_in)
+  for (const RampComp& c : p->comps_in) {
     if (c.scat == RAMP_S_RESCAL || c.scat == RAMP_S_HOST) p->plain_only = true;
+    if (c.scat == RAMP_S_MONO || c.scat == RAMP_S_POWDER1) p->ext = true;
+  }
+  if (ext_source(*source)) p->ext = true;
   for (const RampBlock& B : p->blocks)
     for (int j = B.first; !B.linear && j < B.first + B.count; ++j)
       if (p->comps_in[j].scat == RAMP_S_RESCAL || p->comps_in[j].scat == RAMP_S_HOST) {
@@ -728,6 +734,8 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.workq = &p->status->workq;
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
+  a.ext = p->ext ? 1 : 0;
+  if (a.ext) a.split = 0;
   if (a.split > 0) {
     rc = attach_surv(p, a, (n + 127) / 128, s);
     if (rc) return rc;
@@ -867,9 +875,12 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
       tasks.push_back(t);
     }
   }
+  bool ext = p->ext;
+  for (int v = 0; v < n_variants; ++v) ext = ext || ext_source(variants[v].source);
   if (use_streams) {
     FusedArgs a;
     memset(&a, 0, sizeof(a));
+    a.ext = ext ? 1 : 0;
     a.blocks = p->blocks_dev;
     a.n_blocks = (int32_t)p->blocks.size();
     a.n_comps = nc;
@@ -920,6 +931,8 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.workq = &p->status->workq;
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
+  a.ext = ext ? 1 : 0;
+  if (a.ext) a.split = 0;
   if (a.split > 0) {
     rc = attach_surv(p, a, a.n_tasks * ((task + 127) / 128), s);
     if (rc) return rc;
@@ -1267,6 +1280,9 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.rng.tid_base = 0u;
   a.st = &D->status;
   a.workq = &D->status.workq;
+  a.ext = p->ext ? 1 : 0;
+  for (int v = 0; v < n_variants; ++v)
+    if (ext_source(variants[v].source)) a.ext = 1;
   /* no survivor split here: it would need a buffer sized by the call */
   CK(launch_fused(a, block, fused_grid(n_tasks, grid), s));
   return RAMP_OK;

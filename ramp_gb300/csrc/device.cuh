@@ -320,8 +320,11 @@ DI float cont_weight(const SrcDev& s, float E_val, int32_t num_sim, D* dx) {
   return M / (float)num_sim;
 }
 
-/* generate_neutrons — flat_mod.cl:4-50, cont_mod.cl:11-72, isis_mod.cl:15-104 */
-template <class D = NoDiff>
+/* generate_neutrons — flat_mod.cl:4-50, cont_mod.cl:11-72, isis_mod.cl:15-104.
+ * EXT = false compiles the kernel without the extended kinds (the MISIS
+ * source here, the TAS components in scatter): a smaller whole-chain
+ * kernel for chains that do not use them. */
+template <class D = NoDiff, bool EXT = true>
 DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t seed, Rng& r,
                  D* dx = nullptr) {
   n.x = n.y = n.z = n.vx = n.vy = n.vz = n.px = n.py = n.pz = 0.0f;
@@ -329,7 +332,7 @@ DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t 
   n.wr = 0;
   n.sb = (float)seed + old_sb;
   float E_val, t0 = 0.0f;
-  if (s.kind == RAMP_SRC_ISIS) {
+  if (EXT && s.kind == RAMP_SRC_ISIS) {
     E_val = isis_sample(s, n, r, t0);
     n.p = s.p[13] * s.p[14] * 6.2415093e+12f / (float)num_sim;
   } else {
@@ -1224,7 +1227,7 @@ DI void s_attenuate(const CompDev& c, Nt& n, Is& s, uint32_t& ii) {
   s_finish(c, n, s, ii);
 }
 
-template <class D = NoDiff>
+template <class D = NoDiff, bool EXT = true>
 DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st,
                 D* dx = nullptr, const bool zx = false) {
   switch (c.scat) {
@@ -1242,8 +1245,8 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
       break;
     case RAMP_S_BEAMSTOP: set_die(n, 1.0f); s_finish(c, n, s, ii); break;
     case RAMP_S_ATTENUATE: s_attenuate(c, n, s, ii); break;
-    case RAMP_S_MONO: s_mono(c, n, s, ii, r); break;
-    case RAMP_S_POWDER1: s_powder1(c, n, s, ii, r); break;
+    case RAMP_S_MONO: if constexpr (EXT) s_mono(c, n, s, ii, r); break;
+    case RAMP_S_POWDER1: if constexpr (EXT) s_powder1(c, n, s, ii, r); break;
     default: break;
   }
 }
@@ -1253,7 +1256,7 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
 /* intersect, terminate, scatter, untransform on a live neutron.  The   */
 /* intersection starts at its reset value.                               */
 /* ------------------------------------------------------------------ */
-template <class D = NoDiff>
+template <class D = NoDiff, bool EXT = true>
 DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st,
                     D* dx = nullptr, const bool zx = false) {
   transform(c, n);
@@ -1262,7 +1265,7 @@ DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st
   if (intersect(c, n, s, st)) ii = c.idx;
   /* terminate.cl:16-18 */
   if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
-  if (ii == c.idx && !(n.die > 0.f)) scatter<D>(c, n, s, ii, r, st, dx, zx);
+  if (ii == c.idx && !(n.die > 0.f)) scatter<D, EXT>(c, n, s, ii, r, st, dx, zx);
   if (zx && n.p == 0.0f) {
     set_die(n, 1.0f);
     return;

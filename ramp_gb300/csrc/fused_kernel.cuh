@@ -41,7 +41,7 @@
  * buffer (no atomics) and finish in PHASE 2.  The bounds of both loops are kernel parameters, so the loop
  * counters and descriptor addresses stay warp-uniform.
  */
-template <int MINB, int MODE, bool BATCHED, int PHASE>
+template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
 __global__ void __launch_bounds__(256, MINB)
 k_fused(const FusedArgs a);
 
@@ -51,7 +51,7 @@ k_fused(const FusedArgs a);
  * survivors out 32 to a pass.  A survivor is keyed by its own index and
  * variant, so it continues exactly where stage A left it. */
 #define SURV_GROUP 8
-template <int MODE, bool BATCHED>
+template <int MODE, bool BATCHED, bool EXT>
 DI void fused_tail(const FusedArgs& a) {
   const int lane = threadIdx.x & 31;
   const bool carry = (a.carry_sb != nullptr);
@@ -106,7 +106,7 @@ DI void fused_tail(const FusedArgs& a) {
         if (B.linear) {
           for (int k = B.first > K ? B.first : K; k < e; ++k) {
             if (n.die > 0.f) break;
-            comp_linear(comps[k], n, ii, r, a.st, (NoDiff*)nullptr, zx);
+            comp_linear<NoDiff, EXT>(comps[k], n, ii, r, a.st, (NoDiff*)nullptr, zx);
           }
         } else {
           block_nonlinear(comps, B.first, B.count, B.multi, n, ii, r, a.st);
@@ -117,11 +117,11 @@ DI void fused_tail(const FusedArgs& a) {
   }
 }
 
-template <int MINB, int MODE, bool BATCHED, int PHASE>
+template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
 __global__ void __launch_bounds__(256, MINB)
 k_fused(const FusedArgs a) {
   if constexpr (PHASE == 2) {
-    fused_tail<MODE, BATCHED>(a);
+    fused_tail<MODE, BATCHED, EXT>(a);
     return;
   } else {
     const int lane = threadIdx.x & 31;
@@ -172,7 +172,7 @@ k_fused(const FusedArgs a) {
           rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
           const float old_sb = carry ? a.carry_sb[i] : 0.0f;
           ii = carry ? a.carry_iidx[i] : 0u;
-          generate(V->src, n, old_sb, num_sim, seed, r);
+          generate<NoDiff, EXT>(V->src, n, old_sb, num_sim, seed, r);
           if (zx && n.p == 0.0f) n.die = 1.0f;
           for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
             const RampBlock B = a.blocks[b];
@@ -181,7 +181,7 @@ k_fused(const FusedArgs a) {
               const int e = (PHASE == 1 && B.first + B.count > KE) ? KE : B.first + B.count;
               for (int k = B.first; k < e; ++k) {
                 if (n.die > 0.f) break;
-                comp_linear(comps[k], n, ii, r, a.st, (NoDiff*)nullptr, zx);
+                comp_linear<NoDiff, EXT>(comps[k], n, ii, r, a.st, (NoDiff*)nullptr, zx);
               }
             } else {
               block_nonlinear(comps, B.first, B.count, B.multi, n, ii, r, a.st);
@@ -224,11 +224,13 @@ k_fused(const FusedArgs a) {
  * then stage B of a split launch */
 template <int MINB, int MODE, bool BATCHED>
 cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream_t s) {
-  if (a.split > 0) {
-    k_fused<MINB, MODE, BATCHED, 1><<<grid, block, 0, s>>>(a);
-    k_fused<MINB, MODE, BATCHED, 2><<<grid, block, 0, s>>>(a);
+  if (a.ext) {                   /* extended kinds: whole chain, no split */
+    k_fused<MINB, MODE, BATCHED, 0, true><<<grid, block, 0, s>>>(a);
+  } else if (a.split > 0) {
+    k_fused<MINB, MODE, BATCHED, 1, false><<<grid, block, 0, s>>>(a);
+    k_fused<MINB, MODE, BATCHED, 2, false><<<grid, block, 0, s>>>(a);
   } else {
-    k_fused<MINB, MODE, BATCHED, 0><<<grid, block, 0, s>>>(a);
+    k_fused<MINB, MODE, BATCHED, 0, false><<<grid, block, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
@@ -238,7 +240,7 @@ int occ_mm(int block) {
   static int cached = 0;
   if (cached > 0) return cached;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<MINB, MODE, false, 0>, block,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<MINB, MODE, false, 0, false>, block,
                                                     0) != cudaSuccess || nb <= 0)
     return 1;
   cached = nb;

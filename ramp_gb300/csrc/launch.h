@@ -47,7 +47,9 @@ struct FusedArgs {
   int64_t surv_items;
   unsigned long long* workq;    /* work-queue counter of this launch */
   int32_t var_key;              /* single variant: its index in the RNG key */
-  int32_t pad2;
+  int32_t ext;                  /* the chain uses an extended kind (MISIS source,
+                                   SMonochromator, SPowder1): the kernel built
+                                   with them; no split */
 };
 #define SURV_WORDS 18           /* 15 record lanes (die is 0), iidx, index, variant */
 
