@@ -1,0 +1,104 @@
+"""Instrument definition files: the reference's substitution, comment,
+disable, relative-frame, index and block rules (mcramp.py:35-116, 254-355),
+checked on the host without a GPU."""
+import json
+
+import numpy as np
+import pytest
+
+import ramp_gb300 as m
+from ramp_gb300 import _abi
+from ramp_gb300.instrument import frame_rotate
+
+IDF = """// test instrument
+{
+  "primary": {
+    "linear": true,
+    "mod": {"source": true, "position": [0, 0, 0],
+            "moderator_kernel": {"name": "MFlat", "mod_dim": [0.01, 0.01],
+                                 "target_dim": [0.01, 0.01], "target_dist": $dist$,
+                                 "E_min": $2*E$, "E_max": $xx$}},
+    "arm": {"position": [0, 0, 1.0], "rotation": [0.0, $ang$, 0.0],
+            "geom_kernel": {"name": "GArm"}, "scat_kernel": {"name": "SArm"}},
+    "off": {"disable": $skip$, "position": [0, 0, 2.0],
+            "geom_kernel": {"name": "GArm"}, "scat_kernel": {"name": "SArm"}},
+    "slit": {"position": [0.1, 0.0, 0.5], "relative": "arm", "restore_neutron": true,
+             "geom_kernel": {"name": "GPlane", "width": 0.02, "height": 0.03,
+                             "orientation": "yz"},
+             "scat_kernel": {"name": "SArm"}}   // trailing comment
+  },
+  "environment": {
+    "linear": false,
+    "multi": 3,
+    "can": {"position": [0, 0, 3.0],
+            "geom_kernel": {"name": "GSphere", "radius": 0.01},
+            "scat_kernel": {"name": "SBeamstop"}}
+  },
+  "tail": {
+    "det": {"position": [0, 0, 4.0],
+            "geom_kernel": {"name": "GPlane", "width": 0.1, "height": 0.1},
+            "scat_kernel": {"name": "SDetector1D", "var": "tof", "binning": [0, 10, 1000]}}
+  }
+}
+"""
+
+
+def make(tmp_path, **kw):
+    fn = tmp_path / "inst.json"
+    fn.write_text(IDF)
+    args = dict(dist=1.5, E=2.5, x=3, xx=7, ang=0.3, skip=1)
+    args.update(kw)
+    return m.Instrument(str(fn), "cpu", **args)
+
+
+def test_substitution_and_comments(tmp_path):
+    inst = make(tmp_path)
+    src = inst.source
+    assert src.target_dist == np.float32(1.5)
+    assert src.E_min == np.float32(5.0)
+    # the reference substitutes variable names as substrings, in keyword
+    # order: with x before xx, the token "xx" becomes "33"
+    assert src.E_max == np.float32(33.0)
+
+
+def test_substring_rule_depends_on_keyword_order(tmp_path):
+    fn = tmp_path / "inst.json"
+    fn.write_text(IDF)
+    inst = m.Instrument(str(fn), "cpu", dist=1.5, E=2.5, xx=7, x=3, ang=0.3, skip=1)
+    assert inst.source.E_max == np.float32(7.0)
+
+
+def test_disable_and_indices(tmp_path):
+    names = [n for n, _ in make(tmp_path).components()]
+    assert names == ["arm", "slit", "can", "det"]
+    comps = dict(make(tmp_path).components())
+    # the source takes index 1; disabled components take none
+    assert [comps[n]["idx"] for n in names] == [2, 3, 4, 5]
+    names2 = [n for n, _ in make(tmp_path, skip=0).components()]
+    assert names2 == ["arm", "off", "slit", "can", "det"]
+
+
+def test_relative_frame(tmp_path):
+    comps = dict(make(tmp_path).components())
+    arm, slit = comps["arm"], comps["slit"]
+    want = np.add(frame_rotate([0.1, 0.0, 0.5], [0.0, 0.3, 0.0]), [0.0, 0.0, 1.0])
+    assert np.allclose(slit["pos"], want)
+    assert np.allclose(slit["rot"], arm["rot"])
+    assert slit["restore_neutron"] == 1
+
+
+def test_blocks_and_descriptor_slots(tmp_path):
+    inst = make(tmp_path)
+    src, carr, nc, barr, nb = inst.descriptors([])
+    assert nc == 4 and nb == 3
+    blocks = [(barr[k].first, barr[k].count, barr[k].linear, barr[k].multi) for k in range(nb)]
+    assert blocks == [(0, 2, 1, 1), (2, 1, 0, 3), (3, 1, 1, 1)]
+    assert carr[1].geom == _abi.G_PLANE and carr[1].gi[0] == 1 and carr[1].restore == 1
+    assert carr[2].geom == _abi.G_SPHERE and carr[2].scat == _abi.S_BEAMSTOP
+    assert src.kind == _abi.SRC_FLAT
+
+
+def test_execute_without_a_gpu_fails_loudly(tmp_path):
+    inst = make(tmp_path)
+    with pytest.raises(RuntimeError):
+        inst.execute(10)
