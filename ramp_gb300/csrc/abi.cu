@@ -4,6 +4,7 @@
  * the plain and fused launchers, status readback and error messages.
  */
 #include <climits>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -283,6 +284,15 @@ static int make_src(RampPlan* p, const RampSource& s, SrcDev& d, bool may_upload
     d.dmax[0] = maxwell_h(RC_K_B * s.p[7], s.p[7]);
     d.dmax[1] = maxwell_h(RC_K_B * s.p[9], s.p[9]);
     d.dmax[2] = maxwell_h(RC_K_B * s.p[11], s.p[11]);
+    /* I_q * M(E; T_q) / dmax_q is +0 for every drawn E >= 0 when I_q = 0
+       and T_q, dmax_q are finite and positive: adding it changes no sum */
+    const bool e_ok = s.p[5] >= 0.0f && s.p[6] >= 0.0f && std::isfinite(s.p[5]) &&
+                      std::isfinite(s.p[6]);
+    for (int q = 1; q < 3; ++q) {
+      const float I = s.p[8 + 2 * q], T = s.p[7 + 2 * q], dm = d.dmax[q];
+      if (e_ok && I == 0.0f && T > 0.0f && std::isfinite(T) && dm > 0.0f && std::isfinite(dm))
+        d.zero_terms |= 1u << q;
+    }
   }
   if (s.kind == RAMP_SRC_ISIS) {
     const int64_t nt = s.table_len[1], ne = s.table_len[2];

@@ -301,8 +301,8 @@ template <class D>
 DI float cont_weight(const SrcDev& s, float E_val, int32_t num_sim, D* dx) {
   float E_J = RC_EV_J * E_val;
   float M = s.p[8] * maxwell(E_J, s.p[7]) / s.dmax[0];
-  M += s.p[10] * maxwell(E_J, s.p[9]) / s.dmax[1];
-  M += s.p[12] * maxwell(E_J, s.p[11]) / s.dmax[2];
+  if (!(s.zero_terms & 2u)) M += s.p[10] * maxwell(E_J, s.p[9]) / s.dmax[1];
+  if (!(s.zero_terms & 4u)) M += s.p[12] * maxwell(E_J, s.p[11]) / s.dmax[2];
   if constexpr (D::on) {
     /* weight I M(E;T)/M(kT;T) = I sqrt(x) e^(1-x), x = E/kT, for the
        common temperature T of the three terms: d log/dT = (x - 1/2)/T */

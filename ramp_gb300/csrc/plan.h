@@ -52,6 +52,11 @@ struct SrcDev {
   const float* tab[4];         /* MISIS: flux CDF, time bins, energy edges,
                                   cumulative flux at the edges (device)   */
   int32_t n_t, n_e;            /* MISIS: time bins, energy edges          */
+  uint32_t zero_terms;         /* MCont: bit q set when term q (1 or 2) is
+                                  exactly +0 for every energy the source
+                                  can draw (I_q = 0, finite positive T_q and
+                                  normalisation, E_min, E_max >= 0)       */
+  uint32_t pad_z;
 };
 
 struct RngDev {
