@@ -284,6 +284,11 @@ static int make_src(RampPlan* p, const RampSource& s, SrcDev& d, bool may_upload
     d.dmax[0] = maxwell_h(RC_K_B * s.p[7], s.p[7]);
     d.dmax[1] = maxwell_h(RC_K_B * s.p[9], s.p[9]);
     d.dmax[2] = maxwell_h(RC_K_B * s.p[11], s.p[11]);
+    for (int q = 0; q < 3; ++q) {          /* the per-neutron constants of M(E; T_q) */
+      const float overKT = 1.0f / (RC_K_B * s.p[7 + 2 * q]);
+      d.okt[q] = overKT;
+      d.okc[q] = overKT * sqrtf(overKT);
+    }
     /* I_q * M(E; T_q) / dmax_q is +0 for every drawn E >= 0 when I_q = 0
        and T_q, dmax_q are finite and positive: adding it changes no sum */
     const bool e_ok = s.p[5] >= 0.0f && s.p[6] >= 0.0f && std::isfinite(s.p[5]) &&
@@ -359,6 +364,8 @@ static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo 
   memcpy(d.si, c.si, sizeof(d.si));
   for (int k = 0; k < 6; ++k) d.dslot[k] = -1;
   if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
+  /* chopper slit period 2 pi / n_slits (chopper.cl:21), per component */
+  if (c.scat == RAMP_S_CHOPPER) d.aux[0] = 2.0f * RC_PI / (float)(uint32_t)c.si[0];
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;   /* the BVH replaces the raw points */
@@ -1152,6 +1159,8 @@ static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* mem
   memcpy(d.si, c.si, sizeof(d.si));
   for (int k = 0; k < 6; ++k) d.dslot[k] = -1;
   if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
+  /* chopper slit period 2 pi / n_slits (chopper.cl:21), per component */
+  if (c.scat == RAMP_S_CHOPPER) d.aux[0] = 2.0f * RC_PI / (float)(uint32_t)c.si[0];
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;

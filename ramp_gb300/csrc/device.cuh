@@ -237,6 +237,11 @@ DI float maxwell(float E, float T) {
   float overKT = 1.0f / (RC_K_B * T);
   return 2.0f * rootE / sqrtf(RC_PI) * (overKT * sqrtf(overKT)) * rm_expf(-E * overKT);
 }
+/* the same with 1/(k_B T) and its 3/2 power from the plan */
+DI float maxwell_pre(float E, float overKT, float okc) {
+  float rootE = sqrtf(E);
+  return 2.0f * rootE / sqrtf(RC_PI) * okc * rm_expf(-E * overKT);
+}
 
 /* MISIS table read: entries outside the table read as 0 (the reference
  * reads past both ends for a deviate below the first flux value or above
@@ -300,9 +305,9 @@ DI float isis_sample(const SrcDev& s, Nt& n, Rng& r, float& t0) {
 template <class D>
 DI float cont_weight(const SrcDev& s, float E_val, int32_t num_sim, D* dx) {
   float E_J = RC_EV_J * E_val;
-  float M = s.p[8] * maxwell(E_J, s.p[7]) / s.dmax[0];
-  if (!(s.zero_terms & 2u)) M += s.p[10] * maxwell(E_J, s.p[9]) / s.dmax[1];
-  if (!(s.zero_terms & 4u)) M += s.p[12] * maxwell(E_J, s.p[11]) / s.dmax[2];
+  float M = s.p[8] * maxwell_pre(E_J, s.okt[0], s.okc[0]) / s.dmax[0];
+  if (!(s.zero_terms & 2u)) M += s.p[10] * maxwell_pre(E_J, s.okt[1], s.okc[1]) / s.dmax[1];
+  if (!(s.zero_terms & 4u)) M += s.p[12] * maxwell_pre(E_J, s.okt[2], s.okc[2]) / s.dmax[2];
   if constexpr (D::on) {
     /* weight I M(E;T)/M(kT;T) = I sqrt(x) e^(1-x), x = E/kT, for the
        common temperature T of the three terms: d log/dT = (x - 1/2)/T */
@@ -690,10 +695,9 @@ DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
 DI void s_chopper(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
   const float slit_width = c.sp[0], radius = c.sp[1], freq = c.sp[2], phase = c.sp[3];
   const float jitter = c.sp[4];
-  const uint32_t n_slits = (uint32_t)c.si[0];
   set_pos(n, ip2(s));
   n.t += s.t2;
-  float Tg = 2.0f * RC_PI / (float)n_slits;
+  const float Tg = c.aux[0];              /* 2 pi / n_slits (si[0]), from the plan */
   float pha_error = jitter * 2.0f * (draw(n, r) - 0.5f);
   float thi_chop = freq * (n.t - fabsf(phase)) + pha_error;
   float thi_neut = rm_atan2f(n.x, n.y + radius);

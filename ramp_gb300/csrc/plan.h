@@ -52,6 +52,8 @@ struct SrcDev {
   const float* tab[4];         /* MISIS: flux CDF, time bins, energy edges,
                                   cumulative flux at the edges (device)   */
   int32_t n_t, n_e;            /* MISIS: time bins, energy edges          */
+  float okt[3];                /* MCont: 1 / (k_B T_q), and okt^1.5 as      */
+  float okc[3];                /* maxwell_energy_distn computes them       */
   uint32_t zero_terms;         /* MCont: bit q set when term q (1 or 2) is
                                   exactly +0 for every energy the source
                                   can draw (I_q = 0, finite positive T_q and
