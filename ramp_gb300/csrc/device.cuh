@@ -206,10 +206,20 @@ DI void tally_add(float* h, float* he, long long idx, float p) {
 /* ------------------------------------------------------------------ */
 struct NoDiff {
   static constexpr bool on = false;
+  static constexpr bool pol = true;   /* the spin lanes are output */
+};
+
+/* Whole-chain kernels output tallies only, and no component turns the spin
+ * into a weight, a position or a branch: the spin lanes are dead there.
+ * Their draws are still taken (the RNG counter must advance as it does
+ * with them), their trigonometry and rotations are skipped. */
+struct TallyOnly : NoDiff {
+  static constexpr bool pol = false;
 };
 
 struct AdjDiff {
   static constexpr bool on = true;
+  static constexpr bool pol = false;
   float dlog[RAMP_MAX_DIFF];
   double* grad;      /* nslot accumulators, global                       */
   int nslot;
@@ -354,14 +364,19 @@ DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t 
   float Dx = s.p[2] * (0.5f - draw(n, r)) - n.x;
   float Dy = s.p[3] * (0.5f - draw(n, r)) - n.y;
   set_vel(n, mul(vel, normalize(v3(Dx, Dy, s.p[4]))));
-  float theta = 2 * RC_PI * draw(n, r);
-  float phi = rm_acosf(1 - 2 * draw(n, r));
-  float sp, cp, st, ct;
-  rm_sincosf(phi, &sp, &cp);
-  rm_sincosf(theta, &st, &ct);
-  n.px = sp * ct;
-  n.py = sp * st;
-  n.pz = cp;
+  if constexpr (D::pol) {
+    float theta = 2 * RC_PI * draw(n, r);
+    float phi = rm_acosf(1 - 2 * draw(n, r));
+    float sp, cp, st, ct;
+    rm_sincosf(phi, &sp, &cp);
+    rm_sincosf(theta, &st, &ct);
+    n.px = sp * ct;
+    n.py = sp * st;
+    n.pz = cp;
+  } else {
+    draw(n, r);
+    draw(n, r);
+  }
   n.t = t0;
   n.die = 0.0f;
 }
@@ -380,17 +395,19 @@ DI V3 rot_inv(const float* R, V3 v) {
   return v3(dot(v3(R[0], R[3], R[6]), v), dot(v3(R[1], R[4], R[7]), v),
             dot(v3(R[2], R[5], R[8]), v));
 }
+template <bool POL = true>
 DI void transform(const CompDev& c, Nt& n) {
   set_pos(n, sub(npos(n), v3(c.pos[0], c.pos[1], c.pos[2])));
   set_pos(n, rot_inv(c.R, npos(n)));
   set_vel(n, rot_inv(c.R, nvel(n)));
-  if (c.rotated) set_pol(n, rot_inv(c.R, npol(n)));
+  if (POL && c.rotated) set_pol(n, rot_inv(c.R, npol(n)));
 }
+template <bool POL = true>
 DI void untransform(const CompDev& c, Nt& n) {
   set_pos(n, rot_fwd(c.R, npos(n)));
   set_pos(n, add(npos(n), v3(c.pos[0], c.pos[1], c.pos[2])));
   set_vel(n, rot_fwd(c.R, nvel(n)));
-  if (c.rotated) set_pol(n, rot_fwd(c.R, npol(n)));
+  if (POL && c.rotated) set_pol(n, rot_fwd(c.R, npol(n)));
 }
 
 /* rotate_about_axis — geom.h:1-19 */
@@ -742,6 +759,7 @@ DI void sample_distn(Nt& n, Rng& r, const float* __restrict__ q, const float* __
 }
 
 /* isotropic.cl:75-322 */
+template <bool POL = true>
 DI void s_isotropic(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
   const float temperature = c.sp[0];
   const uint32_t transmit = (uint32_t)c.si[0];
@@ -822,7 +840,8 @@ DI void s_isotropic(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
   set_vel(n, v3(normvel.x * kf * RC_K2V, normvel.y * kf * RC_K2V, normvel.z * kf * RC_K2V));
   V3 dv = sub(oldvel, nvel(n));
   V3 q_norm = normalize(v3(dv.x * RC_V2K, dv.y * RC_V2K, dv.z * RC_V2K));
-  if (flag == 2) {
+  if (!POL) {
+  } else if (flag == 2) {
     const float k = -1.0f / 3.0f;
     set_pol(n, v3(n.px * k, n.py * k, n.pz * k));
   } else if (flag == 3) {
@@ -1238,7 +1257,7 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
     case RAMP_S_ARM: ii = c.idx; is_reset(s); break;
     case RAMP_S_GUIDE: s_guide<D>(c, n, s, ii, st, dx, zx); break;
     case RAMP_S_CHOPPER: s_chopper(c, n, s, ii, r); break;
-    case RAMP_S_ISOTROPIC: s_isotropic(c, n, s, ii, r); break;
+    case RAMP_S_ISOTROPIC: s_isotropic<D::pol>(c, n, s, ii, r); break;
     case RAMP_S_POWDERN: s_powdern<D>(c, n, s, ii, r, st, dx); break;
     case RAMP_S_DET1D: s_det1d<D>(c, n, s, ii, st, dx); break;
     case RAMP_S_DET2D: s_det2d<D>(c, n, s, ii, st, dx); break;
@@ -1263,7 +1282,7 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
 template <class D = NoDiff, bool EXT = true>
 DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st,
                     D* dx = nullptr, const bool zx = false) {
-  transform(c, n);
+  transform<D::pol>(c, n);
   Is s;
   is_reset(s);
   if (intersect(c, n, s, st)) ii = c.idx;
@@ -1274,7 +1293,7 @@ DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st
     set_die(n, 1.0f);
     return;
   }
-  if (!(n.die > 0.f)) untransform(c, n);
+  if (!(n.die > 0.f)) untransform<D::pol>(c, n);
 }
 
 /* one non-linear block (mcramp.py:167-217): "multi" rounds of all
@@ -1288,16 +1307,16 @@ DI void block_nonlinear(const CompDev* comps, int first, int count, int multi, N
     for (int j = first; j < first + count; ++j) {
       if (n.die > 0.f) break;
       const CompDev& c = comps[j];
-      transform(c, n);
+      transform<D::pol>(c, n);
       if (intersect(c, n, s, st)) ii = c.idx;
-      untransform(c, n);
+      untransform<D::pol>(c, n);
     }
     for (int j = first; j < first + count; ++j) {
       if (n.die > 0.f) break;
       const CompDev& c = comps[j];
-      transform(c, n);
+      transform<D::pol>(c, n);
       if (ii == c.idx) scatter<D>(c, n, s, ii, r, st, dx);
-      if (!(n.die > 0.f)) untransform(c, n);
+      if (!(n.die > 0.f)) untransform<D::pol>(c, n);
     }
   }
 }

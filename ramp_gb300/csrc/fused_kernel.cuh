@@ -106,10 +106,10 @@ DI void fused_tail(const FusedArgs& a) {
         if (B.linear) {
           for (int k = B.first > K ? B.first : K; k < e; ++k) {
             if (n.die > 0.f) break;
-            comp_linear<NoDiff, EXT>(comps[k], n, ii, r, a.st, (NoDiff*)nullptr, zx);
+            comp_linear<TallyOnly, EXT>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
           }
         } else {
-          block_nonlinear(comps, B.first, B.count, B.multi, n, ii, r, a.st);
+          block_nonlinear<TallyOnly>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
         }
       }
       if (carry) { a.carry_sb[idx] = n.sb; a.carry_iidx[idx] = ii; }
@@ -172,7 +172,7 @@ k_fused(const FusedArgs a) {
           rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
           const float old_sb = carry ? a.carry_sb[i] : 0.0f;
           ii = carry ? a.carry_iidx[i] : 0u;
-          generate<NoDiff, EXT>(V->src, n, old_sb, num_sim, seed, r);
+          generate<TallyOnly, EXT>(V->src, n, old_sb, num_sim, seed, r);
           if (zx && n.p == 0.0f) n.die = 1.0f;
           for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
             const RampBlock B = a.blocks[b];
@@ -181,10 +181,10 @@ k_fused(const FusedArgs a) {
               const int e = (PHASE == 1 && B.first + B.count > KE) ? KE : B.first + B.count;
               for (int k = B.first; k < e; ++k) {
                 if (n.die > 0.f) break;
-                comp_linear<NoDiff, EXT>(comps[k], n, ii, r, a.st, (NoDiff*)nullptr, zx);
+                comp_linear<TallyOnly, EXT>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
               }
             } else {
-              block_nonlinear(comps, B.first, B.count, B.multi, n, ii, r, a.st);
+              block_nonlinear<TallyOnly>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
             }
           }
         }
