@@ -192,7 +192,15 @@ def run_batched_config(a):
     fn, kws, counts = batched_workload(a.config)
     total = sum(counts)
     B = BatchedInstrument(fn, kws, ctx=dev)
-    tune = None if a.tune in (None, "auto") else json.loads(a.tune)
+    if a.tune == "auto":
+        # the autotuner's register cap for the first variant; per-variant
+        # task sizes stay automatic, and no split (its two launches per
+        # variant measured slower on this scan of mostly short variants)
+        from ramp_gb300 import autotune
+        tune = {k: v for k, v in autotune.tune(B.instruments[0], rng="reference").items()
+                if k == "blocks_per_sm"}
+    else:
+        tune = json.loads(a.tune) if a.tune else None
     for w in range(a.warmup):
         B.execute(counts, rng="reference", seeds=list(range(len(counts))), tune=tune)
     torch.cuda.synchronize()
@@ -234,13 +242,16 @@ def run_batched_config(a):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": name, "variants": len(counts), "histories_per_step": total,
+                       "tune": tune,
                        "rng": "reference keying",
                        "path": "batched fused: one single-instrument launch per variant on "
                                "16 concurrent streams forked from the caller's stream"},
             "plain_path_sequential": {"value": total / (plain_ms / 1000.0), "ms_per_step": plain_ms,
                                       "sample": "first %d variants, scaled by histories" % nplain},
             "batched_over_plain": (total / (statistics.mean(ms) / 1000.0)) / (total / (plain_ms / 1000.0)),
-            "gpu_launches": a.steps * sum(1 for c in counts if c > 0), "clocks": clk}
+            "gpu_launches": a.steps * sum(1 for c in counts if c > 0) *
+                            (2 if int((tune or {}).get("split", 0)) > 0 else 1),
+            "clocks": clk}
     print(json.dumps(line), flush=True)
 
 

@@ -210,9 +210,10 @@ typedef struct RampTune {
                                    ramp_trace_batched_noalloc.           */
   int32_t streams;              /* ramp_trace_batched: 1 = one launch over
                                    a task list; otherwise each variant is
-                                   a launch of its own on up to this many
-                                   concurrent streams (0: 16).  A split
-                                   launch is always one launch.          */
+                                   a launch (or, split, two) of its own on
+                                   up to this many concurrent streams
+                                   (0: 16), with its own region of the
+                                   survivor buffer.                      */
 } RampTune;
 
 typedef struct RampPlan RampPlan;

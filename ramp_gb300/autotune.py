@@ -143,7 +143,7 @@ def _time_config(lib, plan, n, rng, cfg, stream, reps=2):
     return best
 
 
-def tune(inst, n_probe=2_000_000, rng="reference", candidates=None, force=False):
+def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False):
     """Best fused launch configuration for ``inst`` (a dict for
     Instrument.execute(tune=...)); measured once per GPU and instrument
     structure, then read from the cache."""

@@ -749,6 +749,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.carry_iidx = iidx_carry;
   a.st = p->status;
   a.workq = &p->status->workq;
+  a.workq_b = &p->status->workq_b;
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
   a.ext = p->ext ? 1 : 0;
@@ -773,12 +774,28 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
                            int block, int grid, const RampTune* tune, cudaStream_t s) {
   BatchCache& B = p->batch;
   const size_t nv = vars.size();
-  if (B.counters_cap < nv) {
+  if (B.counters_cap < 2 * nv) {             /* stage A and stage B queues */
     if (B.counters) cudaFree(B.counters);
     B.counters = nullptr;
     B.counters_cap = 0;
-    CK(cudaMalloc(&B.counters, nv * sizeof(unsigned long long)));
-    B.counters_cap = nv;
+    CK(cudaMalloc(&B.counters, 2 * nv * sizeof(unsigned long long)));
+    B.counters_cap = 2 * nv;
+  }
+  /* split launches: each variant gets its own region of the survivor
+     buffer (its items' slots, SoA, and its items' counts) */
+  int32_t split = 0;
+  int rc0 = tune_split(p, tune, &split);
+  if (rc0) return rc0;
+  if (base.ext) split = 0;
+  std::vector<int64_t> item_off(nv + 1, 0);
+  for (size_t v = 0; v < nv; ++v)
+    item_off[v + 1] = item_off[v] + (vars[v].n > 0 ? (vars[v].n + 127) / 128 : 0);
+  uint32_t* cnt = nullptr;
+  if (split > 0 && item_off[nv] > 0) {
+    rc0 = ensure_surv(p, item_off[nv]);
+    if (rc0) return rc0;
+    cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS;
+    CK(cudaMemsetAsync(cnt, 0, (size_t)item_off[nv] * sizeof(uint32_t), s));
   }
   StreamSet& S = p->streams;
   if (!S.ready) {
@@ -791,7 +808,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
   }
   const int ns = (tune && tune->streams > 1 && tune->streams < RAMP_BATCH_STREAMS)
                      ? tune->streams : RAMP_BATCH_STREAMS;
-  CK(cudaMemsetAsync(B.counters, 0, nv * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(B.counters, 0, 2 * nv * sizeof(unsigned long long), s));
   CK(cudaEventRecord(S.fork, s));
   for (int k = 0; k < ns; ++k) CK(cudaStreamWaitEvent(S.st[k], S.fork, 0));
   std::vector<int> order(nv);
@@ -808,8 +825,17 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
     a.single = vars[v];
     a.var_key = v;
     a.workq = B.counters + v;
-    a.task_size = auto_task(vars[v].n, grid, (tune && tune->chunk > 0) ? tune->chunk : 0);
+    a.workq_b = B.counters + nv + v;
+    a.task_size = auto_task(vars[v].n, grid, 0);
     a.n_tasks = (vars[v].n + a.task_size - 1) / a.task_size;
+    if (cnt) {
+      const int64_t items = item_off[v + 1] - item_off[v];
+      a.split = split;
+      a.surv = p->surv + (size_t)item_off[v] * 128 * SURV_WORDS;
+      a.surv_cap = items * 128;
+      a.surv_cnt = cnt + item_off[v];
+      a.surv_items = items;
+    }
     CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), S.st[k]));
   }
   for (int k = 0; k < ns; ++k) {
@@ -874,7 +900,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   }
   std::vector<VariantDev> vars((size_t)n_variants);
   std::vector<TaskDev> tasks;
-  const bool use_streams = !(tune && (tune->streams == 1 || tune->split > 0));
+  const bool use_streams = !(tune && tune->streams == 1);
   for (int v = 0; v < n_variants; ++v) {
     int rc = make_src(p, variants[v].source, vars[v].src, true, &memo);
     if (rc) return rc;
@@ -946,6 +972,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.rng.tid_base = 0u;   /* variants key by their own index */
   a.st = p->status;
   a.workq = &p->status->workq;
+  a.workq_b = &p->status->workq_b;
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
   a.ext = ext ? 1 : 0;
@@ -1299,6 +1326,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.rng.tid_base = 0u;
   a.st = &D->status;
   a.workq = &D->status.workq;
+  a.workq_b = &D->status.workq_b;
   a.ext = p->ext ? 1 : 0;
   for (int v = 0; v < n_variants; ++v)
     if (ext_source(variants[v].source)) a.ext = 1;

@@ -60,7 +60,7 @@ DI void fused_tail(const FusedArgs& a) {
   const int64_t cap = a.surv_cap;
   for (;;) {
     unsigned long long g = 0;
-    if (lane == 0) g = atomicAdd(&a.st->workq_b, 1ull);
+    if (lane == 0) g = atomicAdd(a.workq_b, 1ull);
     g = __shfl_sync(FULL_MASK, g, 0);
     const int64_t t0 = (int64_t)g * SURV_GROUP;
     if (t0 >= a.surv_items) break;

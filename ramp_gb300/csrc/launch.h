@@ -46,6 +46,7 @@ struct FusedArgs {
   uint32_t* surv_cnt;           /* survivors per work item */
   int64_t surv_items;
   unsigned long long* workq;    /* work-queue counter of this launch */
+  unsigned long long* workq_b;  /* stage-B work-queue counter (split) */
   int32_t var_key;              /* single variant: its index in the RNG key */
   int32_t ext;                  /* the chain uses an extended kind (MISIS source,
                                    SMonochromator, SPowder1): the kernel built

@@ -288,12 +288,14 @@ def test_fused_split_with_multi_chunk_carry(cuda_lib):
     tallies_close(gi, ci)
 
 
-def test_batched_split_matches_single_runs(cuda_lib):
-    """Parked survivors of different variants share a warp in stage B."""
+@pytest.mark.parametrize("tune", [{"split": 2}, {"split": 2, "streams": 1, "chunk": 4096}])
+def test_batched_split_matches_single_runs(cuda_lib, tune):
+    """Split batched launches: per-variant launches with their own survivor
+    regions, or one task-list launch whose stage B mixes variants."""
     variants = [I.let_like_kwargs(Ei=3.7), I.let_like_kwargs(Ei=8.0), I.let_like_kwargs(Ei=2.5)]
     counts = [300_000, 123_457, 200_003]
     B = BatchedInstrument(I.path("let_like.json"), variants, ctx="cuda")
-    B.execute(counts, rng="native", seeds=[11, 2222, 4000], tune={"split": 2, "chunk": 4096})
+    B.execute(counts, rng="native", seeds=[11, 2222, 4000], tune=tune)
     torch.cuda.synchronize()
     for v, (kw, n, seed) in enumerate(zip(variants, counts, [11, 2222, 4000])):
         ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
