@@ -194,12 +194,19 @@ typedef struct RampVariant {
   int32_t seed;                 /* randint(0,4096) stand-in              */
 } RampVariant;
 
-/* Launch configuration chosen by the autotuner (0 = default).             */
+/* Launch configuration of the whole-chain kernels, chosen by the
+ * autotuner (ramp_gb300/autotune.py); 0 = default.                        */
 typedef struct RampTune {
-  int32_t block;                /* threads per block                     */
-  int32_t blocks_per_sm;        /* persistent CTAs per SM                */
-  int32_t chunk;                /* neutrons claimed per work-queue grab  */
-  int32_t privatize;            /* 1: shared-memory tally privatisation  */
+  int32_t block;                /* reserved, 0: the whole-chain kernels are
+                                   compiled for 256-thread CTAs          */
+  int32_t blocks_per_sm;        /* persistent CTAs per SM (register cap:
+                                   3 or 4; 0: 4)                         */
+  int32_t chunk;                /* neutrons per task-list entry; sizes the
+                                   grid of a single-instrument launch    */
+  int32_t privatize;            /* reserved, 0: tallies are warp-aggregated
+                                   atomics into L2; shared-memory copies
+                                   do not fit detector histograms of the
+                                   sizes traced here (720 x 1000 x 2)    */
   int32_t split;                /* fused path: split the chain before this
                                    component (0: off; not inside a
                                    non-linear block).  Stage A appends the
