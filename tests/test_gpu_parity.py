@@ -318,6 +318,40 @@ def test_autotune_survival_and_split_point(cuda_lib, tmp_path, monkeypatch):
         assert torch.equal(t, b)
 
 
+# ------------------------------------------------ statistical agreement
+def _chi2_two_sample(h1, e1, h2, e2, min_var=0.0):
+    """Two-sample chi-square of weighted histograms (sum p, sum p^2 per bin)
+    over the bins where either has weight."""
+    from scipy.stats import chi2
+    use = (e1 + e2) > min_var
+    stat = float((((h1 - h2) ** 2)[use] / (e1 + e2)[use]).sum())
+    dof = int(use.sum())
+    return stat, dof, float(chi2.sf(stat, dof))
+
+
+@pytest.mark.parametrize("fn,kw,N,shape", [
+    ("small_chain.json", "small", 1_000_000, (20, 25, 20, 25)),
+    ("let_like.json", "let", 20_000_000, (72, 10, 1, 1000))])
+def test_fused_agrees_with_oracle_on_independent_streams(cuda_lib, fn, kw, N, shape):
+    """Different chunk seeds (independent random streams): the fused GPU
+    histogram and the oracle's pass a two-sample chi-square test, p > 0.01,
+    on a coarse rebinning of the detector."""
+    kws = {"small": I.small_chain_kwargs(), "let": I.let_like_kwargs()}[kw]
+    gi = m.Instrument(I.path(fn), "cuda", **kws)
+    random.seed(101)
+    gi.execute(N, path="fused")
+    torch.cuda.synchronize()
+    ci = m.Instrument(I.path(fn), "cpu", **kws)
+    random.seed(202)
+    oracle.run(ci, N)
+    g = [t.double().cpu().numpy() for t in gi.tallies()[-2:]]
+    c = [t.double().numpy() for t in ci.tallies()[-2:]]
+    a, b, d, e = shape
+    rb = lambda x: x.reshape(a, b, d, e).sum(axis=(1, 3))
+    stat, dof, p = _chi2_two_sample(rb(g[0]), rb(g[1]), rb(c[0]), rb(c[1]))
+    assert dof > 10 and p > 0.01, (stat, dof, p)
+
+
 # ---------------------------------------------------------------- shards
 @pytest.mark.parametrize("path", ["plain", "fused"])
 def test_shards_sum_to_single_run(cuda_lib, path):
