@@ -87,6 +87,8 @@ struct RampPlan {
   std::map<TabKey, std::pair<void*, void*>> tabs;
   std::vector<CompDev> adj_host;     /* descriptors of the last adjoint   */
   CompDev* adj_dev = nullptr;
+  uint32_t* adj_list = nullptr;      /* indices counted by the loss detector, */
+  int64_t adj_cap = 0;               /* then its count (uint64) after them    */
   uint32_t* surv = nullptr;          /* survivor buffer of split launches */
   int64_t surv_cap = 0;              /* slots (128 per work item) */
   StreamSet streams;
@@ -419,6 +421,7 @@ int ramp_plan_destroy(RampPlan* p) {
   if (p->batch.vars_dev) cudaFree(p->batch.vars_dev);
   if (p->batch.tasks_dev) cudaFree(p->batch.tasks_dev);
   if (p->surv) cudaFree(p->surv);
+  if (p->adj_list) cudaFree(p->adj_list);
   if (p->batch.counters) cudaFree(p->batch.counters);
   if (p->streams.ready) {
     for (int k = 0; k < RAMP_BATCH_STREAMS; ++k) {
@@ -1081,6 +1084,23 @@ int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det
   a.grad = grad;
   a.lr = lr;
   a.st = p->status;
+  if (p->adj_cap < n) {                  /* n indices and one counter */
+    if (p->adj_list) cudaFree(p->adj_list);
+    p->adj_list = nullptr;
+    p->adj_cap = 0;
+    void* d = nullptr;
+    if (cudaMalloc(&d, (size_t)n * sizeof(uint32_t) + 2 * sizeof(unsigned long long)) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      set_err("ramp_adjoint: no room for %lld recorded indices", (long long)n);
+      return RAMP_E_NOMEM;
+    }
+    p->adj_list = (uint32_t*)d;
+    p->adj_cap = n;
+  }
+  a.list = p->adj_list;
+  a.list_cap = p->adj_cap;
+  a.list_count = (unsigned long long*)(((uintptr_t)(p->adj_list + p->adj_cap) + 7) & ~(uintptr_t)7);
   int64_t g = (n + 255) / 256;
   int64_t cap = (int64_t)p->sm_count * 8;
   CK(launch_adjoint(a, (int)(g < cap ? g : cap), s));

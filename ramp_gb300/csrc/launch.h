@@ -71,6 +71,9 @@ struct AdjointArgs {
   double* grad;
   int32_t lr;
   StatusDev* st;
+  uint32_t* list;               /* pass 1 output: indices the loss detector counts */
+  unsigned long long* list_count;
+  int64_t list_cap;
 };
 
 cudaError_t launch_adjoint(const AdjointArgs& a, int grid, cudaStream_t s);
