@@ -356,11 +356,23 @@ int ramp_plan_set_param(RampPlan* plan, int32_t kind, int32_t comp, float value)
  * (device, double, n_params entries, accumulated).  lr = 1 adds the
  * likelihood-ratio terms of the powder's transmit/scatter branch (an
  * unbiased estimator; lr = 0 is the pathwise derivative that central
- * finite differences with common random numbers measure).               */
+ * finite differences with common random numbers measure).  Only neutrons
+ * the loss detector counts carry a term: a first pass lists them and only
+ * they are replayed with derivatives; after ramp_forward_record with the
+ * same detector, chunk parameters and parameter values, its list is used
+ * and the first pass skipped.                                            */
 int ramp_adjoint(RampPlan* plan, const RampDiffParam* params, int n_params,
                  int det_comp, const float* dL_dH, int64_t n, int32_t num_sim,
                  int32_t seed, const RampRng* rng, int lr, double* grad,
                  void* stream);
+
+/* The forward histograms of a differentiable run (every tally of the
+ * chain, as a fused launch of n neutrons with these chunk parameters
+ * would add) together with the list of neutrons component det_comp
+ * counts, kept in the plan for the next ramp_adjoint on the same run.
+ * No counterpart in the reference.                                       */
+int ramp_forward_record(RampPlan* plan, int32_t det_comp, int64_t n, int32_t num_sim,
+                        int32_t seed, const RampRng* rng, void* stream);
 
 /* ramp_trace_batched without device allocation.  No counterpart in the
  * reference.  For callers that may not allocate device memory while

@@ -147,6 +147,9 @@ _SIGS = {
                      ctypes.c_int),
     "ramp_seed_advance": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "ramp_plan_reserve": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
+    "ramp_forward_record": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                             ctypes.c_int32, ctypes.POINTER(RampRng), ctypes.c_void_p],
+                            ctypes.c_int),
     "ramp_plan_set_buffer": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64],
                              ctypes.c_int),
     "ramp_run_components": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,

@@ -72,6 +72,14 @@ struct StreamSet {
  * variants that share a table share one upload (kind 0 table, 1 BVH) */
 typedef std::tuple<int, int64_t, uint64_t> TabKey;
 
+/* what a recorded index list was made for (ramp_forward_record) */
+struct RecKey {
+  int64_t n;
+  int32_t det, num_sim, seed, mode;
+  uint32_t run_seed, tid_base;
+  uint64_t version;
+};
+
 struct RampPlan {
   RampSource src_in;
   SrcDev src;
@@ -89,6 +97,9 @@ struct RampPlan {
   CompDev* adj_dev = nullptr;
   uint32_t* adj_list = nullptr;      /* indices counted by the loss detector, */
   int64_t adj_cap = 0;               /* then its count (uint64) after them    */
+  RecKey rec;                        /* the launch that filled adj_list       */
+  bool rec_valid = false;
+  uint64_t param_version = 0;        /* bumped when ramp_plan_set_param changes a value */
   uint32_t* surv = nullptr;          /* survivor buffer of split launches */
   int64_t surv_cap = 0;              /* slots (128 per work item) */
   StreamSet streams;
@@ -996,7 +1007,10 @@ int ramp_plan_set_param(RampPlan* p, int32_t kind, int32_t comp, float value) {
       set_err("ramp_plan_set_param: the source has no temperature");
       return RAMP_E_INVALID;
     }
+    if (p->src_in.p[7] == value && p->src_in.p[9] == value && p->src_in.p[11] == value)
+      return RAMP_OK;                      /* unchanged: nothing to do */
     p->src_in.p[7] = p->src_in.p[9] = p->src_in.p[11] = value;
+    p->param_version++;
     return make_src(p, p->src_in, p->src);
   }
   if (comp < 0 || comp >= (int)p->comps_in.size()) {
@@ -1004,31 +1018,30 @@ int ramp_plan_set_param(RampPlan* p, int32_t kind, int32_t comp, float value) {
     return RAMP_E_INVALID;
   }
   RampComp& c = p->comps_in[comp];
+  float* slot = nullptr;
   if (kind >= RAMP_DP_GUIDE_R0 && kind <= RAMP_DP_GUIDE_W) {
     if (c.scat != RAMP_S_GUIDE) { set_err("component %d is not a guide", comp); return RAMP_E_INVALID; }
-    c.sp[5 + (kind - RAMP_DP_GUIDE_R0)] = value;
+    slot = &c.sp[5 + (kind - RAMP_DP_GUIDE_R0)];
   } else if (kind == RAMP_DP_POWDER_SIGMA_ABS) {
     if (c.scat != RAMP_S_POWDERN) { set_err("component %d is not a powder", comp); return RAMP_E_INVALID; }
-    c.sp[0] = value;
+    slot = &c.sp[0];
   } else {
     set_err("ramp_plan_set_param: unknown parameter kind %d", kind);
     return RAMP_E_INVALID;
   }
+  if (memcmp(slot, &value, sizeof(float)) == 0) return RAMP_OK;   /* unchanged */
+  *slot = value;
+  p->param_version++;
   int rc = make_comp(p, c, p->comps[comp]);
   if (rc) return rc;
   CK(cudaMemcpy(p->comps_dev + comp, &p->comps[comp], sizeof(CompDev), cudaMemcpyHostToDevice));
   return RAMP_OK;
 }
 
-int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det_comp,
-                 const float* dL_dH, int64_t n, int32_t num_sim, int32_t seed,
-                 const RampRng* rng, int lr, double* grad, void* stream) {
-  if (!p || !params || n_params <= 0 || n_params > RAMP_MAX_DIFF_PARAMS || !dL_dH || !grad ||
-      n < 0) {
-    set_err("ramp_adjoint: bad arguments");
-    return RAMP_E_INVALID;
-  }
-  if (int rc0 = check_whole_chain(p, "ramp_adjoint")) return rc0;
+/* the adjoint's descriptor copy: derivative slots of params (may be none),
+ * the loss detector marked */
+static int prep_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det_comp,
+                        const float* dL_dH, SrcDev& src, cudaStream_t s) {
   const int nc = (int)p->comps.size();
   if (det_comp < 0 || det_comp >= nc ||
       (p->comps[det_comp].scat != RAMP_S_DET2D && p->comps[det_comp].scat != RAMP_S_DET1D)) {
@@ -1044,7 +1057,7 @@ int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det
   }
   std::vector<CompDev>& A = p->adj_host;
   A = p->comps;
-  SrcDev src = p->src;
+  src = p->src;
   for (int k = 0; k < n_params; ++k) {
     const RampDiffParam& q = params[k];
     if (q.kind == RAMP_DP_SOURCE_T) {
@@ -1065,9 +1078,14 @@ int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det
   }
   A[det_comp].adj_det = 1;
   A[det_comp].dLdH = dL_dH;
-  cudaStream_t s = (cudaStream_t)stream;
   CK(cudaMemcpyAsync(p->adj_dev, A.data(), (size_t)nc * sizeof(CompDev), cudaMemcpyHostToDevice, s));
-  AdjointArgs a;
+  return RAMP_OK;
+}
+
+/* arguments of an adjoint launch over n neutrons, with the index list */
+static int adjoint_args(RampPlan* p, const SrcDev& src, int n_params, int64_t n, int32_t num_sim,
+                        int32_t seed, const RampRng* rng, int lr, double* grad, AdjointArgs& a,
+                        int& grid) {
   memset(&a, 0, sizeof(a));
   a.src = src;
   a.comps = p->adj_dev;
@@ -1097,13 +1115,70 @@ int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det
     }
     p->adj_list = (uint32_t*)d;
     p->adj_cap = n;
+    p->rec_valid = false;
   }
   a.list = p->adj_list;
   a.list_cap = p->adj_cap;
   a.list_count = (unsigned long long*)(((uintptr_t)(p->adj_list + p->adj_cap) + 7) & ~(uintptr_t)7);
   int64_t g = (n + 255) / 256;
   int64_t cap = (int64_t)p->sm_count * 8;
-  CK(launch_adjoint(a, (int)(g < cap ? g : cap), s));
+  grid = (int)(g < cap ? g : cap);
+  return RAMP_OK;
+}
+
+static RecKey rec_key(const RampPlan* p, int det_comp, int64_t n, int32_t num_sim, int32_t seed,
+                      const RampRng* rng) {
+  RecKey k;
+  memset(&k, 0, sizeof(k));
+  k.det = det_comp; k.n = n; k.num_sim = num_sim; k.seed = seed;
+  k.mode = rng ? rng->mode : 0;
+  k.run_seed = rng ? rng->run_seed : 0u;
+  k.tid_base = rng ? rng->tid_base : 0u;
+  k.version = p->param_version;
+  return k;
+}
+
+int ramp_forward_record(RampPlan* p, int32_t det_comp, int64_t n, int32_t num_sim, int32_t seed,
+                        const RampRng* rng, void* stream) {
+  if (!p || n < 0 || (rng && rng->seed_dev)) {
+    set_err("ramp_forward_record: bad arguments (a device seed is not supported)");
+    return RAMP_E_INVALID;
+  }
+  if (int rc0 = check_whole_chain(p, "ramp_forward_record")) return rc0;
+  cudaStream_t s = (cudaStream_t)stream;
+  SrcDev src;
+  int rc = prep_adjoint(p, nullptr, 0, det_comp, nullptr, src, s);
+  if (rc) return rc;
+  AdjointArgs a;
+  int grid;
+  rc = adjoint_args(p, src, 0, n, num_sim, seed, rng, 0, nullptr, a, grid);
+  if (rc) return rc;
+  CK(launch_adjoint(a, grid, 1 | 4, s));
+  p->rec = rec_key(p, det_comp, n, num_sim, seed, rng);
+  p->rec_valid = true;
+  return RAMP_OK;
+}
+
+int ramp_adjoint(RampPlan* p, const RampDiffParam* params, int n_params, int det_comp,
+                 const float* dL_dH, int64_t n, int32_t num_sim, int32_t seed,
+                 const RampRng* rng, int lr, double* grad, void* stream) {
+  if (!p || !params || n_params <= 0 || n_params > RAMP_MAX_DIFF_PARAMS || !dL_dH || !grad ||
+      n < 0) {
+    set_err("ramp_adjoint: bad arguments");
+    return RAMP_E_INVALID;
+  }
+  if (int rc0 = check_whole_chain(p, "ramp_adjoint")) return rc0;
+  cudaStream_t s = (cudaStream_t)stream;
+  SrcDev src;
+  int rc = prep_adjoint(p, params, n_params, det_comp, dL_dH, src, s);
+  if (rc) return rc;
+  AdjointArgs a;
+  int grid;
+  rc = adjoint_args(p, src, n_params, n, num_sim, seed, rng, lr, grad, a, grid);
+  if (rc) return rc;
+  const RecKey k = rec_key(p, det_comp, n, num_sim, seed, rng);
+  const bool reuse = p->rec_valid && !(rng && rng->seed_dev) && memcmp(&k, &p->rec, sizeof(k)) == 0;
+  CK(launch_adjoint(a, grid, reuse ? 2 : (1 | 2), s));
   return RAMP_OK;
 }
 

@@ -36,18 +36,19 @@ DI void adj_trace(const AdjointArgs& a, uint32_t i, D& dx) {
   }
 }
 
-/* pass 1: every neutron, no tallies, the indices the loss detector counts */
-template <int MODE>
+/* pass 1: every neutron, the indices the loss detector counts (with TALLY,
+ * also the forward histograms) */
+template <int MODE, bool TALLY>
 __global__ void __launch_bounds__(256) k_adjoint_record(const AdjointArgs a) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    Recorder dx;
+    RecorderT<TALLY> dx;
     dx.idx = (uint32_t)i;
     dx.done = false;
     dx.list = a.list;
     dx.count = a.list_count;
     dx.cap = a.list_cap;
-    adj_trace<Recorder, MODE>(a, (uint32_t)i, dx);
+    adj_trace<RecorderT<TALLY>, MODE>(a, (uint32_t)i, dx);
   }
 }
 
@@ -64,16 +65,24 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   }
 }
 
-cudaError_t launch_adjoint(const AdjointArgs& a, int grid, cudaStream_t s) {
+/* passes: bit 1 record (bit 4: with tallies), bit 2 replay */
+cudaError_t launch_adjoint(const AdjointArgs& a, int grid, int passes, cudaStream_t s) {
   if (a.n <= 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(a.list_count, 0, sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return e;
-  if (a.rng.mode == 0) {
-    k_adjoint_record<0><<<grid, 256, 0, s>>>(a);
-    k_adjoint<0><<<grid, 256, 0, s>>>(a);
-  } else {
-    k_adjoint_record<1><<<grid, 256, 0, s>>>(a);
-    k_adjoint<1><<<grid, 256, 0, s>>>(a);
+  if (passes & 1) {
+    cudaError_t e = cudaMemsetAsync(a.list_count, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    const bool t = (passes & 4) != 0;
+    if (a.rng.mode == 0) {
+      if (t) k_adjoint_record<0, true><<<grid, 256, 0, s>>>(a);
+      else k_adjoint_record<0, false><<<grid, 256, 0, s>>>(a);
+    } else {
+      if (t) k_adjoint_record<1, true><<<grid, 256, 0, s>>>(a);
+      else k_adjoint_record<1, false><<<grid, 256, 0, s>>>(a);
+    }
+  }
+  if (passes & 2) {
+    if (a.rng.mode == 0) k_adjoint<0><<<grid, 256, 0, s>>>(a);
+    else k_adjoint<1><<<grid, 256, 0, s>>>(a);
   }
   return cudaGetLastError();
 }

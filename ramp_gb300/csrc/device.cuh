@@ -207,7 +207,8 @@ DI void tally_add(float* h, float* he, long long idx, float p) {
 struct NoDiff {
   static constexpr bool on = false;
   static constexpr bool pol = true;   /* the spin lanes are output */
-  static constexpr bool rec = false;
+  static constexpr bool rec = false;  /* record the loss detector's neutrons */
+  static constexpr bool tally = true; /* add to the tallies */
 };
 
 /* Whole-chain kernels output tallies only, and no component turns the spin
@@ -221,10 +222,12 @@ struct TallyOnly : NoDiff {
 /* First pass of the adjoint: trace without tallies and record the index
  * of every neutron the loss detector counts (once per neutron); only those
  * neutrons carry a gradient term, and only they are replayed with AdjDiff. */
-struct Recorder {
+template <bool TALLY>
+struct RecorderT {
   static constexpr bool on = false;
   static constexpr bool pol = false;
   static constexpr bool rec = true;
+  static constexpr bool tally = TALLY;    /* also the forward histogram */
   uint32_t idx;                     /* this neutron's index in the launch */
   bool done;
   uint32_t* list;
@@ -237,11 +240,13 @@ struct Recorder {
     if ((int64_t)k < cap) list[k] = idx;
   }
 };
+using Recorder = RecorderT<false>;
 
 struct AdjDiff {
   static constexpr bool on = true;
   static constexpr bool pol = false;
   static constexpr bool rec = false;
+  static constexpr bool tally = false;
   float dlog[RAMP_MAX_DIFF];
   double* grad;      /* nslot accumulators, global                       */
   int nslot;
@@ -1199,12 +1204,13 @@ DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
     if ((long long)idx < c.tally_len) {
       if constexpr (D::on) {
         if (c.adj_det) dx->tallied(__ldg(c.dLdH + idx), ftz(n.p));
-      } else if constexpr (D::rec) {
-        if (c.adj_det) dx->hit();
       } else {
-        tally_add(c.tally, c.tally_err, idx, n.p);
+        if constexpr (D::rec) {
+          if (c.adj_det) dx->hit();
+        }
+        if constexpr (D::tally) tally_add(c.tally, c.tally_err, idx, n.p);
       }
-    } else if constexpr (!D::on && !D::rec) {
+    } else if constexpr (D::tally) {
       if (n.p != 0.0f) atomicAdd(&st->oob, 1ull);   /* a nonzero weight was lost */
     }
   }
@@ -1250,12 +1256,13 @@ DI void s_det2d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
     if (flat >= 0 && flat < c.tally_len) {
       if constexpr (D::on) {
         if (c.adj_det) dx->tallied(__ldg(c.dLdH + flat), ftz(n.p));
-      } else if constexpr (D::rec) {
-        if (c.adj_det) dx->hit();
       } else {
-        tally_add(c.tally, c.tally_err, flat, n.p);
+        if constexpr (D::rec) {
+          if (c.adj_det) dx->hit();
+        }
+        if constexpr (D::tally) tally_add(c.tally, c.tally_err, flat, n.p);
       }
-    } else if constexpr (!D::on && !D::rec) {
+    } else if constexpr (D::tally) {
       if (n.p != 0.0f) atomicAdd(&st->oob, 1ull);   /* a nonzero weight was lost */
     }
   }
@@ -1288,7 +1295,7 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
     case RAMP_S_DET1D: s_det1d<D>(c, n, s, ii, st, dx); break;
     case RAMP_S_DET2D: s_det2d<D>(c, n, s, ii, st, dx); break;
     case RAMP_S_COUNTER:
-      if (!D::on && !D::rec && c.tally) atomicAdd(c.tally, n.p);
+      if (D::tally && c.tally) atomicAdd(c.tally, n.p);
       n.se = 1.0f; n.wr |= WR_SE;
       s_finish(c, n, s, ii);
       break;

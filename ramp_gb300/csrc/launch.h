@@ -76,7 +76,7 @@ struct AdjointArgs {
   int64_t list_cap;
 };
 
-cudaError_t launch_adjoint(const AdjointArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_adjoint(const AdjointArgs& a, int grid, int passes, cudaStream_t s);
 
 cudaError_t launch_seed_advance(int32_t* seed_dev, cudaStream_t s);
 cudaError_t launch_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out,

@@ -96,16 +96,18 @@ class DiffChain:
 
     def forward(self, n, seed, rng="reference"):
         """The detector histogram (flat, float32, device) of n histories at
-        the current parameters, one chunk with weight 1/n and this seed."""
+        the current parameters, one chunk with weight 1/n and this seed.
+        The run also lists the neutrons the detector counts, which the
+        next ``gradient`` of the same run replays (ramp_forward_record)."""
         lib = self.inst._lib()
         plan = self.inst.plan()
         self.inst.reset_tallies()
         rngd = _abi.RampRng({"reference": 0, "native": 1}[rng], 0, 0, 0, None)
         with torch.cuda.device(self.inst.device):
             stream = self.inst._stream_ptr()
-            _abi.check(lib, lib.ramp_trace_fused(plan, int(n), int(n), int(seed),
-                                                 ctypes.byref(rngd), None, None, None, stream),
-                       "ramp_trace_fused")
+            _abi.check(lib, lib.ramp_forward_record(plan, self.det, int(n), int(n), int(seed),
+                                                    ctypes.byref(rngd), stream),
+                       "ramp_forward_record")
         return self.det_scat.tallies()[0]
 
     def gradient(self, dLdH, n, seed, rng="reference", lr=False):
