@@ -76,3 +76,28 @@ def test_rescal_needs_the_plain_path():
     import pytest
     with pytest.raises(ValueError, match="plain"):
         inst.execute(1000, path="fused")
+
+
+def test_reference_powder_example_peak():
+    """The reference's powder example (its parameters in
+    tests/golden/powder_reference_example.json): PG(002) at the Bragg angle
+    for 3 AA, a d = 3 AA powder line, so the nominal peak is 2theta = 60 deg.
+    The oracle puts the fitted centre at 60.05 deg (sigma 1.07 deg) at 1e7
+    histories; the reference's notebooks record 60.37 deg (sigma 1.02 deg)
+    from an older run that cannot be repeated here."""
+    import oracle
+    from scipy.optimize import curve_fit
+    h, mn, meV = 6.62607015e-34, 1.674929e-27, 1.602176634e-22
+    Ei = 9.09
+    lam = h / np.sqrt(2 * mn * Ei * meV) * 1e10
+    fn = os.path.join(os.path.dirname(__file__), "golden", "powder_reference_example.json")
+    inst = m.Instrument(fn, "cpu", Ei=Ei, Mono_angle=float(np.arcsin(lam / (2 * 3.355))),
+                        detector_binning=[50.0, 0.02, 70.0])
+    random.seed(7)
+    oracle.run(inst, 400_000)
+    det = dict(inst.components())["Detector"]["scat_kernel"].data(None)
+    x = np.asarray(det[0], dtype=float)
+    y = np.asarray(det[1], dtype=float)
+    f = lambda t, c, mu, s: c * np.exp(-(t - mu) ** 2 / (2 * s ** 2))
+    (c, mu, s), _ = curve_fit(f, x, y, p0=[1e9, 60.0, 2.5])
+    assert abs(mu - 60.05) < 0.1 and 0.95 < s < 1.2
