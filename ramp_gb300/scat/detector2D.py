@@ -46,9 +46,7 @@ class SDetector2D(SPrim):
         dev = _device(ctx)
         self.histo_t = torch.zeros(int(self.num_bins), dtype=torch.float32, device=dev)
         self.histo_err_t = torch.zeros(int(self.num_bins), dtype=torch.float32, device=dev)
-        x = np.linspace(self.axis1_binning[0], self.axis1_binning[2], num=int(self.axis1_num_bins))
-        y = np.linspace(self.axis2_binning[0], self.axis2_binning[2], num=int(self.axis2_num_bins))
-        self.X, self.Y = np.meshgrid(x, y)
+        self._XY = None
         self.last_ran_datetime = datetime.datetime.now()
 
     def fill(self, comp, keep):
@@ -66,6 +64,24 @@ class SDetector2D(SPrim):
 
     def tallies(self):
         return [self.histo_t, self.histo_err_t]
+
+    def _grid(self):
+        # bin-coordinate grids, built on first use (two n2 x n1 float64 arrays)
+        if self._XY is None:
+            x = np.linspace(self.axis1_binning[0], self.axis1_binning[2],
+                            num=int(self.axis1_num_bins))
+            y = np.linspace(self.axis2_binning[0], self.axis2_binning[2],
+                            num=int(self.axis2_num_bins))
+            self._XY = np.meshgrid(x, y)
+        return self._XY
+
+    @property
+    def X(self):
+        return self._grid()[0]
+
+    @property
+    def Y(self):
+        return self._grid()[1]
 
     @property
     def histo(self):
