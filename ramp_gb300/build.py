@@ -19,8 +19,12 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libramp_cuda.so")
 
-CU_SOURCES = (["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
-              + ["fused_%d%s%s.cu" % (mb, m, b) for mb in (3, 4) for m in "rn" for b in "sb"])
+CU_SOURCES = ["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
+# fused_inst.cu once per kernel instantiation: (register cap, keying mode,
+# task-list layout, phase, extended kinds); the task-list layout runs the
+# extended kinds whole (phase 0 only)
+FUSED_INSTANCES = [(mb, mode, b, ph, x) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)
+                   for x in (0, 1) for ph in (0, 1, 2) if not (b and x and ph)]
 CPP_SOURCES = ["bvh.cpp"]
 HEADERS = ["device.cuh", "fused_kernel.cuh", "mesh.cuh", "plan.h", "launch.h", "rmath.h", "rconst.h", "bvh.h",
            os.path.join("..", "..", "include", "ramp.h")]
@@ -64,6 +68,14 @@ def build(force=False, verbose=False, extra_nvcc=()):
         objs.append(o)
         if force or _stale(o, [s, __file__] + hdrs):
             jobs.append([nvcc()] + NVCC_FLAGS + list(extra_nvcc) + ["-c", s, "-o", o])
+    fs = os.path.join(CSRC, "fused_inst.cu")
+    # the task-list (batched) kernels take longest to compile: start them first
+    for inst in sorted(FUSED_INSTANCES, key=lambda t: -t[2]):
+        o = os.path.join(OUT, "fused_inst_%d%d%d%d%d.o" % inst)
+        objs.append(o)
+        if force or _stale(o, [fs, __file__] + hdrs):
+            defs = ["-DFK_%s=%d" % kv for kv in zip(("MINB", "MODE", "BATCHED", "PHASE", "EXT"), inst)]
+            jobs.append([nvcc()] + NVCC_FLAGS + list(extra_nvcc) + defs + ["-c", fs, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT, src + ".o")
@@ -72,7 +84,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
             jobs.append(["g++"] + CXX_FLAGS + ["-c", s, "-o", o])
     logs = []
     if jobs:
-        with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 8)) as ex:
             for out in ex.map(_run, jobs):
                 logs.append(out)
     if force or jobs or not os.path.exists(LIB):

@@ -767,7 +767,6 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
   a.ext = p->ext ? 1 : 0;
-  if (a.ext) a.split = 0;
   if (a.split > 0) {
     rc = attach_surv(p, a, (n + 127) / 128, s);
     if (rc) return rc;
@@ -800,7 +799,6 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
   int32_t split = 0;
   int rc0 = tune_split(p, tune, &split);
   if (rc0) return rc0;
-  if (base.ext) split = 0;
   std::vector<int64_t> item_off(nv + 1, 0);
   for (size_t v = 0; v < nv; ++v)
     item_off[v + 1] = item_off[v] + (vars[v].n > 0 ? (vars[v].n + 127) / 128 : 0);
@@ -990,7 +988,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   int rc = tune_split(p, tune, &a.split);
   if (rc) return rc;
   a.ext = ext ? 1 : 0;
-  if (a.ext) a.split = 0;
+  if (a.ext) a.split = 0;   /* the task-list kernel has no split with extended kinds */
   if (a.split > 0) {
     rc = attach_surv(p, a, a.n_tasks * ((task + 127) / 128), s);
     if (rc) return rc;

@@ -1,20 +1,39 @@
 /*
  * fused.cu — dispatch of the fused persistent kernel (fused_kernel.cuh)
- * over its register caps, keying modes and layouts; the instantiations live
- * in fused_{3,4}{r,n}{s,b}.cu.
+ * over its register caps, keying modes, layouts and kind sets, and the
+ * sequencing of a split launch (stage A, then stage B).  The kernels are
+ * instantiated one per translation unit (fused_inst.cu).
  */
 #include "fused_kernel.cuh"
 
-#define EXT(MB, MODE)                                                                       \
-  extern template cudaError_t launch_fk<MB, MODE, false>(const FusedArgs&, int, int,      \
-                                                         cudaStream_t);                   \
-  extern template cudaError_t launch_fk<MB, MODE, true>(const FusedArgs&, int, int,       \
-                                                        cudaStream_t);                    \
+#define PH(MB, MODE, B, PHASE, X)                                                           \
+  extern template cudaError_t launch_phase<MB, MODE, B, PHASE, X>(const FusedArgs&, int, int, \
+                                                                  cudaStream_t);
+#define ONE_MODE(MB, MODE)                                                                  \
+  PH(MB, MODE, false, 0, false) PH(MB, MODE, false, 1, false) PH(MB, MODE, false, 2, false) \
+  PH(MB, MODE, true, 0, false) PH(MB, MODE, true, 1, false) PH(MB, MODE, true, 2, false)    \
+  PH(MB, MODE, false, 0, true) PH(MB, MODE, false, 1, true) PH(MB, MODE, false, 2, true)    \
+  PH(MB, MODE, true, 0, true)                                                               \
   extern template int occ_mm<MB, MODE>(int);
-EXT(3, 0)
-EXT(3, 1)
-EXT(4, 0)
-EXT(4, 1)
+ONE_MODE(3, 0)
+ONE_MODE(3, 1)
+ONE_MODE(4, 0)
+ONE_MODE(4, 1)
+
+/* one register cap, keying mode, layout and kind set: the whole chain, or
+ * stage A then stage B of a split launch (the task-list layout runs the
+ * extended kinds whole) */
+template <int MB, int MODE, bool BATCHED, bool EXT>
+static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream_t s) {
+  if constexpr (!(BATCHED && EXT)) {
+    if (a.split > 0) {
+      const cudaError_t e = launch_phase<MB, MODE, BATCHED, 1, EXT>(a, block, grid, s);
+      if (e != cudaSuccess) return e;
+      return launch_phase<MB, MODE, BATCHED, 2, EXT>(a, block, grid, s);
+    }
+  }
+  return launch_phase<MB, MODE, BATCHED, 0, EXT>(a, block, grid, s);
+}
 
 static int g_fused_minb = 4;
 
@@ -24,8 +43,11 @@ void fused_set_min_blocks(int minb) { g_fused_minb = minb >= 4 ? 4 : 3; }
 
 template <int MB, int MODE>
 static cudaError_t launch_m(const FusedArgs& a, int block, int grid, cudaStream_t s) {
-  return a.variants ? launch_fk<MB, MODE, true>(a, block, grid, s)
-                    : launch_fk<MB, MODE, false>(a, block, grid, s);
+  if (a.ext)
+    return a.variants ? launch_fk<MB, MODE, true, true>(a, block, grid, s)
+                      : launch_fk<MB, MODE, false, true>(a, block, grid, s);
+  return a.variants ? launch_fk<MB, MODE, true, false>(a, block, grid, s)
+                    : launch_fk<MB, MODE, false, false>(a, block, grid, s);
 }
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s) {

@@ -220,21 +220,16 @@ k_fused(const FusedArgs a) {
   }
 }
 
-/* one register cap, keying mode and layout: the whole chain, or stage A
- * then stage B of a split launch */
-template <int MINB, int MODE, bool BATCHED>
-cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream_t s) {
-  if (a.ext) {                   /* extended kinds: whole chain, no split */
-    k_fused<MINB, MODE, BATCHED, 0, true><<<grid, block, 0, s>>>(a);
-  } else if (a.split > 0) {
-    k_fused<MINB, MODE, BATCHED, 1, false><<<grid, block, 0, s>>>(a);
-    k_fused<MINB, MODE, BATCHED, 2, false><<<grid, block, 0, s>>>(a);
-  } else {
-    k_fused<MINB, MODE, BATCHED, 0, false><<<grid, block, 0, s>>>(a);
-  }
+/* one launch of one instantiation; each is compiled in a translation unit
+ * of its own (fused_inst.cu, built once per template argument set) and the
+ * sequencing of phases lives in fused.cu */
+template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
+cudaError_t launch_phase(const FusedArgs& a, int block, int grid, cudaStream_t s) {
+  k_fused<MINB, MODE, BATCHED, PHASE, EXT><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
+/* occupancy of the whole-chain kernel at this register cap (CTAs per SM) */
 template <int MINB, int MODE>
 int occ_mm(int block) {
   static int cached = 0;

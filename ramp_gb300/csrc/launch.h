@@ -49,8 +49,8 @@ struct FusedArgs {
   unsigned long long* workq_b;  /* stage-B work-queue counter (split) */
   int32_t var_key;              /* single variant: its index in the RNG key */
   int32_t ext;                  /* the chain uses an extended kind (MISIS source,
-                                   SMonochromator, SPowder1): the kernel built
-                                   with them; no split */
+                                   SMonochromator, SPowder1): the kernels built
+                                   with them (split only when not BATCHED) */
 };
 #define SURV_WORDS 18           /* 15 record lanes (die is 0), iidx, index, variant */
 

@@ -254,12 +254,16 @@ def test_batched_variants_match_single_runs(cuda_lib, tune):
     ("small_chain.json", "small", 300_000, 2, "native"),
     ("let_like.json", "let", 1_000_000, 2, "reference"),
     ("let_like.json", "let", 1_000_000, 5, "native"),
-    ("mesh_imaging.json", "mesh", 20_000, 1, "reference")])
+    ("mesh_imaging.json", "mesh", 20_000, 1, "reference"),
+    ("let_like_misis.json", "misis", 400_000, 2, "reference"),
+    ("powder_diffractometer.json", "powder", 500_000, 3, "native")])
 def test_fused_split_matches_oracle(cuda_lib, fn, kw, N, split, rng):
     """Compacting survivors into full warps changes only the order in
-    which neutrons are traced."""
+    which neutrons are traced (also with the extended kinds: MISIS source,
+    SMonochromator in stage A, SPowder1 in stage B)."""
     kws = {"small": I.small_chain_kwargs(), "let": I.let_like_kwargs(),
-           "mesh": I.mesh_imaging_kwargs(0.37)}[kw]
+           "mesh": I.mesh_imaging_kwargs(0.37), "misis": I.let_like_misis_kwargs(),
+           "powder": I.powder_diffractometer_kwargs()}[kw]
     gi, ci, r = pair(I.path(fn), kws, N, path="fused", rng=rng, tune={"split": split})
     tallies_close(gi, ci)
     assert gi.oob_drops == r.oob
@@ -299,6 +303,21 @@ def test_batched_split_matches_single_runs(cuda_lib, tune):
     torch.cuda.synchronize()
     for v, (kw, n, seed) in enumerate(zip(variants, counts, [11, 2222, 4000])):
         ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
+        oracle.run(ci, n, rng_mode=1, variant=v, seeds=[seed])
+        tallies_close(B.instruments[v], ci)
+
+
+@pytest.mark.parametrize("tune", [{"split": 2}, {"split": 2, "streams": 1, "chunk": 4096}])
+def test_batched_misis_split_matches_single_runs(cuda_lib, tune):
+    """MISIS variants: split per-variant launches; the task-list launch runs
+    the extended kinds whole."""
+    variants = [I.let_like_misis_kwargs(Ei=3.7), I.let_like_misis_kwargs(Ei=6.0)]
+    counts, seeds = [250_000, 99_999], [5, 3001]
+    B = BatchedInstrument(I.path("let_like_misis.json"), variants, ctx="cuda")
+    B.execute(counts, rng="native", seeds=seeds, tune=tune)
+    torch.cuda.synchronize()
+    for v, (kw, n, seed) in enumerate(zip(variants, counts, seeds)):
+        ci = m.Instrument(I.path("let_like_misis.json"), "cpu", **kw)
         oracle.run(ci, n, rng_mode=1, variant=v, seeds=[seed])
         tallies_close(B.instruments[v], ci)
 
