@@ -193,12 +193,11 @@ def run_batched_config(a):
     total = sum(counts)
     B = BatchedInstrument(fn, kws, ctx=dev)
     if a.tune == "auto":
-        # the autotuner's register cap for the first variant; per-variant
-        # task sizes stay automatic, and no split (its two launches per
-        # variant measured slower on this scan of mostly short variants)
+        # the autotuner's register cap and split point for the first
+        # variant (the variants share the component structure)
         from ramp_gb300 import autotune
         tune = {k: v for k, v in autotune.tune(B.instruments[0], rng="reference").items()
-                if k == "blocks_per_sm"}
+                if k in ("blocks_per_sm", "split")}
     else:
         tune = json.loads(a.tune) if a.tune else None
     for w in range(a.warmup):
@@ -244,13 +243,14 @@ def run_batched_config(a):
             "config": {"workload": name, "variants": len(counts), "histories_per_step": total,
                        "tune": tune,
                        "rng": "reference keying",
-                       "path": "batched fused: one single-instrument launch per variant on "
-                               "16 concurrent streams forked from the caller's stream"},
+                       "path": "batched fused: one launch (two with a split) whose grid "
+                               "row v traces variant v"},
             "plain_path_sequential": {"value": total / (plain_ms / 1000.0), "ms_per_step": plain_ms,
                                       "sample": "first %d variants, scaled by histories" % nplain},
             "batched_over_plain": (total / (statistics.mean(ms) / 1000.0)) / (total / (plain_ms / 1000.0)),
-            "gpu_launches": a.steps * sum(1 for c in counts if c > 0) *
-                            (2 if int((tune or {}).get("split", 0)) > 0 else 1),
+            "gpu_launches": a.steps * (2 if int((tune or {}).get("split", 0)) > 0 else 1) *
+                            (sum(1 for c in counts if c > 0)
+                             if int((tune or {}).get("streams", 0)) > 1 else 1),
             "clocks": clk}
     print(json.dumps(line), flush=True)
 

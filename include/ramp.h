@@ -201,8 +201,9 @@ typedef struct RampTune {
                                    compiled for 256-thread CTAs          */
   int32_t blocks_per_sm;        /* persistent CTAs per SM (register cap:
                                    3 or 4; 0: 4)                         */
-  int32_t chunk;                /* neutrons per task-list entry; sizes the
-                                   grid of a single-instrument launch    */
+  int32_t chunk;                /* neutrons per span; sizes the grid of a
+                                   single-instrument launch (0: about
+                                   eight spans per resident CTA)        */
   int32_t privatize;            /* reserved, 0: tallies are warp-aggregated
                                    atomics into L2; shared-memory copies
                                    do not fit detector histograms of the
@@ -215,12 +216,14 @@ typedef struct RampTune {
                                    launch, owned by the plan) and stage B
                                    traces them 32 to a warp.  Ignored by
                                    ramp_trace_batched_noalloc.           */
-  int32_t streams;              /* ramp_trace_batched: 1 = one launch over
-                                   a task list; otherwise each variant is
-                                   a launch (or, split, two) of its own on
-                                   up to this many concurrent streams
-                                   (0: 16), with its own region of the
-                                   survivor buffer.                      */
+  int32_t streams;              /* ramp_trace_batched: 0 or 1 = one
+                                   launch (or, split, two) whose grid row
+                                   v traces variant v; n >= 2: each
+                                   variant is a launch of its own, on up
+                                   to n concurrent streams (at most 16).
+                                   Either way each variant has its own
+                                   work counters and its own range of
+                                   the survivor buffer.                  */
 } RampTune;
 
 typedef struct RampPlan RampPlan;

@@ -21,8 +21,8 @@ LIB = os.path.join(OUT, "libramp_cuda.so")
 
 CU_SOURCES = ["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
 # fused_inst.cu once per kernel instantiation: (register cap, keying mode,
-# task-list layout, phase, extended kinds); the task-list layout runs the
-# extended kinds whole (phase 0 only)
+# batched one-launch layout, phase, extended kinds); the batched layout runs
+# the extended kinds whole (phase 0 only)
 FUSED_INSTANCES = [(mb, mode, b, ph, x) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)
                    for x in (0, 1) for ph in (0, 1, 2) if not (b and x and ph)]
 CPP_SOURCES = ["bvh.cpp"]
@@ -69,7 +69,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
         if force or _stale(o, [s, __file__] + hdrs):
             jobs.append([nvcc()] + NVCC_FLAGS + list(extra_nvcc) + ["-c", s, "-o", o])
     fs = os.path.join(CSRC, "fused_inst.cu")
-    # the task-list (batched) kernels take longest to compile: start them first
+    # the batched kernels take longest to compile: start them first
     for inst in sorted(FUSED_INSTANCES, key=lambda t: -t[2]):
         o = os.path.join(OUT, "fused_inst_%d%d%d%d%d.o" % inst)
         objs.append(o)

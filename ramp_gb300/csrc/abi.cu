@@ -50,10 +50,7 @@ struct BatchCache {
   size_t comps_cap = 0;
   VariantDev* vars_dev = nullptr;
   size_t vars_cap = 0;
-  TaskDev* tasks_dev = nullptr;
-  size_t tasks_cap = 0;
   std::vector<VariantDev> vars_host;
-  std::vector<TaskDev> tasks_host;
   unsigned long long* counters = nullptr;   /* per-variant work queues */
   size_t counters_cap = 0;
 };
@@ -430,7 +427,6 @@ int ramp_plan_destroy(RampPlan* p) {
   for (void* a : p->allocs) cudaFree(a);
   if (p->batch.comps_dev) cudaFree(p->batch.comps_dev);
   if (p->batch.vars_dev) cudaFree(p->batch.vars_dev);
-  if (p->batch.tasks_dev) cudaFree(p->batch.tasks_dev);
   if (p->surv) cudaFree(p->surv);
   if (p->adj_list) cudaFree(p->adj_list);
   if (p->batch.counters) cudaFree(p->batch.counters);
@@ -559,6 +555,13 @@ int ramp_trace_plain(RampPlan* p, const RampState* st, int64_t n, int32_t num_si
 static int fused_grid(int64_t n_spans, int grid) {
   int64_t need = n_spans < 1 ? 1 : n_spans;
   return (int)(need < grid ? need : grid);
+}
+
+/* CTAs per row of a batched launch: enough for the longest variant to give
+ * every warp one work item (rows of shorter variants leave the rest idle
+ * at once), at most one resident grid */
+static int batched_grid(int64_t n_max, int grid) {
+  return fused_grid((n_max + 8 * 128 - 1) / (8 * 128), grid);
 }
 
 static void tune_defaults(RampPlan* p, const RampTune* tune, int& block, int& grid,
@@ -744,7 +747,6 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   FusedArgs a;
   memset(&a, 0, sizeof(a));
   a.variants = nullptr;
-  a.tasks = nullptr;
   a.task_size = task;
   a.n_tasks = (n + task - 1) / task;
   a.single.src = p->src;
@@ -833,7 +835,6 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
     load[k] += vars[v].n;
     FusedArgs a = base;
     a.variants = nullptr;
-    a.tasks = nullptr;
     a.single = vars[v];
     a.var_key = v;
     a.workq = B.counters + v;
@@ -911,8 +912,10 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     B.comps_host = comps;
   }
   std::vector<VariantDev> vars((size_t)n_variants);
-  std::vector<TaskDev> tasks;
-  const bool use_streams = !(tune && tune->streams == 1);
+  /* default: one launch with a grid row per variant; streams >= 2: one
+     launch per variant over that many concurrent streams */
+  const bool use_streams = tune && tune->streams > 1;
+  int64_t n_max = 0;
   for (int v = 0; v < n_variants; ++v) {
     int rc = make_src(p, variants[v].source, vars[v].src, true, &memo);
     if (rc) return rc;
@@ -920,15 +923,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     vars[v].num_sim = variants[v].num_sim;
     vars[v].seed = variants[v].seed;
     vars[v].comps = B.comps_dev + (size_t)v * nc;
-    if (use_streams) continue;
-    for (int64_t st0 = 0; st0 < variants[v].n; st0 += task) {
-      TaskDev t;
-      t.variant = v;
-      t.start = st0;
-      int64_t rem = variants[v].n - st0;
-      t.count = (int32_t)(rem < task ? rem : task);
-      tasks.push_back(t);
-    }
+    if (vars[v].n > n_max) n_max = vars[v].n;
   }
   bool ext = p->ext;
   for (int v = 0; v < n_variants; ++v) ext = ext || ext_source(variants[v].source);
@@ -945,9 +940,27 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     a.st = p->status;
     return batched_streams(p, a, vars, block, grid, tune, s);
   }
-  if (tasks.empty()) return RAMP_OK;
+  /* one launch: grid row v traces variant v from its own work counter
+     (two with a split), its survivors in its own range of work items */
+  if (n_variants > 65535) {
+    set_err("ramp_trace_batched: %d variants in one launch (at most 65535; use streams)",
+            n_variants);
+    return RAMP_E_RANGE;
+  }
+  if (n_max == 0) return RAMP_OK;
+  int32_t split = 0;
+  int rc = tune_split(p, tune, &split);
+  if (rc) return rc;
+  if (ext) split = 0;   /* the one-launch kernel runs the extended kinds whole */
+  int64_t items = 0;
+  for (int v = 0; v < n_variants; ++v) {
+    vars[v].item_off = items;
+    items += (vars[v].n + 127) / 128;
+  }
   if (B.vars_cap < vars.size()) {
     if (B.vars_dev) cudaFree(B.vars_dev);
+    B.vars_dev = nullptr;
+    B.vars_cap = 0;
     CK(cudaMalloc(&B.vars_dev, vars.size() * sizeof(VariantDev)));
     B.vars_cap = vars.size();
     B.vars_host.clear();
@@ -958,24 +971,17 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
                   cudaMemcpyHostToDevice));
     B.vars_host = vars;
   }
-  if (B.tasks_cap < tasks.size()) {
-    if (B.tasks_dev) cudaFree(B.tasks_dev);
-    CK(cudaMalloc(&B.tasks_dev, tasks.size() * sizeof(TaskDev)));
-    B.tasks_cap = tasks.size();
-    B.tasks_host.clear();
-  }
-  if (B.tasks_host.size() != tasks.size() ||
-      memcmp(B.tasks_host.data(), tasks.data(), tasks.size() * sizeof(TaskDev)) != 0) {
-    CK(cudaMemcpy(B.tasks_dev, tasks.data(), tasks.size() * sizeof(TaskDev),
-                  cudaMemcpyHostToDevice));
-    B.tasks_host = tasks;
+  if (B.counters_cap < 2 * (size_t)n_variants) {
+    if (B.counters) cudaFree(B.counters);
+    B.counters = nullptr;
+    B.counters_cap = 0;
+    CK(cudaMalloc(&B.counters, 2 * (size_t)n_variants * sizeof(unsigned long long)));
+    B.counters_cap = 2 * (size_t)n_variants;
   }
   FusedArgs a;
   memset(&a, 0, sizeof(a));
   a.variants = B.vars_dev;
-  a.tasks = B.tasks_dev;
-  a.n_tasks = (int64_t)tasks.size();
-  a.task_size = task;
+  a.n_variants = n_variants;
   a.blocks = p->blocks_dev;
   a.n_blocks = (int32_t)p->blocks.size();
   a.n_comps = nc;
@@ -983,18 +989,16 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;   /* variants key by their own index */
   a.st = p->status;
-  a.workq = &p->status->workq;
-  a.workq_b = &p->status->workq_b;
-  int rc = tune_split(p, tune, &a.split);
-  if (rc) return rc;
+  a.workq = B.counters;
+  a.workq_b = B.counters + n_variants;
+  a.split = split;
   a.ext = ext ? 1 : 0;
-  if (a.ext) a.split = 0;   /* the task-list kernel has no split with extended kinds */
   if (a.split > 0) {
-    rc = attach_surv(p, a, a.n_tasks * ((task + 127) / 128), s);
+    rc = attach_surv(p, a, items, s);
     if (rc) return rc;
   }
-  CK(cudaMemsetAsync(&p->status->workq, 0, 3 * sizeof(unsigned long long), s));
-  CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
+  CK(cudaMemsetAsync(B.counters, 0, 2 * (size_t)n_variants * sizeof(unsigned long long), s));
+  CK(launch_fused(a, block, batched_grid(n_max, grid), s));
   return RAMP_OK;
 }
 
@@ -1215,14 +1219,14 @@ int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out, void* s
  * memory pool that forbids allocation, or a caller preparing work it will
  * later record into a CUDA graph): it uses only memory that already exists.
  *
- * The per-call scratch of the batched kernel (the device copies of every
- * variant's component descriptors, the variant table, the task list, and
- * the status / work-queue counters) lives in the file-scope array below
- * instead of plan-owned buffers that grow with cudaMalloc.  Its size is
- * fixed: RAMP_NOALLOC_MAX_VARIANTS variants, RAMP_NOALLOC_MAX_DESCS
- * component descriptors in total (variants x components) and
- * RAMP_NOALLOC_MAX_TASKS tasks, about 3.3 MB, held by every GPU on which
- * the library is loaded until the process exits.  Tables (S(q,w), powder
+ * The per-call scratch of the one-launch batched kernel (the device copies
+ * of every variant's component descriptors, the variant table, the status
+ * word and the per-variant work-queue counters) lives in the file-scope
+ * array below instead of plan-owned buffers that grow with cudaMalloc.  Its
+ * size is fixed: RAMP_NOALLOC_MAX_VARIANTS variants and
+ * RAMP_NOALLOC_MAX_DESCS component descriptors in total (variants x
+ * components), about 2.5 MB, held by every GPU on which the library is
+ * loaded until the process exits.  Tables (S(q,w), powder
  * lines, mesh BVHs) must be ones the plan already holds: a variant whose
  * tables differ from every table the plan uploaded is rejected.
  *
@@ -1236,14 +1240,13 @@ int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out, void* s
  * ==================================================================== */
 #define RAMP_NOALLOC_MAX_VARIANTS 256
 #define RAMP_NOALLOC_MAX_DESCS 4096
-#define RAMP_NOALLOC_MAX_TASKS 65536
 
 struct NoallocLayout {
   StatusDev status;
   unsigned char pad[256 - sizeof(StatusDev)];
   VariantDev variants[RAMP_NOALLOC_MAX_VARIANTS];
   CompDev descs[RAMP_NOALLOC_MAX_DESCS];
-  TaskDev tasks[RAMP_NOALLOC_MAX_TASKS];
+  unsigned long long counters[2 * RAMP_NOALLOC_MAX_VARIANTS];   /* per-variant work queues */
 };
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoallocLayout)];
@@ -1347,24 +1350,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   int block, grid;
   int64_t task;
   tune_defaults(p, tune, block, grid, task);
-  {
-    int64_t total = 0;
-    for (int v = 0; v < n_variants; ++v) total += variants[v].n > 0 ? variants[v].n : 0;
-    task = auto_task(total, grid, task);
-  }
-  /* tasks: grow the task size until the list fits the fixed table */
-  int64_t n_tasks = 0;
-  for (;;) {
-    n_tasks = 0;
-    for (int v = 0; v < n_variants; ++v) n_tasks += (variants[v].n + task - 1) / task;
-    if (n_tasks <= RAMP_NOALLOC_MAX_TASKS) break;
-    task *= 2;
-    if (task > (int64_t)1 << 30) {
-      set_err("ramp_trace_batched_noalloc: too many histories for the task table");
-      return RAMP_E_RANGE;
-    }
-  }
-  int64_t t = 0;
+  int64_t n_max = 0;
   HashMemo memo;
   for (int v = 0; v < n_variants; ++v) {
     const RampVariant& V = variants[v];
@@ -1389,28 +1375,21 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
     H.variants[v].num_sim = V.num_sim;
     H.variants[v].seed = V.seed;
     H.variants[v].comps = D->descs + (size_t)v * nc;
-    for (int64_t s0 = 0; s0 < V.n; s0 += task) {
-      H.tasks[t].variant = v;
-      H.tasks[t].start = s0;
-      H.tasks[t].count = (int32_t)((V.n - s0) < task ? (V.n - s0) : task);
-      ++t;
-    }
+    H.variants[v].item_off = 0;
+    if (V.n > n_max) n_max = V.n;
   }
-  if (n_tasks == 0) return RAMP_OK;
+  if (n_max == 0) return RAMP_OK;
   cudaStream_t s = (cudaStream_t)stream;
   CK(cudaMemcpyAsync(D->descs, H.descs, (size_t)n_variants * nc * sizeof(CompDev),
                      cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(D->variants, H.variants, (size_t)n_variants * sizeof(VariantDev),
                      cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(D->tasks, H.tasks, (size_t)n_tasks * sizeof(TaskDev),
-                     cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(&D->status, 0, sizeof(StatusDev), s));
+  CK(cudaMemsetAsync(D->counters, 0, 2 * (size_t)n_variants * sizeof(unsigned long long), s));
   FusedArgs a;
   memset(&a, 0, sizeof(a));
   a.variants = D->variants;
-  a.tasks = D->tasks;
-  a.n_tasks = n_tasks;
-  a.task_size = task;
+  a.n_variants = n_variants;
   a.blocks = p->blocks_dev;
   a.n_blocks = (int32_t)p->blocks.size();
   a.n_comps = nc;
@@ -1418,12 +1397,12 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;
   a.st = &D->status;
-  a.workq = &D->status.workq;
-  a.workq_b = &D->status.workq_b;
+  a.workq = D->counters;
+  a.workq_b = D->counters + n_variants;
   a.ext = p->ext ? 1 : 0;
   for (int v = 0; v < n_variants; ++v)
     if (ext_source(variants[v].source)) a.ext = 1;
   /* no survivor split here: it would need a buffer sized by the call */
-  CK(launch_fused(a, block, fused_grid(n_tasks, grid), s));
+  CK(launch_fused(a, block, batched_grid(n_max, grid), s));
   return RAMP_OK;
 }

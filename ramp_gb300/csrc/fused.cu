@@ -21,8 +21,8 @@ ONE_MODE(4, 0)
 ONE_MODE(4, 1)
 
 /* one register cap, keying mode, layout and kind set: the whole chain, or
- * stage A then stage B of a split launch (the task-list layout runs the
- * extended kinds whole) */
+ * stage A then stage B of a split launch (the batched one-launch layout
+ * runs the extended kinds whole) */
 template <int MB, int MODE, bool BATCHED, bool EXT>
 static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream_t s) {
   if constexpr (!(BATCHED && EXT)) {
@@ -51,7 +51,8 @@ static cudaError_t launch_m(const FusedArgs& a, int block, int grid, cudaStream_
 }
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s) {
-  if (a.n_tasks <= 0) return cudaSuccess;
+  if (a.variants ? a.n_variants <= 0 : a.n_tasks <= 0) return cudaSuccess;
+  if (a.variants && a.n_variants > 65535) return cudaErrorInvalidValue;   /* grid rows */
   if (a.n_blocks > FUSED_MAX_BLOCKS || a.n_comps > RAMP_MAX_COMPS) return cudaErrorInvalidValue;
   if (a.split < 0 || (a.split > 0 && (a.split >= a.n_comps || !a.surv))) return cudaErrorInvalidValue;
   if (g_fused_minb == 4)

@@ -5,9 +5,12 @@
  * takes the next item (128 neutrons of one variant) from a device counter
  * and broadcasts it, so warps never wait on each other (no CTA barrier).
  * Many instrument variants with uneven neutron counts share one launch
- * through an explicit task list (variant, first neutron, count); component
- * descriptors are read through the read-only cache (every lane of a warp
- * reads the same address).  The kernel is instantiated per RNG keying mode
+ * (BATCHED): grid row y traces variant y from its own work counter, so the
+ * variant index is blockIdx.y — uniform by construction, which keeps the
+ * descriptor addresses in uniform registers as in a one-instrument launch
+ * (an index read per warp from a task list made the kernel 5-8x slower).
+ * Component descriptors are read through the read-only cache (every lane
+ * of a warp reads the same address).  The kernel is instantiated per RNG keying mode
  * (fewer live registers) and per register cap (__launch_bounds__ minimum
  * CTAs per SM, chosen by the autotuner).
  *
@@ -47,9 +50,10 @@ k_fused(const FusedArgs a);
 
 /* PHASE 2: the survivors of stage A through components [split, end).
  * Stage A leaves the survivors of work item t at slots [128 t, 128 t +
- * cnt[t]); a warp claims SURV_GROUP items at a time and deals their
- * survivors out 32 to a pass.  A survivor is keyed by its own index and
- * variant, so it continues exactly where stage A left it. */
+ * cnt[t]) (batched: item item_off + t of its variant's row); a warp claims
+ * SURV_GROUP items at a time and deals their survivors out 32 to a pass.
+ * A survivor is keyed by its own index and variant, so it continues
+ * exactly where stage A left it. */
 #define SURV_GROUP 8
 template <int MODE, bool BATCHED, bool EXT>
 DI void fused_tail(const FusedArgs& a) {
@@ -58,13 +62,24 @@ DI void fused_tail(const FusedArgs& a) {
   const bool zx = !carry;
   const int K = a.split;
   const int64_t cap = a.surv_cap;
+  /* this launch's (batched: this row's variant's) work items */
+  const int var = BATCHED ? (int)blockIdx.y : a.var_key;
+  const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
+  const int64_t item0 = BATCHED ? V->item_off : 0;
+  const int64_t n_items = BATCHED ? (V->n + FUSED_WARP_TASK - 1) / FUSED_WARP_TASK : a.surv_items;
+  if (BATCHED && item0 + n_items > a.surv_items) {   /* host sized the buffer for every row */
+    if (lane == 0) raise_flag(a.st, RAMP_F_WORKQ);
+    return;
+  }
+  const CompDev* __restrict__ comps = V->comps;
+  unsigned long long* const q_b = a.workq_b + (BATCHED ? var : 0);
   for (;;) {
     unsigned long long g = 0;
-    if (lane == 0) g = atomicAdd(a.workq_b, 1ull);
+    if (lane == 0) g = atomicAdd(q_b, 1ull);
     g = __shfl_sync(FULL_MASK, g, 0);
     const int64_t t0 = (int64_t)g * SURV_GROUP;
-    if (t0 >= a.surv_items) break;
-    const int c = (lane < SURV_GROUP && t0 + lane < a.surv_items) ? (int)a.surv_cnt[t0 + lane] : 0;
+    if (t0 >= n_items) break;
+    const int c = (lane < SURV_GROUP && t0 + lane < n_items) ? (int)a.surv_cnt[item0 + t0 + lane] : 0;
     int incl = c;
     for (int d = 1; d < SURV_GROUP; d <<= 1) {
       const int y = __shfl_up_sync(FULL_MASK, incl, d);
@@ -81,7 +96,7 @@ DI void fused_tail(const FusedArgs& a) {
         if (ck > 0 && ek <= q) { item = k; base = ek; }
       }
       if (q >= total) continue;
-      const int64_t s = (t0 + item) * FUSED_WARP_TASK + (q - base);
+      const int64_t s = (item0 + t0 + item) * FUSED_WARP_TASK + (q - base);
       const uint32_t* w = a.surv + s;
       Nt n;
       n.x = __uint_as_float(w[0 * cap]);   n.y = __uint_as_float(w[1 * cap]);
@@ -95,10 +110,9 @@ DI void fused_tail(const FusedArgs& a) {
       n.die = 0.0f;
       n.wr = 0u;
       uint32_t ii = w[15 * cap];
-      const uint32_t idx = w[16 * cap], var = w[17 * cap];
+      const uint32_t idx = w[16 * cap];
       Rng r;
-      rng_init(r, MODE, a.rng.tid_base + idx, var, a.rng.run_seed);
-      const CompDev* __restrict__ comps = BATCHED ? a.variants[var].comps : a.single.comps;
+      rng_init(r, MODE, a.rng.tid_base + idx, w[17 * cap], a.rng.run_seed);
       for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
         const RampBlock B = a.blocks[b];
         const int e = B.first + B.count;
@@ -127,33 +141,20 @@ k_fused(const FusedArgs a) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int KE = PHASE == 1 ? a.split : a.n_comps;
+    const int var = BATCHED ? (int)blockIdx.y : a.var_key;
+    const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
+    /* batched: CTAs past what this row's variant can use leave at once */
+    if (BATCHED && (int64_t)blockIdx.x * (blockDim.x / 32) * FUSED_WARP_TASK >= V->n) return;
+    const int64_t item0 = BATCHED ? V->item_off : 0;
+    unsigned long long* const q_a = a.workq + (BATCHED ? var : 0);
     for (;;) {
       unsigned long long t = 0;
-      if (lane == 0) t = atomicAdd(a.workq, 1ull);
+      if (lane == 0) t = atomicAdd(q_a, 1ull);
       t = __shfl_sync(FULL_MASK, t, 0);
-      int var;
-      int64_t start, count;
-      const VariantDev* V;
-      if (BATCHED) {
-        const int64_t spt = (a.task_size + FUSED_WARP_TASK - 1) / FUSED_WARP_TASK;
-        const int64_t jt = (int64_t)(t / (unsigned long long)spt);
-        if (jt >= a.n_tasks) break;
-        const int64_t k = (int64_t)(t % (unsigned long long)spt);
-        const TaskDev T = a.tasks[jt];
-        var = T.variant;
-        start = T.start + k * FUSED_WARP_TASK;
-        count = (int64_t)T.count - k * FUSED_WARP_TASK;
-        if (count <= 0) continue;
-        if (count > FUSED_WARP_TASK) count = FUSED_WARP_TASK;
-        V = a.variants + var;
-      } else {
-        var = a.var_key;
-        start = (int64_t)t * FUSED_WARP_TASK;
-        if (start >= a.single.n) break;
-        count = a.single.n - start;
-        if (count > FUSED_WARP_TASK) count = FUSED_WARP_TASK;
-        V = &a.single;
-      }
+      const int64_t start = (int64_t)t * FUSED_WARP_TASK;
+      if (start >= V->n) break;
+      int64_t count = V->n - start;
+      if (count > FUSED_WARP_TASK) count = FUSED_WARP_TASK;
       const CompDev* __restrict__ comps = V->comps;
       const int32_t num_sim = V->num_sim;
       const int32_t seed = (a.rng.seed_dev && !BATCHED) ? *a.rng.seed_dev : V->seed;
@@ -198,7 +199,7 @@ k_fused(const FusedArgs a) {
         const int rank = kept + __popc(m & lt);
         kept += __popc(m);
         if (!alive) continue;
-        const int64_t s = (int64_t)t * FUSED_WARP_TASK + rank;   /* rank < 128 */
+        const int64_t s = (item0 + (int64_t)t) * FUSED_WARP_TASK + rank;   /* rank < 128 */
         if (s >= a.surv_cap) {          /* cannot happen: one slot per neutron of the item */
           raise_flag(a.st, RAMP_F_WORKQ);
           continue;
@@ -215,7 +216,8 @@ k_fused(const FusedArgs a) {
         w[14 * cap] = __float_as_uint(n.se);
         w[15 * cap] = ii; w[16 * cap] = (uint32_t)i; w[17 * cap] = (uint32_t)var;
       }
-      if (PHASE == 1 && lane == 0 && (int64_t)t < a.surv_items) a.surv_cnt[t] = (uint32_t)kept;
+      if (PHASE == 1 && lane == 0 && item0 + (int64_t)t < a.surv_items)
+        a.surv_cnt[item0 + t] = (uint32_t)kept;
     }
   }
 }
@@ -225,7 +227,8 @@ k_fused(const FusedArgs a) {
  * sequencing of phases lives in fused.cu */
 template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
 cudaError_t launch_phase(const FusedArgs& a, int block, int grid, cudaStream_t s) {
-  k_fused<MINB, MODE, BATCHED, PHASE, EXT><<<grid, block, 0, s>>>(a);
+  const dim3 g((unsigned)grid, BATCHED ? (unsigned)a.n_variants : 1u);
+  k_fused<MINB, MODE, BATCHED, PHASE, EXT><<<g, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 

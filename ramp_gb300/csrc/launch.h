@@ -27,9 +27,9 @@ cudaError_t launch_nonlinear_block(const CompDev* comps_dev, int first, int coun
                                    const PlainArgs& a, cudaStream_t s);
 
 struct FusedArgs {
-  const VariantDev* variants;   /* device; NULL: one variant, "single"  */
-  const TaskDev* tasks;         /* device; NULL: tasks of task_size     */
-  int64_t n_tasks;
+  const VariantDev* variants;   /* device, n_variants entries (one grid row
+                                   each); NULL: one variant, "single"      */
+  int64_t n_tasks;              /* single: spans of task_size (caps the grid) */
   int64_t task_size;
   VariantDev single;
   const RampBlock* blocks;      /* device */
@@ -40,13 +40,14 @@ struct FusedArgs {
   uint32_t* carry_iidx;
   StatusDev* st;
   int32_t split;                /* survivor compaction before this component; 0: off */
-  int32_t pad;
+  int32_t n_variants;           /* rows of a batched grid */
   uint32_t* surv;               /* split: SURV_WORDS x surv_cap survivor records */
   int64_t surv_cap;             /* slots: 128 per work item */
   uint32_t* surv_cnt;           /* survivors per work item */
   int64_t surv_items;
-  unsigned long long* workq;    /* work-queue counter of this launch */
-  unsigned long long* workq_b;  /* stage-B work-queue counter (split) */
+  unsigned long long* workq;    /* work-queue counter of this launch (batched:
+                                   one per variant) */
+  unsigned long long* workq_b;  /* stage-B work-queue counter(s) (split) */
   int32_t var_key;              /* single variant: its index in the RNG key */
   int32_t ext;                  /* the chain uses an extended kind (MISIS source,
                                    SMonochromator, SPowder1): the kernels built

@@ -83,20 +83,13 @@ struct StatusDev {
 #define RAMP_MAX_COMPS 64
 #define RAMP_MAX_DIFF 32   /* differentiable parameters per adjoint launch */
 
-/* one task of the persistent batched kernel: neutrons [start, start+count)
- * of variant v */
-struct TaskDev {
-  int32_t variant;
-  int32_t count;
-  int64_t start;
-};
-
 struct VariantDev {
   SrcDev src;
   int64_t n;
   int32_t num_sim;
   int32_t seed;
   const CompDev* comps;        /* n_comps descriptors in device memory    */
+  int64_t item_off;            /* batched split: first survivor work item */
 };
 
 #endif /* RAMP_PLAN_H */

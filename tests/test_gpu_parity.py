@@ -228,12 +228,13 @@ def test_fused_equals_plain_at_1e7(cuda_lib):
 
 
 # ---------------------------------------------------------------- batching
-@pytest.mark.parametrize("tune", [None, {"streams": 1}, {"streams": 2, "blocks_per_sm": 4}])
+@pytest.mark.parametrize("tune", [None, {"streams": 1, "blocks_per_sm": 3},
+                                  {"streams": 2, "blocks_per_sm": 4}, {"streams": 16}])
 def test_batched_variants_match_single_runs(cuda_lib, tune):
     """Variants with different Ei, slit width and neutron count, traced as
-    concurrent per-variant launches (default), as one launch over a task
-    list (streams 1), or on two streams; each equals its own oracle run
-    with the same seed and keying."""
+    one launch with a grid row per variant (default, streams 1) or as
+    per-variant launches on 2 or 16 streams; each equals its own oracle
+    run with the same seed and keying."""
     variants = [I.let_like_kwargs(Ei=3.7, use_slit=1, slit_w=0.03),
                 I.let_like_kwargs(Ei=8.0, use_slit=1, slit_w=0.015),
                 I.let_like_kwargs(Ei=2.5, use_slit=1, slit_w=0.04)]
@@ -292,10 +293,11 @@ def test_fused_split_with_multi_chunk_carry(cuda_lib):
     tallies_close(gi, ci)
 
 
-@pytest.mark.parametrize("tune", [{"split": 2}, {"split": 2, "streams": 1, "chunk": 4096}])
+@pytest.mark.parametrize("tune", [{"split": 2}, {"split": 2, "streams": 4}])
 def test_batched_split_matches_single_runs(cuda_lib, tune):
-    """Split batched launches: per-variant launches with their own survivor
-    regions, or one task-list launch whose stage B mixes variants."""
+    """Split batched launches: per-variant launches, or one launch with a
+    grid row per variant; either way each variant has its own survivor
+    range and stage-B counter."""
     variants = [I.let_like_kwargs(Ei=3.7), I.let_like_kwargs(Ei=8.0), I.let_like_kwargs(Ei=2.5)]
     counts = [300_000, 123_457, 200_003]
     B = BatchedInstrument(I.path("let_like.json"), variants, ctx="cuda")
@@ -307,10 +309,10 @@ def test_batched_split_matches_single_runs(cuda_lib, tune):
         tallies_close(B.instruments[v], ci)
 
 
-@pytest.mark.parametrize("tune", [{"split": 2}, {"split": 2, "streams": 1, "chunk": 4096}])
+@pytest.mark.parametrize("tune", [{"split": 2}, {"split": 2, "streams": 4}])
 def test_batched_misis_split_matches_single_runs(cuda_lib, tune):
-    """MISIS variants: split per-variant launches; the task-list launch runs
-    the extended kinds whole."""
+    """MISIS variants: the one-launch layout runs the extended kinds
+    whole; per-variant launches split them."""
     variants = [I.let_like_misis_kwargs(Ei=3.7), I.let_like_misis_kwargs(Ei=6.0)]
     counts, seeds = [250_000, 99_999], [5, 3001]
     B = BatchedInstrument(I.path("let_like_misis.json"), variants, ctx="cuda")
