@@ -309,6 +309,22 @@ def test_batched_split_matches_single_runs(cuda_lib, tune):
         tallies_close(B.instruments[v], ci)
 
 
+@pytest.mark.parametrize("tune", [None, {"split": 2}, {"streams": 4}])
+def test_batched_empty_and_ragged_variants(cuda_lib, tune):
+    """Variants of 0, 1, 37 and 200,003 histories in one call: the empty
+    one tallies nothing, the others equal their own oracle runs."""
+    variants = [I.let_like_kwargs(Ei=e) for e in (3.7, 5.0, 2.5, 3.7)]
+    counts, seeds = [0, 1, 37, 200_003], [9, 10, 11, 12]
+    B = BatchedInstrument(I.path("let_like.json"), variants, ctx="cuda")
+    B.execute(counts, rng="native", seeds=seeds, tune=tune)
+    torch.cuda.synchronize()
+    assert all(float(t.abs().sum()) == 0.0 for t in B.instruments[0].tallies())
+    for v in range(1, 4):
+        ci = m.Instrument(I.path("let_like.json"), "cpu", **variants[v])
+        oracle.run(ci, counts[v], rng_mode=1, variant=v, seeds=[seeds[v]])
+        tallies_close(B.instruments[v], ci)
+
+
 @pytest.mark.parametrize("tune", [{"split": 2}, {"split": 2, "streams": 4}])
 def test_batched_misis_split_matches_single_runs(cuda_lib, tune):
     """MISIS variants: the one-launch layout runs the extended kinds
