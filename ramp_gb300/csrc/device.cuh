@@ -677,62 +677,87 @@ DI void guide_dlogR(const CompDev& c, float q, float R, D* dx) {
   for (int k = 0; k < 5; ++k) dx->add(c.dslot[k], dR[k] / R);
 }
 
+/* One pass of the bounce loop of guide.cl:49-135 (the loop body with its
+ * condition): i is the loop variable (reset to 0 and set to the wall hit,
+ * then incremented, each pass, as in the reference), guard the hard cap.
+ * Returns 1 after a bounce (loop again), 0 when the loop is over (exit
+ * plane reached, cap reached or i >= max_bounces; s_guide_end follows) and
+ * -1 when the neutron was retired at zero weight (nothing follows). */
+template <class D = NoDiff>
+DI int guide_pass(const CompDev& c, Nt& n, uint32_t& i, int& guard, StatusDev* st, D* dx,
+                  const bool zx) {
+  const float l = c.sp[4], R0 = c.sp[5];
+  const uint32_t max_bounces = (uint32_t)c.si[0];
+  const float ww = c.aux[0], hh = c.aux[1], Av = c.aux[2], Ah = c.aux[3];
+  if (!(i < max_bounces)) return 0;
+  if (++guard > RC_GUIDE_HARD_CAP) {
+    set_die(n, 1.0f);
+    raise_flag(st, RAMP_F_GUIDE_CAP);
+    return 0;
+  }
+  float av = l * n.vx, bv = ww * n.vz, ah = l * n.vy, bh = hh * n.vz;
+  float vdotn_v1 = bv + av, vdotn_v2 = bv - av, vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
+  float cv1 = Av - n.z * ww, cv2 = n.x * l;
+  float ch1 = Ah - n.z * hh, ch2 = n.y * l;
+  float t1 = (l - n.z) / n.vz, t2;
+  i = 0;
+  if (vdotn_v1 < 0.0f && (t2 = (cv1 - cv2) / vdotn_v1) < t1) { t1 = t2; i = 1; }
+  if (vdotn_v2 < 0.0f && (t2 = (cv1 + cv2) / vdotn_v2) < t1) { t1 = t2; i = 2; }
+  if (vdotn_h1 < 0.0f && (t2 = (ch1 - ch2) / vdotn_h1) < t1) { t1 = t2; i = 3; }
+  if (vdotn_h2 < 0.0f && (t2 = (ch1 + ch2) / vdotn_h2) < t1) { t1 = t2; i = 4; }
+  if (i == 0) return 0;
+  n.x = n.x + t1 * n.vx; n.y = n.y + t1 * n.vy; n.z = n.z + t1 * n.vz;
+  n.t += t1;
+  const bool vert = (i <= 2);
+  const float wv = vert ? ww : hh;
+  const float nlen2 = vert ? c.aux[4] : c.aux[6];
+  const float snlen = vert ? c.aux[5] : c.aux[7];
+  const float vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1 : vdotn_h2;
+  const float q = RC_V2K * (-2.0f) * vdn / snlen;
+  const float d = 2.0f * vdn / nlen2;
+  if (i == 1) n.vx = n.vx - d * l;
+  else if (i == 2) n.vx = n.vx + d * l;
+  else if (i == 3) n.vy = n.vy - d * l;
+  else n.vy = n.vy + d * l;
+  n.vz = n.vz - d * wv;
+  float refl = reflectivity_pre(q, c.aux, R0);
+  n.p *= refl;
+  if (refl < 1e-12f || refl > 1.0f) n.p = 0.0f;
+  if (zx && n.p == 0.0f) {   /* retire: it can only add zeros from here */
+    set_die(n, 1.0f);
+    return -1;
+  }
+  if constexpr (D::on) {
+    if (n.p != 0.0f) guide_dlogR(c, q, refl, dx);
+  }
+  i++;
+  return 1;
+}
+
+/* guide.cl:36-37: move to the entrance plane */
+DI void s_guide_begin(Nt& n, const Is& s) {
+  set_pos(n, ip2(s));
+  n.t += s.t2;
+}
+
+/* after the bounce loop (guide.cl:137-148) */
+DI void s_guide_end(const CompDev& c, Nt& n, Is& s, uint32_t& ii, uint32_t i) {
+  if (i >= (uint32_t)c.si[0]) set_die(n, 1.0f);
+  s_finish(c, n, s, ii);
+}
+
 /* guide.cl:9-149 */
 template <class D = NoDiff>
 DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* dx = nullptr,
                 const bool zx = false) {
-  const float l = c.sp[4], R0 = c.sp[5];
-  const uint32_t max_bounces = (uint32_t)c.si[0];
-  const float ww = c.aux[0], hh = c.aux[1], Av = c.aux[2], Ah = c.aux[3];
-  set_pos(n, ip2(s));
-  n.t += s.t2;
+  s_guide_begin(n, s);
   uint32_t i = 0;
   int guard = 0;
-  while (i < max_bounces) {
-    if (++guard > RC_GUIDE_HARD_CAP) {
-      set_die(n, 1.0f);
-      raise_flag(st, RAMP_F_GUIDE_CAP);
-      break;
-    }
-    float av = l * n.vx, bv = ww * n.vz, ah = l * n.vy, bh = hh * n.vz;
-    float vdotn_v1 = bv + av, vdotn_v2 = bv - av, vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
-    float cv1 = Av - n.z * ww, cv2 = n.x * l;
-    float ch1 = Ah - n.z * hh, ch2 = n.y * l;
-    float t1 = (l - n.z) / n.vz, t2;
-    i = 0;
-    if (vdotn_v1 < 0.0f && (t2 = (cv1 - cv2) / vdotn_v1) < t1) { t1 = t2; i = 1; }
-    if (vdotn_v2 < 0.0f && (t2 = (cv1 + cv2) / vdotn_v2) < t1) { t1 = t2; i = 2; }
-    if (vdotn_h1 < 0.0f && (t2 = (ch1 - ch2) / vdotn_h1) < t1) { t1 = t2; i = 3; }
-    if (vdotn_h2 < 0.0f && (t2 = (ch1 + ch2) / vdotn_h2) < t1) { t1 = t2; i = 4; }
-    if (i == 0) break;
-    n.x = n.x + t1 * n.vx; n.y = n.y + t1 * n.vy; n.z = n.z + t1 * n.vz;
-    n.t += t1;
-    const bool vert = (i <= 2);
-    const float wv = vert ? ww : hh;
-    const float nlen2 = vert ? c.aux[4] : c.aux[6];
-    const float snlen = vert ? c.aux[5] : c.aux[7];
-    const float vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1 : vdotn_h2;
-    const float q = RC_V2K * (-2.0f) * vdn / snlen;
-    const float d = 2.0f * vdn / nlen2;
-    if (i == 1) n.vx = n.vx - d * l;
-    else if (i == 2) n.vx = n.vx + d * l;
-    else if (i == 3) n.vy = n.vy - d * l;
-    else n.vy = n.vy + d * l;
-    n.vz = n.vz - d * wv;
-    float refl = reflectivity_pre(q, c.aux, R0);
-    n.p *= refl;
-    if (refl < 1e-12f || refl > 1.0f) n.p = 0.0f;
-    if (zx && n.p == 0.0f) {   /* retire: it can only add zeros from here */
-      set_die(n, 1.0f);
-      return;
-    }
-    if constexpr (D::on) {
-      if (n.p != 0.0f) guide_dlogR(c, q, refl, dx);
-    }
-    i++;
+  int k;
+  while ((k = guide_pass<D>(c, n, i, guard, st, dx, zx)) > 0) {
   }
-  if (i >= max_bounces) set_die(n, 1.0f);
-  s_finish(c, n, s, ii);
+  if (k < 0) return;
+  s_guide_end(c, n, s, ii, i);
 }
 
 /* chopper.cl:4-59 */
