@@ -401,8 +401,10 @@ DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t 
     n.py = sp * st;
     n.pz = cp;
   } else {
-    draw(n, r);
-    draw(n, r);
+    /* the spin's two draws only advance the counter: their values are
+       unused, and a native-mode block is recomputed from its index */
+    n.sb += 1.0f;
+    n.sb += 1.0f;
   }
   n.t = t0;
   n.die = 0.0f;
