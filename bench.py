@@ -42,6 +42,11 @@ sys.path.insert(0, HERE)
 N_HIST = 100_000_000
 THREEFRY_OPS = 148          # integer operations per Threefry-4x32-20 draw
 CPU_SAMPLE = 2_000_000      # histories per CPU-baseline step
+# DRAM bytes (read + write) of one split launch (stage A + stage B, split
+# before chopper 2) per 1e7 histories, from the ncu capture summarised in
+# profiles/let_like_fused_split_1e7.md (49 + 83 MB and 121 + 5 MB); the
+# traffic grows with the histories traced
+FUSED_SPLIT2_DRAM_PER_1E7 = (48.59 + 82.98 + 121.37 + 5.09) * 1e6
 
 
 def args_():
@@ -552,7 +557,12 @@ def main():
         "let_like_misis": misis,
         "fused_over_plain": value / plain_value,
         "roofline": {"bound": "issue", "achieved": achieved_ops / 1e9, "peak": peak_ops / 1e9,
-                     "unit": "Gop/s", "frac": achieved_ops / peak_ops, "traffic": None,
+                     "unit": "Gop/s", "frac": achieved_ops / peak_ops,
+                     "traffic": (FUSED_SPLIT2_DRAM_PER_1E7 * plain.last_chunk / 1e7
+                                 if int((tune or {}).get("split", 0)) == 2 else None),
+                     "traffic_unit": "bytes per launch (stage A + B)",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "1e7-history split launch, scaled by histories",
                      "kernel": "k_fused", "kernel_ms": kern_ms, "draws_per_launch": draws,
                      "ops_per_draw": THREEFRY_OPS,
                      "peak_source": "measured: Threefry-only kernel (ramp_debug_rng_peak), "
