@@ -380,10 +380,11 @@ int ramp_forward_record(RampPlan* plan, int32_t det_comp, int64_t n, int32_t num
 /* ramp_trace_batched without device allocation.  No counterpart in the
  * reference.  For callers that may not allocate device memory while
  * tracing (a fixed memory budget, an external pool that forbids
- * allocation): the descriptor, variant and task tables and the status and
- * work counters of the batched kernel live in one fixed file-scope device
- * array (at most 256 variants, 4096 component descriptors and 65536 tasks,
- * about 3.3 MB per GPU, held until exit) instead of plan-owned buffers.
+ * allocation): the descriptor and variant tables and the status word and
+ * per-variant work counters of the one-launch batched kernel (a grid row
+ * per variant, no split) live in one fixed file-scope device array (at
+ * most 256 variants and 4096 component descriptors, about 2.5 MB per GPU,
+ * held until exit) instead of plan-owned buffers.
  * Every variant's tables must already be held by the plan.  The first call
  * on a device resolves the array's address; make it before any stream
  * capture.  Calls share the array, so calls whose kernels overlap on the

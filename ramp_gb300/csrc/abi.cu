@@ -1253,7 +1253,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoallocL
 
 #define RAMP_NOALLOC_MAX_DEVICES 64
 static NoallocLayout* g_noalloc_dev[RAMP_NOALLOC_MAX_DEVICES];
-/* host staging of the descriptor, variant and task tables (pageable copies
+/* host staging of the descriptor and variant tables (pageable copies
  * complete before cudaMemcpyAsync returns, so one buffer serves all calls) */
 static NoallocLayout g_noalloc_host;
 static std::mutex g_noalloc_mutex;
