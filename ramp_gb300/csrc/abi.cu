@@ -565,13 +565,14 @@ static int batched_grid(int64_t n_max, int grid) {
 }
 
 static void tune_defaults(RampPlan* p, const RampTune* tune, int& block, int& grid,
-                          int64_t& task) {
+                          int64_t& task, int32_t& minb) {
   block = 256;   /* the fused kernel is compiled for 256-thread CTAs */
-  /* default register cap: 4 CTAs per SM, the fastest measured on GB300 for
-     every chain tried (single, split, batched) */
-  fused_set_min_blocks((tune && tune->blocks_per_sm > 0) ? tune->blocks_per_sm : 4);
+  /* register cap (minimum CTAs per SM the kernel is compiled for): 4 by
+     default, the fastest measured on GB300 for every chain tried (single,
+     split, batched); 3 on request */
+  minb = (tune && tune->blocks_per_sm > 0 && tune->blocks_per_sm < 4) ? 3 : 4;
   int bps = (tune && tune->blocks_per_sm > 0) ? tune->blocks_per_sm
-                                              : fused_max_blocks_per_sm(block, (int)p->comps.size());
+                                              : fused_max_blocks_per_sm(block, minb);
   grid = p->sm_count * bps;
   task = (tune && tune->chunk > 0) ? tune->chunk : 0;   /* 0: auto_task() */
 }
@@ -742,10 +743,12 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   cudaStream_t s = (cudaStream_t)stream;
   int block, grid;
   int64_t task;
-  tune_defaults(p, tune, block, grid, task);
+  int32_t minb;
+  tune_defaults(p, tune, block, grid, task, minb);
   task = auto_task(n, grid, task);
   FusedArgs a;
   memset(&a, 0, sizeof(a));
+  a.minb = minb;
   a.variants = nullptr;
   a.task_size = task;
   a.n_tasks = (n + task - 1) / task;
@@ -873,7 +876,8 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   cudaStream_t s = (cudaStream_t)stream;
   int block, grid;
   int64_t task;
-  tune_defaults(p, tune, block, grid, task);
+  int32_t minb;
+  tune_defaults(p, tune, block, grid, task, minb);
   {
     int64_t total = 0;
     for (int v = 0; v < n_variants; ++v) total += variants[v].n > 0 ? variants[v].n : 0;
@@ -930,6 +934,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   if (use_streams) {
     FusedArgs a;
     memset(&a, 0, sizeof(a));
+    a.minb = minb;
     a.ext = ext ? 1 : 0;
     a.blocks = p->blocks_dev;
     a.n_blocks = (int32_t)p->blocks.size();
@@ -980,6 +985,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   }
   FusedArgs a;
   memset(&a, 0, sizeof(a));
+  a.minb = minb;
   a.variants = B.vars_dev;
   a.n_variants = n_variants;
   a.blocks = p->blocks_dev;
@@ -1349,7 +1355,8 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   NoallocLayout& H = g_noalloc_host;
   int block, grid;
   int64_t task;
-  tune_defaults(p, tune, block, grid, task);
+  int32_t minb;
+  tune_defaults(p, tune, block, grid, task, minb);
   int64_t n_max = 0;
   HashMemo memo;
   for (int v = 0; v < n_variants; ++v) {
@@ -1388,6 +1395,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   CK(cudaMemsetAsync(D->counters, 0, 2 * (size_t)n_variants * sizeof(unsigned long long), s));
   FusedArgs a;
   memset(&a, 0, sizeof(a));
+  a.minb = minb;
   a.variants = D->variants;
   a.n_variants = n_variants;
   a.blocks = p->blocks_dev;

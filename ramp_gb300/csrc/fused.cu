@@ -35,12 +35,6 @@ static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream
   return launch_phase<MB, MODE, BATCHED, 0, EXT>(a, block, grid, s);
 }
 
-static int g_fused_minb = 4;
-
-/* register cap: 3 or 4 CTAs of 256 threads per SM (at 2 the kernel is
- * never faster on GB300) */
-void fused_set_min_blocks(int minb) { g_fused_minb = minb >= 4 ? 4 : 3; }
-
 template <int MB, int MODE>
 static cudaError_t launch_m(const FusedArgs& a, int block, int grid, cudaStream_t s) {
   if (a.ext)
@@ -55,12 +49,13 @@ cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s
   if (a.variants && a.n_variants > 65535) return cudaErrorInvalidValue;   /* grid rows */
   if (a.n_blocks > FUSED_MAX_BLOCKS || a.n_comps > RAMP_MAX_COMPS) return cudaErrorInvalidValue;
   if (a.split < 0 || (a.split > 0 && (a.split >= a.n_comps || !a.surv))) return cudaErrorInvalidValue;
-  if (g_fused_minb == 4)
+  /* register cap: 3 or 4 CTAs of 256 threads per SM (at 2 the kernel is
+     never faster on GB300) */
+  if (a.minb != 3)
     return a.rng.mode == 0 ? launch_m<4, 0>(a, block, grid, s) : launch_m<4, 1>(a, block, grid, s);
   return a.rng.mode == 0 ? launch_m<3, 0>(a, block, grid, s) : launch_m<3, 1>(a, block, grid, s);
 }
 
-int fused_max_blocks_per_sm(int block, int n_comps) {
-  (void)n_comps;
-  return g_fused_minb == 4 ? occ_mm<4, 0>(block) : occ_mm<3, 0>(block);
+int fused_max_blocks_per_sm(int block, int minb) {
+  return minb != 3 ? occ_mm<4, 0>(block) : occ_mm<3, 0>(block);
 }

@@ -49,6 +49,7 @@ struct FusedArgs {
                                    one per variant) */
   unsigned long long* workq_b;  /* stage-B work-queue counter(s) (split) */
   int32_t var_key;              /* single variant: its index in the RNG key */
+  int32_t minb;                 /* register cap: the build for 3 or 4 CTAs per SM */
   int32_t ext;                  /* the chain uses an extended kind (MISIS source,
                                    SMonochromator, SPowder1): the kernels built
                                    with them (split only when not BATCHED) */
@@ -56,8 +57,7 @@ struct FusedArgs {
 #define SURV_WORDS 18           /* 15 record lanes (die is 0), iidx, index, variant */
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s);
-int fused_max_blocks_per_sm(int block, int n_comps);
-void fused_set_min_blocks(int minb);
+int fused_max_blocks_per_sm(int block, int minb);
 
 struct AdjointArgs {
   SrcDev src;
