@@ -2,7 +2,8 @@
  * bvh.cpp — host construction of the bounding volume hierarchy used by the
  * GMesh kernel (binned surface-area heuristic, 16 bins per axis, leaves of
  * at most 4 triangles, depth capped so a 64-entry traversal stack always
- * suffices).  Output layout is described in mesh.cuh.
+ * suffices), stored with each inner node holding its children's boxes.
+ * Output layout is described in mesh.cuh.
  */
 #include <algorithm>
 #include <cmath>
@@ -141,7 +142,44 @@ int ramp_bvh_build(const float* pts, int64_t n_tri, std::vector<float>& nodes,
   }
   int root = B.new_node();
   B.build(root, 0, (int)n_tri, 0);
-  nodes.swap(B.nodes);
+  /* store each inner node as its two children's boxes and references, so
+     one 64-byte read tests both children: per child (lo.xyz, a),
+     (hi.xyz, b) with b >= 1 a leaf of b triangles from a, b == 0 the inner
+     node a, b == -1 no child (only beside a root that is a leaf) */
+  const std::vector<float>& bn = B.nodes;
+  const size_t n_old = bn.size() / 8;
+  std::vector<int> newid(n_old, -1);
+  int n_inner = 0;
+  for (size_t i = 0; i < n_old; ++i) {
+    int wb;
+    std::memcpy(&wb, &bn[8 * i + 7], 4);
+    if (wb >= 0) newid[i] = n_inner++;
+  }
+  auto child = [&](float* o, size_t c) {
+    int wa, wb;
+    std::memcpy(&wa, &bn[8 * c + 3], 4);
+    std::memcpy(&wb, &bn[8 * c + 7], 4);
+    for (int k = 0; k < 3; ++k) { o[k] = bn[8 * c + k]; o[4 + k] = bn[8 * c + 4 + k]; }
+    const int a = wb >= 0 ? newid[c] : wa, b = wb >= 0 ? 0 : -wb;
+    std::memcpy(&o[3], &a, 4);
+    std::memcpy(&o[7], &b, 4);
+  };
+  nodes.assign(16 * (size_t)std::max(n_inner, 1), 0.0f);
+  if (n_inner == 0) {            /* the root is a leaf: one node, one child */
+    child(&nodes[0], 0);
+    const int none = -1;
+    std::memcpy(&nodes[15], &none, 4);
+  } else {
+    for (size_t i = 0; i < n_old; ++i) {
+      if (newid[i] < 0) continue;
+      int wa, wb;
+      std::memcpy(&wa, &bn[8 * i + 3], 4);
+      std::memcpy(&wb, &bn[8 * i + 7], 4);
+      float* o = &nodes[16 * (size_t)newid[i]];
+      child(o, (size_t)wa);
+      child(o + 8, (size_t)wb);
+    }
+  }
   tris.assign(12 * (size_t)n_tri, 0.0f);
   for (int64_t i = 0; i < n_tri; ++i) {
     const float* p = pts + 9 * (size_t)B.order[i];

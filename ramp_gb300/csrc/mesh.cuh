@@ -17,8 +17,11 @@
  * double: exact for the few dozen crossings of one ray, so independent of
  * the visiting order; clamped at 0.
  *
- * Node layout: 2 float4 per node, (min.xyz, a) (max.xyz, b); b >= 0: inner
- * node with children a and b; b < 0: leaf with triangles [a, a - b).
+ * Node layout: each inner node is 4 float4, its two children's boxes and
+ * references, per child (min.xyz, a) (max.xyz, b): b >= 1 a leaf with
+ * triangles [a, a + b), b == 0 the inner node a, b == -1 no child; node 0
+ * is the root.  One 64-byte read tests both children; leaves are tested at
+ * once, and the traversal continues into the nearer inner child.
  * Triangle layout: 3 float4, the vertices v0, v1, v2; edges are formed as
  * the reference forms them (v1 - v0, v2 - v0 in float).
  */
@@ -87,25 +90,34 @@ DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
   const float4* __restrict__ tris = c.bvh_tris;
   int stack[RAMP_BVH_STACK];
   int sp = 0;
-  stack[sp++] = 0;
-  while (sp > 0) {
-    int ni = stack[--sp];
-    float4 a = __ldg(nodes + 2 * ni), b = __ldg(nodes + 2 * ni + 1);
-    float tx0 = (a.x - pos.x) * ix, tx1 = (b.x - pos.x) * ix;
-    float ty0 = (a.y - pos.y) * iy, ty1 = (b.y - pos.y) * iy;
-    float tz0 = (a.z - pos.z) * iz, tz1 = (b.z - pos.z) * iz;
-    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-    if (tn > tf || tf < -1e-6f) continue;
-    if (!need_all && tn > fmaxf(o3, o7)) continue;
-    int wa = __float_as_int(a.w), wb = __float_as_int(b.w);
-    if (wb >= 0) {
-      if (sp + 2 > RAMP_BVH_STACK) { raise_flag(st, RAMP_F_BVH_STACK); return false; }
-      stack[sp++] = wa;
-      stack[sp++] = wb;
-      continue;
+  int node = 0;
+  for (;;) {
+    const float4* q = nodes + 4 * node;
+    const float4 a0 = __ldg(q), b0 = __ldg(q + 1), a1 = __ldg(q + 2), b1 = __ldg(q + 3);
+    const int r0 = __float_as_int(a0.w), c0 = __float_as_int(b0.w);
+    const int r1 = __float_as_int(a1.w), c1 = __float_as_int(b1.w);
+    float tn0 = 0.0f, tn1 = 0.0f;
+    bool h0 = false, h1 = false;
+    if (c0 >= 0) {
+      float tx0 = (a0.x - pos.x) * ix, tx1 = (b0.x - pos.x) * ix;
+      float ty0 = (a0.y - pos.y) * iy, ty1 = (b0.y - pos.y) * iy;
+      float tz0 = (a0.z - pos.z) * iz, tz1 = (b0.z - pos.z) * iz;
+      tn0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+      float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+      h0 = !(tn0 > tf || tf < -1e-6f) && (need_all || !(tn0 > fmaxf(o3, o7)));
     }
-    for (int k = wa; k < wa - wb; ++k) {
+    if (c1 >= 0) {
+      float tx0 = (a1.x - pos.x) * ix, tx1 = (b1.x - pos.x) * ix;
+      float ty0 = (a1.y - pos.y) * iy, ty1 = (b1.y - pos.y) * iy;
+      float tz0 = (a1.z - pos.z) * iz, tz1 = (b1.z - pos.z) * iz;
+      tn1 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+      float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+      h1 = !(tn1 > tf || tf < -1e-6f) && (need_all || !(tn1 > fmaxf(o3, o7)));
+    }
+    /* the triangles of the leaf children that were hit, as one range */
+    const int n0 = (h0 && c0 > 0) ? c0 : 0, n1 = (h1 && c1 > 0) ? c1 : 0;
+    for (int j = 0; j < n0 + n1; ++j) {
+      const int k = j < n0 ? r0 + j : r1 + (j - n0);
       float4 q0 = __ldg(tris + 3 * k), q1 = __ldg(tris + 3 * k + 1), q2 = __ldg(tris + 3 * k + 2);
       V3 v0 = v3(q0.x, q0.y, q0.z), v1 = v3(q1.x, q1.y, q1.z), v2 = v3(q2.x, q2.y, q2.z);
       V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
@@ -137,6 +149,21 @@ DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
       if ((t > eps) && (t < o7) && (nv > 0)) {
         o4 = pos.x + vel.x * t; o5 = pos.y + vel.y * t; o6 = pos.z + vel.z * t; o7 = t;
       }
+    }
+    /* inner children: continue into the nearer, keep the other */
+    const bool i0 = h0 && c0 == 0, i1 = h1 && c1 == 0;
+    if (i0 && i1) {
+      if (sp + 1 > RAMP_BVH_STACK) { raise_flag(st, RAMP_F_BVH_STACK); return false; }
+      const bool first0 = !(tn1 < tn0);
+      stack[sp++] = first0 ? r1 : r0;
+      node = first0 ? r0 : r1;
+    } else if (i0) {
+      node = r0;
+    } else if (i1) {
+      node = r1;
+    } else {
+      if (sp == 0) break;
+      node = stack[--sp];
     }
   }
   if ((c.gi[0] == 1) && (num_intersections % 2 == 1)) {
