@@ -58,6 +58,8 @@ def args_():
     p.add_argument("--n", type=int, default=N_HIST)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--variants", type=int, default=0,
+                   help="configs 3 and 5: trace only the first N variants (0: all)")
     p.add_argument("--tune", default="auto",
                    help='fused launch config: "auto" (autotuner) or JSON, e.g. {"blocks_per_sm": 3}')
     p.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
@@ -195,6 +197,8 @@ def run_batched_config(a):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     fn, kws, counts = batched_workload(a.config)
+    if a.variants:            # the first variants only (a small case for profiling)
+        kws, counts = kws[:a.variants], counts[:a.variants]
     total = sum(counts)
     B = BatchedInstrument(fn, kws, ctx=dev)
     if a.tune == "auto":
