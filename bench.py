@@ -206,7 +206,7 @@ def run_batched_config(a):
         # variant (the variants share the component structure)
         from ramp_gb300 import autotune
         tune = {k: v for k, v in autotune.tune(B.instruments[0], rng="reference").items()
-                if k in ("blocks_per_sm", "split")}
+                if k in ("blocks_per_sm", "split", "walk")}
     else:
         tune = json.loads(a.tune) if a.tune else None
     for w in range(a.warmup):
@@ -257,7 +257,8 @@ def run_batched_config(a):
             "plain_path_sequential": {"value": total / (plain_ms / 1000.0), "ms_per_step": plain_ms,
                                       "sample": "first %d variants, scaled by histories" % nplain},
             "batched_over_plain": (total / (statistics.mean(ms) / 1000.0)) / (total / (plain_ms / 1000.0)),
-            "gpu_launches": a.steps * (2 if int((tune or {}).get("split", 0)) > 0 else 1) *
+            "gpu_launches": a.steps * (2 if (int((tune or {}).get("split", 0)) > 0
+                                             or int((tune or {}).get("walk", 0)) > 0) else 1) *
                             (sum(1 for c in counts if c > 0)
                              if int((tune or {}).get("streams", 0)) > 1 else 1),
             "clocks": clk}

@@ -224,6 +224,16 @@ typedef struct RampTune {
                                    Either way each variant has its own
                                    work counters and its own range of
                                    the survivor buffer.                  */
+  int32_t walk;                 /* fused path, chains without the
+                                   extended kinds: 1 = split before the
+                                   first GMesh component of a linear
+                                   block (replacing `split`); the second
+                                   kernel walks the mesh hierarchy one
+                                   node per pass on each lane and a lane
+                                   whose walk is over takes the next
+                                   waiting neutron (buffer as for
+                                   `split`).  Ignored without such a
+                                   component.                            */
 } RampTune;
 
 typedef struct RampPlan RampPlan;

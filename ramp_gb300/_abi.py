@@ -82,10 +82,11 @@ DP_GUIDE_R0, DP_GUIDE_QC, DP_GUIDE_ALPHA, DP_GUIDE_M, DP_GUIDE_W, DP_SOURCE_T, \
 class RampTune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("chunk", ctypes.c_int32), ("privatize", ctypes.c_int32),
-                ("split", ctypes.c_int32), ("streams", ctypes.c_int32)]
+                ("split", ctypes.c_int32), ("streams", ctypes.c_int32),
+                ("walk", ctypes.c_int32)]
 
 
-TUNE_KEYS = ("block", "blocks_per_sm", "chunk", "privatize", "split", "streams")
+TUNE_KEYS = ("block", "blocks_per_sm", "chunk", "privatize", "split", "streams", "walk")
 
 
 def tune_struct(tune):

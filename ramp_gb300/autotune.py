@@ -4,10 +4,10 @@ The fused kernel's result does not depend on its launch configuration (the
 RNG is counter-based and keyed by neutron index), so the configuration can
 be chosen purely for speed.  ``tune(inst)`` times short fused runs of the
 instrument over the candidates (register cap = minimum CTAs per SM, the
-span of neutrons a task covers, and whether survivors are compacted into
+span of neutrons a task covers, whether survivors are compacted into
 full warps before the first component that less than half of the
-histories reach — found by a plain-path pilot, ``survival``) and keeps the
-fastest; results are
+histories reach — found by a plain-path pilot, ``survival`` — and, for
+chains with a mesh, the per-lane mesh walk) and keeps the fastest; results are
 cached in a JSON file keyed by GPU name, the instrument's component
 structure and the keying mode.  Tuning uses fixed seeds and restores the
 instrument's tallies afterwards: it leaves no trace in the results or in
@@ -126,6 +126,14 @@ def split_point(inst, alive, threshold=0.5):
     return 0
 
 
+def has_mesh(inst):
+    """Whether a linear block of the chain holds a GMesh component (the
+    candidates then include the per-lane mesh walk, RampTune.walk)."""
+    _, carr, nc, barr, nb = inst.descriptors([])
+    return any(barr[k].linear and carr[j].geom == _abi.G_MESH
+               for k in range(nb) for j in range(barr[k].first, barr[k].first + barr[k].count))
+
+
 def _time_config(lib, plan, n, rng, cfg, stream, reps=2):
     tune = _abi.tune_struct(cfg)
     best = None
@@ -160,6 +168,8 @@ def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False
     if candidates is None:
         split = split_point(inst, survival(inst, min(n_probe, 1_000_000), rng))
         candidates = [dict(c, split=k) for c in CANDIDATES for k in ((0, split) if split else (0,))]
+        if has_mesh(inst):
+            candidates += [dict(c, walk=1) for c in CANDIDATES]
     with torch.cuda.device(inst.device):
         stream = torch.cuda.current_stream(inst.device)
         for cfg in candidates:

@@ -596,6 +596,27 @@ static int tune_split(const RampPlan* p, const RampTune* tune, int32_t* out) {
   return RAMP_OK;
 }
 
+/* the launch's stage split: RampTune.walk (chains without the extended
+ * kinds that hold a GMesh component in a linear block: split before the
+ * first such component, which may be component 0, and walk the mesh per
+ * lane in stage B), else RampTune.split */
+static int tune_stage(const RampPlan* p, const RampTune* tune, bool ext, int32_t* split,
+                      int32_t* walk) {
+  *walk = 0;
+  if (tune && tune->walk > 0 && !ext) {
+    for (const RampBlock& B : p->blocks) {
+      if (!B.linear) continue;
+      for (int k = B.first; k < B.first + B.count; ++k)
+        if (p->comps[k].geom == RAMP_G_MESH) {
+          *split = k;
+          *walk = 1;
+          return RAMP_OK;
+        }
+    }
+  }
+  return tune_split(p, tune, split);
+}
+
 /* survivor buffer for split launches covering up to n_items work items
  * of 128 neutrons: SURV_WORDS words per slot plus one count per item
  * (grows, never shrinks) */
@@ -769,10 +790,10 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.st = p->status;
   a.workq = &p->status->workq;
   a.workq_b = &p->status->workq_b;
-  int rc = tune_split(p, tune, &a.split);
+  int rc = tune_stage(p, tune, p->ext, &a.split, &a.walk);
   if (rc) return rc;
   a.ext = p->ext ? 1 : 0;
-  if (a.split > 0) {
+  if (a.split > 0 || a.walk) {
     rc = attach_surv(p, a, (n + 127) / 128, s);
     if (rc) return rc;
   }
@@ -801,14 +822,14 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
   }
   /* split launches: each variant gets its own region of the survivor
      buffer (its items' slots, SoA, and its items' counts) */
-  int32_t split = 0;
-  int rc0 = tune_split(p, tune, &split);
+  int32_t split = 0, walk = 0;
+  int rc0 = tune_stage(p, tune, base.ext != 0, &split, &walk);
   if (rc0) return rc0;
   std::vector<int64_t> item_off(nv + 1, 0);
   for (size_t v = 0; v < nv; ++v)
     item_off[v + 1] = item_off[v] + (vars[v].n > 0 ? (vars[v].n + 127) / 128 : 0);
   uint32_t* cnt = nullptr;
-  if (split > 0 && item_off[nv] > 0) {
+  if ((split > 0 || walk) && item_off[nv] > 0) {
     rc0 = ensure_surv(p, item_off[nv]);
     if (rc0) return rc0;
     cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS;
@@ -847,6 +868,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
     if (cnt) {
       const int64_t items = item_off[v + 1] - item_off[v];
       a.split = split;
+      a.walk = walk;
       a.surv = p->surv + (size_t)item_off[v] * 128 * SURV_WORDS;
       a.surv_cap = items * 128;
       a.surv_cnt = cnt + item_off[v];
@@ -953,8 +975,8 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     return RAMP_E_RANGE;
   }
   if (n_max == 0) return RAMP_OK;
-  int32_t split = 0;
-  int rc = tune_split(p, tune, &split);
+  int32_t split = 0, walk = 0;
+  int rc = tune_stage(p, tune, ext, &split, &walk);
   if (rc) return rc;
   if (ext) split = 0;   /* the one-launch kernel runs the extended kinds whole */
   int64_t items = 0;
@@ -998,8 +1020,9 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.workq = B.counters;
   a.workq_b = B.counters + n_variants;
   a.split = split;
+  a.walk = walk;
   a.ext = ext ? 1 : 0;
-  if (a.split > 0) {
+  if (a.split > 0 || a.walk) {
     rc = attach_surv(p, a, items, s);
     if (rc) return rc;
   }

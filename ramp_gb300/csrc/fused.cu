@@ -13,7 +13,7 @@
   PH(MB, MODE, false, 0, false) PH(MB, MODE, false, 1, false) PH(MB, MODE, false, 2, false) \
   PH(MB, MODE, true, 0, false) PH(MB, MODE, true, 1, false) PH(MB, MODE, true, 2, false)    \
   PH(MB, MODE, false, 0, true) PH(MB, MODE, false, 1, true) PH(MB, MODE, false, 2, true)    \
-  PH(MB, MODE, true, 0, true)                                                               \
+  PH(MB, MODE, true, 0, true) PH(MB, MODE, false, 4, false) PH(MB, MODE, true, 4, false)    \
   extern template int occ_mm<MB, MODE>(int);
 ONE_MODE(3, 0)
 ONE_MODE(3, 1)
@@ -25,6 +25,13 @@ ONE_MODE(4, 1)
  * runs the extended kinds whole) */
 template <int MB, int MODE, bool BATCHED, bool EXT>
 static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream_t s) {
+  if constexpr (!EXT) {
+    if (a.walk) {
+      const cudaError_t e = launch_phase<MB, MODE, BATCHED, 1, false>(a, block, grid, s);
+      if (e != cudaSuccess) return e;
+      return launch_phase<MB, MODE, BATCHED, 4, false>(a, block, grid, s);
+    }
+  }
   if constexpr (!(BATCHED && EXT)) {
     if (a.split > 0) {
       const cudaError_t e = launch_phase<MB, MODE, BATCHED, 1, EXT>(a, block, grid, s);
@@ -49,6 +56,7 @@ cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s
   if (a.variants && a.n_variants > 65535) return cudaErrorInvalidValue;   /* grid rows */
   if (a.n_blocks > FUSED_MAX_BLOCKS || a.n_comps > RAMP_MAX_COMPS) return cudaErrorInvalidValue;
   if (a.split < 0 || (a.split > 0 && (a.split >= a.n_comps || !a.surv))) return cudaErrorInvalidValue;
+  if (a.walk && (a.ext || a.split >= a.n_comps || !a.surv)) return cudaErrorInvalidValue;
   /* register cap: 3 or 4 CTAs of 256 threads per SM (at 2 the kernel is
      never faster on GB300) */
   if (a.minb != 3)

@@ -131,11 +131,168 @@ DI void fused_tail(const FusedArgs& a) {
   }
 }
 
+/* a neutron whose walk through the GMesh component K is over (k = 0: the
+ * walk ended, -1: the stack overflowed, -2: the ray missed the mesh box):
+ * read it back from its survivor record, bring it into K's frame again
+ * (the same operations give the same values), take the walk's records, then
+ * the rest of comp_linear of K and the components after it */
+template <int MODE, bool EXT>
+DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, int64_t slot,
+                 MeshWalk& w, int k, bool zx, bool carry) {
+  const int64_t cap = a.surv_cap;
+  const uint32_t* wp = a.surv + slot;
+  Nt n;
+  n.x = __uint_as_float(wp[0 * cap]);   n.y = __uint_as_float(wp[1 * cap]);
+  n.z = __uint_as_float(wp[2 * cap]);   n.vx = __uint_as_float(wp[3 * cap]);
+  n.vy = __uint_as_float(wp[4 * cap]);  n.vz = __uint_as_float(wp[5 * cap]);
+  n.px = __uint_as_float(wp[6 * cap]);  n.py = __uint_as_float(wp[7 * cap]);
+  n.pz = __uint_as_float(wp[8 * cap]);  n.p = __uint_as_float(wp[9 * cap]);
+  n.t = __uint_as_float(wp[10 * cap]);  n.sb = __uint_as_float(wp[11 * cap]);
+  n.sc = __uint_as_float(wp[12 * cap]); n.sd = __uint_as_float(wp[13 * cap]);
+  n.se = __uint_as_float(wp[14 * cap]);
+  n.die = 0.0f;
+  n.wr = 0u;
+  uint32_t ii = wp[15 * cap];
+  const uint32_t idx = wp[16 * cap];
+  Rng r;
+  rng_init(r, MODE, a.rng.tid_base + idx, wp[17 * cap], a.rng.run_seed);
+  const CompDev& cK = comps[K];
+  transform<false>(cK, n);
+  Is s;
+  is_reset(s);
+  if (k == 0 && mesh_end(cK, n, s, w)) ii = cK.idx;
+  if (len3(ip2(s)) == 0.0f && cK.restore == 0) set_die(n, 1.f);
+  if (ii == cK.idx && !(n.die > 0.f))
+    scatter<TallyOnly, EXT>(cK, n, s, ii, r, a.st, (TallyOnly*)nullptr, zx);
+  if (zx && n.p == 0.0f) set_die(n, 1.0f);
+  else if (!(n.die > 0.f)) untransform<false>(cK, n);
+  for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
+    const RampBlock B = a.blocks[b];
+    const int e = B.first + B.count;
+    if (e <= K + 1) continue;
+    if (B.linear) {
+      for (int j = B.first > K + 1 ? B.first : K + 1; j < e; ++j) {
+        if (n.die > 0.f) break;
+        comp_linear<TallyOnly, EXT>(comps[j], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
+      }
+    } else {
+      block_nonlinear<TallyOnly>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
+    }
+  }
+  if (carry) { a.carry_sb[idx] = n.sb; a.carry_iidx[idx] = ii; }
+}
+
+/* PHASE 4: stage B of a launch split before a GMesh component K (a linear
+ * block's), for chains where the walk through the mesh hierarchy is most of
+ * the work.  Walk lengths differ a lot between rays (a ray outside the mesh
+ * box has none), so with one ray per lane a warp runs at a few lanes.  Here
+ * each lane walks its ray one node per pass, and a lane whose walk is over
+ * finishes that neutron (the rest of component K and the components after
+ * it) and takes the next waiting survivor; the warp claims the next group of
+ * work items as soon as every survivor of the current one is taken.  Every
+ * neutron goes through the same operations as in PHASE 2. */
+template <int MODE, bool BATCHED, bool EXT>
+DI void fused_tail_walk(const FusedArgs& a) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const bool carry = (a.carry_sb != nullptr);
+  const bool zx = !carry;
+  const int K = a.split;
+  const int64_t cap = a.surv_cap;
+  const int var = BATCHED ? (int)blockIdx.y : a.var_key;
+  const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
+  const int64_t item0 = BATCHED ? V->item_off : 0;
+  const int64_t n_items = BATCHED ? (V->n + FUSED_WARP_TASK - 1) / FUSED_WARP_TASK : a.surv_items;
+  if (BATCHED && item0 + n_items > a.surv_items) {
+    if (lane == 0) raise_flag(a.st, RAMP_F_WORKQ);
+    return;
+  }
+  const CompDev* __restrict__ comps = V->comps;
+  const CompDev& cK = comps[K];
+  unsigned long long* const q_b = a.workq_b + (BATCHED ? var : 0);
+  /* the current group of work items (warp-uniform) */
+  int64_t t0 = 0;
+  int c = 0, excl = 0, total = 0, handed = 0;
+  bool groups_left = true;
+  /* this lane's walk: only the ray and the walk state stay live while it
+     runs; the neutron is read back from its survivor record when it ends */
+  bool walking = false;
+  int64_t slot = 0;
+  MeshWalk w;
+  for (;;) {
+    /* hand the waiting survivors to the idle lanes (a lane whose ray misses
+       the mesh box finishes it at once and is idle again) */
+    for (;;) {
+      const unsigned m = __ballot_sync(FULL_MASK, !walking);
+      if (m == 0u) break;
+      if (handed >= total) {
+        if (!groups_left) break;
+        unsigned long long g = 0;
+        if (lane == 0) g = atomicAdd(q_b, 1ull);
+        g = __shfl_sync(FULL_MASK, g, 0);
+        t0 = (int64_t)g * SURV_GROUP;
+        handed = 0;
+        if (t0 >= n_items) {
+          groups_left = false;
+          c = 0; excl = 0; total = 0;
+          break;
+        }
+        c = (lane < SURV_GROUP && t0 + lane < n_items) ? (int)a.surv_cnt[item0 + t0 + lane] : 0;
+        int incl = c;
+        for (int d = 1; d < SURV_GROUP; d <<= 1) {
+          const int y = __shfl_up_sync(FULL_MASK, incl, d);
+          if (lane >= d) incl += y;
+        }
+        excl = incl - c;
+        total = __shfl_sync(FULL_MASK, incl, SURV_GROUP - 1);
+        continue;
+      }
+      const int qk = handed + __popc(m & lt);
+      int item = 0, base = 0;
+      for (int k = 0; k < SURV_GROUP; ++k) {   /* last item starting at or before qk */
+        const int ek = __shfl_sync(FULL_MASK, excl, k);
+        const int ck = __shfl_sync(FULL_MASK, c, k);
+        if (ck > 0 && ek <= qk) { item = k; base = ek; }
+      }
+      handed = (handed + __popc(m) < total) ? handed + __popc(m) : total;
+      if (!walking && qk < total) {
+        slot = (item0 + t0 + item) * FUSED_WARP_TASK + (qk - base);
+        const uint32_t* wp = a.surv + slot;
+        Nt ray;                           /* position and velocity suffice for the walk */
+        ray.x = __uint_as_float(wp[0 * cap]);  ray.y = __uint_as_float(wp[1 * cap]);
+        ray.z = __uint_as_float(wp[2 * cap]);  ray.vx = __uint_as_float(wp[3 * cap]);
+        ray.vy = __uint_as_float(wp[4 * cap]); ray.vz = __uint_as_float(wp[5 * cap]);
+        transform<false>(cK, ray);        /* comp_linear of component K */
+        if (mesh_begin(cK, ray, w)) walking = true;
+        else walk_end<MODE, EXT>(a, comps, K, slot, w, -2, zx, carry);
+      }
+    }
+    const bool more = groups_left || handed < total;   /* survivors still waiting */
+    if (!more && !__any_sync(FULL_MASK, walking)) break;
+    /* walk until a quarter of the lanes are idle (or, with nothing left
+       to hand out, until every walk is over) */
+    for (;;) {
+      if (walking) {
+        const int k = mesh_step(cK, w, a.st);
+        if (k <= 0) {
+          walking = false;
+          walk_end<MODE, EXT>(a, comps, K, slot, w, k, zx, carry);
+        }
+      }
+      const int idle = __popc(__ballot_sync(FULL_MASK, !walking));
+      if (idle == 32 || (more && idle >= 8)) break;
+    }
+  }
+}
+
 template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
 __global__ void __launch_bounds__(256, MINB)
 k_fused(const FusedArgs a) {
   if constexpr (PHASE == 2) {
     fused_tail<MODE, BATCHED, EXT>(a);
+    return;
+  } else if constexpr (PHASE == 4) {
+    fused_tail_walk<MODE, BATCHED, EXT>(a);
     return;
   } else {
     const int lane = threadIdx.x & 31;

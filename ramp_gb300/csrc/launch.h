@@ -50,6 +50,8 @@ struct FusedArgs {
   unsigned long long* workq_b;  /* stage-B work-queue counter(s) (split) */
   int32_t var_key;              /* single variant: its index in the RNG key */
   int32_t minb;                 /* register cap: the build for 3 or 4 CTAs per SM */
+  int32_t walk;                 /* split before the GMesh component `split` (may
+                                   be 0): stage B walks the mesh per lane (PHASE 4) */
   int32_t ext;                  /* the chain uses an extended kind (MISIS source,
                                    SMonochromator, SPowder1): the kernels built
                                    with them (split only when not BATCHED) */

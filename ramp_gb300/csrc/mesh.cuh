@@ -66,9 +66,26 @@ DI float watertight_t(const Shear& S, V3 org, V3 v0, V3 v1, V3 v2) {
   return T / det;
 }
 
-DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
+/* The walk of one ray through the hierarchy, resumable node by node
+ * (mesh_begin, then mesh_step until it returns 0 or -1, then mesh_end):
+ * g_mesh runs it to the end for one neutron; a kernel may also interleave
+ * the walks of many rays on one lane. */
+struct MeshWalk {
+  V3 pos, vel;
+  float ix, iy, iz;
+  float o0, o1, o2, o3, o4, o5, o6, o7;
+  double chord;
+  uint32_t num_intersections;
+  int sp, node;
+  bool need_all, want_chord;
+  Shear S;
+  int stack[RAMP_BVH_STACK];
+};
+
+/* bounding box of the whole mesh (mesh.cl:22-40); false: the ray misses it
+ * and the intersection is false */
+DI bool mesh_begin(const CompDev& c, const Nt& n, MeshWalk& w) {
   V3 pos = npos(n), vel = nvel(n);
-  /* bounding box of the whole mesh, mesh.cl:22-40 */
   V3 ll = v3(c.gp[0], c.gp[2], c.gp[4]), ur = v3(c.gp[1], c.gp[3], c.gp[5]);
   V3 dA = sub(ll, pos), dB = sub(ur, pos);
   float t1 = dA.x / vel.x, t2 = dB.x / vel.x, t3 = dA.y / vel.y;
@@ -76,108 +93,130 @@ DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
   float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
   float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
   if (tmax < 0.0f || tmin > tmax) return false;
+  w.pos = pos;
+  w.vel = vel;
+  w.need_all = (c.gi[0] == 1) || (c.scat == RAMP_S_ATTENUATE);
+  w.num_intersections = 0;
+  w.o0 = 0.0f; w.o1 = 0.0f; w.o2 = 0.0f; w.o3 = 1e8f;
+  w.o4 = 0.0f; w.o5 = 0.0f; w.o6 = 0.0f; w.o7 = 1e8f;
+  w.want_chord = (c.scat == RAMP_S_ATTENUATE);
+  if (w.want_chord) w.S = make_shear(vel);
+  w.chord = 0.0;
+  w.ix = 1.0f / vel.x; w.iy = 1.0f / vel.y; w.iz = 1.0f / vel.z;
+  w.sp = 0;
+  w.node = 0;
+  return true;
+}
 
+/* one inner node of the walk: test both children, the triangles of the
+ * leaf children that were hit, then move on.  Returns 1 while nodes
+ * remain, 0 when the walk is over, -1 when the stack would overflow (the
+ * intersection is then false and the status flag raised). */
+DI int mesh_step(const CompDev& c, MeshWalk& w, StatusDev* st) {
   const float eps = 0.000000001f;
-  const bool need_all = (c.gi[0] == 1) || (c.scat == RAMP_S_ATTENUATE);
-  uint32_t num_intersections = 0;
-  float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, o3 = 1e8f, o4 = 0.0f, o5 = 0.0f, o6 = 0.0f, o7 = 1e8f;
-  const bool want_chord = (c.scat == RAMP_S_ATTENUATE);
-  Shear S;
-  if (want_chord) S = make_shear(vel);
-  double chord = 0.0;
-  const float ix = 1.0f / vel.x, iy = 1.0f / vel.y, iz = 1.0f / vel.z;
+  const V3 pos = w.pos, vel = w.vel;
+  const float ix = w.ix, iy = w.iy, iz = w.iz;
   const float4* __restrict__ nodes = c.bvh_nodes;
   const float4* __restrict__ tris = c.bvh_tris;
-  int stack[RAMP_BVH_STACK];
-  int sp = 0;
-  int node = 0;
-  for (;;) {
-    const float4* q = nodes + 4 * node;
-    const float4 a0 = __ldg(q), b0 = __ldg(q + 1), a1 = __ldg(q + 2), b1 = __ldg(q + 3);
-    const int r0 = __float_as_int(a0.w), c0 = __float_as_int(b0.w);
-    const int r1 = __float_as_int(a1.w), c1 = __float_as_int(b1.w);
-    float tn0 = 0.0f, tn1 = 0.0f;
-    bool h0 = false, h1 = false;
-    if (c0 >= 0) {
-      float tx0 = (a0.x - pos.x) * ix, tx1 = (b0.x - pos.x) * ix;
-      float ty0 = (a0.y - pos.y) * iy, ty1 = (b0.y - pos.y) * iy;
-      float tz0 = (a0.z - pos.z) * iz, tz1 = (b0.z - pos.z) * iz;
-      tn0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-      float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-      h0 = !(tn0 > tf || tf < -1e-6f) && (need_all || !(tn0 > fmaxf(o3, o7)));
-    }
-    if (c1 >= 0) {
-      float tx0 = (a1.x - pos.x) * ix, tx1 = (b1.x - pos.x) * ix;
-      float ty0 = (a1.y - pos.y) * iy, ty1 = (b1.y - pos.y) * iy;
-      float tz0 = (a1.z - pos.z) * iz, tz1 = (b1.z - pos.z) * iz;
-      tn1 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-      float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-      h1 = !(tn1 > tf || tf < -1e-6f) && (need_all || !(tn1 > fmaxf(o3, o7)));
-    }
-    /* the triangles of the leaf children that were hit, as one range */
-    const int n0 = (h0 && c0 > 0) ? c0 : 0, n1 = (h1 && c1 > 0) ? c1 : 0;
-    for (int j = 0; j < n0 + n1; ++j) {
-      const int k = j < n0 ? r0 + j : r1 + (j - n0);
-      float4 q0 = __ldg(tris + 3 * k), q1 = __ldg(tris + 3 * k + 1), q2 = __ldg(tris + 3 * k + 2);
-      V3 v0 = v3(q0.x, q0.y, q0.z), v1 = v3(q1.x, q1.y, q1.z), v2 = v3(q2.x, q2.y, q2.z);
-      V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
-      if (want_chord) {
-        float tw = watertight_t(S, pos, v0, v1, v2);
-        if (tw > eps) {
-          float nvw = dot(cross(e1, e2), vel);
-          if (nvw > 0) chord += (double)tw;
-          else if (nvw < 0) chord -= (double)tw;
-        }
-      }
-      V3 h = cross(vel, e2);
-      float aa = dot(e1, h);
-      if (fabsf(aa) < eps) continue;
-      float f = 1.0f / aa;
-      V3 sv = sub(pos, v0);
-      float u = f * dot(sv, h);
-      if (u < 0.0f || u > 1.0f) continue;
-      V3 qv = cross(sv, e1);
-      float v = f * dot(vel, qv);
-      if (v < 0.0f || u + v > 1.0f) continue;
-      float t = f * dot(e2, qv);
-      if (t > eps) num_intersections++;
-      V3 nrm = cross(e1, e2);
-      float nv = dot(nrm, vel);
-      if ((t > eps) && (t < o3) && (nv < 0)) {
-        o0 = pos.x + vel.x * t; o1 = pos.y + vel.y * t; o2 = pos.z + vel.z * t; o3 = t;
-      }
-      if ((t > eps) && (t < o7) && (nv > 0)) {
-        o4 = pos.x + vel.x * t; o5 = pos.y + vel.y * t; o6 = pos.z + vel.z * t; o7 = t;
+  const float4* q = nodes + 4 * w.node;
+  const float4 a0 = __ldg(q), b0 = __ldg(q + 1), a1 = __ldg(q + 2), b1 = __ldg(q + 3);
+  const int r0 = __float_as_int(a0.w), c0 = __float_as_int(b0.w);
+  const int r1 = __float_as_int(a1.w), c1 = __float_as_int(b1.w);
+  float tn0 = 0.0f, tn1 = 0.0f;
+  bool h0 = false, h1 = false;
+  if (c0 >= 0) {
+    float tx0 = (a0.x - pos.x) * ix, tx1 = (b0.x - pos.x) * ix;
+    float ty0 = (a0.y - pos.y) * iy, ty1 = (b0.y - pos.y) * iy;
+    float tz0 = (a0.z - pos.z) * iz, tz1 = (b0.z - pos.z) * iz;
+    tn0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+    h0 = !(tn0 > tf || tf < -1e-6f) && (w.need_all || !(tn0 > fmaxf(w.o3, w.o7)));
+  }
+  if (c1 >= 0) {
+    float tx0 = (a1.x - pos.x) * ix, tx1 = (b1.x - pos.x) * ix;
+    float ty0 = (a1.y - pos.y) * iy, ty1 = (b1.y - pos.y) * iy;
+    float tz0 = (a1.z - pos.z) * iz, tz1 = (b1.z - pos.z) * iz;
+    tn1 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+    h1 = !(tn1 > tf || tf < -1e-6f) && (w.need_all || !(tn1 > fmaxf(w.o3, w.o7)));
+  }
+  /* the triangles of the leaf children that were hit, as one range */
+  const int n0 = (h0 && c0 > 0) ? c0 : 0, n1 = (h1 && c1 > 0) ? c1 : 0;
+  for (int j = 0; j < n0 + n1; ++j) {
+    const int k = j < n0 ? r0 + j : r1 + (j - n0);
+    float4 q0 = __ldg(tris + 3 * k), q1 = __ldg(tris + 3 * k + 1), q2 = __ldg(tris + 3 * k + 2);
+    V3 v0 = v3(q0.x, q0.y, q0.z), v1 = v3(q1.x, q1.y, q1.z), v2 = v3(q2.x, q2.y, q2.z);
+    V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+    if (w.want_chord) {
+      float tw = watertight_t(w.S, pos, v0, v1, v2);
+      if (tw > eps) {
+        float nvw = dot(cross(e1, e2), vel);
+        if (nvw > 0) w.chord += (double)tw;
+        else if (nvw < 0) w.chord -= (double)tw;
       }
     }
-    /* inner children: continue into the nearer, keep the other */
-    const bool i0 = h0 && c0 == 0, i1 = h1 && c1 == 0;
-    if (i0 && i1) {
-      if (sp + 1 > RAMP_BVH_STACK) { raise_flag(st, RAMP_F_BVH_STACK); return false; }
-      const bool first0 = !(tn1 < tn0);
-      stack[sp++] = first0 ? r1 : r0;
-      node = first0 ? r0 : r1;
-    } else if (i0) {
-      node = r0;
-    } else if (i1) {
-      node = r1;
-    } else {
-      if (sp == 0) break;
-      node = stack[--sp];
+    V3 h = cross(vel, e2);
+    float aa = dot(e1, h);
+    if (fabsf(aa) < eps) continue;
+    float f = 1.0f / aa;
+    V3 sv = sub(pos, v0);
+    float u = f * dot(sv, h);
+    if (u < 0.0f || u > 1.0f) continue;
+    V3 qv = cross(sv, e1);
+    float v = f * dot(vel, qv);
+    if (v < 0.0f || u + v > 1.0f) continue;
+    float t = f * dot(e2, qv);
+    if (t > eps) w.num_intersections++;
+    V3 nrm = cross(e1, e2);
+    float nv = dot(nrm, vel);
+    if ((t > eps) && (t < w.o3) && (nv < 0)) {
+      w.o0 = pos.x + vel.x * t; w.o1 = pos.y + vel.y * t; w.o2 = pos.z + vel.z * t; w.o3 = t;
+    }
+    if ((t > eps) && (t < w.o7) && (nv > 0)) {
+      w.o4 = pos.x + vel.x * t; w.o5 = pos.y + vel.y * t; w.o6 = pos.z + vel.z * t; w.o7 = t;
     }
   }
-  if ((c.gi[0] == 1) && (num_intersections % 2 == 1)) {
-    o4 = o0; o5 = o1; o6 = o2; o7 = o3;
-  } else if ((c.gi[0] == 1) && (num_intersections % 2 == 0)) {
+  /* inner children: continue into the nearer, keep the other */
+  const bool i0 = h0 && c0 == 0, i1 = h1 && c1 == 0;
+  if (i0 && i1) {
+    if (w.sp + 1 > RAMP_BVH_STACK) { raise_flag(st, RAMP_F_BVH_STACK); return -1; }
+    const bool first0 = !(tn1 < tn0);
+    w.stack[w.sp++] = first0 ? r1 : r0;
+    w.node = first0 ? r0 : r1;
+    return 1;
+  }
+  if (i0) { w.node = r0; return 1; }
+  if (i1) { w.node = r1; return 1; }
+  if (w.sp == 0) return 0;
+  w.node = w.stack[--w.sp];
+  return 1;
+}
+
+/* the records of a finished walk (mesh.cl:114-129): interior parity, then
+ * the entering and exiting hits if they come before the current record */
+DI bool mesh_end(const CompDev& c, Nt& n, Is& s, MeshWalk& w) {
+  if ((c.gi[0] == 1) && (w.num_intersections % 2 == 1)) {
+    w.o4 = w.o0; w.o5 = w.o1; w.o6 = w.o2; w.o7 = w.o3;
+  } else if ((c.gi[0] == 1) && (w.num_intersections % 2 == 0)) {
     return false;
   }
-  if (o3 < s.t1) {
-    s.x1 = o0; s.y1 = o1; s.z1 = o2; s.t1 = o3;
-    s.x2 = o4; s.y2 = o5; s.z2 = o6; s.t2 = o7;
-    if (want_chord) { n.sd = chord > 0.0 ? (float)chord : 0.0f; n.wr |= WR_SD; }
+  if (w.o3 < s.t1) {
+    s.x1 = w.o0; s.y1 = w.o1; s.z1 = w.o2; s.t1 = w.o3;
+    s.x2 = w.o4; s.y2 = w.o5; s.z2 = w.o6; s.t2 = w.o7;
+    if (w.want_chord) { n.sd = w.chord > 0.0 ? (float)w.chord : 0.0f; n.wr |= WR_SD; }
     return true;
   }
   return false;
+}
+
+DI bool g_mesh(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
+  MeshWalk w;
+  if (!mesh_begin(c, n, w)) return false;
+  int k;
+  while ((k = mesh_step(c, w, st)) > 0) {
+  }
+  if (k < 0) return false;
+  return mesh_end(c, n, s, w);
 }
 
 #endif /* RAMP_MESH_CUH */

@@ -270,6 +270,34 @@ def test_fused_split_matches_oracle(cuda_lib, fn, kw, N, split, rng):
     assert gi.oob_drops == r.oob
 
 
+@pytest.mark.parametrize("tune,chunk,rng", [({"walk": 1}, None, "reference"),
+                                             ({"walk": 1, "blocks_per_sm": 3}, None, "native"),
+                                             ({"walk": 1}, 7_000, "reference")])
+def test_fused_mesh_walk_matches_oracle(cuda_lib, tune, chunk, rng):
+    """Stage B walking the mesh one node per pass on each lane, lanes taking
+    the next waiting ray when their walk is over (the mesh is component 0,
+    so stage A is the moderator alone); with carry buffers across chunks."""
+    gi, ci, r = pair(I.path("mesh_imaging.json"), I.mesh_imaging_kwargs(0.37), 20_000,
+                     path="fused", rng=rng, chunk=chunk, tune=tune)
+    tallies_close(gi, ci)
+    assert gi.oob_drops == r.oob
+
+
+@pytest.mark.parametrize("tune", [{"walk": 1}, {"walk": 1, "streams": 4}])
+def test_batched_mesh_walk_matches_single_runs(cuda_lib, tune):
+    """Three views of the mesh in one call (grid rows or streams), walked
+    per lane; each equals its own oracle run."""
+    angles, counts, seeds = [0.0, 0.7, 2.1], [9_000, 5_001, 7_777], [3, 4, 5]
+    variants = [I.mesh_imaging_kwargs(angle=t) for t in angles]
+    B = BatchedInstrument(I.path("mesh_imaging.json"), variants, ctx="cuda")
+    B.execute(counts, rng="native", seeds=seeds, tune=tune)
+    torch.cuda.synchronize()
+    for v, (kw, n, seed) in enumerate(zip(variants, counts, seeds)):
+        ci = m.Instrument(I.path("mesh_imaging.json"), "cpu", **kw)
+        oracle.run(ci, n, rng_mode=1, variant=v, seeds=[seed])
+        tallies_close(B.instruments[v], ci)
+
+
 @pytest.mark.parametrize("split", [1, 4])
 def test_fused_split_at_nonlinear_block_boundaries(cuda_lib, split):
     gi, ci, r = pair(os.path.join(GOLD_DIR, "nonlinear_env.json"), I.small_chain_kwargs(),
