@@ -3,7 +3,6 @@
 A geometry plugin keeps its constructor arguments and writes them into the
 geometry slots of a component descriptor (``fill``).  The intersection code
 itself runs inside the CUDA component kernels."""
-from .. import _abi
 
 
 class GPrim:

@@ -1,6 +1,3 @@
-import numpy as np
-
-from .gprim import GPrim
 from .sphere import GSphere
 from .. import _abi
 

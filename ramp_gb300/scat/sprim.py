@@ -6,8 +6,6 @@ parameters into the scatter slots of a component descriptor (``fill``) and
 owns its result buffers as device tensors."""
 import torch
 
-from .. import _abi
-
 
 def _device(ctx):
     if isinstance(ctx, torch.device):

@@ -1,7 +1,6 @@
 """MCPL files: RAMP's writer layout byte for byte (golden bytes from the
 reference's mcpl_out.py, made by tests/golden/make_mcpl_golden.py), the
 standard direction packing round trip, and the reader's header handling."""
-import gzip
 import os
 
 import numpy as np
