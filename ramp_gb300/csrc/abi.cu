@@ -452,12 +452,12 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
   RampPlan* p = new RampPlan();
   p->src_in = *source;
   int rc = make_src(p, *source, p->src);
-  if (rc) { delete p; return rc; }
+  if (rc) { ramp_plan_destroy(p); return rc; }   /* frees any table it uploaded */
   for (int b = 0; b < n_blocks; ++b) {
     const RampBlock& B = blocks[b];
     if (B.first < 0 || B.count < 0 || B.first + B.count > n_comps || (!B.linear && B.multi < 0)) {
       set_err("block %d covers components outside [0, %d)", b, n_comps);
-      delete p;
+      ramp_plan_destroy(p);
       return RAMP_E_INVALID;
     }
   }
