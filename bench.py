@@ -59,7 +59,8 @@ def args_():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--variants", type=int, default=0,
-                   help="configs 3 and 5: trace only the first N variants (0: all)")
+                   help="batched scan and mesh imaging (--config 3, 5): trace only the "
+                        "first N variants (0: all)")
     p.add_argument("--tune", default="auto",
                    help='fused launch config: "auto" (autotuner) or JSON, e.g. {"blocks_per_sm": 3}')
     p.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
@@ -168,7 +169,7 @@ class Clocks:
                 "samples": len(rows)}
 
 
-# ---------------------------------------------------------------- configs 3 and 5
+# ------------------------------------------- batched scan and mesh imaging
 def batched_workload(config, seed=11):
     """Variants of the batched workloads: (IDF, list of kwargs, counts)."""
     import numpy as np
@@ -265,7 +266,7 @@ def run_batched_config(a):
     print(json.dumps(line), flush=True)
 
 
-# ---------------------------------------------------------------- config 4
+# ------------------------------------------- gradients of a histogram loss
 def run_gradients(a, n=10_000_000):
     """grads/s: forward histogram + loss + adjoint gradient of 22 parameters
     (4 guides x R0, Qc, alpha, m, W; moderator T; powder sigma_abs) on the
