@@ -97,3 +97,34 @@ def test_guide_without_reflection_passes_only_straight_neutrons(tmp_path, r0):
         ref = instrument(tmp_path, GUIDE_IDF, r0=0.99)
         oracle.run(ref, 20_000, seeds=[3])
         assert total < det_sum(ref, "mon")
+
+
+# ----------------------------------------------------------------- GPU
+def _gpu_pair(tmp_path, text, N, path, **kw):
+    import random
+    import torch
+    fn = tmp_path / "inst.json"
+    fn.write_text(text)
+    gi = m.Instrument(str(fn), "cuda", **kw)
+    random.seed(99)
+    gi.execute(N, path=path)
+    torch.cuda.synchronize()
+    ci = m.Instrument(str(fn), "cpu", **kw)
+    random.seed(99)
+    r = oracle.run(ci, N)
+    return gi, ci, r
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("text,kw", [(SAMPLE_IDF, dict(f2=0.0, sa=5.0)),
+                                     (GUIDE_IDF, dict(r0=0.0))],
+                         ids=["powder_without_line_cross_section", "guide_without_reflection"])
+def test_edge_instruments_match_oracle_on_the_gpu(cuda_lib, tmp_path, text, kw):
+    from helpers import records_equal, tallies_close
+    gi, ci, r = _gpu_pair(tmp_path, text, 30_000, "plain", **kw)
+    recs, iidx = gi.neutron_state()
+    records_equal(recs, r.neutrons)
+    assert np.array_equal(iidx, r.iidx)
+    tallies_close(gi, ci)
+    gf, cf, _ = _gpu_pair(tmp_path, text, 30_000, "fused", **kw)
+    tallies_close(gf, cf)
