@@ -47,6 +47,10 @@ CPU_SAMPLE = 2_000_000      # histories per CPU-baseline step
 # profiles/let_like_fused_split_1e7.md (49 + 83 MB and 121 + 5 MB); the
 # traffic grows with the histories traced
 FUSED_SPLIT2_DRAM_PER_1E7 = (48.59 + 82.98 + 121.37 + 5.09) * 1e6
+# the same capture's issue figures for stage A (88 % of the split launch):
+# warp instructions issued on 77.4 % of scheduler cycles, 15.8 of 32 lanes
+# active per instruction
+FUSED_SPLIT2_STAGE_A_ISSUE = {"issue_active_pct": 77.4, "threads_per_instruction": 15.8}
 
 
 def args_():
@@ -567,6 +571,8 @@ def main():
                      "traffic": (FUSED_SPLIT2_DRAM_PER_1E7 * plain.last_chunk / 1e7
                                  if int((tune or {}).get("split", 0)) == 2 else None),
                      "traffic_unit": "bytes per launch (stage A + B)",
+                     "ncu_stage_a": (FUSED_SPLIT2_STAGE_A_ISSUE
+                                     if int((tune or {}).get("split", 0)) == 2 else None),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                        "1e7-history split launch, scaled by histories",
                      "kernel": "k_fused", "kernel_ms": kern_ms, "draws_per_launch": draws,
