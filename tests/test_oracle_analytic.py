@@ -34,6 +34,12 @@ GUIDE = """"guide": {"position": [0, 0, 1.0],
                               "h2": 0.02, "l": 6.0, "R0": %s, "Qc": 0.0219,
                               "alpha": 3.0, "m": 2, "W": 0.003}},"""
 
+ABSORBER = """"can": {"position": [0, 0, 1.0],
+            "geom_kernel": {"name": "GCylinderExt", "radius": 0.005, "height": 0.04},
+            "scat_kernel": {"name": "SPowderN", "d_spacing": [2.0], "pack": 1.0, "vc": 60.0,
+                            "sigma_abs": 5.0, "multiplicity": [1], "DW": 1.0, "F2": [0.0],
+                            "d_phi": 180.0}},"""
+
 CHOPPER = """"chop": {"position": [0, 0, 1.0],
              "geom_kernel": {"name": "GPlane", "width": 0.6, "height": 0.6},
              "scat_kernel": {"name": "SChopper", "radius": 0.28, "freq": 1884.955592,
@@ -100,3 +106,20 @@ def test_chopper_transmission_is_its_open_fraction(tmp_path):
     p = np.arctan2(0.04, 0.28) / Tg
     sigma = np.sqrt(p * (1 - p) / N)
     assert abs(h.sum() - p) < 4 * sigma
+
+
+def test_cylinder_chord_through_an_absorber(tmp_path):
+    """A pencil beam through the axis of a cylinder of radius r crosses a
+    chord of 2 r: with only absorption (all F^2 = 0) the powder kernel
+    transmits with probability 1 - p and weight factor 1 - p, where
+    p = 1 - exp(-Sigma_abs 2 r) and Sigma_abs = (pack sigma_abs / vc 100)
+    2200 / v (powderN.py:65, powderN.cl:40-58), so the weight reaching
+    the monitor is (1 - p)^2 per neutron."""
+    E, N = 5.0, 100_000
+    h, _, _ = run(tmp_path, PENCIL, N, md=1e-5, e0=E, e1=E, zm=1.5, var="tof",
+                  b0=0.0, bs=10.0, b1=20000.0, middle=ABSORBER)
+    v = SE2V * np.sqrt(E)
+    sig = (1.0 * 5.0 / 60.0 * 100.0) * 2200.0 / v
+    q = np.exp(-sig * 2 * 0.005)                   # 1 - p
+    sigma = q * np.sqrt(q * (1 - q) / N)
+    assert abs(h.sum() - q * q) < 4 * sigma
