@@ -35,7 +35,7 @@ GUIDE = """"guide": {"position": [0, 0, 1.0],
                               "alpha": 3.0, "m": 2, "W": 0.003}},"""
 
 ABSORBER = """"can": {"position": [0, 0, 1.0],
-            "geom_kernel": {"name": "GCylinderExt", "radius": 0.005, "height": 0.04},
+            "geom_kernel": %s,
             "scat_kernel": {"name": "SPowderN", "d_spacing": [2.0], "pack": 1.0, "vc": 60.0,
                             "sigma_abs": 5.0, "multiplicity": [1], "DW": 1.0, "F2": [0.0],
                             "d_phi": 180.0}},"""
@@ -108,16 +108,18 @@ def test_chopper_transmission_is_its_open_fraction(tmp_path):
     assert abs(h.sum() - p) < 4 * sigma
 
 
-def test_cylinder_chord_through_an_absorber(tmp_path):
-    """A pencil beam through the axis of a cylinder of radius r crosses a
-    chord of 2 r: with only absorption (all F^2 = 0) the powder kernel
+@pytest.mark.parametrize("geom", ['{"name": "GCylinderExt", "radius": 0.005, "height": 0.04}',
+                                  '{"name": "GSphere", "radius": 0.005}'])
+def test_chord_through_an_absorber(tmp_path, geom):
+    """A pencil beam through the axis of a cylinder (or the centre of a
+    sphere) of radius r crosses a chord of 2 r: with only absorption (all F^2 = 0) the powder kernel
     transmits with probability 1 - p and weight factor 1 - p, where
     p = 1 - exp(-Sigma_abs 2 r) and Sigma_abs = (pack sigma_abs / vc 100)
     2200 / v (powderN.py:65, powderN.cl:40-58), so the weight reaching
     the monitor is (1 - p)^2 per neutron."""
     E, N = 5.0, 100_000
     h, _, _ = run(tmp_path, PENCIL, N, md=1e-5, e0=E, e1=E, zm=1.5, var="tof",
-                  b0=0.0, bs=10.0, b1=20000.0, middle=ABSORBER)
+                  b0=0.0, bs=10.0, b1=20000.0, middle=ABSORBER % geom)
     v = SE2V * np.sqrt(E)
     sig = (1.0 * 5.0 / 60.0 * 100.0) * 2200.0 / v
     q = np.exp(-sig * 2 * 0.005)                   # 1 - p
