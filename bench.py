@@ -395,7 +395,10 @@ def main():
 
     import ramp_gb300 as m
     from ramp_gb300 import _abi, build, instruments as I
-    build.build()
+    if local == 0:            # one build per node; the other ranks wait for it
+        build.build()
+    if world > 1:
+        dist.barrier()
     lib = _abi.load()
     fn, kw = I.path("let_like.json"), I.let_like_kwargs()
     n = a.n
