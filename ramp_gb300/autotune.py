@@ -52,7 +52,7 @@ def _load():
 def _save(cache):
     p = cache_path()
     os.makedirs(os.path.dirname(p), exist_ok=True)
-    tmp = p + ".tmp"
+    tmp = "%s.%d.tmp" % (p, os.getpid())   # ranks of one job may save at once
     with open(tmp, "w") as f:
         json.dump(cache, f, indent=1, sort_keys=True)
     os.replace(tmp, p)
