@@ -1,0 +1,96 @@
+"""Golden instrument parses of the reference's own parser: imports the
+mcramp package of a RAMP checkout with stand-ins for the modules this image
+lacks (pyopencl: buffers keep their host arrays and programs do nothing;
+matplotlib, mcpl, numpy-stl: empty modules; scipy.integrate.simps, removed
+from SciPy: simpson), builds Instrument objects from instrument files of
+this repository and records, per component in the reference's order, the
+name, index, lab position and rotation, and restore flag, plus the block
+structure, in tests/golden/idf_parse.json.  No bytecode is written into the
+checkout.
+
+    python tests/golden/make_idf_golden.py /path/to/RAMP
+"""
+import json
+import os
+import sys
+import types
+
+sys.dont_write_bytecode = True
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+
+
+def cases():
+    """(instrument file, keyword arguments) parsed by both parsers."""
+    from ramp_gb300 import instruments as I
+    G = os.path.join(ROOT, "tests", "golden")
+    return [
+        ("let_like.json", I.path("let_like.json"), I.let_like_kwargs(Ei=4.2, use_slit=1,
+                                                                   slit_w=0.02)),
+        ("powder_reference_example.json", os.path.join(G, "powder_reference_example.json"),
+         dict(Ei=9.09, Mono_angle=0.4637, detector_binning=[50.0, 0.02, 70.0])),
+        ("nonlinear_env.json", os.path.join(G, "nonlinear_env.json"), I.small_chain_kwargs()),
+    ]
+
+
+def stubs():
+    from make_misis_golden import fake_pyopencl
+    fake_pyopencl()
+    cl = sys.modules["pyopencl"]
+    for flag, v in (("READ_WRITE", 4), ("WRITE_ONLY", 8), ("ALLOC_HOST_PTR", 16)):
+        setattr(cl.mem_flags, flag, v)
+    cl.array.vec.float3 = np.dtype([("s0", np.float32), ("s1", np.float32),
+                                    ("s2", np.float32), ("s3", np.float32)])
+    cl.array.zeros = lambda queue, shape, dtype: np.zeros(shape, dtype)
+
+    class CommandQueue:
+        def __init__(self, *a, **k):
+            pass
+    cl.CommandQueue = CommandQueue
+    cl.enqueue_copy = lambda *a, **k: None
+    cl.enqueue_fill_buffer = lambda *a, **k: None
+    for name in ("matplotlib", "matplotlib.pyplot", "mcpl", "stl"):
+        sys.modules[name] = types.ModuleType(name)
+    sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+    sys.modules["stl"].mesh = types.SimpleNamespace(Mesh=None)
+    import scipy.integrate
+    if not hasattr(scipy.integrate, "simps"):
+        scipy.integrate.simps = scipy.integrate.simpson
+
+
+class FakeCtx:
+    devices = [None]
+
+
+def main(ref_root):
+    stubs()
+    sys.path.insert(0, ref_root)
+    import mcramp
+    out = {}
+    for key, fn, kw in cases():
+        inst = mcramp.Instrument(fn, FakeCtx(), None, **kw)
+        blocks = []
+        for b in inst.blocks:
+            comps = []
+            for name, c in b.components.items():
+                comps.append({
+                    "name": name,
+                    "idx": int(c["scat_kernel"].idx) if hasattr(c["scat_kernel"], "idx") else None,
+                    "pos": [float(c["pos"][k]) for k in ("s0", "s1", "s2")],
+                    "rot": [float(c["rot"][k]) for k in ("s0", "s1", "s2")],
+                    "restore": int(c["restore_neutron"]),
+                })
+            blocks.append({"linear": bool(b.linear), "components": comps})
+        out[key] = blocks
+    with open(os.path.join(HERE, "idf_parse.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", os.path.join(HERE, "idf_parse.json"))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

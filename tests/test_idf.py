@@ -102,3 +102,30 @@ def test_execute_without_a_gpu_fails_loudly(tmp_path):
     inst = make(tmp_path)
     with pytest.raises(RuntimeError):
         inst.execute(10)
+
+
+def test_parses_equal_the_reference_parser():
+    """Component order, indices, lab positions and rotations (float32),
+    restore flags and block structure of three instrument files equal the
+    reference parser's own (tests/golden/idf_parse.json, made by
+    tests/golden/make_idf_golden.py running mcramp.Instrument)."""
+    import os
+    import sys
+    gold_dir = os.path.join(os.path.dirname(__file__), "golden")
+    sys.path.insert(0, gold_dir)
+    from make_idf_golden import cases
+    gold = json.load(open(os.path.join(gold_dir, "idf_parse.json")))
+    for key, fn, kw in cases():
+        inst = m.Instrument(fn, "cpu", **kw)
+        want = gold[key]
+        assert [b.linear for b in inst.blocks] == [b["linear"] for b in want]
+        for b, wb in zip(inst.blocks, want):
+            got = list(b.components.items())
+            assert [n for n, _ in got] == [c["name"] for c in wb["components"]]
+            for (name, c), w in zip(got, wb["components"]):
+                assert c["idx"] == w["idx"], (key, name)
+                assert np.array_equal(np.asarray(c["pos"], np.float32),
+                                      np.asarray(w["pos"], np.float32)), (key, name)
+                assert np.array_equal(np.asarray(c["rot"], np.float32),
+                                      np.asarray(w["rot"], np.float32)), (key, name)
+                assert int(c["restore_neutron"]) == w["restore"], (key, name)
