@@ -51,6 +51,11 @@ FUSED_SPLIT2_DRAM_PER_1E7 = (48.59 + 82.98 + 121.37 + 5.09) * 1e6
 # warp instructions issued on 77.4 % of scheduler cycles, 15.8 of 32 lanes
 # active per instruction
 FUSED_SPLIT2_STAGE_A_ISSUE = {"issue_active_pct": 77.4, "threads_per_instruction": 15.8}
+# warp instructions per history of the split launch in that capture
+# (stage A 1.363e9 + stage B 1.136e8 per 1e7 histories): with the live
+# throughput this gives the launch's issue rate against the scheduler peak
+# (4 warp instructions per SM per cycle)
+FUSED_SPLIT2_WARP_INSTR_PER_HISTORY = (1.363146e9 + 1.136426e8) / 1e7
 
 
 def args_():
@@ -371,6 +376,24 @@ def graph_small_n(inst_factory, tune, dev, sizes=(100_000, 1_000_000), reps=20):
     return out
 
 
+def issue_roofline(value, clk, dev, tune):
+    """Warp instructions issued per second by the split fused launch (live
+    histories/s x the profiled instructions per history) against the
+    schedulers' peak at the clock measured during the timed steps."""
+    import torch
+    if int((tune or {}).get("split", 0)) != 2 or not clk.get("sm_mhz"):
+        return None
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak = 4.0 * sms * clk["sm_mhz"] * 1e6
+    achieved = value * FUSED_SPLIT2_WARP_INSTR_PER_HISTORY
+    return {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9,
+            "unit": "G warp instructions/s", "frac": achieved / peak,
+            "instructions_per_history": FUSED_SPLIT2_WARP_INSTR_PER_HISTORY,
+            "source": "instructions per history from the ncu capture of a 1e7-history "
+                      "split launch; peak = 4 per SM per cycle x %d SMs x %.0f MHz"
+                      % (sms, clk["sm_mhz"])}
+
+
 def main():
     a = args_()
     if a.impl == "reference":
@@ -583,6 +606,7 @@ def main():
                      "peak_source": "measured: Threefry-only kernel (ramp_debug_rng_peak), "
                                     "%d threads x %d x 2 blocks" % (out.numel(), iters),
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "issue_roofline": issue_roofline(value, clk, dev, tune),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "histories/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
