@@ -381,9 +381,12 @@ def issue_roofline(value, clk, dev, tune):
     histories/s x the profiled instructions per history) against the
     schedulers' peak at the clock measured during the timed steps."""
     import torch
-    if int((tune or {}).get("split", 0)) != 2 or not clk.get("sm_mhz"):
+    if not isinstance(tune, dict) or int(tune.get("split", 0)) != 2 or not clk.get("sm_mhz"):
         return None
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    try:
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    except (RuntimeError, AssertionError) as e:     # a diagnostic: never lose the line
+        return {"unavailable": str(e)}
     peak = 4.0 * sms * clk["sm_mhz"] * 1e6
     achieved = value * FUSED_SPLIT2_WARP_INSTR_PER_HISTORY
     return {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9,
