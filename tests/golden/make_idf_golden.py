@@ -67,12 +67,31 @@ class FakeCtx:
     devices = [None]
 
 
-def main(ref_root):
-    stubs()
-    sys.path.insert(0, ref_root)
+def example_cases():
+    """The reference's own example instruments (examples/LET.json and
+    TAS.json of the checkout, read from their directory) with the parameters
+    of examples/LET_RAMP.py and TAS_RAMP.py."""
+    h, mn, meV, overAA = 6.62607015e-34, 1.674929e-27, 1.602176634e-22, 1e10
+    mono_d = 3.3539
+    mono_q = 2 * np.pi / mono_d
+    ki = 2 * np.pi / (h / np.sqrt(2 * mn * 5.0 * meV) * overAA)
+    kf = ki
+    rot = 1.3
+    target = [float(np.sin(rot)), 0.0, float(np.cos(rot))]   # frame_rotate([0,0,1], [0,rot,0])
+    return [
+        ("examples/LET.json", "LET.json", dict(v_foc=1000.0, pha_offset=222e-6)),
+        ("examples/TAS.json", "TAS.json",
+         dict(Mono_angle=float(np.arcsin(mono_q / 2.0 / ki)), d_spacing=6.0,
+              Ana_angle=float(np.arcsin(mono_q / 2.0 / kf)), monodspacing=mono_d,
+              sample_target=target, sample_trot=rot)),
+    ]
+
+
+def parse(cases_):
+    """Parses by the reference's mcramp.Instrument (stand-ins installed)."""
     import mcramp
     out = {}
-    for key, fn, kw in cases():
+    for key, fn, kw in cases_:
         inst = mcramp.Instrument(fn, FakeCtx(), None, **kw)
         blocks = []
         for b in inst.blocks:
@@ -87,10 +106,29 @@ def main(ref_root):
                 })
             blocks.append({"linear": bool(b.linear), "components": comps})
         out[key] = blocks
+    return out
+
+
+def main(ref_root):
+    stubs()
+    sys.path.insert(0, ref_root)
+    out = parse(cases())
     with open(os.path.join(HERE, "idf_parse.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(HERE, "idf_parse.json"))
 
 
+def main_examples(ref_root, out_fn):
+    """Parse the checkout's examples (run from its examples directory, where
+    their relative file names resolve) into out_fn."""
+    stubs()
+    sys.path.insert(0, ref_root)
+    with open(out_fn, "w") as f:
+        json.dump(parse(example_cases()), f, indent=1)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 1 and sys.argv[1] == "--examples":
+        main_examples(sys.argv[2], sys.argv[3])
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

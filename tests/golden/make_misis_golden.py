@@ -12,6 +12,8 @@ total, str_area and the time offset in tests/golden/misis_tables.npz.
 import importlib.util
 import os
 import sys
+
+sys.dont_write_bytecode = True   # nothing is written into the checkout
 import tempfile
 import types
 

@@ -10,6 +10,8 @@ tests/golden/powdern_host.npz.
 import os
 import sys
 
+sys.dont_write_bytecode = True   # nothing is written into the checkout
+
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))

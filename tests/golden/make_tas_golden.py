@@ -10,6 +10,8 @@ tests/golden/tas_host.npz.
 import importlib.util
 import os
 import sys
+
+sys.dont_write_bytecode = True   # nothing is written into the checkout
 import types
 
 import numpy as np

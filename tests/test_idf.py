@@ -129,3 +129,46 @@ def test_parses_equal_the_reference_parser():
                 assert np.array_equal(np.asarray(c["rot"], np.float32),
                                       np.asarray(w["rot"], np.float32)), (key, name)
                 assert int(c["restore_neutron"]) == w["restore"], (key, name)
+
+
+def test_reference_examples_parse_and_trace(tmp_path, monkeypatch):
+    """The reference's own example instruments (examples/LET.json with the
+    MISIS moderator and its spectrum file, examples/TAS.json with relative
+    frames and SRescal), read unchanged from a checkout with the parameters
+    of its scripts: our parse equals the reference parser's (run in a
+    subprocess with stand-ins), and the chains trace through the oracle.
+    Skipped without a checkout."""
+    import os
+    import subprocess
+    import sys
+    import oracle
+    from oracle import build as ob
+    ex = os.path.join(ob.REFERENCE, "examples")
+    if not os.path.isdir(ex):
+        pytest.skip("reference checkout not available")
+    gold_dir = os.path.join(os.path.dirname(__file__), "golden")
+    sys.path.insert(0, gold_dir)
+    from make_idf_golden import example_cases
+    out = tmp_path / "examples_parse.json"
+    env = dict(os.environ, PYTHONDONTWRITEBYTECODE="1")
+    subprocess.run([sys.executable, os.path.join(gold_dir, "make_idf_golden.py"), "--examples",
+                    ob.REFERENCE, str(out)], cwd=ex, env=env, check=True)
+    want = json.load(open(out))
+    monkeypatch.chdir(ex)
+    for key, fn, kw in example_cases():
+        inst = m.Instrument(fn, "cpu", **kw)
+        assert [b.linear for b in inst.blocks] == [b["linear"] for b in want[key]]
+        for b, wb in zip(inst.blocks, want[key]):
+            got = list(b.components.items())
+            assert [n for n, _ in got] == [c["name"] for c in wb["components"]]
+            for (name, c), w in zip(got, wb["components"]):
+                assert c["idx"] == w["idx"], (key, name)
+                assert np.array_equal(np.asarray(c["pos"], np.float32),
+                                      np.asarray(w["pos"], np.float32)), (key, name)
+                assert np.array_equal(np.asarray(c["rot"], np.float32),
+                                      np.asarray(w["rot"], np.float32)), (key, name)
+                assert int(c["restore_neutron"]) == w["restore"], (key, name)
+        r = oracle.run(inst, 20_000, seeds=[11])
+        assert r.flags == 0
+        sums = [float(t.sum()) for t in inst.tallies()]
+        assert all(np.isfinite(sums)) and max(sums) > 0, key
