@@ -78,8 +78,13 @@ def example_cases():
     kf = ki
     rot = 1.3
     target = [float(np.sin(rot)), 0.0, float(np.cos(rot))]   # frame_rotate([0,0,1], [0,rot,0])
+    let = dict(v_foc=1000.0, pha_offset=222e-6)
     return [
-        ("examples/LET.json", "LET.json", dict(v_foc=1000.0, pha_offset=222e-6)),
+        ("examples/LET.json", "LET.json", let),
+        # MCPL_test.json gives MFlat a toff_max keyword that MFlat does not
+        # take: both parsers raise TypeError on it
+        ("examples/MCPL_test.json", "MCPL_test.json", let),
+        ("examples/MCPL_testback.json", "MCPL_testback.json", let),
         ("examples/TAS.json", "TAS.json",
          dict(Mono_angle=float(np.arcsin(mono_q / 2.0 / ki)), d_spacing=6.0,
               Ana_angle=float(np.arcsin(mono_q / 2.0 / kf)), monodspacing=mono_d,
@@ -87,19 +92,33 @@ def example_cases():
     ]
 
 
+def component_index(c):
+    """The index the parser gave a component, as its kernels keep it (the
+    reference's SMCPLIn and SMCPLOut do not store theirs; their geometry
+    does)."""
+    for k in ("scat_kernel", "geom_kernel"):
+        if hasattr(c[k], "idx"):
+            return int(c[k].idx)
+    return None
+
+
 def parse(cases_):
     """Parses by the reference's mcramp.Instrument (stand-ins installed)."""
     import mcramp
     out = {}
     for key, fn, kw in cases_:
-        inst = mcramp.Instrument(fn, FakeCtx(), None, **kw)
+        try:
+            inst = mcramp.Instrument(fn, FakeCtx(), None, **kw)
+        except Exception as e:      # the parse fails: record how
+            out[key] = {"error": type(e).__name__}
+            continue
         blocks = []
         for b in inst.blocks:
             comps = []
             for name, c in b.components.items():
                 comps.append({
                     "name": name,
-                    "idx": int(c["scat_kernel"].idx) if hasattr(c["scat_kernel"], "idx") else None,
+                    "idx": component_index(c),
                     "pos": [float(c["pos"][k]) for k in ("s0", "s1", "s2")],
                     "rot": [float(c["rot"][k]) for k in ("s0", "s1", "s2")],
                     "restore": int(c["restore_neutron"]),
