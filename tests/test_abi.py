@@ -53,3 +53,40 @@ def test_invalid_arguments_are_rejected_without_a_gpu(lib):
     assert lib.ramp_plan_create(ctypes.byref(src), None, 0, None, 0, ctypes.byref(out)) == -5
     assert lib.ramp_trace_fused(None, 10, 10, 0, None, None, None, None, None) == -1
     assert lib.ramp_plan_destroy(None) == 0
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "ramp.h"
+int main(void) {
+  RampPlan* plan = NULL;
+  RampSource src;
+  char msg[256];
+  memset(&src, 0, sizeof src);
+  if (ramp_version() != 1) return 1;
+  /* no components and no GPU: an error code, never a crash */
+  int rc = ramp_plan_create(NULL, NULL, 0, NULL, 0, &plan);
+  if (rc >= 0) return 2;
+  ramp_last_error(msg, sizeof msg);
+  printf("%d %zu %zu %s\n", rc, sizeof(RampComp), sizeof(RampSource), msg);
+  return 0;
+}
+"""
+
+
+def test_header_is_plain_c_and_links(lib, tmp_path):
+    """include/ramp.h compiles as C11 (no C++ or torch types) and a C
+    program links against libramp_cuda.so and calls it."""
+    import subprocess
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_abi.LIB_PATH)
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I", os.path.dirname(HEADER),
+                    str(src), "-L", libdir, "-lramp_cuda", "-Wl,-rpath," + libdir, "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert int(out[0]) < 0
+    assert int(out[1]) == ctypes.sizeof(_abi.RampComp)
+    assert int(out[2]) == ctypes.sizeof(_abi.RampSource)
