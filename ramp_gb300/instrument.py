@@ -260,6 +260,39 @@ class Instrument:
             t.zero_()
 
     # ------------------------------------------------------------------
+    # checkpoint / resume (no reference counterpart)
+    # ------------------------------------------------------------------
+    def checkpoint(self):
+        """The state a run resumes from between execute() calls: a host
+        copy of every tally and the state of Python's ``random``, from which
+        execute() draws each chunk's seed (flat_mod.py:32).  Histories are
+        keyed by (chunk seed, index), so a run restored from this state and
+        continued gives the tallies the uninterrupted run would."""
+        import random
+        return {"format": "ramp_gb300 checkpoint 1",
+                "tallies": [t.detach().to("cpu").clone() for t in self.tallies()],
+                "random": random.getstate()}
+
+    def restore(self, state):
+        """Load tallies and the chunk-seed generator from checkpoint()."""
+        import random
+        if state.get("format") != "ramp_gb300 checkpoint 1":
+            raise ValueError("not a ramp_gb300 checkpoint")
+        mine = self.tallies()
+        if len(state["tallies"]) != len(mine) or any(
+                a.shape != b.shape for a, b in zip(state["tallies"], mine)):
+            raise ValueError("the checkpoint's tallies do not match this instrument")
+        for dst, src in zip(mine, state["tallies"]):
+            dst.copy_(src)
+        random.setstate(state["random"])
+
+    def save_checkpoint(self, path):
+        torch.save(self.checkpoint(), path)
+
+    def load_checkpoint(self, path):
+        self.restore(torch.load(path))
+
+    # ------------------------------------------------------------------
     # execution
     # ------------------------------------------------------------------
     def _lib(self):
