@@ -327,8 +327,11 @@ int ramp_trace_fused(RampPlan* plan, int64_t n, int32_t num_sim,
                      void* stream);
 
 /* Batched fused path: n_variants instrument variants with uneven neutron
- * counts in one persistent launch (no reference counterpart: the
- * reference runs one Instrument per execute()).                          */
+ * counts, by default in one launch whose grid row v traces variant v
+ * (RampTune.streams >= 2: one launch per variant over that many streams).
+ * Variant v's histories are keyed by its own index, count and seed, so
+ * each variant's tallies are those of tracing it alone (no reference
+ * counterpart: the reference runs one Instrument per execute()).          */
 int ramp_trace_batched(RampPlan* plan, const RampVariant* variants,
                        int n_variants, const RampRng* rng,
                        const RampTune* tune, void* stream);
