@@ -41,7 +41,8 @@ sys.path.insert(0, HERE)
 
 N_HIST = 100_000_000
 THREEFRY_OPS = 148          # integer operations per Threefry-4x32-20 draw
-CPU_SAMPLE = 2_000_000      # histories per CPU-baseline step
+CPU_CHUNK = 2_000_000       # histories per chunk of a CPU-baseline step
+CPU_SECONDS = 12.0          # CPU work per CPU-baseline step (whole chunks)
 # DRAM bytes (read + write) of one split launch (stage A + stage B, split
 # before chopper 2) per 1e7 histories, from the ncu capture summarised in
 # profiles/let_like_fused_split_1e7.md (49 + 83 MB and 121 + 5 MB); the
@@ -97,22 +98,31 @@ def peaks_file():
 
 
 # ---------------------------------------------------------------- CPU arm
-def cpu_histories_per_s(n, steps=1, warmup=1):
+def cpu_histories_per_s(steps=1, warmup=1, seconds=CPU_SECONDS):
+    """The oracle on every host core over the LET-like chain: one-chunk
+    warm-ups, the last of them timed, size each timed step to about
+    ``seconds`` of work in whole chunks of CPU_CHUNK histories (bounded
+    memory); returns (histories/s of the best step, threads, step times,
+    histories per step)."""
     import oracle
     import ramp_gb300 as m
     from ramp_gb300 import instruments as I
     inst = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
     threads = os.cpu_count() or 1
-    for _ in range(warmup):
-        random.seed(1)
-        oracle.run(inst, n, threads=threads)
+    pilot = None
+    for w in range(max(warmup, 1) + 1):       # the last warm-up chunk is timed
+        random.seed(1 + w)
+        t0 = time.perf_counter()
+        oracle.run(inst, CPU_CHUNK, threads=threads)
+        pilot = time.perf_counter() - t0
+    n = max(1, int(round(seconds / max(pilot, 1e-3)))) * CPU_CHUNK
     times = []
     for k in range(steps):
         random.seed(100 + k)
         t0 = time.perf_counter()
-        oracle.run(inst, n, threads=threads)
+        oracle.run(inst, n, chunk=CPU_CHUNK, threads=threads)
         times.append(time.perf_counter() - t0)
-    return n / min(times), threads, times
+    return n / min(times), threads, times, n
 
 
 def run_reference(a):
@@ -120,16 +130,17 @@ def run_reference(a):
     if rank != 0:
         return
     steps = max(1, a.steps)
-    v, threads, times = cpu_histories_per_s(CPU_SAMPLE, steps=steps, warmup=max(1, min(a.warmup, 2)))
-    sample = ("%d histories of the LET-like chain per step (a bounded sample of the %d-history "
-              "workload), CPU restatement of the reference kernels in reference sequencing "
-              "(5 passes per component, array-of-structs records), OpenMP" % (CPU_SAMPLE, a.n))
+    v, threads, times, ns = cpu_histories_per_s(steps=steps, warmup=max(1, min(a.warmup, 2)))
+    sample = ("%d histories of the LET-like chain per step in chunks of %d (a bounded sample, "
+              "about %.0f s of CPU work, of the %d-history workload), CPU restatement of the "
+              "reference kernels in reference sequencing (5 passes per component, "
+              "array-of-structs records), OpenMP" % (ns, CPU_CHUNK, CPU_SECONDS, a.n))
     line = {"metric": "neutron histories/s", "value": v, "unit": "histories/s",
             "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
             "ms_per_step": 1000.0 * statistics.mean(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": workload_config(CPU_SAMPLE, 1, "CPU restatement, reference sequencing"),
+            "config": workload_config(ns, 1, "CPU restatement, reference sequencing"),
             "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0,
@@ -579,10 +590,11 @@ def main():
         return
     cpu = None
     if not a.no_cpu_baseline:
-        v, threads, _ = cpu_histories_per_s(CPU_SAMPLE, steps=1, warmup=1)
+        v, threads, _, ns = cpu_histories_per_s(steps=1, warmup=1)
         cpu = {"value": v, "unit": "histories/s", "cores": threads, "kind": "port",
-               "sample": "%d LET-like histories, CPU restatement of the reference kernels "
-                         "(reference sequencing), OpenMP, best of 1 after 1 warm-up" % CPU_SAMPLE}
+               "sample": "%d LET-like histories in chunks of %d (about %.0f s of CPU work), "
+                         "CPU restatement of the reference kernels (reference sequencing), "
+                         "OpenMP, after one-chunk warm-ups" % (ns, CPU_CHUNK, CPU_SECONDS)}
     peaks = peaks_file()
     line = {
         "metric": "neutron histories/s", "value": value, "unit": "histories/s",
