@@ -392,17 +392,18 @@ int ramp_forward_record(RampPlan* plan, int32_t det_comp, int64_t n, int32_t num
 
 /* ramp_trace_batched without device allocation.  No counterpart in the
  * reference.  For callers that may not allocate device memory while
- * tracing (a fixed memory budget, an external pool that forbids
- * allocation): the descriptor and variant tables and the status word and
- * per-variant work counters of the one-launch batched kernel (a grid row
- * per variant, no split) live in one fixed file-scope device array (at
- * most 256 variants and 4096 component descriptors, about 2.5 MB per GPU,
- * held until exit) instead of plan-owned buffers.
- * Every variant's tables must already be held by the plan.  The first call
- * on a device resolves the array's address; make it before any stream
- * capture.  Calls share the array, so calls whose kernels overlap on the
- * GPU race; order them on one stream.  Sizes beyond the maximum return
- * RAMP_E_RANGE.                                                           */
+ * tracing (a host loop under a fixed device-memory budget, or one whose
+ * memory comes from an external pool that forbids further allocation):
+ * the descriptor and variant tables and the per-variant work counters of
+ * the one-launch batched kernel (a grid row per variant, no split) live in
+ * one fixed file-scope device array (at most 256 variants and 4096
+ * component descriptors, about 2.5 MB per GPU, held until exit) instead of
+ * plan-owned buffers.  Every variant's tables must already be held by the
+ * plan.  Status flags and dropped tally writes go to the plan's status
+ * word, read by ramp_plan_status.  The first call on a device resolves the
+ * array's address; make it before any stream capture.  Calls share the
+ * array, so calls whose kernels overlap on the GPU race; order them on one
+ * stream.  Sizes beyond the maximum return RAMP_E_RANGE.                  */
 int ramp_trace_batched_noalloc(RampPlan* plan, const RampVariant* variants,
                                int n_variants, const RampRng* rng,
                                const RampTune* tune, void* stream);

@@ -277,6 +277,8 @@ static int get_table(RampPlan* p, const float* host, int64_t len, const float** 
 
 static int lookup_table(RampPlan* p, const float* host, int64_t len, const float** dev,
                         HashMemo* memo);
+static int lookup_bvh(RampPlan* p, const float* pts, int64_t len, const float4** nodes_dev,
+                      const float4** tris_dev, HashMemo* memo);
 
 /* device source descriptor; MISIS tables are uploaded (or, for callers
  * that may not allocate, looked up among the plan's tables) */
@@ -361,8 +363,11 @@ static int get_bvh(RampPlan* p, const float* pts, int64_t len, const float4** no
   return RAMP_OK;
 }
 
-/* Convert one caller descriptor into its device form. */
-static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo = nullptr) {
+/* Convert one caller descriptor into its device form.  Tables (and a mesh's
+ * BVH) are uploaded when the plan does not hold them yet; with may_upload
+ * false they must already be held (callers that may not allocate). */
+static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo = nullptr,
+                     bool may_upload = true) {
   memset(&d, 0, sizeof(d));
   d.geom = c.geom; d.scat = c.scat; d.idx = c.idx; d.restore = c.restore;
   memcpy(d.pos, c.pos, sizeof(d.pos));
@@ -379,14 +384,22 @@ static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo 
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;   /* the BVH replaces the raw points */
-    int rc = get_table(p, c.table[k], c.table_len[k], &d.tab[k], memo);
-    if (rc) return rc;
+    int rc = may_upload ? get_table(p, c.table[k], c.table_len[k], &d.tab[k], memo)
+                        : lookup_table(p, c.table[k], c.table_len[k], &d.tab[k], memo);
+    if (rc) {
+      if (!may_upload)
+        set_err("table %d of a component is not held by the plan (create the plan from a "
+                "variant with the same tables)", k);
+      return rc;
+    }
   }
   d.tally = c.tally;
   d.tally_err = c.tally_err;
   d.tally_len = c.tally_len;
   if (c.geom == RAMP_G_MESH) {
-    int rc = get_bvh(p, c.table[0], c.table_len[0], &d.bvh_nodes, &d.bvh_tris, memo);
+    int rc = may_upload ? get_bvh(p, c.table[0], c.table_len[0], &d.bvh_nodes, &d.bvh_tris, memo)
+                        : lookup_bvh(p, c.table[0], c.table_len[0], &d.bvh_nodes, &d.bvh_tris,
+                                     memo);
     if (rc) return rc;
   }
   return RAMP_OK;
@@ -1243,21 +1256,23 @@ int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out, void* s
 
 /* ======================================================================
  * ramp_trace_batched_noalloc — the batched fused path for callers that
- * must not allocate device memory while they trace (for example a host
- * loop that runs under a strict device-memory budget or an external
- * memory pool that forbids allocation, or a caller preparing work it will
- * later record into a CUDA graph): it uses only memory that already exists.
+ * must not allocate device memory while they trace: a host loop that runs
+ * under a strict device-memory budget, or one whose device memory comes
+ * from an external pool that forbids further allocation.  It uses only
+ * memory that already exists.
  *
  * The per-call scratch of the one-launch batched kernel (the device copies
- * of every variant's component descriptors, the variant table, the status
- * word and the per-variant work-queue counters) lives in the file-scope
- * array below instead of plan-owned buffers that grow with cudaMalloc.  Its
- * size is fixed: RAMP_NOALLOC_MAX_VARIANTS variants and
- * RAMP_NOALLOC_MAX_DESCS component descriptors in total (variants x
- * components), about 2.5 MB, held by every GPU on which the library is
- * loaded until the process exits.  Tables (S(q,w), powder
- * lines, mesh BVHs) must be ones the plan already holds: a variant whose
- * tables differ from every table the plan uploaded is rejected.
+ * of every variant's component descriptors, the variant table and the
+ * per-variant work-queue counters) lives in the file-scope array below
+ * instead of plan-owned buffers that grow with cudaMalloc.  Its size is
+ * fixed: RAMP_NOALLOC_MAX_VARIANTS variants and RAMP_NOALLOC_MAX_DESCS
+ * component descriptors in total (variants x components), about 2.5 MB,
+ * held by every GPU on which the library is loaded until the process
+ * exits.  Tables (S(q,w), powder lines, mesh BVHs) must be ones the plan
+ * already holds: a variant whose tables differ from every table the plan
+ * uploaded is rejected.  Device status flags and dropped tally writes go to
+ * the plan's own status word (allocated with the plan), so
+ * ramp_plan_status reports them as for every other entry point.
  *
  * The first call on a device looks up the device address of the array
  * (cudaGetSymbolAddress, with that device current) and caches it; make that
@@ -1271,8 +1286,6 @@ int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out, void* s
 #define RAMP_NOALLOC_MAX_DESCS 4096
 
 struct NoallocLayout {
-  StatusDev status;
-  unsigned char pad[256 - sizeof(StatusDev)];
   VariantDev variants[RAMP_NOALLOC_MAX_VARIANTS];
   CompDev descs[RAMP_NOALLOC_MAX_DESCS];
   unsigned long long counters[2 * RAMP_NOALLOC_MAX_VARIANTS];   /* per-variant work queues */
@@ -1299,43 +1312,16 @@ static int lookup_table(RampPlan* p, const float* host, int64_t len, const float
   return RAMP_OK;
 }
 
-static int lookup_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo) {
-  memset(&d, 0, sizeof(d));
-  d.geom = c.geom; d.scat = c.scat; d.idx = c.idx; d.restore = c.restore;
-  memcpy(d.pos, c.pos, sizeof(d.pos));
-  rot_matrix(c.rot, d.R);
-  d.rotated = (c.rot[0] != 0.0f || c.rot[1] != 0.0f || c.rot[2] != 0.0f);
-  memcpy(d.gp, c.gp, sizeof(d.gp));
-  memcpy(d.sp, c.sp, sizeof(d.sp));
-  memcpy(d.gi, c.gi, sizeof(d.gi));
-  memcpy(d.si, c.si, sizeof(d.si));
-  for (int k = 0; k < 6; ++k) d.dslot[k] = -1;
-  if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
-  /* chopper slit period 2 pi / n_slits (chopper.cl:21), per component */
-  if (c.scat == RAMP_S_CHOPPER) d.aux[0] = 2.0f * RC_PI / (float)(uint32_t)c.si[0];
-  for (int k = 0; k < RAMP_NTAB; ++k) {
-    d.tab_len[k] = c.table_len[k];
-    if (c.geom == RAMP_G_MESH && k == 0) continue;
-    if (lookup_table(p, c.table[k], c.table_len[k], &d.tab[k], memo)) {
-      set_err("ramp_trace_batched_noalloc: table %d of a variant component is not held by "
-              "the plan (create the plan from a variant with the same tables)", k);
-      return RAMP_E_INVALID;
-    }
+static int lookup_bvh(RampPlan* p, const float* pts, int64_t len, const float4** nodes_dev,
+                      const float4** tris_dev, HashMemo* memo) {
+  TabKey key(1, len, table_hash(pts, len * (int64_t)sizeof(float), memo));
+  auto it = p->tabs.find(key);
+  if (it == p->tabs.end()) {
+    set_err("the mesh of a component is not held by the plan");
+    return RAMP_E_INVALID;
   }
-  d.tally = c.tally;
-  d.tally_err = c.tally_err;
-  d.tally_len = c.tally_len;
-  if (c.geom == RAMP_G_MESH) {
-    TabKey key(1, c.table_len[0],
-               table_hash(c.table[0], c.table_len[0] * (int64_t)sizeof(float), memo));
-    auto it = p->tabs.find(key);
-    if (it == p->tabs.end()) {
-      set_err("ramp_trace_batched_noalloc: mesh of a variant is not held by the plan");
-      return RAMP_E_INVALID;
-    }
-    d.bvh_nodes = (const float4*)it->second.first;
-    d.bvh_tris = (const float4*)it->second.second;
-  }
+  *nodes_dev = (const float4*)it->second.first;
+  *tris_dev = (const float4*)it->second.second;
   return RAMP_OK;
 }
 
@@ -1396,7 +1382,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
         return RAMP_E_INVALID;
       }
       int rc = validate_comp(c, j);
-      if (!rc) rc = lookup_comp(p, c, H.descs[(size_t)v * nc + j], &memo);
+      if (!rc) rc = make_comp(p, c, H.descs[(size_t)v * nc + j], &memo, false);
       if (rc) return rc;
     }
     int rc = make_src(p, V.source, H.variants[v].src, false, &memo);
@@ -1414,7 +1400,6 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
                      cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(D->variants, H.variants, (size_t)n_variants * sizeof(VariantDev),
                      cudaMemcpyHostToDevice, s));
-  CK(cudaMemsetAsync(&D->status, 0, sizeof(StatusDev), s));
   CK(cudaMemsetAsync(D->counters, 0, 2 * (size_t)n_variants * sizeof(unsigned long long), s));
   FusedArgs a;
   memset(&a, 0, sizeof(a));
@@ -1427,7 +1412,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.rng.mode = rng ? rng->mode : 1;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
   a.rng.tid_base = 0u;
-  a.st = &D->status;
+  a.st = p->status;             /* allocated with the plan: read by ramp_plan_status */
   a.workq = D->counters;
   a.workq_b = D->counters + n_variants;
   a.ext = p->ext ? 1 : 0;

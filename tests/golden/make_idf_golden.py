@@ -146,8 +146,16 @@ def main_examples(ref_root, out_fn):
         json.dump(parse(example_cases()), f, indent=1)
 
 
+def reference_root():
+    """The RAMP checkout: the first argument, else $RAMP_REFERENCE."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RAMP_REFERENCE")
+    if not root or not os.path.isdir(os.path.join(root, "mcramp")):
+        raise SystemExit("give the RAMP checkout as the first argument or in RAMP_REFERENCE")
+    return root
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--examples":
         main_examples(sys.argv[2], sys.argv[3])
     else:
-        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+        main(reference_root())

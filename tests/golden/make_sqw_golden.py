@@ -64,5 +64,13 @@ def main(ref_root):
     print("wrote", os.path.join(HERE, "sqw_host.npz"))
 
 
+def reference_root():
+    """The RAMP checkout: the first argument, else $RAMP_REFERENCE."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RAMP_REFERENCE")
+    if not root or not os.path.isdir(os.path.join(root, "mcramp")):
+        raise SystemExit("give the RAMP checkout as the first argument or in RAMP_REFERENCE")
+    return root
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(reference_root())

@@ -384,37 +384,48 @@ def test_autotune_survival_and_split_point(cuda_lib, tmp_path, monkeypatch):
 
 
 # ------------------------------------------------ statistical agreement
-def _chi2_two_sample(h1, e1, h2, e2, min_var=0.0):
+def _chi2_two_sample(h1, e1, h2, e2, min_count=0.0):
     """Two-sample chi-square of weighted histograms (sum p, sum p^2 per bin)
-    over the bins where either has weight."""
+    over the bins whose pooled effective count (h1 + h2)^2 / (e1 + e2)
+    reaches min_count (a cut symmetric in the two samples)."""
     from scipy.stats import chi2
-    use = (e1 + e2) > min_var
-    stat = float((((h1 - h2) ** 2)[use] / (e1 + e2)[use]).sum())
+    v = e1 + e2
+    n_eff = np.where(v > 0, (h1 + h2) ** 2 / np.where(v > 0, v, 1.0), 0.0)
+    use = (v > 0) & (n_eff >= min_count)
+    stat = float((((h1 - h2) ** 2)[use] / v[use]).sum())
     dof = int(use.sum())
     return stat, dof, float(chi2.sf(stat, dof))
 
 
-@pytest.mark.parametrize("fn,kw,N,shape", [
-    ("small_chain.json", "small", 1_000_000, (20, 25, 20, 25)),
-    ("let_like.json", "let", 20_000_000, (72, 10, 1, 1000))])
-def test_fused_agrees_with_oracle_on_independent_streams(cuda_lib, fn, kw, N, shape):
+@pytest.mark.parametrize("fn,kw,N,shape,min_count", [
+    # 500 x 500 (2theta x TOF) detector rebinned to 50 x 50: both axes kept
+    ("small_chain.json", "small", 10_000_000, (50, 10, 50, 10), 5.0),
+    # the LET-like detector at its full 50-us TOF resolution (the axis the
+    # five choppers shape) and 2.5-degree angle bins
+    ("let_like.json", "let", 200_000_000, (72, 10, 1000, 1), 3.0)])
+def test_fused_agrees_with_oracle_on_independent_streams(cuda_lib, fn, kw, N, shape, min_count):
     """Different chunk seeds (independent random streams): the fused GPU
     histogram and the oracle's pass a two-sample chi-square test, p > 0.01,
-    on a coarse rebinning of the detector."""
+    on a two-dimensional (angle x time-of-flight) rebinning of the
+    detector, over the bins with a pooled effective count >= min_count."""
     kws = {"small": I.small_chain_kwargs(), "let": I.let_like_kwargs()}[kw]
     gi = m.Instrument(I.path(fn), "cuda", **kws)
+    chunk = 10_000_000             # the same chunk weights 1/N_chunk on both sides
     random.seed(101)
-    gi.execute(N, path="fused")
+    gi.execute(N, path="fused", chunk=chunk)
     torch.cuda.synchronize()
     ci = m.Instrument(I.path(fn), "cpu", **kws)
     random.seed(202)
-    oracle.run(ci, N)
+    oracle.run(ci, N, chunk=chunk)
     g = [t.double().cpu().numpy() for t in gi.tallies()[-2:]]
     c = [t.double().numpy() for t in ci.tallies()[-2:]]
     a, b, d, e = shape
     rb = lambda x: x.reshape(a, b, d, e).sum(axis=(1, 3))
-    stat, dof, p = _chi2_two_sample(rb(g[0]), rb(g[1]), rb(c[0]), rb(c[1]))
+    stat, dof, p = _chi2_two_sample(rb(g[0]), rb(g[1]), rb(c[0]), rb(c[1]), min_count)
     assert dof > 10 and p > 0.01, (stat, dof, p)
+    # the tested bins span several time-of-flight bins, not one per angle
+    used = np.argwhere(rb(c[0]) > 0)
+    assert len(np.unique(used[:, 1])) > 3
 
 
 # ---------------------------------------------------------------- shards

@@ -8,6 +8,7 @@ Kept in a file of its own, collected last, and self-contained, so that it
 runs the same alone in a fresh process and after the other GPU tests.
 """
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -19,6 +20,7 @@ from ramp_gb300 import _abi, instruments as I
 pytestmark = pytest.mark.gpu
 
 U32 = 2.0 ** -24
+GOLD_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def assert_tallies_match(a_inst, b_inst):
@@ -86,3 +88,39 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(cuda_lib):
     rc = lib.ramp_trace_batched_noalloc(plan, arr, 257, ctypes.byref(rng), None, None)
     assert rc == -6
     assert "exceed the fixed scratch" in _abi.last_error(lib)
+
+
+def plan_status(lib, plan):
+    flags, oob = ctypes.c_uint32(), ctypes.c_uint64()
+    _abi.check(lib, lib.ramp_plan_status(plan, ctypes.byref(flags), ctypes.byref(oob)),
+               "ramp_plan_status")
+    return flags.value, oob.value
+
+
+def test_noalloc_reports_device_status_through_the_plan(cuda_lib):
+    """A chain whose monitors drop out-of-range tally writes: the drops
+    counted by the no-allocation entry point reach ramp_plan_status, as
+    those of the allocating entry point do, on two calls in a row."""
+    lib = cuda_lib
+    fn = os.path.join(GOLD_DIR, "guides_monitors.json")
+    kw = I.small_chain_kwargs()
+    A = m.Instrument(fn, "cuda", **kw)
+    B = m.Instrument(fn, "cuda", **kw)
+    plan_a, plan_b = A.plan(), B.plan()
+    va, keep_a = variants_of([A, A], [100_000, 60_001], [5, 9])
+    vb, keep_b = variants_of([B, B], [100_000, 60_001], [5, 9])
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    plan_status(lib, plan_a)
+    plan_status(lib, plan_b)
+    for _ in range(2):
+        rng = _abi.RampRng(0, 0, 0, 0)
+        _abi.check(lib, lib.ramp_trace_batched(plan_a, va, 2, ctypes.byref(rng), None, stream),
+                   "ramp_trace_batched")
+        _abi.check(lib, lib.ramp_trace_batched_noalloc(plan_b, vb, 2, ctypes.byref(rng), None,
+                                                       stream), "ramp_trace_batched_noalloc")
+        fa, oa = plan_status(lib, plan_a)
+        fb, ob = plan_status(lib, plan_b)
+        assert oa > 0
+        assert (fb, ob) == (fa, oa)
+        assert fb & _abi.F_WORKQ == 0
+    assert_tallies_match(A, B)
