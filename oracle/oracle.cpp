@@ -24,10 +24,12 @@
  *
  * Parity pins: the RNG (Threefry-4x32-20 and u01 conversion, rand.h) and
  * the supermirror reflectivity (include/ref.h) are checked against the
- * reference's own sources compiled with gcc (oracle/ref_pins); the other
- * kernels have no reference outputs to check against (the reference's
- * OpenCL path cannot run in this environment), so their parity against
- * the running reference is unpinned.
+ * reference's own sources compiled with gcc (oracle/ref_pins), and every
+ * kernel restated here against the reference's own .cl kernels compiled as
+ * host C++ and run with the reference sequencing (oracle/refcl): with the
+ * same math library the final records are bit-identical on every chain the
+ * tests trace; the committed golden records (tests/golden/
+ * refcl_records.npz) carry that pin where the reference is absent.
  *
  * Build: g++ -O2 -fopenmp -ffp-contract=off -shared -fPIC (oracle/build.py)
  */
@@ -533,7 +535,9 @@ void g_sphere_int(float* n, float* s, uint32_t* iidx, const RampComp& k) {
   }
 }
 
-/* intersect_box — mcramp/geom/box.cl:3-53 (no earliest-hit comparison) */
+/* intersect_box — mcramp/geom/box.cl:3-53 (no earliest-hit comparison).
+ * The kernel never loads the intersection record (box.cl:10) and writes
+ * its local copy back on a miss too (:52): uninitialised, read as zeros. */
 void g_box(float* n, float* s, uint32_t* iidx, const RampComp& k) {
   V3 pos = npos(n), vel = nvel(n);
   V3 A = v3(-k.gp[0] / 2.0f, -k.gp[1] / 2.0f, -k.gp[2] / 2.0f);
@@ -543,8 +547,8 @@ void g_box(float* n, float* s, uint32_t* iidx, const RampComp& k) {
   float t4 = dB.y / vel.y, t5 = dA.z / vel.z, t6 = dB.z / vel.z;
   float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
   float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
-  if (tmax < 0.0f) {
-  } else if (tmin > tmax) {
+  if (tmax < 0.0f || tmin > tmax) {
+    for (int q = 0; q < 8; ++q) s[q] = 0.0f;
   } else {
     V3 p1 = add(pos, mul(tmin, vel)), p2 = add(pos, mul(tmax, vel));
     s[0] = p1.x; s[1] = p1.y; s[2] = p1.z; s[3] = tmin;

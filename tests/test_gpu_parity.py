@@ -22,11 +22,13 @@ from ramp_gb300 import _abi, instruments as I
 from ramp_gb300.batch import BatchedInstrument
 
 from helpers import U32, _Host, records_equal, tallies_close  # noqa: F401
+from tests_chains import GOLDEN_CHAINS, chain
 
 pytestmark = pytest.mark.gpu
 
 GOLD_DIR = os.path.join(os.path.dirname(__file__), "golden")
 GOLD = np.load(os.path.join(GOLD_DIR, "ref_pins.npz"))
+REFCL = np.load(os.path.join(GOLD_DIR, "refcl_records.npz"))
 
 
 def pair(fn, kw, N, path="plain", rng="reference", chunk=None, seed=1234, tune=None):
@@ -49,6 +51,24 @@ def check_plain(fn, kw, N, **k):
     assert gi.oob_drops == r.oob
     assert gi.status_flags == r.flags
     return gi, ci, r
+
+
+# ------------------------------------------------ the reference's kernels
+@pytest.mark.parametrize("key", GOLDEN_CHAINS)
+def test_plain_path_equals_reference_kernel_golden_records(cuda_lib, key):
+    """The plain path against the reference's own kernels (compiled from
+    its OpenCL sources on the host with the shared math library,
+    tests/golden/make_refcl_golden.py): final records and index buffer of
+    1000 seeded histories, bit for bit."""
+    fn, kw = chain(key)
+    gi = m.Instrument(fn, "cuda", **kw)
+    seed = int(REFCL["seed"])
+    gi.source.next_seed = lambda: seed
+    gi.execute(int(REFCL["n"]), path="plain")
+    torch.cuda.synchronize()
+    recs, iidx = gi.neutron_state()
+    records_equal(recs, REFCL["%s/rmath/records" % key])
+    assert np.array_equal(iidx, REFCL["%s/rmath/iidx" % key])
 
 
 # ---------------------------------------------------------------- RNG / math

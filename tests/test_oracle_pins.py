@@ -64,3 +64,40 @@ def test_live_reference_pins_when_available():
     ref = np.zeros_like(c0)
     P.ref_pin_threefry(c0.ctypes.data, tid.ctypes.data, ref.ctypes.data, c0.size)
     assert np.array_equal(oracle.threefry(c0, tid), ref)
+
+
+# ------------------------------------------------ the reference's kernels
+REFCL = np.load(os.path.join(os.path.dirname(__file__), "golden", "refcl_records.npz"))
+REFCL_CHAINS = sorted({k.split("/")[0] for k in REFCL.files if "/" in k})
+
+
+@pytest.mark.parametrize("key", REFCL_CHAINS)
+def test_oracle_equals_reference_kernel_golden_records(key):
+    """Final records of 1000 seeded histories of each chain, as the
+    reference's own kernels compute them with the shared math library
+    (tests/golden/make_refcl_golden.py): the oracle gives the same bits."""
+    import ramp_gb300 as m
+    from helpers import records_equal
+    from tests_chains import chain
+    fn, kw = chain(key)
+    r = oracle.run(m.Instrument(fn, "cpu", **kw), int(REFCL["n"]), seeds=[int(REFCL["seed"])])
+    records_equal(r.neutrons, REFCL["%s/rmath/records" % key])
+    assert np.array_equal(r.iidx, REFCL["%s/rmath/iidx" % key])
+
+
+@pytest.mark.parametrize("key", ["small_chain", "let_like"])
+def test_oracle_within_1e5_of_reference_kernels_with_the_c_math_library(key):
+    """The same chains through the reference kernels built with the C
+    library's math: same branches, vectors and times within 1e-5."""
+    import ramp_gb300 as m
+    from tests_chains import chain
+    fn, kw = chain(key)
+    r = oracle.run(m.Instrument(fn, "cpu", **kw), int(REFCL["n"]), seeds=[int(REFCL["seed"])])
+    x = r.neutrons.astype(np.float64)
+    y = REFCL["%s/libm/records" % key].astype(np.float64)
+    assert np.array_equal(r.iidx, REFCL["%s/libm/iidx" % key])
+    assert np.array_equal(x[:, [11, 12, 15]], y[:, [11, 12, 15]])
+    for lo in (0, 3, 6):
+        d = np.linalg.norm(x[:, lo:lo + 3] - y[:, lo:lo + 3], axis=1)
+        assert (d <= 1e-5 * np.linalg.norm(x[:, lo:lo + 3], axis=1)).all()
+    assert (np.abs(x[:, 10] - y[:, 10]) <= 1e-5 * np.abs(x[:, 10])).all()

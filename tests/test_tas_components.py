@@ -82,9 +82,11 @@ def test_reference_powder_example_peak():
     """The reference's powder example (its parameters in
     tests/golden/powder_reference_example.json): PG(002) at the Bragg angle
     for 3 AA, a d = 3 AA powder line, so the nominal peak is 2theta = 60 deg.
-    The oracle puts the fitted centre at 60.05 deg (sigma 1.07 deg) at 1e7
-    histories; the reference's notebooks record 60.37 deg (sigma 1.02 deg)
-    from an older run that cannot be repeated here."""
+    The fitted centre is 60.05 deg (sigma 1.07 deg) at 4e5 histories: what
+    the reference's own present kernels give for its own doc/user/powder.json
+    (tests/test_reference_kernels.py runs them); the notebook outputs'
+    60.37 deg come from a run that the present kernels and files do not
+    reproduce."""
     import oracle
     from scipy.optimize import curve_fit
     h, mn, meV = 6.62607015e-34, 1.674929e-27, 1.602176634e-22
