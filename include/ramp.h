@@ -234,6 +234,21 @@ typedef struct RampTune {
                                    waiting neutron (buffer as for
                                    `split`).  Ignored without such a
                                    component.                            */
+  int32_t regroup;              /* fused path with a split: 1 + index of
+                                   a guide component of a linear block
+                                   before the split point (0: off;
+                                   ignored by a mesh walk, by chains with
+                                   an extended kind and by
+                                   ramp_trace_batched_noalloc).  Each warp
+                                   traces its work item (128 neutrons)
+                                   up to that guide, holds them in
+                                   shared memory (52 KB per CTA) and
+                                   takes them 32 at a time in order of
+                                   the guide's expected bounce passes,
+                                   so a warp's lanes leave the bounce
+                                   loop together.  Traces are unchanged;
+                                   only the order of tally additions
+                                   differs.                              */
 } RampTune;
 
 typedef struct RampPlan RampPlan;

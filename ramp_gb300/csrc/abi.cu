@@ -630,6 +630,31 @@ static int tune_stage(const RampPlan* p, const RampTune* tune, bool ext, int32_t
   return tune_split(p, tune, split);
 }
 
+/* the regroup point of a fused launch (RampTune.regroup = 1 + index of a
+ * guide component): in a linear block and before the launch's stage
+ * split (regrouping is a form of stage A; a mesh walk launch ignores it) */
+static int tune_regroup(const RampPlan* p, const RampTune* tune, int32_t split, int32_t* out) {
+  *out = 0;
+  if (!tune || tune->regroup <= 0) return RAMP_OK;
+  const int g = tune->regroup - 1;
+  if (g >= (int)p->comps.size() || p->comps[g].scat != RAMP_S_GUIDE) {
+    set_err("RampTune.regroup %d: component %d is not a guide", tune->regroup, g);
+    return RAMP_E_INVALID;
+  }
+  if (split <= 0 || g >= split) {
+    set_err("RampTune.regroup %d: regrouping is part of stage A: it needs a split after the "
+            "guide (split %d)", tune->regroup, split);
+    return RAMP_E_INVALID;
+  }
+  for (const RampBlock& B : p->blocks)
+    if (!B.linear && B.first <= g && g < B.first + B.count) {
+      set_err("RampTune.regroup %d: the guide is inside a non-linear block", tune->regroup);
+      return RAMP_E_INVALID;
+    }
+  *out = g + 1;
+  return RAMP_OK;
+}
+
 /* survivor buffer for split launches covering up to n_items work items
  * of 128 neutrons: SURV_WORDS words per slot plus one count per item
  * (grows, never shrinks) */
@@ -804,6 +829,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.workq = &p->status->workq;
   a.workq_b = &p->status->workq_b;
   int rc = tune_stage(p, tune, p->ext, &a.split, &a.walk);
+  if (!rc && !p->ext) rc = tune_regroup(p, tune, a.split, &a.regroup);
   if (rc) return rc;
   a.ext = p->ext ? 1 : 0;
   if (a.split > 0 || a.walk) {
@@ -837,6 +863,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
      buffer (its items' slots, SoA, and its items' counts) */
   int32_t split = 0, walk = 0;
   int rc0 = tune_stage(p, tune, base.ext != 0, &split, &walk);
+  if (!rc0 && !base.ext) rc0 = tune_regroup(p, tune, split, &base.regroup);
   if (rc0) return rc0;
   std::vector<int64_t> item_off(nv + 1, 0);
   for (size_t v = 0; v < nv; ++v)
@@ -1035,6 +1062,8 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.split = split;
   a.walk = walk;
   a.ext = ext ? 1 : 0;
+  if (!ext) rc = tune_regroup(p, tune, split, &a.regroup);
+  if (rc) return rc;
   if (a.split > 0 || a.walk) {
     rc = attach_surv(p, a, items, s);
     if (rc) return rc;

@@ -707,12 +707,30 @@ DI int guide_pass(const CompDev& c, Nt& n, uint32_t& i, int& guard, StatusDev* s
   float vdotn_v1 = bv + av, vdotn_v2 = bv - av, vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
   float cv1 = Av - n.z * ww, cv2 = n.x * l;
   float ch1 = Ah - n.z * hh, ch2 = n.y * l;
-  float t1 = (l - n.z) / n.vz, t2;
+  float t1 = (l - n.z) / n.vz;
   i = 0;
-  if (vdotn_v1 < 0.0f && (t2 = (cv1 - cv2) / vdotn_v1) < t1) { t1 = t2; i = 1; }
-  if (vdotn_v2 < 0.0f && (t2 = (cv1 + cv2) / vdotn_v2) < t1) { t1 = t2; i = 2; }
-  if (vdotn_h1 < 0.0f && (t2 = (ch1 - ch2) / vdotn_h1) < t1) { t1 = t2; i = 3; }
-  if (vdotn_h2 < 0.0f && (t2 = (ch1 + ch2) / vdotn_h2) < t1) { t1 = t2; i = 4; }
+  /* The four wall tests of guide.cl:66-85 in their order.  Of each pair of
+     opposite walls one approaches the neutron (both only in a narrowing
+     guide): its division is selected first and done by every lane, so a
+     warp whose neutrons fly left and right divides once, not twice. */
+  const bool v1 = vdotn_v1 < 0.0f, v2 = vdotn_v2 < 0.0f;
+  if (v1 || v2) {
+    const float tv = (v1 ? (cv1 - cv2) : (cv1 + cv2)) / (v1 ? vdotn_v1 : vdotn_v2);
+    if (tv < t1) { t1 = tv; i = v1 ? 1u : 2u; }
+    if (v1 && v2) {
+      const float tw = (cv1 + cv2) / vdotn_v2;
+      if (tw < t1) { t1 = tw; i = 2; }
+    }
+  }
+  const bool h1 = vdotn_h1 < 0.0f, h2 = vdotn_h2 < 0.0f;
+  if (h1 || h2) {
+    const float th = (h1 ? (ch1 - ch2) : (ch1 + ch2)) / (h1 ? vdotn_h1 : vdotn_h2);
+    if (th < t1) { t1 = th; i = h1 ? 3u : 4u; }
+    if (h1 && h2) {
+      const float tw = (ch1 + ch2) / vdotn_h2;
+      if (tw < t1) { t1 = tw; i = 4; }
+    }
+  }
   if (i == 0) return 0;
   n.x = n.x + t1 * n.vx; n.y = n.y + t1 * n.vy; n.z = n.z + t1 * n.vz;
   n.t += t1;
@@ -766,6 +784,34 @@ DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
   }
   if (k < 0) return;
   s_guide_end(c, n, s, ii, i);
+}
+
+/* Expected passes of guide c's bounce loop for a neutron about to reach it:
+ * a grouping key for the fused path (which neutrons share a warp), never a
+ * value of the trace.  In the guide's frame the neutron crosses the
+ * entrance plane at (x0, y0); unfolding the walls of a straight guide of
+ * width w, it leaves after |floor(u / w)| reflections in x, u = x0 + w/2 +
+ * l vx/vz, and likewise in y.  A reflection with zero reflectivity (q
+ * beyond m Qc + 10 W, q = 2 V2K |v| for the walls of a straight guide) ends
+ * the loop at the first wall.  0: the neutron misses the entrance. */
+DI uint32_t guide_passes_key(const CompDev& c, const Nt& n0) {
+  Nt n = n0;
+  transform<false>(c, n);
+  if (!(n.vz > 0.0f)) return 0u;
+  const float w = c.sp[0], h = c.sp[1], l = c.sp[4];
+  const float ivz = __frcp_rn(n.vz);
+  const float t0 = -n.z * ivz;
+  const float x0 = n.x + t0 * n.vx, y0 = n.y + t0 * n.vy;
+  if (!(fabsf(x0) < 0.5f * w && fabsf(y0) < 0.5f * h)) return 0u;
+  const float ux = (x0 + 0.5f * w + l * n.vx * ivz) / w;
+  const float uy = (y0 + 0.5f * h + l * n.vy * ivz) / h;
+  const float nx = fabsf(floorf(ux)), ny = fabsf(floorf(uy));
+  const float W = c.aux[9];
+  const float qcut = (W > 0.0f && c.aux[15] == 0.0f) ? c.aux[12] + 10.0f * W : -1.0f;
+  const bool kx = nx > 0.0f && 2.0f * RC_V2K * fabsf(n.vx) > qcut;
+  const bool ky = ny > 0.0f && 2.0f * RC_V2K * fabsf(n.vy) > qcut;
+  const float passes = (kx || ky) ? 2.0f : 1.0f + fminf(nx + ny, 60.0f);
+  return (uint32_t)passes;
 }
 
 /* chopper.cl:4-59 */
