@@ -9,6 +9,7 @@ from .geom import (GPrim, GPlane, GCylinderExt, GBanana, GSphere, GSphereInt, GB
 from .scat import (SPrim, SArm, SBeamstop, SGuide, SChopper, SIsotropic, SPowderN,
                    SDetector1D, SDetector2D, SCounter, SAttenuate, SMonochromator, SPowder1,
                    SRescal, SMCPLOut, SMCPLIn)
-from .instrument import Instrument, ExecutionBlock, KernelRef, frame_rotate, build_kernel
+from .instrument import Instrument, frame_rotate, build_kernel
+from .idf import Block
 
 __version__ = "0.1.0"

@@ -1,30 +1,22 @@
-"""Instrument facade and instrument-definition-file (IDF) parser.
+"""Instrument facade (mcramp/mcramp.py:254-455).
 
-Mirrors mcramp/mcramp.py (Instrument 254-455, ExecutionBlock 35-251,
-frame_rotate 457-476): the same JSON grammar ($expr$ substitution evaluated
-with eval, // comments, "disable", "relative", "restore_neutron",
-"visualise", block "linear"/"multi"), the same component index assignment
-(the first index is 1 and every component, the source included, takes one),
-the same chunking (chunk = max_mem_alloc / 256 neutrons, a
-random.randint(0, 4096) seed per chunk, weights 1/N_chunk) and the same
-results API (data, save, plot).  Execution goes through libramp_cuda.so:
+The instrument file is read by ramp_gb300.idf (the reference's IDF grammar
+and index rules); this module keeps the reference's chunking (chunk =
+max_mem_alloc / 256 neutrons, a random.randint(0, 4096) seed per chunk,
+weights 1/N_chunk) and its results API (data, save, plot).  Execution goes through libramp_cuda.so:
 ``path="plain"`` launches one kernel per component (the reference's call
 structure), ``path="fused"`` runs the whole chain in one persistent kernel.
 There is no CPU fallback: without a CUDA device or without the library,
 execute() raises.
 """
-import importlib
-import json
 import logging
-import os
-import re
 import warnings
-from collections import OrderedDict
 
 import numpy as np
 import torch
 
-from . import _abi
+from . import _abi, idf
+from .idf import frame_rotate  # noqa: F401  (module-level API, mcramp.py:457)
 from .shard import chunk_slices
 from .scat.sprim import _device
 
@@ -37,100 +29,6 @@ def build_kernel(filename, ctx=None):
     reuse the built-in kernels through their descriptor slots."""
     raise NotImplementedError("OpenCL kernels are not supported; ramp_gb300 runs built-in "
                               "CUDA kernels selected by the plugin's descriptor kind")
-
-
-def frame_rotate(vec, rot):
-    """Rotate vec by Euler angles rot = [x, y, z] (mcramp.py:457-476)."""
-    x_a, y_a, z_a = rot[0], rot[1], rot[2]
-    r00 = np.cos(y_a) * np.cos(z_a)
-    r01 = -np.cos(x_a) * np.sin(z_a) + np.sin(x_a) * np.sin(y_a) * np.cos(z_a)
-    r02 = np.sin(x_a) * np.sin(z_a) + np.cos(x_a) * np.sin(y_a) * np.cos(z_a)
-    r10 = np.cos(y_a) * np.sin(z_a)
-    r11 = np.cos(x_a) * np.cos(z_a) + np.sin(x_a) * np.sin(y_a) * np.sin(z_a)
-    r12 = -np.sin(x_a) * np.cos(z_a) + np.cos(x_a) * np.sin(y_a) * np.sin(z_a)
-    r20 = -np.sin(y_a)
-    r21 = np.sin(x_a) * np.cos(y_a)
-    r22 = np.cos(x_a) * np.cos(y_a)
-    return [np.dot([r00, r01, r02], vec), np.dot([r10, r11, r12], vec),
-            np.dot([r20, r21, r22], vec)]
-
-
-def _resolve(name):
-    """Plugin class lookup (mcramp.py:80-92): built-ins first, then a module
-    of the same name on sys.path (user plugins)."""
-    pkg = importlib.import_module(__package__)
-    try:
-        return getattr(pkg, name)
-    except AttributeError:
-        return getattr(importlib.import_module(name), name)
-
-
-class KernelRef:
-    def __init__(self, block, comp, pos, rot, vis):
-        self.block = block
-        self.comp = comp
-        self.pos = pos
-        self.rot = rot
-        self.vis = vis
-        self.comp_name = self.comp["name"]
-
-
-class ExecutionBlock:
-    def __init__(self, source, components, parent, linear, max_events):
-        self.source = source
-        self.max_events = max_events
-        self.linear = linear
-        self.components = components
-        self.parent = parent
-
-    @staticmethod
-    def fromJSON(block, parent, linear, events, idx):
-        comps = OrderedDict()
-        source = None
-        for (name, comp) in block.items():
-            if name == "linear" or name == "multi":
-                continue
-            if "disable" in comp and comp["disable"]:
-                continue
-            if "source" in comp:
-                mk = _resolve(comp['moderator_kernel']['name'])
-                args = {k: v for (k, v) in comp['moderator_kernel'].items() if not k == 'name'}
-                args['ctx'] = parent.device
-                source = mk(**args)
-            else:
-                pos = comp['position'] if 'position' in comp else [0, 0, 0]
-                rot = comp['rotation'] if 'rotation' in comp else [0, 0, 0]
-                vis = comp['visualise'] if 'visualise' in comp else True
-                restore_neutron = comp['restore_neutron'] if 'restore_neutron' in comp else False
-                if 'relative' in comp:
-                    rcomp = comps[comp['relative']]
-                    rpos, rrot = rcomp["pos"], rcomp["rot"]
-                    pos = frame_rotate(pos, [rrot[0], rrot[1], rrot[2]])
-                    pos = np.add(pos, [rpos[0], rpos[1], rpos[2]])
-                    rot = np.add(rot, [rrot[0], rrot[1], rrot[2]])
-                gk = _resolve(comp['geom_kernel']['name'])
-                gargs = {k: v for (k, v) in comp['geom_kernel'].items() if not k == 'name'}
-                gargs['idx'] = parent.idx
-                gargs['ctx'] = parent.device
-                sk = _resolve(comp['scat_kernel']['name'])
-                sargs = {k: v for (k, v) in comp['scat_kernel'].items() if not k == 'name'}
-                sargs['idx'] = parent.idx
-                sargs['ctx'] = parent.device
-                sargs['inst'] = parent
-                sargs['block'] = idx
-                comps[name] = {
-                    "name": name,
-                    "geom_kernel": gk(**gargs),
-                    "scat_kernel": sk(**sargs),
-                    "restore_neutron": np.uint32(1) if restore_neutron else np.uint32(0),
-                    "pos": np.array((pos[0], pos[1], pos[2]), dtype=np.float32),
-                    "rot": np.array((rot[0], rot[1], rot[2]), dtype=np.float32),
-                    "vis": vis,
-                    "idx": int(parent.idx),
-                }
-                parent.kernel_refs.append(KernelRef(idx, comps[name], pos, rot, vis))
-            parent.idx += 1
-        return ExecutionBlock(source, comps, parent, linear, events)
 
 
 class Instrument:
@@ -153,10 +51,8 @@ class Instrument:
         self.ctx = ctx
         self.queue = queue
         self.device = _device(ctx)
-        self.kernel_refs = []
-        self.idx = 1
         self.fn = fn
-        self.blocks = self._fromJSON(fn, ctx, queue, **kwargs)
+        self.blocks = idf.load(fn, self, self.device, kwargs)
         self._plan = None
         self._keep = []
         self.state = None
@@ -164,40 +60,6 @@ class Instrument:
         self.last_chunk = 0
         self.oob_drops = 0
         self.status_flags = 0
-
-    # ------------------------------------------------------------------
-    # IDF
-    # ------------------------------------------------------------------
-    def _substitute_params(self, json_str, **kwargs):
-        # as the reference (mcramp.py:328-355): a token that contains another
-        # variable name as a substring is substituted textually
-        pattern = r"(?:\$)(.*?)(?:\$)"
-        tokens = re.findall(pattern, json_str)
-        for t in tokens:
-            subbed_t = t
-            for key, value in kwargs.items():
-                subbed_t = subbed_t.replace("{}".format(key), str(value))
-            json_str = json_str.replace("${}$".format(t), str(eval(subbed_t)))
-        split_str = json_str.split("\n")
-        for line_num, line in enumerate(split_str):
-            if '//' in line:
-                split_str[line_num] = line.split("//", 1)[0]
-        return '\n'.join(split_str)
-
-    def _fromJSON(self, fn, ctx, queue, **kwargs):
-        with open(fn, 'r') as f:
-            json_str = self._substitute_params(f.read(), **kwargs)
-        inst = json.loads(json_str, object_pairs_hook=OrderedDict)
-        blocks = []
-        for i, block in enumerate(inst.values()):
-            if "linear" in block:
-                linear = block["linear"]
-                events = block["multi"] if (not linear and "multi" in block) else 1
-            else:
-                linear = True
-                events = 1
-            blocks.append(ExecutionBlock.fromJSON(block, self, linear, events, i))
-        return blocks
 
     @property
     def source(self):
@@ -242,7 +104,7 @@ class Instrument:
             b.first = first
             b.count = len(comps) - first
             b.linear = 1 if block.linear else 0
-            b.multi = int(block.max_events)
+            b.multi = int(block.multi)
             blocks.append(b)
         carr = (_abi.RampComp * max(1, len(comps)))(*comps)
         barr = (_abi.RampBlock * max(1, len(blocks)))(*blocks)
@@ -530,17 +392,17 @@ class Instrument:
     # ------------------------------------------------------------------
     def data(self):
         """name -> data of every component (mcramp.py:281-293)."""
-        return {d.comp_name: d.comp["scat_kernel"].data(self.queue) for d in self.kernel_refs}
+        return {name: comp["scat_kernel"].data(self.queue) for name, comp in self.components()}
 
     def plot(self):
         from matplotlib.pyplot import show
-        for d in self.kernel_refs:
-            d.comp["scat_kernel"].plot(self.queue)
+        for _, comp in self.components():
+            comp["scat_kernel"].plot(self.queue)
         show()
 
     def save(self):
-        for d in self.kernel_refs:
-            d.comp["scat_kernel"].save(self.queue)
+        for _, comp in self.components():
+            comp["scat_kernel"].save(self.queue)
 
     def visualise(self, *args, **kwargs):
         raise NotImplementedError("instrument visualisation is not part of ramp_gb300")
