@@ -443,6 +443,26 @@ int ramp_debug_math(int fn, const float* a_dev, const float* b_dev,
 int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out_dev,
                         void* stream);
 
+/* Measurement kernels for the rooflines: the L2 read bandwidth (n_threads
+ * threads, a multiple of 256, each read `iters` (even) float4 of buf, len
+ * floats with len/4 a power of two, through loads that bypass L1; out
+ * receives n_threads floats) and the L2 float-atomic throughput (n_threads
+ * threads each add 1 to `iters` bins of an n_bins histogram, n_bins a power
+ * of two, a warp's lanes to one 128-byte line).                         */
+int ramp_debug_l2_peak(const float* buf, int64_t len, int64_t n_threads, int32_t iters,
+                       float* out, void* stream);
+int ramp_debug_atomic_peak(float* bins, int64_t n_bins, int64_t n_threads, int32_t iters,
+                           void* stream);
+
+/* Host helper (no GPU): the hierarchy the plan builds for a GMesh over
+ * pts[n_tri*9], walked for n_rays rays (6 floats each: position and
+ * velocity in the mesh frame) as a walk that needs every crossing reads
+ * it: out[0] inner nodes read (64 bytes each), out[1] triangles read (48
+ * bytes each), out[2] rays meeting the mesh box.  The algorithmic L2
+ * bytes of the mesh imaging roofline.                                   */
+int ramp_bvh_walk_counts(const float* pts, int64_t n_tri, const float* rays, int64_t n_rays,
+                         int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

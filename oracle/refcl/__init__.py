@@ -20,10 +20,19 @@ _libs = {}
 
 
 def available():
-    """The reference's kernels can be built: from the checkout, or from the
-    sources generated from it into oracle/_ref/refcl_src."""
-    return (os.path.isdir(os.path.join(_build.reference_root(), "mcramp")) or
-            _build.generated_sources_present())
+    """The reference's kernels can be built here: from the checkout, or from
+    the sources generated from it into oracle/_ref/refcl_src, on a machine
+    whose architecture the reference's Random123 accepts."""
+    return _build.supported_here() and (
+        os.path.isdir(os.path.join(_build.reference_root(), "mcramp")) or
+        _build.generated_sources_present())
+
+
+def unavailable_reason():
+    import platform
+    if not _build.supported_here():
+        return _build.UNSUPPORTED_REASON % platform.machine()
+    return "no reference checkout and no sources generated from one"
 
 
 def checkout_available():

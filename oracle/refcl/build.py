@@ -24,9 +24,11 @@ oracle/refcl/clshim.h and the sequencing driver oracle/refcl/driver.cpp:
 Both use g++ -fsingle-precision-constant (unsuffixed constants are float, as
 on an OpenCL device without cl_khr_fp64) and -ffp-contract=off.  Nothing is
 built where neither the checkout nor the generated sources exist (none of
-these files is committed).
+these files is committed), nor on machines other than x86 and powerpc, where
+the reference's vendored Random123 headers stop the compilation.
 """
 import os
+import platform
 import re
 import shutil
 import subprocess
@@ -96,7 +98,21 @@ def _generate(root, force):
                 os.replace(dst + ".tmp", dst)
 
 
+def supported_here():
+    """The reference vendors Random123, whose compiler-feature header stops
+    the build on machines other than x86 and powerpc (features/
+    gccfeatures.h:37-40): on others (the aarch64 GPU hosts) nothing is
+    built and the checker falls back to the oracle alone."""
+    return platform.machine().lower() in ("x86_64", "amd64", "i386", "i686", "ppc64le", "ppc64")
+
+
+UNSUPPORTED_REASON = ("the reference's vendored Random123 refuses to compile on %s "
+                      "(Random123/features/gccfeatures.h:37-40: x86 and powerpc only)")
+
+
 def build(force=False):
+    if not supported_here():
+        return None
     root = os.path.join(reference_root(), "mcramp")
     if os.path.isdir(root):
         _generate(root, force)

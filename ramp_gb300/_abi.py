@@ -171,6 +171,12 @@ _SIGS = {
                          ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_rng_peak": ([ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
                             ctypes.c_int),
+    "ramp_debug_l2_peak": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+                            ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "ramp_debug_atomic_peak": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+                                ctypes.c_void_p], ctypes.c_int),
+    "ramp_bvh_walk_counts": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                              ctypes.c_void_p], ctypes.c_int),
 }
 
 

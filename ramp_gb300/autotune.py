@@ -6,8 +6,9 @@ be chosen purely for speed.  ``tune(inst)`` times short fused runs of the
 instrument over the candidates (register cap = minimum CTAs per SM, the
 span of neutrons a task covers, whether survivors are compacted into
 full warps before the first component that less than half of the
-histories reach — found by a plain-path pilot, ``survival`` — and, for
-chains with a mesh, the per-lane mesh walk) and keeps the fastest; results are
+histories reach — found by a plain-path pilot, ``survival`` — whether
+stage A regroups each warp's neutrons by expected bounce passes before
+the first guide, and, for chains with a mesh, the per-lane mesh walk) and keeps the fastest; results are
 cached in a JSON file keyed by GPU name, the instrument's component
 structure and the keying mode.  Tuning uses fixed seeds and restores the
 instrument's tallies afterwards: it leaves no trace in the results or in
@@ -126,6 +127,24 @@ def split_point(inst, alive, threshold=0.5):
     return 0
 
 
+def regroup_point(inst, split):
+    """RampTune.regroup for the first guide component before the split
+    point (in a linear block, no extended kinds in the chain), or 0."""
+    if split <= 0:
+        return 0
+    src, carr, nc, barr, nb = inst.descriptors([])
+    if src.kind == _abi.SRC_ISIS or any(carr[j].scat in (_abi.S_MONO, _abi.S_POWDER1)
+                                        for j in range(nc)):
+        return 0
+    for k in range(nb):
+        if not barr[k].linear:
+            continue
+        for j in range(barr[k].first, min(barr[k].first + barr[k].count, split)):
+            if carr[j].scat == _abi.S_GUIDE:
+                return j + 1
+    return 0
+
+
 def has_mesh(inst):
     """Whether a linear block of the chain holds a GMesh component (the
     candidates then include the per-lane mesh walk, RampTune.walk)."""
@@ -168,6 +187,9 @@ def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False
     if candidates is None:
         split = split_point(inst, survival(inst, min(n_probe, 1_000_000), rng))
         candidates = [dict(c, split=k) for c in CANDIDATES for k in ((0, split) if split else (0,))]
+        g = regroup_point(inst, split)
+        if g:
+            candidates += [dict(c, split=split, regroup=g) for c in CANDIDATES]
         if has_mesh(inst):
             candidates += [dict(c, walk=1) for c in CANDIDATES]
     with torch.cuda.device(inst.device):

@@ -1281,6 +1281,32 @@ int ramp_debug_rng_peak(int64_t n_threads, int32_t iters, uint32_t* out, void* s
   return RAMP_OK;
 }
 
+static bool pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
+
+int ramp_debug_l2_peak(const float* buf, int64_t len, int64_t n_threads, int32_t iters,
+                       float* out, void* stream) {
+  if (!buf || !out || len % 4 != 0 || !pow2(len / 4) || n_threads < 0 || n_threads % 256 ||
+      n_threads / 256 > INT32_MAX || iters < 0 || iters % 2 || ((uintptr_t)buf & 15)) {
+    set_err("ramp_debug_l2_peak: buf 16-byte aligned, len/4 a power of two, n_threads a "
+            "multiple of 256, iters even");
+    return RAMP_E_INVALID;
+  }
+  CK(launch_debug_l2_peak((const float4*)buf, len / 4, n_threads, iters, out,
+                          (cudaStream_t)stream));
+  return RAMP_OK;
+}
+
+int ramp_debug_atomic_peak(float* bins, int64_t n_bins, int64_t n_threads, int32_t iters,
+                           void* stream) {
+  if (!bins || !pow2(n_bins) || n_bins > ((int64_t)1 << 31) || n_threads < 0 ||
+      n_threads % 256 || n_threads / 256 > INT32_MAX || n_threads > UINT32_MAX || iters < 0) {
+    set_err("ramp_debug_atomic_peak: n_bins a power of two, n_threads a multiple of 256");
+    return RAMP_E_INVALID;
+  }
+  CK(launch_debug_atomic_peak(bins, n_bins, n_threads, iters, (cudaStream_t)stream));
+  return RAMP_OK;
+}
+
 }  // extern "C"
 
 /* ======================================================================

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "bvh.h"
+#include "../../include/ramp.h"
 
 namespace {
 
@@ -188,5 +189,68 @@ int ramp_bvh_build(const float* pts, int64_t n_tri, std::vector<float>& nodes,
     o[4] = p[3]; o[5] = p[4]; o[6] = p[5];
     o[8] = p[6]; o[9] = p[7]; o[10] = p[8];
   }
+  return 0;
+}
+
+/* Memory the GMesh walk reads for a set of rays when it needs every
+ * crossing (interior parity or a chord, as SAttenuate): every inner node
+ * whose box the ray meets is read once (64 bytes: both children's boxes)
+ * and every triangle of a leaf whose box it meets is read once (48 bytes).
+ * The walk order does not change these counts.  The slab tests are the
+ * device's (mesh.cuh), in float.  rays: 6 floats each (position, velocity)
+ * in the mesh's frame; out[0] inner nodes read, out[1] triangles read,
+ * out[2] rays that meet the mesh's bounding box. */
+extern "C" int ramp_bvh_walk_counts(const float* pts, int64_t n_tri, const float* rays,
+                                    int64_t n_rays, int64_t* out) {
+  if (!pts || !rays || !out || n_tri <= 0 || n_rays < 0) return -1;
+  std::vector<float> nodes, tris;
+  if (ramp_bvh_build(pts, n_tri, nodes, tris) != 0) return -1;
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = 0; i < 3 * n_tri; ++i)
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::min(lo[k], pts[3 * i + k]);
+      hi[k] = std::max(hi[k], pts[3 * i + k]);
+    }
+  int64_t n_nodes = 0, n_tris = 0, n_in = 0;
+  std::vector<int> stack;
+  for (int64_t r = 0; r < n_rays; ++r) {
+    const float* p = rays + 6 * r;
+    const float* v = p + 3;
+    float tmin = -INFINITY, tmax = INFINITY;
+    for (int k = 0; k < 3; ++k) {
+      const float t1 = (lo[k] - p[k]) / v[k], t2 = (hi[k] - p[k]) / v[k];
+      tmin = std::max(tmin, std::min(t1, t2));
+      tmax = std::min(tmax, std::max(t1, t2));
+    }
+    if (tmax < 0.0f || tmin > tmax) continue;
+    ++n_in;
+    const float inv[3] = {1.0f / v[0], 1.0f / v[1], 1.0f / v[2]};
+    stack.assign(1, 0);
+    while (!stack.empty()) {
+      const int nd = stack.back();
+      stack.pop_back();
+      ++n_nodes;
+      const float* q = &nodes[16 * (size_t)nd];
+      for (int c = 0; c < 2; ++c) {
+        const float* b = q + 8 * c;
+        int a, cnt;
+        std::memcpy(&a, &b[3], 4);
+        std::memcpy(&cnt, &b[7], 4);
+        if (cnt < 0) continue;
+        float tn = -INFINITY, tf = INFINITY;
+        for (int k = 0; k < 3; ++k) {
+          const float t0 = (b[k] - p[k]) * inv[k], t1 = (b[4 + k] - p[k]) * inv[k];
+          tn = std::max(tn, std::min(t0, t1));
+          tf = std::min(tf, std::max(t0, t1));
+        }
+        if (tn > tf || tf < -1e-6f) continue;
+        if (cnt > 0) n_tris += cnt;
+        else stack.push_back(a);
+      }
+    }
+  }
+  out[0] = n_nodes;
+  out[1] = n_tris;
+  out[2] = n_in;
   return 0;
 }

@@ -91,6 +91,10 @@ cudaError_t launch_seed_advance(int32_t* seed_dev, cudaStream_t s);
 cudaError_t launch_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out,
                                   int64_t n, cudaStream_t s);
 cudaError_t launch_debug_rng_peak(int64_t n, int32_t iters, uint32_t* out, cudaStream_t s);
+cudaError_t launch_debug_l2_peak(const float4* buf, int64_t len4, int64_t n, int32_t iters,
+                                 float* out, cudaStream_t s);
+cudaError_t launch_debug_atomic_peak(float* bins, int64_t n_bins, int64_t n, int32_t iters,
+                                     cudaStream_t s);
 cudaError_t launch_debug_math(int fn, const float* a, const float* b, float* out, int64_t n,
                               cudaStream_t s);
 

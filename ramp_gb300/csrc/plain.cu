@@ -392,6 +392,55 @@ cudaError_t launch_debug_rng_peak(int64_t n, int32_t iters, uint32_t* out, cudaS
   return cudaGetLastError();
 }
 
+/* L2 read bandwidth: every thread reads `iters` float4 of a buffer of len
+ * float4 (a power of two, small enough to stay in L2) through loads that
+ * bypass L1 (ld.global.cg); the warps of a pass read consecutive 512-byte
+ * runs.  out[thread] keeps the sums live. */
+__global__ void __launch_bounds__(256) k_debug_l2_peak(const float4* __restrict__ buf,
+                                                        uint64_t mask, int32_t iters,
+                                                        float* out) {
+  const uint64_t nt = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t j = i;
+  float a0 = 0.0f, a1 = 0.0f;
+  for (int k = 0; k < iters; k += 2) {
+    const float4 u = __ldcg(buf + (j & mask));
+    const float4 v = __ldcg(buf + ((j + nt) & mask));
+    a0 += (u.x + u.y) + (u.z + u.w);
+    a1 += (v.x + v.y) + (v.z + v.w);
+    j += 2 * nt;
+  }
+  out[i] = a0 + a1;
+}
+
+cudaError_t launch_debug_l2_peak(const float4* buf, int64_t len4, int64_t n, int32_t iters,
+                                 float* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_debug_l2_peak<<<(unsigned)(n / 256), 256, 0, s>>>(buf, (uint64_t)len4 - 1, iters, out);
+  return cudaGetLastError();
+}
+
+/* L2 float-atomic throughput: every thread adds 1 to `iters` bins of an
+ * L2-resident histogram of n_bins floats (a power of two), the 32 lanes of
+ * a warp to 32 consecutive bins (one 128-byte line), no two lanes of a
+ * warp on one bin, as the tallies' warp-aggregated adds issue them. */
+__global__ void __launch_bounds__(256) k_debug_atomic_peak(float* bins, uint32_t mask,
+                                                            int32_t iters) {
+  const uint32_t nt = gridDim.x * blockDim.x;
+  uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int k = 0; k < iters; ++k) {
+    atomicAdd(bins + (j & mask), 1.0f);
+    j += nt;
+  }
+}
+
+cudaError_t launch_debug_atomic_peak(float* bins, int64_t n_bins, int64_t n, int32_t iters,
+                                     cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_debug_atomic_peak<<<(unsigned)(n / 256), 256, 0, s>>>(bins, (uint32_t)(n_bins - 1), iters);
+  return cudaGetLastError();
+}
+
 /* next chunk seed in [0, 4096] from a 64-bit LCG (Knuth's MMIX constants) */
 __global__ void k_seed_advance(int32_t* seed_dev) {
   unsigned long long* st = reinterpret_cast<unsigned long long*>(seed_dev + 2);

@@ -153,3 +153,65 @@ def test_leaves_partition_the_triangles_and_walks_reach_every_hit(builder, nu, n
         hits_total += int(hit.sum())
         assert not (hit & ~mask).any()
     assert keep or hits_total > 0
+
+
+def walk_counts(nodes, pos, vel):
+    """(inner nodes read, triangles read) of the walk by the rules above."""
+    ni = nodes.view(np.int32)
+    with np.errstate(divide="ignore"):
+        inv = (np.float32(1) / vel).astype(np.float32)
+    n_nodes, n_tris, stack = 0, 0, [0]
+    while stack:
+        node = stack.pop()
+        n_nodes += 1
+        for c in (0, 8):
+            b = ni[node, c + 7]
+            if b < 0:
+                continue
+            lo, hi = nodes[node, c:c + 3], nodes[node, c + 4:c + 7]
+            with np.errstate(invalid="ignore"):
+                t0, t1 = (lo - pos) * inv, (hi - pos) * inv
+            tn, tf = np.max(np.minimum(t0, t1)), np.min(np.maximum(t0, t1))
+            if tn > tf or tf < -1e-6:
+                continue
+            if b >= 1:
+                n_tris += int(b)
+            else:
+                stack.append(ni[node, c + 3])
+    return n_nodes, n_tris
+
+
+def test_library_walk_counts_match_the_layout_walk(builder):
+    """ramp_bvh_walk_counts (the mesh roofline's algorithmic L2 bytes) reads
+    the hierarchy the library builds as the layout walk does; a ray that
+    misses the mesh's box reads nothing."""
+    import ctypes
+    from ramp_gb300 import _abi
+    lib = _abi.load()
+    rng = np.random.default_rng(9)
+    pts = torus(rng, 60, 30)
+    nodes, _ = builder(pts)
+    rays = []
+    for _ in range(120):
+        pos = rng.uniform(-0.1, 0.1, 3).astype(np.float32)
+        pos[2] = -0.5
+        tgt = rng.uniform(-0.08, 0.08, 3).astype(np.float32)
+        tgt[2] = 0.0
+        rays.append(np.concatenate([pos, (tgt - pos) * np.float32(300.0)]))
+    rays.append(np.array([5.0, 5.0, -0.5, 0.0, 0.0, 300.0], np.float32))   # misses the box
+    rays = np.ascontiguousarray(np.array(rays, np.float32))
+    lo, hi = pts.reshape(-1, 3).min(0), pts.reshape(-1, 3).max(0)
+    want = np.zeros(3, np.int64)
+    for r in rays:
+        pos, vel = r[:3], r[3:]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            t1, t2 = (lo - pos) / vel, (hi - pos) / vel
+        if np.min(np.maximum(t1, t2)) < 0 or np.max(np.minimum(t1, t2)) > np.min(np.maximum(t1, t2)):
+            continue
+        a, b = walk_counts(nodes, pos, vel)
+        want += (a, b, 1)
+    out = np.zeros(3, np.int64)
+    assert lib.ramp_bvh_walk_counts(pts.ctypes.data, len(pts), rays.ctypes.data, len(rays),
+                                    out.ctypes.data) == 0
+    assert 10 < want[2] < len(rays)
+    assert np.array_equal(out, want)
