@@ -3,6 +3,7 @@
 (1e8 histories per step, FP32, reference RNG keying) on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config 2|3|4|5] [--no-extra]
 
 A step is one Instrument.execute(1e8) of the LET-like instrument (Maxwellian
 moderator, 4 supermirror guides, 5 disk choppers, 40-line powder sample,
@@ -18,15 +19,25 @@ construction (IDF parse, table upload), execute and the histogram readback.
 roofline: the fused kernel is bound by integer issue (Threefry-4x32-20,
 about 150 integer operations per random draw), not by HBM or tensor cores;
 achieved = draws x ops per draw / kernel time, peak = the same operation
-rate measured by a Threefry-only kernel on this GPU.
+rate measured by a Threefry-only kernel on this GPU.  The DRAM traffic and
+the instruction count per history come from the ncu capture recorded in
+profiles/ with a hash of the kernel sources; they are reported only when
+that hash equals the sources being run.
+Beside the headline (one GPU, unless --no-extra): the batched scan of 256
+variants (config 3), gradients of a histogram loss (config 4, grads/s) and
+the mesh imaging workload (config 5, rays/s with an L2 roofline from the
+walk's counted node and triangle reads), the tallies' L2 atomics against a
+measured L2-atomic peak, and small-N CUDA-graph replays.
 Multi-GPU (torchrun): each rank traces its own 1e8-history slice of one
 chunk of N x 1e8 (weak scaling, no collective in the timed region); the
 histograms are summed once afterwards.
---impl reference times the CPU restatement of the reference kernels (the
-reference's OpenCL path cannot run here) on a bounded sample with all host
-threads.
+--impl reference times the reference's own kernels compiled for the host
+cores (oracle/refcl, where they build) or else the CPU restatement of them
+(the reference's OpenCL runtime path cannot run here), on a bounded sample
+with all host threads.
 """
 import argparse
+import hashlib
 import json
 import os
 import random
@@ -43,20 +54,8 @@ N_HIST = 100_000_000
 THREEFRY_OPS = 148          # integer operations per Threefry-4x32-20 draw
 CPU_CHUNK = 2_000_000       # histories per chunk of a CPU-baseline step
 CPU_SECONDS = 12.0          # CPU work per CPU-baseline step (whole chunks)
-# DRAM bytes (read + write) of one split launch (stage A + stage B, split
-# before chopper 2) per 1e7 histories, from the ncu capture summarised in
-# profiles/let_like_fused_split_1e7.md (49 + 83 MB and 121 + 5 MB); the
-# traffic grows with the histories traced
-FUSED_SPLIT2_DRAM_PER_1E7 = (48.59 + 82.98 + 121.37 + 5.09) * 1e6
-# the same capture's issue figures for stage A (88 % of the split launch):
-# warp instructions issued on 77.4 % of scheduler cycles, 15.8 of 32 lanes
-# active per instruction
-FUSED_SPLIT2_STAGE_A_ISSUE = {"issue_active_pct": 77.4, "threads_per_instruction": 15.8}
-# warp instructions per history of the split launch in that capture
-# (stage A 1.363e9 + stage B 1.136e8 per 1e7 histories): with the live
-# throughput this gives the launch's issue rate against the scheduler peak
-# (4 warp instructions per SM per cycle)
-FUSED_SPLIT2_WARP_INSTR_PER_HISTORY = (1.363146e9 + 1.136426e8) / 1e7
+NODE_BYTES, TRI_BYTES = 64, 48   # one BVH inner node / triangle as the walk reads them
+COUNTERS = os.path.join(HERE, "profiles", "let_like_fused_counters.json")
 
 
 def args_():
@@ -68,6 +67,8 @@ def args_():
     p.add_argument("--n", type=int, default=N_HIST)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the config 3/4/5 legs, the atomic roofline and the graph replays")
     p.add_argument("--variants", type=int, default=0,
                    help="batched scan and mesh imaging (--config 3, 5): trace only the "
                         "first N variants (0: all)")
@@ -97,32 +98,77 @@ def peaks_file():
         return {}
 
 
+def kernel_source_sha():
+    """Hash of the sources and build recipe of libramp_cuda.so."""
+    h = hashlib.sha256()
+    csrc = os.path.join(HERE, "ramp_gb300", "csrc")
+    files = sorted(os.path.join(csrc, f) for f in os.listdir(csrc)
+                   if f.endswith((".cu", ".cuh", ".h", ".cpp")))
+    files += [os.path.join(HERE, "include", "ramp.h"),
+              os.path.join(HERE, "ramp_gb300", "build.py")]
+    for f in files:
+        h.update(os.path.basename(f).encode())
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def profile_counters(tune):
+    """Per-history DRAM bytes and warp instructions of the fused launch
+    from the recorded ncu capture, when it was made from these kernel
+    sources with this launch configuration; else None with the reason."""
+    try:
+        with open(COUNTERS) as f:
+            c = json.load(f)
+    except (OSError, ValueError):
+        return None, "no recorded capture"
+    if c.get("kernel_source_sha") != kernel_source_sha():
+        return None, "recorded capture is of other kernel sources (%s)" % c.get(
+            "kernel_source_sha")
+    keys = ("split", "regroup", "walk")
+    if any(int((tune or {}).get(k, 0)) != int(c.get("tune", {}).get(k, 0)) for k in keys):
+        return None, "recorded capture is of another launch configuration"
+    return c, None
+
+
 # ---------------------------------------------------------------- CPU arm
 def cpu_histories_per_s(steps=1, warmup=1, seconds=CPU_SECONDS):
-    """The oracle on every host core over the LET-like chain: one-chunk
-    warm-ups, the last of them timed, size each timed step to about
-    ``seconds`` of work in whole chunks of CPU_CHUNK histories (bounded
-    memory); returns (histories/s of the best step, threads, step times,
-    histories per step)."""
+    """The reference's kernels compiled for the host (oracle/refcl, C
+    library math), or where they do not build the oracle, on every host
+    core over the LET-like chain: one-chunk warm-ups, the last of them
+    timed, size each timed step to about ``seconds`` of work in whole
+    chunks of CPU_CHUNK histories (bounded memory).  Returns (histories/s
+    of the best step, threads, step times, histories per step, kind, what
+    ran)."""
     import oracle
     import ramp_gb300 as m
+    from oracle import refcl
     from ramp_gb300 import instruments as I
     inst = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
     threads = os.cpu_count() or 1
+    if refcl.available():
+        kind, what = "reference", ("the reference's OpenCL kernels compiled for the host "
+                                   "(oracle/refcl, C library math), reference sequencing")
+        run = lambda n, chunk: refcl.run(inst, n, chunk=chunk, math="libm", threads=threads)
+    else:
+        kind, what = "port", ("CPU restatement of the reference kernels (reference "
+                              "sequencing; the reference's kernels do not build here: %s)"
+                              % refcl.unavailable_reason())
+        run = lambda n, chunk: oracle.run(inst, n, chunk=chunk, threads=threads)
     pilot = None
     for w in range(max(warmup, 1) + 1):       # the last warm-up chunk is timed
         random.seed(1 + w)
         t0 = time.perf_counter()
-        oracle.run(inst, CPU_CHUNK, threads=threads)
+        run(CPU_CHUNK, None)
         pilot = time.perf_counter() - t0
     n = max(1, int(round(seconds / max(pilot, 1e-3)))) * CPU_CHUNK
     times = []
     for k in range(steps):
         random.seed(100 + k)
         t0 = time.perf_counter()
-        oracle.run(inst, n, chunk=CPU_CHUNK, threads=threads)
+        run(n, CPU_CHUNK)
         times.append(time.perf_counter() - t0)
-    return n / min(times), threads, times, n
+    return n / min(times), threads, times, n, kind, what
 
 
 def run_reference(a):
@@ -130,19 +176,19 @@ def run_reference(a):
     if rank != 0:
         return
     steps = max(1, a.steps)
-    v, threads, times, ns = cpu_histories_per_s(steps=steps, warmup=max(1, min(a.warmup, 2)))
+    v, threads, times, ns, kind, what = cpu_histories_per_s(steps=steps,
+                                                            warmup=max(1, min(a.warmup, 2)))
     sample = ("%d histories of the LET-like chain per step in chunks of %d (a bounded sample, "
-              "about %.0f s of CPU work, of the %d-history workload), CPU restatement of the "
-              "reference kernels in reference sequencing (5 passes per component, "
-              "array-of-structs records), OpenMP" % (ns, CPU_CHUNK, CPU_SECONDS, a.n))
+              "about %.0f s of CPU work, of the %d-history workload): %s, array-of-structs "
+              "records, OpenMP" % (ns, CPU_CHUNK, CPU_SECONDS, a.n, what))
     line = {"metric": "neutron histories/s", "value": v, "unit": "histories/s",
             "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
             "ms_per_step": 1000.0 * statistics.mean(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": workload_config(ns, 1, "CPU restatement, reference sequencing"),
+            "config": workload_config(ns, 1, what),
             "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads,
-                             "kind": "port", "sample": sample},
+                             "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -189,6 +235,61 @@ class Clocks:
                 "samples": len(rows)}
 
 
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+# ------------------------------------------------ measurement micro-kernels
+def l2_read_peak(lib, dev, mb=32, iters=256):
+    """L2 read bandwidth (GB/s) of ramp_debug_l2_peak over an L2-resident
+    buffer, best of three."""
+    import torch
+    from ramp_gb300 import _abi
+    buf = torch.ones(mb * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    nth = torch.cuda.get_device_properties(dev).multi_processor_count * 2048
+    out = torch.empty(nth, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = _abi.ctypes.c_void_p(stream.cuda_stream)
+    best = None
+    for k in range(4):
+        s, e = _events()
+        s.record(stream)
+        _abi.check(lib, lib.ramp_debug_l2_peak(buf.data_ptr(), buf.numel(), nth, iters,
+                                               out.data_ptr(), sp), "ramp_debug_l2_peak")
+        e.record(stream)
+        e.synchronize()
+        if k:
+            gbs = nth * iters * 16 / (s.elapsed_time(e) / 1e3) / 1e9
+            best = gbs if best is None else max(best, gbs)
+    return best, "ramp_debug_l2_peak: %d threads x %d float4 reads of a %d MB buffer" % (
+        nth, iters, mb)
+
+
+def atomic_peak(lib, dev, n_bins=1 << 20, iters=64):
+    """L2 float-atomic adds per second of ramp_debug_atomic_peak, best of
+    three."""
+    import torch
+    from ramp_gb300 import _abi
+    bins = torch.zeros(n_bins, dtype=torch.float32, device=dev)
+    nth = torch.cuda.get_device_properties(dev).multi_processor_count * 2048
+    stream = torch.cuda.current_stream(dev)
+    sp = _abi.ctypes.c_void_p(stream.cuda_stream)
+    best = None
+    for k in range(4):
+        s, e = _events()
+        s.record(stream)
+        _abi.check(lib, lib.ramp_debug_atomic_peak(bins.data_ptr(), n_bins, nth, iters, sp),
+                   "ramp_debug_atomic_peak")
+        e.record(stream)
+        e.synchronize()
+        if k:
+            r = nth * iters / (s.elapsed_time(e) / 1e3)
+            best = r if best is None else max(best, r)
+    return best, "ramp_debug_atomic_peak: %d threads x %d float adds into %d bins" % (
+        nth, iters, n_bins)
+
+
 # ------------------------------------------- batched scan and mesh imaging
 def batched_workload(config, seed=11):
     """Variants of the batched workloads: (IDF, list of kwargs, counts)."""
@@ -207,37 +308,76 @@ def batched_workload(config, seed=11):
     return I.path("mesh_imaging.json"), kws, [3_000_000] * 360
 
 
-def run_batched_config(a):
-    """Batched fused path (one launch for all variants) against the plain
-    path run variant after variant, on the same histories."""
+def mesh_walk_bytes_per_ray(kws, sample=20_000, views=8, seed=3):
+    """Algorithmic L2 bytes per ray of the mesh imaging walk: rays drawn as
+    the flat moderator draws them (0.06 x 0.06 m source and target, the
+    target 1e6 m away), taken into the frame of the mesh (0.5 m downstream,
+    rotated about y by each sampled view's angle) and walked through the
+    hierarchy the plan builds (ramp_bvh_walk_counts: 64 bytes per inner node
+    read, 48 per triangle read)."""
+    import numpy as np
+    from ramp_gb300 import _abi
+    from ramp_gb300.geom.mesh import read_stl_cached
+    lib = _abi.load()
+    stl = eval(kws[0]["stl_file"])
+    pts = np.ascontiguousarray(read_stl_cached(stl), dtype=np.float32)
+    rng = np.random.default_rng(seed)
+    tot = np.zeros(3, np.int64)
+    nr = 0
+    for v in np.linspace(0, len(kws) - 1, views).astype(int):
+        ang = float(kws[v]["angle"])
+        o = np.stack([rng.uniform(-0.03, 0.03, sample), rng.uniform(-0.03, 0.03, sample),
+                      np.zeros(sample)], 1)
+        t = np.stack([rng.uniform(-0.03, 0.03, sample), rng.uniform(-0.03, 0.03, sample),
+                      np.full(sample, 1e6)], 1)
+        d = (t - o) / np.linalg.norm(t - o, axis=1, keepdims=True)
+        c, s = np.cos(ang), np.sin(ang)
+        Ry = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])   # rotation [0, angle, 0]
+        p = (o - [0.0, 0.0, 0.5]) @ Ry                        # R^T (o - centre)
+        u = d @ Ry
+        rays = np.ascontiguousarray(np.concatenate([p, 1000.0 * u], 1), dtype=np.float32)
+        out = np.zeros(3, np.int64)
+        _abi.check(lib, lib.ramp_bvh_walk_counts(pts.ctypes.data, len(pts), rays.ctypes.data,
+                                                 len(rays), out.ctypes.data),
+                   "ramp_bvh_walk_counts")
+        tot += out
+        nr += len(rays)
+    return (NODE_BYTES * float(tot[0]) + TRI_BYTES * float(tot[1])) / nr, {
+        "nodes_per_ray": float(tot[0]) / nr, "triangles_per_ray": float(tot[1]) / nr,
+        "rays_in_mesh_box": float(tot[2]) / nr, "sample_rays": nr}
+
+
+def measure_batched(config, steps, warmup, tune_arg="auto", variants=0, plain=True):
+    """Batched fused path (one launch for all variants) over the full
+    workload; the plain path variant after variant on the first 32 variants
+    beside it, scaled to all histories."""
     import torch
     import ramp_gb300 as m
-    from ramp_gb300 import _abi, build
     from ramp_gb300.batch import BatchedInstrument
-    build.build()
     dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
-    fn, kws, counts = batched_workload(a.config)
-    if a.variants:            # the first variants only (a small case for profiling)
-        kws, counts = kws[:a.variants], counts[:a.variants]
+    fn, kws, counts = batched_workload(config)
+    if variants:            # the first variants only (a small case for profiling)
+        kws, counts = kws[:variants], counts[:variants]
     total = sum(counts)
+    t0 = time.perf_counter()
     B = BatchedInstrument(fn, kws, ctx=dev)
-    if a.tune == "auto":
-        # the autotuner's register cap and split point for the first
-        # variant (the variants share the component structure)
+    setup_s = time.perf_counter() - t0
+    if tune_arg == "auto":
+        # the autotuner's choice for the first variant (the variants share
+        # the component structure)
         from ramp_gb300 import autotune
         tune = {k: v for k, v in autotune.tune(B.instruments[0], rng="reference").items()
-                if k in ("blocks_per_sm", "split", "walk")}
+                if k in ("blocks_per_sm", "split", "walk", "regroup")}
     else:
-        tune = json.loads(a.tune) if a.tune else None
-    for w in range(a.warmup):
+        tune = json.loads(tune_arg) if tune_arg else None
+    for w in range(warmup):
         B.execute(counts, rng="reference", seeds=list(range(len(counts))), tune=tune)
     torch.cuda.synchronize()
     clocks = Clocks(0)
     clocks.start()
     ms = []
-    for k in range(a.steps):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for k in range(steps):
+        s, e = _events()
         s.record()
         B.execute(counts, rng="reference", seeds=[(k * 7919 + v) % 4097 for v in range(len(counts))],
                   tune=tune)
@@ -245,49 +385,62 @@ def run_batched_config(a):
         e.synchronize()
         ms.append(s.elapsed_time(e))
     clk = clocks.stop()
-    # plain path, variant after variant, on the first 32 variants (each has its
-    # own plan; mesh plans build their own BVH), scaled to all histories
-    nplain = min(32, len(kws))
-    plain_insts = [m.Instrument(fn, dev, **kw) for kw in kws[:nplain]]
-    for inst in plain_insts:
-        inst.plan()
-    torch.cuda.synchronize()
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    import random as _r
-    s.record()
-    for inst, n in zip(plain_insts, counts[:nplain]):
-        _r.seed(n)
-        inst.execute(n, path="plain")
-    e.record()
-    e.synchronize()
-    plain_ms = s.elapsed_time(e) * total / sum(counts[:nplain])
-    value = total * a.steps / (sum(ms) / 1000.0)
+    out = {"value": total / (statistics.mean(ms) / 1000.0), "ms_per_step": statistics.mean(ms),
+           "steps": steps, "warmup": warmup, "variants": len(counts), "histories_per_step": total,
+           "tune": tune, "setup_s": setup_s, "clocks": clk,
+           "gpu_launches_per_step": (2 if (int((tune or {}).get("split", 0)) > 0 or
+                                           int((tune or {}).get("walk", 0)) > 0) else 1) *
+                                    (sum(1 for c in counts if c > 0)
+                                     if int((tune or {}).get("streams", 0)) > 1 else 1)}
+    if plain:
+        nplain = min(32, len(kws))
+        plain_insts = [m.Instrument(fn, dev, **kw) for kw in kws[:nplain]]
+        for inst in plain_insts:
+            inst.plan()
+        torch.cuda.synchronize()
+        s, e = _events()
+        import random as _r
+        s.record()
+        for inst, n in zip(plain_insts, counts[:nplain]):
+            _r.seed(n)
+            inst.execute(n, path="plain")
+        e.record()
+        e.synchronize()
+        plain_ms = s.elapsed_time(e) * total / sum(counts[:nplain])
+        out["plain_path_sequential"] = {
+            "value": total / (plain_ms / 1000.0), "ms_per_step": plain_ms,
+            "sample": "first %d variants, scaled by histories" % nplain}
+        out["batched_over_plain"] = out["value"] / out["plain_path_sequential"]["value"]
+    return out
+
+
+def run_batched_config(a):
+    import torch
+    from ramp_gb300 import build
+    build.build()
+    torch.cuda.set_device(0)
+    r = measure_batched(a.config, a.steps, a.warmup, a.tune, a.variants)
     name = {3: "batched scan: 256 LET-like variants (Ei log-uniform 2-20 meV with matched "
                "chopper phases, slit 10-40 mm, N log-uniform 1e5-4e6), 720x1000 histogram each",
             5: "mesh imaging: 360 views x 3e6 rays through a 200,704-triangle noisy torus "
                "(BVH, watertight chords, mu 0.5/cm), 1024x1024 detector per view"}[a.config]
-    line = {"metric": "neutron histories/s", "value": value, "unit": "histories/s", "n_gpus": 1,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": statistics.mean(ms),
+    line = {"metric": "neutron histories/s", "value": r["value"], "unit": "histories/s",
+            "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": name, "variants": len(counts), "histories_per_step": total,
-                       "tune": tune,
+            "config": {"workload": name, "variants": r["variants"],
+                       "histories_per_step": r["histories_per_step"], "tune": r["tune"],
                        "rng": "reference keying",
                        "path": "batched fused: one launch (two with a split) whose grid "
                                "row v traces variant v"},
-            "plain_path_sequential": {"value": total / (plain_ms / 1000.0), "ms_per_step": plain_ms,
-                                      "sample": "first %d variants, scaled by histories" % nplain},
-            "batched_over_plain": (total / (statistics.mean(ms) / 1000.0)) / (total / (plain_ms / 1000.0)),
-            "gpu_launches": a.steps * (2 if (int((tune or {}).get("split", 0)) > 0
-                                             or int((tune or {}).get("walk", 0)) > 0) else 1) *
-                            (sum(1 for c in counts if c > 0)
-                             if int((tune or {}).get("streams", 0)) > 1 else 1),
-            "clocks": clk}
+            "plain_path_sequential": r.get("plain_path_sequential"),
+            "batched_over_plain": r.get("batched_over_plain"),
+            "gpu_launches": a.steps * r["gpu_launches_per_step"], "clocks": r["clocks"]}
     print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------- gradients of a histogram loss
-def run_gradients(a, n=10_000_000):
+def measure_gradients(steps, warmup, n=10_000_000, fd_check=True):
     """grads/s: forward histogram + loss + adjoint gradient of 22 parameters
     (4 guides x R0, Qc, alpha, m, W; moderator T; powder sigma_abs) on the
     LET-like chain at 1e7 histories; the gradient is also compared with
@@ -295,11 +448,9 @@ def run_gradients(a, n=10_000_000):
     import numpy as np
     import torch
     import ramp_gb300 as m
-    from ramp_gb300 import build, instruments as I
+    from ramp_gb300 import instruments as I
     from ramp_gb300.diff import DiffChain, LET_LIKE_PARAMS, histogram
-    build.build()
     dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
     inst = m.Instrument(I.path("let_like.json"), dev, **I.let_like_kwargs())
     chain = DiffChain(inst, LET_LIKE_PARAMS, detector="detector")
     theta0 = chain.values()
@@ -313,44 +464,60 @@ def run_gradients(a, n=10_000_000):
         L.backward()
         return th.grad
 
-    for w in range(a.warmup):
+    for w in range(warmup):
         step(10 + w)
     torch.cuda.synchronize()
     clocks = Clocks(0)
     clocks.start()
     ms = []
-    for k in range(a.steps):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for k in range(steps):
+        s, e = _events()
         s.record()
-        g = step(100 + k)
+        step(100 + k)
         e.record()
         e.synchronize()
         ms.append(s.elapsed_time(e))
     clk = clocks.stop()
-    g = step(1)
-    fd = torch.zeros_like(g)
-    with torch.no_grad():
-        for k in range(len(theta0)):
-            h = 1e-3 * float(theta0[k])
-            tp, tm = theta0.clone(), theta0.clone()
-            tp[k] += h
-            tm[k] -= h
-            Lp = ((histogram(chain, tp, n, 1).double() - Ht) ** 2).sum()
-            Lm = ((histogram(chain, tm, n, 1).double() - Ht) ** 2).sum()
-            fd[k] = (Lp - Lm) / (2 * h)
-    rel = ((g - fd).abs() / fd.abs().clamp_min(1e-300)).tolist()
-    table = {nm: {"adjoint": float(x), "fd": float(y), "rel_err": float(z)}
-             for nm, x, y, z in zip(chain.names, g.tolist(), fd.tolist(), rel)}
-    line = {"metric": "grads/s", "value": 1000.0 / statistics.mean(ms), "unit": "grads/s",
-            "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": statistics.mean(ms),
+    out = {"value": 1000.0 / statistics.mean(ms), "unit": "grads/s",
+           "ms_per_step": statistics.mean(ms), "steps": steps, "warmup": warmup,
+           "histories_per_s_forward_and_adjoint": n / (statistics.mean(ms) / 1000.0),
+           "parameters": len(theta0), "histories": n, "clocks": clk}
+    if fd_check:
+        g = step(1)
+        fd = torch.zeros_like(g)
+        with torch.no_grad():
+            for k in range(len(theta0)):
+                h = 1e-3 * float(theta0[k])
+                tp, tm = theta0.clone(), theta0.clone()
+                tp[k] += h
+                tm[k] -= h
+                Lp = ((histogram(chain, tp, n, 1).double() - Ht) ** 2).sum()
+                Lm = ((histogram(chain, tm, n, 1).double() - Ht) ** 2).sum()
+                fd[k] = (Lp - Lm) / (2 * h)
+        rel = ((g - fd).abs() / fd.abs().clamp_min(1e-300)).tolist()
+        out["gradient_vs_central_fd"] = {
+            nm: {"adjoint": float(x), "fd": float(y), "rel_err": float(z)}
+            for nm, x, y, z in zip(chain.names, g.tolist(), fd.tolist(), rel)}
+        out["max_rel_err_vs_fd"] = max(rel)
+    return out
+
+
+def run_gradients(a):
+    import torch
+    from ramp_gb300 import build
+    build.build()
+    torch.cuda.set_device(0)
+    r = measure_gradients(a.steps, a.warmup)
+    line = {"metric": "grads/s", "value": r["value"], "unit": "grads/s",
+            "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "LET-like chain, 1e7 histories, loss sum (H - H*)^2 over the "
                                    "720x1000 detector, 22 parameters, fused forward + adjoint",
-                       "histories": n},
-            "histories_per_s_forward_and_adjoint": n / (statistics.mean(ms) / 1000.0),
-            "gpu_launches": a.steps * 2, "clocks": clk,
-            "gradient_vs_central_fd": table}
+                       "histories": r["histories"]},
+            "histories_per_s_forward_and_adjoint": r["histories_per_s_forward_and_adjoint"],
+            "gpu_launches": a.steps * 2, "clocks": r["clocks"],
+            "gradient_vs_central_fd": r.get("gradient_vs_central_fd")}
     print(json.dumps(line), flush=True)
 
 
@@ -387,25 +554,64 @@ def graph_small_n(inst_factory, tune, dev, sizes=(100_000, 1_000_000), reps=20):
     return out
 
 
-def issue_roofline(value, clk, dev, tune):
-    """Warp instructions issued per second by the split fused launch (live
-    histories/s x the profiled instructions per history) against the
+def issue_roofline(value, clk, dev, counters):
+    """Warp instructions issued per second by the fused launch (live
+    histories/s x the captured instructions per history) against the
     schedulers' peak at the clock measured during the timed steps."""
     import torch
-    if not isinstance(tune, dict) or int(tune.get("split", 0)) != 2 or not clk.get("sm_mhz"):
+    if counters is None or not clk.get("sm_mhz"):
         return None
-    try:
-        sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    except (RuntimeError, AssertionError) as e:     # a diagnostic: never lose the line
-        return {"unavailable": str(e)}
+    ipr = counters.get("warp_instructions_per_history")
+    if not ipr:
+        return None
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     peak = 4.0 * sms * clk["sm_mhz"] * 1e6
-    achieved = value * FUSED_SPLIT2_WARP_INSTR_PER_HISTORY
+    achieved = value * ipr
     return {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9,
             "unit": "G warp instructions/s", "frac": achieved / peak,
-            "instructions_per_history": FUSED_SPLIT2_WARP_INSTR_PER_HISTORY,
-            "source": "instructions per history from the ncu capture of a 1e7-history "
-                      "split launch; peak = 4 per SM per cycle x %d SMs x %.0f MHz"
-                      % (sms, clk["sm_mhz"])}
+            "instructions_per_history": ipr,
+            "source": "instructions per history from the ncu capture recorded for these kernel "
+                      "sources (%s); peak = 4 per SM per cycle x %d SMs x %.0f MHz"
+                      % (counters.get("kernel_source_sha"), sms, clk["sm_mhz"])}
+
+
+def extra_legs(a, lib, dev, peaks):
+    """The config 3/4/5 workloads at full size with bounded step counts, and
+    the L2 roofline of the mesh walk; each leg is reported on its own and a
+    failing leg leaves an error string, never the line."""
+    out = {}
+    steps, warmup = max(2, min(a.steps, 5)), max(1, min(a.warmup, 3))
+    try:
+        out["batched_scan"] = dict(measure_batched(3, steps, warmup), unit="histories/s",
+                                   workload="config 3: 256 LET-like variants in one launch, "
+                                            "720x1000 histogram each")
+    except Exception as e:          # a diagnostic leg: never lose the headline
+        out["batched_scan"] = {"error": repr(e)[:300]}
+    try:
+        out["gradients"] = dict(measure_gradients(steps, warmup),
+                                workload="config 4: 22 gradients of sum (H - H*)^2, LET-like, "
+                                         "1e7 histories, fused forward + adjoint")
+    except Exception as e:
+        out["gradients"] = {"error": repr(e)[:300]}
+    try:
+        r = measure_batched(5, max(1, min(a.steps, 2)), 1, plain=False)
+        fn, kws, counts = batched_workload(5)
+        bpr, detail = mesh_walk_bytes_per_ray(kws)
+        l2, l2_how = l2_read_peak(lib, dev)
+        rays = r["histories_per_step"]
+        achieved = bpr * rays / (r["ms_per_step"] / 1e3) / 1e9
+        r.update(unit="rays/s",
+                 workload="config 5: 360 views x 3e6 rays through a 200,704-triangle torus, "
+                          "1024x1024 detector per view",
+                 roofline={"bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s",
+                           "frac": achieved / l2 if l2 else None,
+                           "algorithmic_bytes_per_ray": bpr, "walk": detail,
+                           "peak_source": "measured: " + l2_how,
+                           "time": "whole launch (moderator stage and mesh walk) per step"})
+        out["mesh_imaging"] = r
+    except Exception as e:
+        out["mesh_imaging"] = {"error": repr(e)[:300]}
+    return out
 
 
 def main():
@@ -462,7 +668,7 @@ def main():
         ms = []
         for k in range(steps):
             flush.fill_(float(k))
-            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s, e = _events()
             random.seed(1000 + k)
             s.record()
             inst.execute(n * world if shard else n, path=path, shard=shard,
@@ -494,19 +700,23 @@ def main():
 
     # ---- roofline of the fused kernel: draws from the plain records ----
     stream = torch.cuda.current_stream(dev)
-    recs = plain.state[_abi.LANE["mc"], :plain.last_chunk]
-    seed_last = None
+    nlast = plain.last_chunk
     random.seed(1000 + len(plain_ms) - 1)
     seed_last = plain.source.next_seed()
-    draws = float((recs.double() - seed_last).sum())
+    draws = float((plain.state[_abi.LANE["mc"], :nlast].double() - seed_last).sum())
+    # neutrons whose last component is the detector: each adds to both of
+    # its histograms (sum p, sum p^2), two float atomics per tally
+    det_idx = [c["idx"] for name, c in plain.components() if name == "detector"][0]
+    tally_events = int(((plain.state[_abi.LANE["prevcomp"], :nlast] == det_idx) &
+                        (plain.state[_abi.LANE["p"], :nlast] != 0)).sum())
     kern = []
     for k in range(3):
         random.seed(1000 + len(plain_ms) - 1)
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s, e = _events()
         rngd = _abi.RampRng()
         tuned = _abi.tune_struct(tune or {})
         s.record(stream)
-        rc = lib.ramp_trace_fused(inst.plan(), plain.last_chunk, plain.last_chunk, seed_last,
+        rc = lib.ramp_trace_fused(inst.plan(), nlast, nlast, seed_last,
                                   _abi.ctypes.byref(rngd), None, None, _abi.ctypes.byref(tuned),
                                   _abi.ctypes.c_void_p(stream.cuda_stream))
         e.record(stream)
@@ -516,52 +726,69 @@ def main():
     kern_ms = statistics.median(kern)
     out = torch.empty(152 * 2048 * 4, dtype=torch.int32, device=dev)
     iters = 256
+    sp = _abi.ctypes.c_void_p(stream.cuda_stream)
     for _ in range(2):
-        lib.ramp_debug_rng_peak(out.numel(), iters, out.data_ptr(), _abi.ctypes.c_void_p(stream.cuda_stream))
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        lib.ramp_debug_rng_peak(out.numel(), iters, out.data_ptr(), sp)
+    s, e = _events()
     s.record(stream)
-    lib.ramp_debug_rng_peak(out.numel(), iters, out.data_ptr(), _abi.ctypes.c_void_p(stream.cuda_stream))
+    lib.ramp_debug_rng_peak(out.numel(), iters, out.data_ptr(), sp)
     e.record(stream)
     e.synchronize()
     peak_draws_s = out.numel() * iters * 2 / (s.elapsed_time(e) / 1000.0)
     achieved_ops = draws * THREEFRY_OPS / (kern_ms / 1000.0)
     peak_ops = peak_draws_s * THREEFRY_OPS
     inst._check_status(lib, inst.plan())
+    counters, stale = profile_counters(tune)
+    traffic = (counters["dram_bytes_per_history"] * nlast) if counters else None
 
-    # ---- plain path against HBM: 56 B per generated record, 112 B per
-    # record alive at a component's entry, 4 B (die flag) per dead one ----
+    # ---- plain path: its HBM traffic (56 B per generated record, 112 B per
+    # record alive at a component's entry, 4 B (die flag) per dead one) ----
     random.seed(1000 + len(plain_ms) - 1)
     from ramp_gb300.autotune import survival
     alive = survival(plain, n, "reference", plain.source.next_seed())
     plain_bytes = 56.0 * n + sum(a_ * 112.0 + (n - a_) * 4.0 for a_ in alive if a_ is not None)
     plain_step_s = plain_total_ms / len(plain_ms) / 1000.0
-    hbm_peak = peaks_file().get("hbm_gbs")
-    plain_roof = {"bound": "hbm", "achieved": plain_bytes / plain_step_s / 1e9,
-                  "peak": hbm_peak, "unit": "GB/s",
-                  "frac": (plain_bytes / plain_step_s / 1e9 / hbm_peak) if hbm_peak else None,
-                  "algorithmic_bytes_per_step": plain_bytes,
-                  "alive_at_component_entry": alive,
-                  "peak_source": "measured (copy bandwidth)" if hbm_peak else None}
+    peaks = peaks_file()
+    hbm_peak = peaks.get("hbm_gbs")
+    plain_hbm = {"achieved": plain_bytes / plain_step_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                 "frac": (plain_bytes / plain_step_s / 1e9 / hbm_peak) if hbm_peak else None,
+                 "algorithmic_bytes_per_step": plain_bytes,
+                 "alive_at_component_entry": alive,
+                 "peak_source": "measured (copy bandwidth)" if hbm_peak else None}
 
-    # ---- CUDA graphs at small N ----
-    graphs = graph_small_n(lambda: m.Instrument(fn, dev, **kw), tune, dev)
-
-    # ---- the same chain fed by the tabulated ISIS moderator (MISIS) ----
-    mi = m.Instrument(I.path("let_like_misis.json"), dev, **I.let_like_misis_kwargs())
-    misis_ms = []
-    for k in range(4):
-        random.seed(2000 + k)
-        s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record()
-        mi.execute(n, path="fused", tune=tune)
-        e0.record()
-        e0.synchronize()
-        if k > 0:
-            misis_ms.append(s0.elapsed_time(e0))
-    misis = {"value": n / (statistics.mean(misis_ms) / 1000.0), "unit": "histories/s",
-             "ms_per_step": statistics.mean(misis_ms),
-             "workload": "LET-like chain with the MISIS moderator (synthetic 60 x 100 "
-                         "time-energy spectrum), %d histories, fused" % n}
+    extras = {}
+    if not a.no_extra and world == 1:
+        # ---- tallies: float atomics into L2 against a measured peak ----
+        ap, ap_how = atomic_peak(lib, dev)
+        atomics = 2.0 * tally_events             # sum p and sum p^2: two adds per event
+        extras["atomics"] = {
+            "bound": "l2_atomics", "achieved": atomics / (kern_ms / 1e3), "peak": ap,
+            "unit": "atomics/s", "frac": atomics / (kern_ms / 1e3) / ap if ap else None,
+            "per_launch": atomics,
+            "counted": "neutrons of nonzero weight whose last component is the detector "
+                       "(%d of %d), "
+                       "two float atomic adds each into the sum-p and sum-p^2 histograms, "
+                       "before warp aggregation" % (tally_events, nlast),
+            "peak_source": "measured: " + ap_how}
+        # ---- CUDA graphs at small N ----
+        extras["graph_small_n"] = graph_small_n(lambda: m.Instrument(fn, dev, **kw), tune, dev)
+        # ---- the same chain fed by the tabulated ISIS moderator (MISIS) ----
+        mi = m.Instrument(I.path("let_like_misis.json"), dev, **I.let_like_misis_kwargs())
+        misis_ms = []
+        for k in range(4):
+            random.seed(2000 + k)
+            s0, e0 = _events()
+            s0.record()
+            mi.execute(n, path="fused", tune=tune)
+            e0.record()
+            e0.synchronize()
+            if k > 0:
+                misis_ms.append(s0.elapsed_time(e0))
+        extras["let_like_misis"] = {
+            "value": n / (statistics.mean(misis_ms) / 1000.0), "unit": "histories/s",
+            "ms_per_step": statistics.mean(misis_ms),
+            "workload": "LET-like chain with the MISIS moderator (synthetic 60 x 100 "
+                        "time-energy spectrum), %d histories, fused" % n}
 
     # ---- end to end through the public API ----
     e2e_steps = 0 if a.no_e2e else max(2, a.steps // 2)
@@ -586,16 +813,17 @@ def main():
         del ei, d
     e2e = world * n / (statistics.mean(e2e_ms) / 1000.0) if e2e_ms else None
 
+    if not a.no_extra and world == 1:
+        extras.update(extra_legs(a, lib, dev, peaks))
+
     if rank != 0:
         return
     cpu = None
     if not a.no_cpu_baseline:
-        v, threads, _, ns = cpu_histories_per_s(steps=1, warmup=1)
-        cpu = {"value": v, "unit": "histories/s", "cores": threads, "kind": "port",
-               "sample": "%d LET-like histories in chunks of %d (about %.0f s of CPU work), "
-                         "CPU restatement of the reference kernels (reference sequencing), "
-                         "OpenMP, after one-chunk warm-ups" % (ns, CPU_CHUNK, CPU_SECONDS)}
-    peaks = peaks_file()
+        v, threads, _, ns, kind, what = cpu_histories_per_s(steps=1, warmup=1)
+        cpu = {"value": v, "unit": "histories/s", "cores": threads, "kind": kind,
+               "sample": "%d LET-like histories in chunks of %d (about %.0f s of CPU work): %s, "
+                         "OpenMP, after one-chunk warm-ups" % (ns, CPU_CHUNK, CPU_SECONDS, what)}
     line = {
         "metric": "neutron histories/s", "value": value, "unit": "histories/s",
         "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
@@ -603,25 +831,24 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": dict(workload_config(n, world), tune=tune),
         "plain_path": {"value": plain_value, "unit": "histories/s",
-                       "ms_per_step": plain_total_ms / len(plain_ms), "roofline": plain_roof},
-        "graph_small_n": graphs,
-        "let_like_misis": misis,
+                       "ms_per_step": plain_total_ms / len(plain_ms),
+                       "bound": "issue (guide bounce loops and Threefry, not HBM)",
+                       "hbm": plain_hbm},
         "fused_over_plain": value / plain_value,
         "roofline": {"bound": "issue", "achieved": achieved_ops / 1e9, "peak": peak_ops / 1e9,
                      "unit": "Gop/s", "frac": achieved_ops / peak_ops,
-                     "traffic": (FUSED_SPLIT2_DRAM_PER_1E7 * plain.last_chunk / 1e7
-                                 if int((tune or {}).get("split", 0)) == 2 else None),
-                     "traffic_unit": "bytes per launch (stage A + B)",
-                     "ncu_stage_a": (FUSED_SPLIT2_STAGE_A_ISSUE
-                                     if int((tune or {}).get("split", 0)) == 2 else None),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                       "1e7-history split launch, scaled by histories",
+                     "traffic": traffic,
+                     "traffic_unit": "DRAM bytes per launch (all its kernels)",
+                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per "
+                                        "history of the capture recorded for these kernel "
+                                        "sources, times the histories of the launch"
+                                        if counters else stale),
                      "kernel": "k_fused", "kernel_ms": kern_ms, "draws_per_launch": draws,
                      "ops_per_draw": THREEFRY_OPS,
                      "peak_source": "measured: Threefry-only kernel (ramp_debug_rng_peak), "
                                     "%d threads x %d x 2 blocks" % (out.numel(), iters),
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
-        "issue_roofline": issue_roofline(value, clk, dev, tune),
+        "issue_roofline": issue_roofline(value, clk, dev, counters),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "histories/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
@@ -630,6 +857,7 @@ def main():
         "gpu_launches": a.steps * (2 if int((tune or {}).get("split", 0)) > 0 else 1),
         "clocks": clk,
     }
+    line.update(extras)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

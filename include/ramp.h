@@ -234,14 +234,14 @@ typedef struct RampTune {
                                    waiting neutron (buffer as for
                                    `split`).  Ignored without such a
                                    component.                            */
-  int32_t regroup;              /* fused path with a split: 1 + index of
-                                   a guide component of a linear block
-                                   before the split point (0: off;
-                                   ignored by a mesh walk, by chains with
-                                   an extended kind and by
+  int32_t regroup;              /* fused path with a split: 1 when the
+                                   first component is a guide of a
+                                   linear block before the split point
+                                   (0: off; ignored by a mesh walk, by
+                                   chains with an extended kind and by
                                    ramp_trace_batched_noalloc).  Each warp
-                                   traces its work item (128 neutrons)
-                                   up to that guide, holds them in
+                                   draws its work item (128 neutrons)
+                                   from the moderator, holds them in
                                    shared memory (52 KB per CTA) and
                                    takes them 32 at a time in order of
                                    the guide's expected bounce passes,

@@ -536,8 +536,9 @@ void g_sphere_int(float* n, float* s, uint32_t* iidx, const RampComp& k) {
 }
 
 /* intersect_box — mcramp/geom/box.cl:3-53 (no earliest-hit comparison).
- * The kernel never loads the intersection record (box.cl:10) and writes
- * its local copy back on a miss too (:52): uninitialised, read as zeros. */
+ * The kernel never loads the intersection record (box.cl:10) and stores
+ * its local copy back on a miss too (:52): a store of an undefined value,
+ * which an optimising OpenCL compiler removes, so the record is kept. */
 void g_box(float* n, float* s, uint32_t* iidx, const RampComp& k) {
   V3 pos = npos(n), vel = nvel(n);
   V3 A = v3(-k.gp[0] / 2.0f, -k.gp[1] / 2.0f, -k.gp[2] / 2.0f);
@@ -547,8 +548,8 @@ void g_box(float* n, float* s, uint32_t* iidx, const RampComp& k) {
   float t4 = dB.y / vel.y, t5 = dA.z / vel.z, t6 = dB.z / vel.z;
   float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
   float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
-  if (tmax < 0.0f || tmin > tmax) {
-    for (int q = 0; q < 8; ++q) s[q] = 0.0f;
+  if (tmax < 0.0f) {
+  } else if (tmin > tmax) {
   } else {
     V3 p1 = add(pos, mul(tmin, vel)), p2 = add(pos, mul(tmax, vel));
     s[0] = p1.x; s[1] = p1.y; s[2] = p1.z; s[3] = tmin;

@@ -23,7 +23,10 @@
  *
  * The build (oracle/refcl/build.py) compiles with -fsingle-precision-constant
  * (unsuffixed floating constants are float, as on an OpenCL device without
- * cl_khr_fp64) and -ffp-contract=off.  The only change made to the
+ * cl_khr_fp64), -ffp-contract=off and -ftrivial-auto-var-init=zero (a scalar
+ * read before it is written reads 0).  Vector variables declared without a
+ * value hold an "undefined" pattern instead, which a store to memory skips
+ * (see refcl_undef below).  The only change made to the
  * reference sources is the mechanical rewrite of OpenCL vector literals
  * "(floatN)(...)" / "(floatN){...}" to "floatN(...)" / "floatN{...}", which
  * C++ would otherwise parse as a cast of a comma expression.
@@ -66,6 +69,24 @@ extern thread_local uint refcl_gid;
 static inline uint get_global_id(uint) { return refcl_gid; }
 
 /* ---- vector types ------------------------------------------------------ */
+/* The bit pattern of an uninitialised vector component.  The reference's
+ * box.cl declares its intersection record without initialising it and, on
+ * a miss, stores it back unchanged (box.cl:10,52): the store of an undefined
+ * value, which LLVM-based OpenCL compilers remove, so the record in memory
+ * keeps its previous contents.  Vector components carry this pattern until
+ * they are assigned, and a vector store skips them. */
+static inline float refcl_undef() {
+  const uint32_t u = 0x7fa5a5a5u;
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+static inline bool refcl_is_undef(float f) {
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return u == 0x7fa5a5a5u;
+}
+
 /* a multi-component swizzle: a view of components I... of the enclosing
  * vector (all union members start at the vector's first component) */
 template <int... I> struct swz;
@@ -121,9 +142,18 @@ template <int... I> struct swz {
 };
 
 #define REFCL_VEC_COMMON(T, N)                                             \
-  T() { for (int k = 0; k < N; ++k) v[k] = 0.0f; }                         \
+  /* an uninitialised vector: every component holds the "undefined"     \
+     pattern (a signalling NaN that arithmetic never produces) */          \
+  T() { for (int k = 0; k < N; ++k) v[k] = refcl_undef(); }               \
   T(const T& o) { memcpy(v, o.v, sizeof(v)); }                             \
-  T& operator=(const T& o) { memcpy(v, o.v, sizeof(v)); return *this; }   \
+  /* storing a vector: components still undefined leave the destination   \
+     as it was, as an optimising OpenCL compiler drops the store of an     \
+     undefined value */                                                    \
+  T& operator=(const T& o) {                                               \
+    for (int k = 0; k < N; ++k)                                            \
+      if (!refcl_is_undef(o.v[k])) v[k] = o.v[k];                          \
+    return *this;                                                          \
+  }                                                                        \
   /* (T)(scalar): every component; (T)(a, b, ...): the parts in order */   \
   template <class A0, class... A,                                          \
             class = typename std::enable_if<                               \

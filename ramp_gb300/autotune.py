@@ -128,20 +128,17 @@ def split_point(inst, alive, threshold=0.5):
 
 
 def regroup_point(inst, split):
-    """RampTune.regroup for the first guide component before the split
-    point (in a linear block, no extended kinds in the chain), or 0."""
+    """RampTune.regroup (1) when the chain's first component is a guide in a
+    linear block before the split point and the chain has no extended
+    kinds, else 0."""
     if split <= 0:
         return 0
     src, carr, nc, barr, nb = inst.descriptors([])
     if src.kind == _abi.SRC_ISIS or any(carr[j].scat in (_abi.S_MONO, _abi.S_POWDER1)
                                         for j in range(nc)):
         return 0
-    for k in range(nb):
-        if not barr[k].linear:
-            continue
-        for j in range(barr[k].first, min(barr[k].first + barr[k].count, split)):
-            if carr[j].scat == _abi.S_GUIDE:
-                return j + 1
+    if nc and nb and barr[0].first == 0 and barr[0].linear and carr[0].scat == _abi.S_GUIDE:
+        return 1
     return 0
 
 

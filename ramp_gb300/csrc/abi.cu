@@ -641,6 +641,11 @@ static int tune_regroup(const RampPlan* p, const RampTune* tune, int32_t split, 
     set_err("RampTune.regroup %d: component %d is not a guide", tune->regroup, g);
     return RAMP_E_INVALID;
   }
+  if (g != 0) {
+    set_err("RampTune.regroup %d: regrouping is done at the moderator, before component 0",
+            tune->regroup);
+    return RAMP_E_INVALID;
+  }
   if (split <= 0 || g >= split) {
     set_err("RampTune.regroup %d: regrouping is part of stage A: it needs a split after the "
             "guide (split %d)", tune->regroup, split);

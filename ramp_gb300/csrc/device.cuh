@@ -583,14 +583,11 @@ DI bool g_box(const CompDev& c, const Nt& n, Is& s) {
   float t4 = dB.y / vel.y, t5 = dA.z / vel.z, t6 = dB.z / vel.z;
   float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
   float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
-  if (tmax < 0.0f || tmin > tmax) {
-    /* box.cl:10,52: the kernel never loads the record and writes its
-       uninitialised local copy back on a miss; read as zeros, that clears
-       the hit of an earlier component of a non-linear block */
-    s.x1 = 0.0f; s.y1 = 0.0f; s.z1 = 0.0f; s.t1 = 0.0f;
-    s.x2 = 0.0f; s.y2 = 0.0f; s.z2 = 0.0f; s.t2 = 0.0f;
-    return false;
-  }
+  /* box.cl:10,52: on a miss the kernel stores its never-initialised local
+     record, a store of an undefined value that the OpenCL compiler drops:
+     the record keeps what earlier components left */
+  if (tmax < 0.0f) return false;
+  if (tmin > tmax) return false;
   V3 p1 = add(pos, mul(tmin, vel)), p2 = add(pos, mul(tmax, vel));
   s.x1 = p1.x; s.y1 = p1.y; s.z1 = p1.z; s.t1 = tmin;
   s.x2 = p2.x; s.y2 = p2.y; s.z2 = p2.z; s.t2 = tmax;

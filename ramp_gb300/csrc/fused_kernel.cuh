@@ -100,9 +100,10 @@ template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
 __global__ void __launch_bounds__(256, MINB)
 k_fused(const FusedArgs a);
 
-/* PHASE 5: stage A as PHASE 1, regrouped before guide a.regroup - 1: each
- * warp takes its work item up to the guide, holds it in shared memory and
- * continues it 32 neutrons at a time in order of expected bounce passes.
+/* PHASE 5: stage A as PHASE 1, regrouped before guide a.regroup - 1 (the
+ * first component): each warp draws its work item from the moderator,
+ * holds it in shared memory and continues it 32 neutrons at a time in
+ * order of the guide's expected bounce passes.
  *
  * PHASE 2: the survivors of stage A through components [split, end).
  * Stage A leaves the survivors of work item t at slots [128 t, 128 t +
@@ -376,11 +377,12 @@ k_fused(const FusedArgs a) {
       const bool zx = !carry;
       int kept = 0;      /* PHASE 1, 5: survivors of this item so far (warp-uniform) */
       if constexpr (RG) {
-        /* Regrouped item: every neutron runs up to guide G, waits in this
-         * warp's shared-memory slots, and the warp then takes them 32 at a
-         * time in order of the guide's expected bounce passes, so the lanes
-         * of a warp leave the bounce loop at about the same pass.  Each
-         * neutron's trace is the same as without regrouping. */
+        /* Regrouped item: every neutron leaves the moderator, waits in
+         * this warp's shared-memory slots, and the warp then takes them 32
+         * at a time in order of the expected bounce passes of guide G (the
+         * first component), so the lanes of a warp leave the bounce loop at
+         * about the same pass.  Each neutron's trace is the same as without
+         * regrouping. */
         extern __shared__ uint32_t rg_smem[];
         const int G = a.regroup - 1;
         uint32_t* const S = rg_smem + (threadIdx.x >> 5) * (RG_WORDS * FUSED_WARP_TASK);
@@ -398,7 +400,6 @@ k_fused(const FusedArgs a) {
             uint32_t ii = carry ? a.carry_iidx[i] : 0u;
             generate<TallyOnly, EXT>(V->src, n, old_sb, num_sim, seed, r);
             if (zx && n.p == 0.0f) n.die = 1.0f;
-            run_range<EXT>(a, comps, 0, G, n, ii, r, zx);
             if (!(n.die > 0.f)) {
               uint32_t* w = S + j;
               w[0 * FUSED_WARP_TASK] = __float_as_uint(n.x);

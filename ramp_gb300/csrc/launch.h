@@ -55,7 +55,7 @@ struct FusedArgs {
   int32_t ext;                  /* the chain uses an extended kind (MISIS source,
                                    SMonochromator, SPowder1): the kernels built
                                    with them (split only when not BATCHED) */
-  int32_t regroup;              /* 1 + index of a guide component of stage A
+  int32_t regroup;              /* 1: the first component is a guide of stage A,
                                    before which each warp regroups its work
                                    item by expected bounce passes (PHASE 5:
                                    shared memory, RG_WORDS x 128 words per

@@ -6,6 +6,8 @@ import torch
 from .sprim import SPrim, _device
 from .. import _abi
 
+_GRIDS = {}   # (binnings, bin counts) -> (X, Y) coordinate grids
+
 VAR_DICT = {"x": 0, "y": 1, "theta": 2, "alpha": 3, "phi": 4, "tof": 5, "divX": 6, "divY": 7,
             "wavelength": 8, "energy": 9, "angle": 10}
 
@@ -66,13 +68,22 @@ class SDetector2D(SPrim):
         return [self.histo_t, self.histo_err_t]
 
     def _grid(self):
-        # bin-coordinate grids, built on first use (two n2 x n1 float64 arrays)
+        # bin-coordinate grids (two n2 x n1 float64 arrays), built once per
+        # binning in the process and shared read-only by every detector
         if self._XY is None:
-            x = np.linspace(self.axis1_binning[0], self.axis1_binning[2],
-                            num=int(self.axis1_num_bins))
-            y = np.linspace(self.axis2_binning[0], self.axis2_binning[2],
-                            num=int(self.axis2_num_bins))
-            self._XY = np.meshgrid(x, y)
+            key = (tuple(self.axis1_binning.tolist()), int(self.axis1_num_bins),
+                   tuple(self.axis2_binning.tolist()), int(self.axis2_num_bins))
+            XY = _GRIDS.get(key)
+            if XY is None:
+                x = np.linspace(self.axis1_binning[0], self.axis1_binning[2],
+                                num=int(self.axis1_num_bins))
+                y = np.linspace(self.axis2_binning[0], self.axis2_binning[2],
+                                num=int(self.axis2_num_bins))
+                XY = np.meshgrid(x, y)
+                for g in XY:
+                    g.setflags(write=False)
+                _GRIDS[key] = XY
+            self._XY = XY
         return self._XY
 
     @property

@@ -344,14 +344,14 @@ def test_fused_split_with_multi_chunk_carry(cuda_lib):
 @pytest.mark.parametrize("tune,rng,chunk,N", [
     ({"split": 2, "regroup": 1}, "reference", None, 1_000_000),
     ({"split": 2, "regroup": 1, "blocks_per_sm": 3}, "native", None, 600_001),
-    ({"split": 5, "regroup": 4}, "reference", None, 1_000_000),
+    ({"split": 5, "regroup": 1}, "reference", None, 1_000_000),
     ({"split": 2, "regroup": 1}, "reference", 100_000, 250_001)])
 def test_fused_regroup_matches_oracle(cuda_lib, tune, rng, chunk, N):
     """Stage A regrouped before a guide (each warp's 128 neutrons held in
     shared memory and continued in order of expected bounce passes): the
     traces are unchanged, so the tallies equal the oracle's up to the order
-    of additions; also with carry buffers across chunks and before a later
-    guide (component 3: guide 2 behind choppers 1 and 2)."""
+    of additions; also with carry buffers across chunks and with a longer
+    stage A (split before guide 3)."""
     gi, ci, r = pair(I.path("let_like.json"), I.let_like_kwargs(), N, path="fused", rng=rng,
                      chunk=chunk, tune=tune)
     tallies_close(gi, ci)
@@ -364,6 +364,8 @@ def test_fused_regroup_refused_where_it_cannot_apply(cuda_lib):
         gi.execute(1000, path="fused", tune={"split": 3, "regroup": 2})    # a chopper
     with pytest.raises(RuntimeError, match="needs a split"):
         gi.execute(1000, path="fused", tune={"regroup": 1})
+    with pytest.raises(RuntimeError, match="at the moderator"):
+        gi.execute(1000, path="fused", tune={"split": 5, "regroup": 4})   # guide 2
 
 
 @pytest.mark.parametrize("tune", [{"split": 2, "regroup": 1},
