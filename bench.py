@@ -125,7 +125,7 @@ def profile_counters(tune):
     if c.get("kernel_source_sha") != kernel_source_sha():
         return None, "recorded capture is of other kernel sources (%s)" % c.get(
             "kernel_source_sha")
-    keys = ("split", "regroup", "walk")
+    keys = ("split", "walk", "privatize", "block")
     if any(int((tune or {}).get(k, 0)) != int(c.get("tune", {}).get(k, 0)) for k in keys):
         return None, "recorded capture is of another launch configuration"
     return c, None
@@ -367,7 +367,7 @@ def measure_batched(config, steps, warmup, tune_arg="auto", variants=0, plain=Tr
         # the component structure)
         from ramp_gb300 import autotune
         tune = {k: v for k, v in autotune.tune(B.instruments[0], rng="reference").items()
-                if k in ("blocks_per_sm", "split", "walk", "regroup")}
+                if k in ("block", "blocks_per_sm", "split", "walk")}
     else:
         tune = json.loads(tune_arg) if tune_arg else None
     for w in range(warmup):

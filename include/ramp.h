@@ -197,17 +197,23 @@ typedef struct RampVariant {
 /* Launch configuration of the whole-chain kernels, chosen by the
  * autotuner (ramp_gb300/autotune.py); 0 = default.                        */
 typedef struct RampTune {
-  int32_t block;                /* reserved, 0: the whole-chain kernels are
-                                   compiled for 256-thread CTAs          */
+  int32_t block;                /* threads per CTA: 256 (0) or 128 (the
+                                   whole-chain kernels are compiled for at
+                                   most 256); blocks_per_sm counts CTAs
+                                   of this size                          */
   int32_t blocks_per_sm;        /* persistent CTAs per SM (register cap:
                                    3 or 4; 0: 4)                         */
   int32_t chunk;                /* neutrons per span; sizes the grid of a
                                    single-instrument launch (0: about
                                    eight spans per resident CTA)        */
-  int32_t privatize;            /* reserved, 0: tallies are warp-aggregated
-                                   atomics into L2; shared-memory copies
-                                   do not fit detector histograms of the
-                                   sizes traced here (720 x 1000 x 2)    */
+  int32_t privatize;            /* ramp_trace_fused without split or walk:
+                                   1 = detectors (SDetector1D/2D) whose two
+                                   histograms fit, in chain order, in 48 KB
+                                   of shared memory are accumulated per
+                                   CTA there and merged into global memory
+                                   as the CTA ends (0: warp-aggregated
+                                   atomics into L2, the only choice for
+                                   larger histograms)                   */
   int32_t split;                /* fused path: split the chain before this
                                    component (0: off; not inside a
                                    non-linear block).  Stage A appends the
@@ -234,21 +240,6 @@ typedef struct RampTune {
                                    waiting neutron (buffer as for
                                    `split`).  Ignored without such a
                                    component.                            */
-  int32_t regroup;              /* fused path with a split: 1 when the
-                                   first component is a guide of a
-                                   linear block before the split point
-                                   (0: off; ignored by a mesh walk, by
-                                   chains with an extended kind and by
-                                   ramp_trace_batched_noalloc).  Each warp
-                                   draws its work item (128 neutrons)
-                                   from the moderator, holds them in
-                                   shared memory (52 KB per CTA) and
-                                   takes them 32 at a time in order of
-                                   the guide's expected bounce passes,
-                                   so a warp's lanes leave the bounce
-                                   loop together.  Traces are unchanged;
-                                   only the order of tally additions
-                                   differs.                              */
 } RampTune;
 
 typedef struct RampPlan RampPlan;

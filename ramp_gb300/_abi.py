@@ -83,11 +83,10 @@ class RampTune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("chunk", ctypes.c_int32), ("privatize", ctypes.c_int32),
                 ("split", ctypes.c_int32), ("streams", ctypes.c_int32),
-                ("walk", ctypes.c_int32), ("regroup", ctypes.c_int32)]
+                ("walk", ctypes.c_int32)]
 
 
-TUNE_KEYS = ("block", "blocks_per_sm", "chunk", "privatize", "split", "streams", "walk",
-             "regroup")
+TUNE_KEYS = ("block", "blocks_per_sm", "chunk", "privatize", "split", "streams", "walk")
 
 
 def tune_struct(tune):

@@ -6,9 +6,10 @@ be chosen purely for speed.  ``tune(inst)`` times short fused runs of the
 instrument over the candidates (register cap = minimum CTAs per SM, the
 span of neutrons a task covers, whether survivors are compacted into
 full warps before the first component that less than half of the
-histories reach — found by a plain-path pilot, ``survival`` — whether
-stage A regroups each warp's neutrons by expected bounce passes before
-the first guide, and, for chains with a mesh, the per-lane mesh walk) and keeps the fastest; results are
+histories reach — found by a plain-path pilot, ``survival`` — 128- against
+256-thread CTAs, shared-memory private
+tallies for chains whose detectors fit, and, for chains with a mesh, the
+per-lane mesh walk) and keeps the fastest; results are
 cached in a JSON file keyed by GPU name, the instrument's component
 structure and the keying mode.  Tuning uses fixed seeds and restores the
 instrument's tallies afterwards: it leaves no trace in the results or in
@@ -127,19 +128,13 @@ def split_point(inst, alive, threshold=0.5):
     return 0
 
 
-def regroup_point(inst, split):
-    """RampTune.regroup (1) when the chain's first component is a guide in a
-    linear block before the split point and the chain has no extended
-    kinds, else 0."""
-    if split <= 0:
-        return 0
-    src, carr, nc, barr, nb = inst.descriptors([])
-    if src.kind == _abi.SRC_ISIS or any(carr[j].scat in (_abi.S_MONO, _abi.S_POWDER1)
-                                        for j in range(nc)):
-        return 0
-    if nc and nb and barr[0].first == 0 and barr[0].linear and carr[0].scat == _abi.S_GUIDE:
-        return 1
-    return 0
+def privatizable(inst):
+    """Whether a detector of the chain has histograms small enough for the
+    shared-memory private tallies of a whole-chain launch (two float
+    histograms within 48 KB)."""
+    _, carr, nc, _, _ = inst.descriptors([])
+    return any(carr[j].scat in (_abi.S_DET1D, _abi.S_DET2D) and
+               0 < 2 * carr[j].tally_len <= 12288 for j in range(nc))
 
 
 def has_mesh(inst):
@@ -184,9 +179,11 @@ def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False
     if candidates is None:
         split = split_point(inst, survival(inst, min(n_probe, 1_000_000), rng))
         candidates = [dict(c, split=k) for c in CANDIDATES for k in ((0, split) if split else (0,))]
-        g = regroup_point(inst, split)
-        if g:
-            candidates += [dict(c, split=split, regroup=g) for c in CANDIDATES]
+        # 128-thread CTAs at the same threads per SM, with the best split
+        candidates += [dict(block=128, blocks_per_sm=2 * b, split=split)
+                       for b in (3, 4)]
+        if privatizable(inst):
+            candidates += [dict(c, privatize=1) for c in CANDIDATES]
         if has_mesh(inst):
             candidates += [dict(c, walk=1) for c in CANDIDATES]
     with torch.cuda.device(inst.device):

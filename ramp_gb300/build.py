@@ -26,9 +26,7 @@ CU_SOURCES = ["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
 FUSED_INSTANCES = ([(mb, mode, b, ph, x) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)
                     for x in (0, 1) for ph in (0, 1, 2) if not (b and x and ph)]
                    # phase 4: stage B walking a mesh per lane (without the extended kinds)
-                   + [(mb, mode, b, 4, 0) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)]
-                   # phase 5: stage A regrouped before a guide (without the extended kinds)
-                   + [(mb, mode, b, 5, 0) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)])
+                   + [(mb, mode, b, 4, 0) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)])
 CPP_SOURCES = ["bvh.cpp"]
 HEADERS = ["device.cuh", "fused_kernel.cuh", "mesh.cuh", "plan.h", "launch.h", "rmath.h", "rconst.h", "bvh.h",
            os.path.join("..", "..", "include", "ramp.h")]

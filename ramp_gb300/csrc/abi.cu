@@ -97,6 +97,7 @@ struct RampPlan {
   RecKey rec;                        /* the launch that filled adj_list       */
   bool rec_valid = false;
   uint64_t param_version = 0;        /* bumped when ramp_plan_set_param changes a value */
+  CompDev* priv_dev = nullptr;       /* descriptors of a private-tally launch */
   uint32_t* surv = nullptr;          /* survivor buffer of split launches */
   int64_t surv_cap = 0;              /* slots (128 per work item) */
   StreamSet streams;
@@ -378,6 +379,7 @@ static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo 
   memcpy(d.gi, c.gi, sizeof(d.gi));
   memcpy(d.si, c.si, sizeof(d.si));
   for (int k = 0; k < 6; ++k) d.dslot[k] = -1;
+  d.priv_off = -1;
   if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
   /* chopper slit period 2 pi / n_slits (chopper.cl:21), per component */
   if (c.scat == RAMP_S_CHOPPER) d.aux[0] = 2.0f * RC_PI / (float)(uint32_t)c.si[0];
@@ -579,11 +581,14 @@ static int batched_grid(int64_t n_max, int grid) {
 
 static void tune_defaults(RampPlan* p, const RampTune* tune, int& block, int& grid,
                           int64_t& task, int32_t& minb) {
-  block = 256;   /* the fused kernel is compiled for 256-thread CTAs */
-  /* register cap (minimum CTAs per SM the kernel is compiled for): 4 by
-     default, the fastest measured on GB300 for every chain tried (single,
-     split, batched); 3 on request */
-  minb = (tune && tune->blocks_per_sm > 0 && tune->blocks_per_sm < 4) ? 3 : 4;
+  /* CTAs of 256 threads, or 128 on request (the kernels are compiled for
+     at most 256 threads a CTA) */
+  block = (tune && tune->block == 128) ? 128 : 256;
+  /* register cap (minimum 256-thread CTAs per SM the kernel is compiled
+     for): 4 by default, the fastest measured on GB300 for every chain
+     tried (single, split, batched); 3 when fewer than 4 x 256 threads per
+     SM are asked for */
+  minb = (tune && tune->blocks_per_sm > 0 && tune->blocks_per_sm * block < 4 * 256) ? 3 : 4;
   int bps = (tune && tune->blocks_per_sm > 0) ? tune->blocks_per_sm
                                               : fused_max_blocks_per_sm(block, minb);
   grid = p->sm_count * bps;
@@ -630,33 +635,43 @@ static int tune_stage(const RampPlan* p, const RampTune* tune, bool ext, int32_t
   return tune_split(p, tune, split);
 }
 
-/* the regroup point of a fused launch (RampTune.regroup = 1 + index of a
- * guide component): in a linear block and before the launch's stage
- * split (regrouping is a form of stage A; a mesh walk launch ignores it) */
-static int tune_regroup(const RampPlan* p, const RampTune* tune, int32_t split, int32_t* out) {
-  *out = 0;
-  if (!tune || tune->regroup <= 0) return RAMP_OK;
-  const int g = tune->regroup - 1;
-  if (g >= (int)p->comps.size() || p->comps[g].scat != RAMP_S_GUIDE) {
-    set_err("RampTune.regroup %d: component %d is not a guide", tune->regroup, g);
-    return RAMP_E_INVALID;
+/* The descriptors of a whole-chain launch with private tallies
+ * (RampTune.privatize): detectors (SDetector1D, SDetector2D) whose two
+ * histograms fit in what is left of RAMP_PRIV_FLOATS shared-memory floats
+ * get an offset there, in chain order; the copy goes to a plan-owned
+ * device array.  Returns the floats used (0: none fits, nothing to do). */
+static int priv_descriptors(RampPlan* p, cudaStream_t s, int32_t* floats) {
+  *floats = 0;
+  std::vector<CompDev> c = p->comps;
+  int used = 0;
+  for (CompDev& d : c) {
+    if (d.scat != RAMP_S_DET1D && d.scat != RAMP_S_DET2D) continue;
+    if (!d.tally || !d.tally_err || d.tally_len <= 0) continue;
+    const int64_t need = 2 * d.tally_len;
+    if (used + need > RAMP_PRIV_FLOATS) continue;
+    d.priv_off = used;
+    used += (int)need;
   }
-  if (g != 0) {
-    set_err("RampTune.regroup %d: regrouping is done at the moderator, before component 0",
-            tune->regroup);
-    return RAMP_E_INVALID;
-  }
-  if (split <= 0 || g >= split) {
-    set_err("RampTune.regroup %d: regrouping is part of stage A: it needs a split after the "
-            "guide (split %d)", tune->regroup, split);
-    return RAMP_E_INVALID;
-  }
-  for (const RampBlock& B : p->blocks)
-    if (!B.linear && B.first <= g && g < B.first + B.count) {
-      set_err("RampTune.regroup %d: the guide is inside a non-linear block", tune->regroup);
-      return RAMP_E_INVALID;
+  if (used == 0) return RAMP_OK;
+  if (!p->priv_dev) {
+    void* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, c.size() * sizeof(CompDev));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_err("private-tally descriptors: %s", cudaGetErrorString(e));
+      return RAMP_E_NOMEM;
     }
-  *out = g + 1;
+    p->priv_dev = (CompDev*)d;
+    p->allocs.push_back(d);
+  }
+  /* pageable source: the copy is staged before cudaMemcpyAsync returns */
+  cudaError_t e = cudaMemcpyAsync(p->priv_dev, c.data(), c.size() * sizeof(CompDev),
+                                  cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) {
+    set_err("private-tally descriptors: %s", cudaGetErrorString(e));
+    return RAMP_E_CUDA;
+  }
+  *floats = used;
   return RAMP_OK;
 }
 
@@ -834,7 +849,10 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.workq = &p->status->workq;
   a.workq_b = &p->status->workq_b;
   int rc = tune_stage(p, tune, p->ext, &a.split, &a.walk);
-  if (!rc && !p->ext) rc = tune_regroup(p, tune, a.split, &a.regroup);
+  if (!rc && tune && tune->privatize > 0 && a.split == 0 && !a.walk) {
+    rc = priv_descriptors(p, s, &a.priv_floats);
+    if (!rc && a.priv_floats > 0) a.single.comps = p->priv_dev;
+  }
   if (rc) return rc;
   a.ext = p->ext ? 1 : 0;
   if (a.split > 0 || a.walk) {
@@ -868,7 +886,6 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
      buffer (its items' slots, SoA, and its items' counts) */
   int32_t split = 0, walk = 0;
   int rc0 = tune_stage(p, tune, base.ext != 0, &split, &walk);
-  if (!rc0 && !base.ext) rc0 = tune_regroup(p, tune, split, &base.regroup);
   if (rc0) return rc0;
   std::vector<int64_t> item_off(nv + 1, 0);
   for (size_t v = 0; v < nv; ++v)
@@ -1067,8 +1084,6 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.split = split;
   a.walk = walk;
   a.ext = ext ? 1 : 0;
-  if (!ext) rc = tune_regroup(p, tune, split, &a.regroup);
-  if (rc) return rc;
   if (a.split > 0 || a.walk) {
     rc = attach_surv(p, a, items, s);
     if (rc) return rc;

@@ -173,7 +173,19 @@ DI void raise_flag(StatusDev* st, unsigned int f) { atomicOr(&st->flags, f); }
  * flushes the same way). */
 DI float ftz(float x) { return fabsf(x) < 1.17549435e-38f ? copysignf(0.0f, x) : x; }
 
-DI void tally_add(float* h, float* he, long long idx, float p) {
+/* shared memory of a whole-chain launch with private tallies */
+extern __shared__ float ramp_dyn_smem[];
+
+/* A detector's histograms: its CTA-private copies in shared memory when the
+ * launch privatises them (merged into global memory as the CTA ends), else
+ * the global ones. */
+DI void tally_add(const CompDev& c, long long idx, float p) {
+  float* h = c.tally;
+  float* he = c.tally_err;
+  if (c.priv_off >= 0) {
+    h = ramp_dyn_smem + c.priv_off;
+    he = c.tally_err ? h + c.tally_len : nullptr;
+  }
   unsigned m = __activemask();
   unsigned peers = __match_any_sync(m, idx) & __match_any_sync(m, (unsigned long long)h);
   int lane = threadIdx.x & 31;
@@ -783,34 +795,6 @@ DI void s_guide(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
   s_guide_end(c, n, s, ii, i);
 }
 
-/* Expected passes of guide c's bounce loop for a neutron about to reach it:
- * a grouping key for the fused path (which neutrons share a warp), never a
- * value of the trace.  In the guide's frame the neutron crosses the
- * entrance plane at (x0, y0); unfolding the walls of a straight guide of
- * width w, it leaves after |floor(u / w)| reflections in x, u = x0 + w/2 +
- * l vx/vz, and likewise in y.  A reflection with zero reflectivity (q
- * beyond m Qc + 10 W, q = 2 V2K |v| for the walls of a straight guide) ends
- * the loop at the first wall.  0: the neutron misses the entrance. */
-DI uint32_t guide_passes_key(const CompDev& c, const Nt& n0) {
-  Nt n = n0;
-  transform<false>(c, n);
-  if (!(n.vz > 0.0f)) return 0u;
-  const float w = c.sp[0], h = c.sp[1], l = c.sp[4];
-  const float ivz = __frcp_rn(n.vz);
-  const float t0 = -n.z * ivz;
-  const float x0 = n.x + t0 * n.vx, y0 = n.y + t0 * n.vy;
-  if (!(fabsf(x0) < 0.5f * w && fabsf(y0) < 0.5f * h)) return 0u;
-  const float ux = (x0 + 0.5f * w + l * n.vx * ivz) / w;
-  const float uy = (y0 + 0.5f * h + l * n.vy * ivz) / h;
-  const float nx = fabsf(floorf(ux)), ny = fabsf(floorf(uy));
-  const float W = c.aux[9];
-  const float qcut = (W > 0.0f && c.aux[15] == 0.0f) ? c.aux[12] + 10.0f * W : -1.0f;
-  const bool kx = nx > 0.0f && 2.0f * RC_V2K * fabsf(n.vx) > qcut;
-  const bool ky = ny > 0.0f && 2.0f * RC_V2K * fabsf(n.vy) > qcut;
-  const float passes = (kx || ky) ? 2.0f : 1.0f + fminf(nx + ny, 60.0f);
-  return (uint32_t)passes;
-}
-
 /* chopper.cl:4-59 */
 DI void s_chopper(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r) {
   const float slit_width = c.sp[0], radius = c.sp[1], freq = c.sp[2], phase = c.sp[3];
@@ -1284,7 +1268,7 @@ DI void s_det1d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
         if constexpr (D::rec) {
           if (c.adj_det) dx->hit();
         }
-        if constexpr (D::tally) tally_add(c.tally, c.tally_err, idx, n.p);
+        if constexpr (D::tally) tally_add(c, idx, n.p);
       }
     } else if constexpr (D::tally) {
       if (n.p != 0.0f) atomicAdd(&st->oob, 1ull);   /* a nonzero weight was lost */
@@ -1336,7 +1320,7 @@ DI void s_det2d(const CompDev& c, Nt& n, Is& s, uint32_t& ii, StatusDev* st, D* 
         if constexpr (D::rec) {
           if (c.adj_det) dx->hit();
         }
-        if constexpr (D::tally) tally_add(c.tally, c.tally_err, flat, n.p);
+        if constexpr (D::tally) tally_add(c, flat, n.p);
       }
     } else if constexpr (D::tally) {
       if (n.p != 0.0f) atomicAdd(&st->oob, 1ull);   /* a nonzero weight was lost */

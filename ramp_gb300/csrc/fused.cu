@@ -14,7 +14,6 @@
   PH(MB, MODE, true, 0, false) PH(MB, MODE, true, 1, false) PH(MB, MODE, true, 2, false)    \
   PH(MB, MODE, false, 0, true) PH(MB, MODE, false, 1, true) PH(MB, MODE, false, 2, true)    \
   PH(MB, MODE, true, 0, true) PH(MB, MODE, false, 4, false) PH(MB, MODE, true, 4, false)    \
-  PH(MB, MODE, false, 5, false) PH(MB, MODE, true, 5, false)                                \
   extern template int occ_mm<MB, MODE>(int);
 ONE_MODE(3, 0)
 ONE_MODE(3, 1)
@@ -31,13 +30,6 @@ static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream
       const cudaError_t e = launch_phase<MB, MODE, BATCHED, 1, false>(a, block, grid, s);
       if (e != cudaSuccess) return e;
       return launch_phase<MB, MODE, BATCHED, 4, false>(a, block, grid, s);
-    }
-  }
-  if constexpr (!EXT) {
-    if (a.split > 0 && a.regroup > 0) {
-      const cudaError_t e = launch_phase<MB, MODE, BATCHED, 5, false>(a, block, grid, s);
-      if (e != cudaSuccess) return e;
-      return launch_phase<MB, MODE, BATCHED, 2, false>(a, block, grid, s);
     }
   }
   if constexpr (!(BATCHED && EXT)) {

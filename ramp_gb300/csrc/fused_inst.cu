@@ -3,8 +3,7 @@
  * The build compiles this file once per template argument set, each with
  * -DFK_MINB (register cap: minimum CTAs per SM), -DFK_MODE (RNG keying),
  * -DFK_BATCHED (one launch, a grid row per variant), -DFK_PHASE (0 whole
- * chain, 1 stage A, 2 stage B, 4 stage B walking a mesh per lane, 5 stage
- * A regrouped before a guide) and
+ * chain, 1 stage A, 2 stage B, 4 stage B walking a mesh per lane) and
  * -DFK_EXT (extended component kinds), so that the kernels compile in
  * parallel.
  */

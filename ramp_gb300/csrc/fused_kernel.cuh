@@ -37,58 +37,6 @@
  * retired at once (zx; the plain path, whose records are output, keeps
  * tracing it as the reference does). */
 
-/* components [k0, k1) of the chain for one neutron, block by block (a
- * non-linear block runs whole; k0 never falls inside one) */
-template <bool EXT>
-DI void run_range(const FusedArgs& a, const CompDev* __restrict__ comps, int k0, int k1, Nt& n,
-                  uint32_t& ii, Rng& r, bool zx) {
-  for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
-    const RampBlock B = a.blocks[b];
-    if (B.first >= k1) break;
-    if (B.first + B.count <= k0) continue;
-    if (B.linear) {
-      const int s0 = B.first > k0 ? B.first : k0;
-      const int e = B.first + B.count > k1 ? k1 : B.first + B.count;
-      for (int k = s0; k < e; ++k) {
-        if (n.die > 0.f) break;
-        comp_linear<TallyOnly, EXT>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
-      }
-    } else {
-      block_nonlinear<TallyOnly>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
-    }
-  }
-}
-
-/* Ascending bitonic sort of the 128 values a warp holds, four per lane
- * (element k*32 + lane in v[k]); every lane runs every step. */
-DI void warp_sort128(uint32_t (&v)[4]) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int size = 2; size <= 128; size <<= 1) {
-#pragma unroll
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int e = k * 32 + lane;
-        const bool up = (e & size) == 0;
-        if (stride >= 32) {
-          const int kk = k ^ (stride >> 5);
-          if (kk > k) {
-            const uint32_t lo = min(v[k], v[kk]), hi = max(v[k], v[kk]);
-            v[k] = up ? lo : hi;
-            v[kk] = up ? hi : lo;
-          }
-        } else {
-          const uint32_t o = __shfl_xor_sync(FULL_MASK, v[k], stride);
-          const bool lower = (lane & stride) == 0;
-          const uint32_t lo = min(v[k], o), hi = max(v[k], o);
-          v[k] = (lower == up) ? lo : hi;
-        }
-      }
-    }
-  }
-}
-
 /*
  * PHASE 0: the whole chain per neutron.  PHASE 1: stage A of a split
  * launch — the moderator and components [0, split); the survivors of work
@@ -100,12 +48,7 @@ template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
 __global__ void __launch_bounds__(256, MINB)
 k_fused(const FusedArgs a);
 
-/* PHASE 5: stage A as PHASE 1, regrouped before guide a.regroup - 1 (the
- * first component): each warp draws its work item from the moderator,
- * holds it in shared memory and continues it 32 neutrons at a time in
- * order of the guide's expected bounce passes.
- *
- * PHASE 2: the survivors of stage A through components [split, end).
+/* PHASE 2: the survivors of stage A through components [split, end).
  * Stage A leaves the survivors of work item t at slots [128 t, 128 t +
  * cnt[t]) (batched: item item_off + t of its variant's row); a warp claims
  * SURV_GROUP items at a time and deals their survivors out 32 to a pass.
@@ -352,16 +295,20 @@ k_fused(const FusedArgs a) {
     fused_tail_walk<MODE, BATCHED, EXT>(a);
     return;
   } else {
-    constexpr bool RG = PHASE == 5;    /* stage A regrouped before a guide */
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    const int KE = (PHASE == 1 || RG) ? a.split : a.n_comps;
+    const int KE = PHASE == 1 ? a.split : a.n_comps;
     const int var = BATCHED ? (int)blockIdx.y : a.var_key;
     const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
     /* batched: CTAs past what this row's variant can use leave at once */
     if (BATCHED && (int64_t)blockIdx.x * (blockDim.x / 32) * FUSED_WARP_TASK >= V->n) return;
     const int64_t item0 = BATCHED ? V->item_off : 0;
     unsigned long long* const q_a = a.workq + (BATCHED ? var : 0);
+    const bool priv = PHASE == 0 && !BATCHED && a.priv_floats > 0;
+    if (priv) {                   /* the CTA's private tallies start at zero */
+      for (int k = threadIdx.x; k < a.priv_floats; k += blockDim.x) ramp_dyn_smem[k] = 0.0f;
+      __syncthreads();
+    }
     for (;;) {
       unsigned long long t = 0;
       if (lane == 0) t = atomicAdd(q_a, 1ull);
@@ -375,117 +322,7 @@ k_fused(const FusedArgs a) {
       const int32_t seed = (a.rng.seed_dev && !BATCHED) ? *a.rng.seed_dev : V->seed;
       const bool carry = (a.carry_sb != nullptr);
       const bool zx = !carry;
-      int kept = 0;      /* PHASE 1, 5: survivors of this item so far (warp-uniform) */
-      if constexpr (RG) {
-        /* Regrouped item: every neutron leaves the moderator, waits in
-         * this warp's shared-memory slots, and the warp then takes them 32
-         * at a time in order of the expected bounce passes of guide G (the
-         * first component), so the lanes of a warp leave the bounce loop at
-         * about the same pass.  Each neutron's trace is the same as without
-         * regrouping. */
-        extern __shared__ uint32_t rg_smem[];
-        const int G = a.regroup - 1;
-        uint32_t* const S = rg_smem + (threadIdx.x >> 5) * (RG_WORDS * FUSED_WARP_TASK);
-        uint32_t key[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int j = k * 32 + lane;
-          uint32_t kv = 0u;
-          if (j < count) {
-            const int64_t i = start + j;
-            Nt n;
-            Rng r;
-            rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
-            const float old_sb = carry ? a.carry_sb[i] : 0.0f;
-            uint32_t ii = carry ? a.carry_iidx[i] : 0u;
-            generate<TallyOnly, EXT>(V->src, n, old_sb, num_sim, seed, r);
-            if (zx && n.p == 0.0f) n.die = 1.0f;
-            if (!(n.die > 0.f)) {
-              uint32_t* w = S + j;
-              w[0 * FUSED_WARP_TASK] = __float_as_uint(n.x);
-              w[1 * FUSED_WARP_TASK] = __float_as_uint(n.y);
-              w[2 * FUSED_WARP_TASK] = __float_as_uint(n.z);
-              w[3 * FUSED_WARP_TASK] = __float_as_uint(n.vx);
-              w[4 * FUSED_WARP_TASK] = __float_as_uint(n.vy);
-              w[5 * FUSED_WARP_TASK] = __float_as_uint(n.vz);
-              w[6 * FUSED_WARP_TASK] = __float_as_uint(n.p);
-              w[7 * FUSED_WARP_TASK] = __float_as_uint(n.t);
-              w[8 * FUSED_WARP_TASK] = __float_as_uint(n.sb);
-              w[9 * FUSED_WARP_TASK] = __float_as_uint(n.sc);
-              w[10 * FUSED_WARP_TASK] = __float_as_uint(n.sd);
-              w[11 * FUSED_WARP_TASK] = __float_as_uint(n.se);
-              w[12 * FUSED_WARP_TASK] = ii;
-              kv = ((guide_passes_key(comps[G], n) + 1u) << 7) | (uint32_t)j;
-            } else if (carry) {
-              a.carry_sb[i] = n.sb;
-              a.carry_iidx[i] = ii;
-            }
-          }
-          key[k] = kv;
-        }
-        __syncwarp();
-        warp_sort128(key);
-#pragma unroll 1
-        for (int k = 3; k >= 0; --k) {
-          /* a select chain, not key[k]: an indexed register array would
-             live in local memory */
-          const uint32_t kv = k == 3 ? key[3] : k == 2 ? key[2] : k == 1 ? key[1] : key[0];
-          const bool has = kv != 0u;
-          if (!__any_sync(FULL_MASK, has)) break;     /* the rest hold no neutron */
-          const int j = (int)(kv & 127u);
-          const int64_t i = start + j;
-          Nt n;
-          Rng r;
-          uint32_t ii = 0u;
-          if (has) {
-            const uint32_t* w = S + j;
-            n.x = __uint_as_float(w[0 * FUSED_WARP_TASK]);
-            n.y = __uint_as_float(w[1 * FUSED_WARP_TASK]);
-            n.z = __uint_as_float(w[2 * FUSED_WARP_TASK]);
-            n.vx = __uint_as_float(w[3 * FUSED_WARP_TASK]);
-            n.vy = __uint_as_float(w[4 * FUSED_WARP_TASK]);
-            n.vz = __uint_as_float(w[5 * FUSED_WARP_TASK]);
-            n.px = 0.0f; n.py = 0.0f; n.pz = 0.0f;
-            n.p = __uint_as_float(w[6 * FUSED_WARP_TASK]);
-            n.t = __uint_as_float(w[7 * FUSED_WARP_TASK]);
-            n.sb = __uint_as_float(w[8 * FUSED_WARP_TASK]);
-            n.sc = __uint_as_float(w[9 * FUSED_WARP_TASK]);
-            n.sd = __uint_as_float(w[10 * FUSED_WARP_TASK]);
-            n.se = __uint_as_float(w[11 * FUSED_WARP_TASK]);
-            n.die = 0.0f;
-            n.wr = 0u;
-            ii = w[12 * FUSED_WARP_TASK];
-            rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
-            run_range<EXT>(a, comps, G, KE, n, ii, r, zx);
-          }
-          const bool alive = has && !(n.die > 0.f);
-          if (has && !alive && carry) { a.carry_sb[i] = n.sb; a.carry_iidx[i] = ii; }
-          const unsigned m = __ballot_sync(FULL_MASK, alive);
-          const int rank = kept + __popc(m & lt);
-          kept += __popc(m);
-          if (!alive) continue;
-          const int64_t sl = (item0 + (int64_t)t) * FUSED_WARP_TASK + rank;
-          if (sl >= a.surv_cap) {
-            raise_flag(a.st, RAMP_F_WORKQ);
-            continue;
-          }
-          const int64_t cap = a.surv_cap;
-          uint32_t* w = a.surv + sl;
-          w[0 * cap] = __float_as_uint(n.x);   w[1 * cap] = __float_as_uint(n.y);
-          w[2 * cap] = __float_as_uint(n.z);   w[3 * cap] = __float_as_uint(n.vx);
-          w[4 * cap] = __float_as_uint(n.vy);  w[5 * cap] = __float_as_uint(n.vz);
-          w[6 * cap] = __float_as_uint(n.px);  w[7 * cap] = __float_as_uint(n.py);
-          w[8 * cap] = __float_as_uint(n.pz);  w[9 * cap] = __float_as_uint(n.p);
-          w[10 * cap] = __float_as_uint(n.t);  w[11 * cap] = __float_as_uint(n.sb);
-          w[12 * cap] = __float_as_uint(n.sc); w[13 * cap] = __float_as_uint(n.sd);
-          w[14 * cap] = __float_as_uint(n.se);
-          w[15 * cap] = ii; w[16 * cap] = (uint32_t)i; w[17 * cap] = (uint32_t)var;
-        }
-        __syncwarp();     /* the slots are refilled by the next item */
-        if (lane == 0 && item0 + (int64_t)t < a.surv_items)
-          a.surv_cnt[item0 + t] = (uint32_t)kept;
-        continue;
-      } else {
+      int kept = 0;      /* PHASE 1: survivors of this item so far (warp-uniform) */
       /* PHASE 1 keeps the whole warp in the loop for the ballot */
       const int jend = PHASE == 1 ? (int)((count + 31) & ~31ll) : (int)count;
       for (int j = lane; j < jend; j += 32) {
@@ -543,6 +380,24 @@ k_fused(const FusedArgs a) {
       }
       if (PHASE == 1 && lane == 0 && item0 + (int64_t)t < a.surv_items)
         a.surv_cnt[item0 + t] = (uint32_t)kept;
+    }
+    if (priv) {                   /* merge the private tallies, nonzero bins only */
+      __syncthreads();
+      const CompDev* __restrict__ comps = V->comps;
+      for (int j = 0; j < a.n_comps; ++j) {
+        const int off = comps[j].priv_off;
+        if (off < 0) continue;
+        const int64_t len = comps[j].tally_len;
+        float* const h = comps[j].tally;
+        float* const he = comps[j].tally_err;
+        for (int64_t k = threadIdx.x; k < len; k += blockDim.x) {
+          const float v = ramp_dyn_smem[off + k];
+          if (v != 0.0f) atomicAdd(h + k, v);
+          if (he) {
+            const float w = ramp_dyn_smem[off + len + k];
+            if (w != 0.0f) atomicAdd(he + k, w);
+          }
+        }
       }
     }
   }
@@ -555,17 +410,8 @@ template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
 cudaError_t launch_phase(const FusedArgs& a, int block, int grid, cudaStream_t s) {
   const dim3 g((unsigned)grid, BATCHED ? (unsigned)a.n_variants : 1u);
   size_t smem = 0;
-  if (PHASE == 5) {
-    smem = (size_t)(block / 32) * RG_WORDS * FUSED_WARP_TASK * sizeof(uint32_t);
-    static size_t allowed = 0;      /* one attribute call per instantiation and size */
-    if (smem > allowed) {
-      const cudaError_t e = cudaFuncSetAttribute(k_fused<MINB, MODE, BATCHED, PHASE, EXT>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem);
-      if (e != cudaSuccess) return e;
-      allowed = smem;
-    }
-  }
+  if (PHASE == 0 && !BATCHED && a.priv_floats > 0)
+    smem = (size_t)a.priv_floats * sizeof(float);    /* at most 48 KB: no attribute */
   k_fused<MINB, MODE, BATCHED, PHASE, EXT><<<g, block, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -573,13 +419,14 @@ cudaError_t launch_phase(const FusedArgs& a, int block, int grid, cudaStream_t s
 /* occupancy of the whole-chain kernel at this register cap (CTAs per SM) */
 template <int MINB, int MODE>
 int occ_mm(int block) {
-  static int cached = 0;
-  if (cached > 0) return cached;
+  static int cached[2] = {0, 0};     /* 256- and 128-thread CTAs */
+  const int slot = block == 128 ? 1 : 0;
+  if (cached[slot] > 0) return cached[slot];
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<MINB, MODE, false, 0, false>, block,
                                                     0) != cudaSuccess || nb <= 0)
     return 1;
-  cached = nb;
+  cached[slot] = nb;
   return nb;
 }
 

@@ -55,13 +55,11 @@ struct FusedArgs {
   int32_t ext;                  /* the chain uses an extended kind (MISIS source,
                                    SMonochromator, SPowder1): the kernels built
                                    with them (split only when not BATCHED) */
-  int32_t regroup;              /* 1: the first component is a guide of stage A,
-                                   before which each warp regroups its work
-                                   item by expected bounce passes (PHASE 5:
-                                   shared memory, RG_WORDS x 128 words per
-                                   warp); 0: off */
+  int32_t priv_floats;          /* whole chain, one instrument: shared-memory
+                                   floats of the private tallies (descriptors
+                                   with priv_off >= 0); 0: off */
 };
-#define RG_WORDS 13             /* regroup slot: x y z vx vy vz p t sb sc sd se iidx */
+#define RAMP_PRIV_FLOATS 12288  /* shared memory for private tallies: 48 KB per CTA */
 #define SURV_WORDS 18           /* 15 record lanes (die is 0), iidx, index, variant */
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s);

@@ -38,7 +38,10 @@ struct alignas(16) CompDev {
   const float4* bvh_nodes;     /* mesh: 2 float4 per node                 */
   const float4* bvh_tris;      /* mesh: 3 float4 per triangle (v0,e1,e2)  */
   int32_t bvh_root_leaf;
-  int32_t pad;
+  int32_t priv_off;            /* whole-chain launch with RampTune.privatize:
+                                  offset (floats) of this detector's sum-p and
+                                  sum-p^2 histograms in the CTA's shared
+                                  memory; -1: the tallies go to global memory */
 };
 
 struct SrcDev {

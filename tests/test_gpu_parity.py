@@ -341,45 +341,22 @@ def test_fused_split_with_multi_chunk_carry(cuda_lib):
     tallies_close(gi, ci)
 
 
-@pytest.mark.parametrize("tune,rng,chunk,N", [
-    ({"split": 2, "regroup": 1}, "reference", None, 1_000_000),
-    ({"split": 2, "regroup": 1, "blocks_per_sm": 3}, "native", None, 600_001),
-    ({"split": 5, "regroup": 1}, "reference", None, 1_000_000),
-    ({"split": 2, "regroup": 1}, "reference", 100_000, 250_001)])
-def test_fused_regroup_matches_oracle(cuda_lib, tune, rng, chunk, N):
-    """Stage A regrouped before a guide (each warp's 128 neutrons held in
-    shared memory and continued in order of expected bounce passes): the
-    traces are unchanged, so the tallies equal the oracle's up to the order
-    of additions; also with carry buffers across chunks and with a longer
-    stage A (split before guide 3)."""
-    gi, ci, r = pair(I.path("let_like.json"), I.let_like_kwargs(), N, path="fused", rng=rng,
-                     chunk=chunk, tune=tune)
+@pytest.mark.parametrize("fn,kw,N,tune", [
+    ("powder_diffractometer.json", "powder", 500_000, {"privatize": 1}),
+    ("guides_monitors.json", "small", 300_000, {"privatize": 1, "blocks_per_sm": 3}),
+    ("let_like.json", "let", 1_000_000, {"block": 128, "blocks_per_sm": 8, "split": 2}),
+    ("let_like.json", "let", 600_001, {"block": 128, "blocks_per_sm": 6})])
+def test_fused_private_tallies_and_small_ctas_match_oracle(cuda_lib, fn, kw, N, tune):
+    """Detectors whose histograms fit in shared memory accumulated per CTA
+    and merged as the CTA ends (the powder diffractometer's 1600-bin 2theta
+    histogram, the monitors of the guide chain), and 128-thread CTAs: only
+    the order of tally additions changes."""
+    kws = {"small": I.small_chain_kwargs(), "let": I.let_like_kwargs(),
+           "powder": I.powder_diffractometer_kwargs()}[kw]
+    path = os.path.join(GOLD_DIR, fn) if fn == "guides_monitors.json" else I.path(fn)
+    gi, ci, r = pair(path, kws, N, path="fused", tune=tune)
     tallies_close(gi, ci)
     assert gi.oob_drops == r.oob
-
-
-def test_fused_regroup_refused_where_it_cannot_apply(cuda_lib):
-    gi = m.Instrument(I.path("let_like.json"), "cuda", **I.let_like_kwargs())
-    with pytest.raises(RuntimeError, match="not a guide"):
-        gi.execute(1000, path="fused", tune={"split": 3, "regroup": 2})    # a chopper
-    with pytest.raises(RuntimeError, match="needs a split"):
-        gi.execute(1000, path="fused", tune={"regroup": 1})
-    with pytest.raises(RuntimeError, match="at the moderator"):
-        gi.execute(1000, path="fused", tune={"split": 5, "regroup": 4})   # guide 2
-
-
-@pytest.mark.parametrize("tune", [{"split": 2, "regroup": 1},
-                                  {"split": 2, "regroup": 1, "streams": 4}])
-def test_batched_regroup_matches_single_runs(cuda_lib, tune):
-    variants = [I.let_like_kwargs(Ei=3.7), I.let_like_kwargs(Ei=8.0), I.let_like_kwargs(Ei=2.5)]
-    counts = [300_000, 123_457, 200_003]
-    B = BatchedInstrument(I.path("let_like.json"), variants, ctx="cuda")
-    B.execute(counts, rng="native", seeds=[11, 2222, 4000], tune=tune)
-    torch.cuda.synchronize()
-    for v, (kw, n, seed) in enumerate(zip(variants, counts, [11, 2222, 4000])):
-        ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
-        oracle.run(ci, n, rng_mode=1, variant=v, seeds=[seed])
-        tallies_close(B.instruments[v], ci)
 
 
 @pytest.mark.parametrize("tune", [{"split": 2}, {"split": 2, "streams": 4}])
@@ -439,7 +416,7 @@ def test_autotune_survival_and_split_point(cuda_lib, tmp_path, monkeypatch):
     assert autotune.split_point(inst, alive) == 2
     before = [t.clone() for t in inst.tallies()]
     cfg = autotune.tune(inst, n_probe=200_000)
-    assert set(cfg) <= set(("blocks_per_sm", "chunk", "split", "regroup"))
+    assert set(cfg) <= set(("block", "blocks_per_sm", "chunk", "split", "privatize"))
     for t, b in zip(inst.tallies(), before):
         assert torch.equal(t, b)
 

@@ -28,16 +28,11 @@ def test_split_point_rule():
     assert autotune.split_point(inst, alive, threshold=0.01) == 5
 
 
-def test_regroup_candidate_is_the_first_guide_before_the_split():
-    let = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
-    assert autotune.regroup_point(let, 2) == 1          # guide 1 is component 0
-    assert autotune.regroup_point(let, 0) == 0          # no split: no stage A
-    misis = m.Instrument(I.path("let_like_misis.json"), "cpu", **I.let_like_misis_kwargs())
-    assert autotune.regroup_point(misis, 2) == 0        # extended kinds: not offered
-    small = m.Instrument(I.path("small_chain.json"), "cpu", **I.small_chain_kwargs())
-    assert autotune.regroup_point(small, 2) == 0        # no guide
-    t = _abi.tune_struct({"split": 2, "regroup": 1})
-    assert (t.split, t.regroup) == (2, 1)
+def test_private_tally_candidates_only_for_small_detectors():
+    assert autotune.privatizable(m.Instrument(I.path("powder_diffractometer.json"), "cpu",
+                                              **I.powder_diffractometer_kwargs()))
+    assert not autotune.privatizable(m.Instrument(I.path("let_like.json"), "cpu",
+                                                  **I.let_like_kwargs()))   # 720 x 1000
 
 
 def test_mesh_chains_get_the_walk_candidate():
