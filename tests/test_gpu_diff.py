@@ -127,8 +127,8 @@ def test_likelihood_ratio_pathwise_and_finite_differences_agree_statistically(cu
                                   L(histogram(chain, tm, N, seed))) / (2 * h)))
         fd.append(row)
     path, lr, fd = np.array(path), np.array(lr), np.array(fd)
-    for k in (1, 2):                       # weights only: one estimator
-        assert np.array_equal(path[:, k], lr[:, k])
+    for k in (1, 2):                       # weights only: one estimator (up to the
+        assert np.allclose(path[:, k], lr[:, k], rtol=1e-9, atol=0)   # order of additions)
         assert abs(path[:, k].mean() - fd[:, k].mean()) <= 1e-3 * abs(fd[:, k].mean())
     d = lr[:, 0] - fd[:, 0]
     se = d.std(ddof=1) / np.sqrt(len(d))
