@@ -34,7 +34,20 @@ def cache_path():
         os.path.expanduser("~"), ".cache", "ramp_gb300", "autotune.json")
 
 
+_MEMO = {}   # signature -> configuration, for the lookups after the first in a process
+
+
 def signature(inst, rng):
+    memo = getattr(inst, "_tune_sig", None)
+    if memo is None:
+        memo = inst._tune_sig = {}
+    if rng in memo:                  # the component structure of an instrument is fixed
+        return memo[rng]
+    memo[rng] = _signature(inst, rng)
+    return memo[rng]
+
+
+def _signature(inst, rng):
     src, carr, nc, barr, nb = inst.descriptors([])
     kinds = [(carr[j].geom, carr[j].scat) for j in range(nc)]
     blocks = [(barr[k].first, barr[k].count, barr[k].linear, barr[k].multi) for k in range(nb)]
@@ -167,8 +180,11 @@ def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False
     Instrument.execute(tune=...)); measured once per GPU and instrument
     structure, then read from the cache."""
     key = signature(inst, rng)
+    if not force and key in _MEMO:
+        return dict(_MEMO[key])
     cache = _load()
     if not force and key in cache:
+        _MEMO[key] = dict(cache[key]["config"])
         return dict(cache[key]["config"])
     lib = inst._lib()
     plan = inst.plan()
@@ -199,4 +215,5 @@ def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False
     cache[key] = {"config": best, "ms": results[0][0], "n_probe": n_probe, "split_candidate": split,
                   "all": [[ms, c] for ms, c in results]}
     _save(cache)
+    _MEMO[key] = dict(best)
     return dict(best)
