@@ -136,7 +136,10 @@ class Instrument:
                 "random": random.getstate()}
 
     def restore(self, state):
-        """Load tallies and the chunk-seed generator from checkpoint()."""
+        """Load tallies and the chunk-seed generator from checkpoint().
+        The generator is Python's process-wide ``random`` (as the reference
+        draws its chunk seeds from it): restoring rewinds it for every
+        instrument and every other user of ``random`` in the process."""
         import random
         if state.get("format") != "ramp_gb300 checkpoint 1":
             raise ValueError("not a ramp_gb300 checkpoint")

@@ -78,3 +78,26 @@ def test_plain_graph_refuses_stale_parameters(cuda_lib):
     chain.set(chain.values())
     with pytest.raises(RuntimeError, match="capture it again"):
         g.replay()
+
+
+@pytest.mark.parametrize("path", ["plain", "fused"])
+def test_gpu_run_resumed_from_a_checkpoint_equals_the_uninterrupted_run(cuda_lib, tmp_path, path):
+    """execute() twice, against execute() once, a checkpoint, a fresh
+    instrument restored from it and execute() again (the GPU paths)."""
+    import random
+    kw = I.small_chain_kwargs()
+    whole = m.Instrument(I.path("small_chain.json"), "cuda", **kw)
+    random.seed(21)
+    whole.execute(200_000, path=path)
+    whole.execute(200_000, path=path)
+    first = m.Instrument(I.path("small_chain.json"), "cuda", **kw)
+    random.seed(21)
+    first.execute(200_000, path=path)
+    first.save_checkpoint(tmp_path / "run.pt")
+    random.seed(12345)                   # the process moves on
+    resumed = m.Instrument(I.path("small_chain.json"), "cuda", **kw)
+    resumed.load_checkpoint(tmp_path / "run.pt")
+    resumed.execute(200_000, path=path)
+    torch.cuda.synchronize()
+    tallies_close(_Host(resumed), _Host(whole))
+    assert sum(float(t.sum()) for t in whole.tallies()) > 0

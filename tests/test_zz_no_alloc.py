@@ -124,3 +124,33 @@ def test_noalloc_reports_device_status_through_the_plan(cuda_lib):
         assert (fb, ob) == (fa, oa)
         assert fb & _abi.F_WORKQ == 0
     assert_tallies_match(A, B)
+
+
+@pytest.mark.parametrize("fn,kws,counts,seeds", [
+    ("mesh_imaging.json", [I.mesh_imaging_kwargs(angle=0.0), I.mesh_imaging_kwargs(angle=0.9)],
+     [30_000, 20_011], [7, 8]),
+    ("let_like_misis.json", [I.let_like_misis_kwargs(Ei=3.7), I.let_like_misis_kwargs(Ei=6.0)],
+     [200_000, 90_001], [3, 4000])])
+def test_noalloc_mesh_and_extended_kinds_equal_allocating_entry_point(cuda_lib, fn, kws,
+                                                                      counts, seeds):
+    """Descriptors that point at tables the plan already holds (a mesh's
+    hierarchy, the MISIS spectrum tables) are looked up, not uploaded, and
+    trace as the allocating entry point does, on two calls in a row."""
+    lib = cuda_lib
+    A = [m.Instrument(I.path(fn), "cuda", **kw) for kw in kws]
+    B = [m.Instrument(I.path(fn), "cuda", **kw) for kw in kws]
+    plan_a, plan_b = A[0].plan(), B[0].plan()
+    va, keep_a = variants_of(A, counts, seeds)
+    vb, keep_b = variants_of(B, counts, seeds)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for mode in (0, 1):
+        rng = _abi.RampRng(mode, 5, 0, 0)
+        _abi.check(lib, lib.ramp_trace_batched(plan_a, va, len(A), ctypes.byref(rng), None,
+                                               stream), "ramp_trace_batched")
+        _abi.check(lib, lib.ramp_trace_batched_noalloc(plan_b, vb, len(B), ctypes.byref(rng),
+                                                       None, stream),
+                   "ramp_trace_batched_noalloc")
+        torch.cuda.synchronize()
+        for a, b in zip(A, B):
+            assert_tallies_match(a, b)
+    assert sum(float(t.sum()) for b in B for t in b.tallies()) > 0
