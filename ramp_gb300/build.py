@@ -21,12 +21,13 @@ LIB = os.path.join(OUT, "libramp_cuda.so")
 
 CU_SOURCES = ["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
 # fused_inst.cu once per kernel instantiation: (register cap, keying mode,
-# batched one-launch layout, phase, extended kinds); the batched layout runs
-# the extended kinds whole (phase 0 only)
-FUSED_INSTANCES = ([(mb, mode, b, ph, x) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)
-                    for x in (0, 1) for ph in (0, 1, 2) if not (b and x and ph)]
-                   # phase 4: stage B walking a mesh per lane (without the extended kinds)
-                   + [(mb, mode, b, 4, 0) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)])
+# batched one-launch layout, phase, kind set); kind sets: 0 core kinds, 1
+# everything (extended kinds and the mesh), 2 core kinds and the mesh.  The
+# batched layout runs the extended kinds whole (phase 0 only); phase 4
+# (stage B walking a mesh per lane) exists for kind set 2
+FUSED_INSTANCES = ([(mb, mode, b, ph, ks) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)
+                    for ks in (0, 1, 2) for ph in (0, 1, 2) if not (b and ks == 1 and ph)]
+                   + [(mb, mode, b, 4, 2) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)])
 CPP_SOURCES = ["bvh.cpp"]
 HEADERS = ["device.cuh", "fused_kernel.cuh", "mesh.cuh", "plan.h", "launch.h", "rmath.h", "rconst.h", "bvh.h",
            os.path.join("..", "..", "include", "ramp.h")]

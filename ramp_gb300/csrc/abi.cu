@@ -103,9 +103,15 @@ struct RampPlan {
   StreamSet streams;
   bool plain_only = false;           /* a component writes per-index output */
   bool ext = false;                  /* an extended kind: MISIS, SMonochromator, SPowder1 */
+  bool mesh = false;                 /* a GMesh or SAttenuate component */
 };
 
 static bool ext_source(const RampSource& s) { return s.kind == RAMP_SRC_ISIS; }
+
+/* kind set of the whole-chain kernels a launch runs (FusedArgs.ext): the
+ * extended kinds (with everything else) before the mesh, the mesh before
+ * the core kinds alone */
+static int32_t kind_set(bool ext, bool mesh) { return ext ? 1 : (mesh ? 2 : 0); }
 
 /* whole-chain kernels (fused, batched, adjoint) cannot write per-index
  * component output */
@@ -487,6 +493,7 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
   for (const RampComp& c : p->comps_in) {
     if (c.scat == RAMP_S_RESCAL || c.scat == RAMP_S_HOST) p->plain_only = true;
     if (c.scat == RAMP_S_MONO || c.scat == RAMP_S_POWDER1) p->ext = true;
+    if (c.geom == RAMP_G_MESH || c.scat == RAMP_S_ATTENUATE) p->mesh = true;
   }
   if (ext_source(*source)) p->ext = true;
   for (const RampBlock& B : p->blocks)
@@ -854,7 +861,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
     if (!rc && a.priv_floats > 0) a.single.comps = p->priv_dev;
   }
   if (rc) return rc;
-  a.ext = p->ext ? 1 : 0;
+  a.ext = kind_set(p->ext, p->mesh);
   if (a.split > 0 || a.walk) {
     rc = attach_surv(p, a, (n + 127) / 128, s);
     if (rc) return rc;
@@ -885,7 +892,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
   /* split launches: each variant gets its own region of the survivor
      buffer (its items' slots, SoA, and its items' counts) */
   int32_t split = 0, walk = 0;
-  int rc0 = tune_stage(p, tune, base.ext != 0, &split, &walk);
+  int rc0 = tune_stage(p, tune, base.ext == 1, &split, &walk);
   if (rc0) return rc0;
   std::vector<int64_t> item_off(nv + 1, 0);
   for (size_t v = 0; v < nv; ++v)
@@ -1019,7 +1026,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     FusedArgs a;
     memset(&a, 0, sizeof(a));
     a.minb = minb;
-    a.ext = ext ? 1 : 0;
+    a.ext = kind_set(ext, p->mesh);
     a.blocks = p->blocks_dev;
     a.n_blocks = (int32_t)p->blocks.size();
     a.n_comps = nc;
@@ -1083,7 +1090,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.workq_b = B.counters + n_variants;
   a.split = split;
   a.walk = walk;
-  a.ext = ext ? 1 : 0;
+  a.ext = kind_set(ext, p->mesh);
   if (a.split > 0 || a.walk) {
     rc = attach_surv(p, a, items, s);
     if (rc) return rc;
@@ -1490,9 +1497,10 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.st = p->status;             /* allocated with the plan: read by ramp_plan_status */
   a.workq = D->counters;
   a.workq_b = D->counters + n_variants;
-  a.ext = p->ext ? 1 : 0;
+  bool ext = p->ext;
   for (int v = 0; v < n_variants; ++v)
-    if (ext_source(variants[v].source)) a.ext = 1;
+    if (ext_source(variants[v].source)) ext = true;
+  a.ext = kind_set(ext, p->mesh);
   /* no survivor split here: it would need a buffer sized by the call */
   CK(launch_fused(a, block, batched_grid(n_max, grid), s));
   return RAMP_OK;

@@ -614,7 +614,11 @@ DI bool g_arm(Is& s) {
 
 #include "mesh.cuh"
 
-/* dispatch; a mesh paired with SAttenuate leaves its chord sum in sd */
+/* dispatch; a mesh paired with SAttenuate leaves its chord sum in sd.
+ * MESH = false compiles the kernel without the mesh hierarchy walk (its
+ * 64-entry stack and live state raise register pressure in the whole
+ * kernel); a plan holding a GMesh never runs such a kernel. */
+template <bool MESH = true>
 DI bool intersect(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
   switch (c.geom) {
     case RAMP_G_PLANE: return g_plane(c, n, s);
@@ -624,7 +628,9 @@ DI bool intersect(const CompDev& c, Nt& n, Is& s, StatusDev* st) {
     case RAMP_G_SPHERE_INT: return g_sphere<true>(c, n, s);
     case RAMP_G_BOX: return g_box(c, n, s);
     case RAMP_G_ARM: return g_arm(s);
-    case RAMP_G_MESH: return g_mesh(c, n, s, st);
+    case RAMP_G_MESH:
+      if constexpr (MESH) return g_mesh(c, n, s, st);
+      return false;
     default: return false;
   }
 }
@@ -1343,7 +1349,7 @@ DI void s_attenuate(const CompDev& c, Nt& n, Is& s, uint32_t& ii) {
   s_finish(c, n, s, ii);
 }
 
-template <class D = NoDiff, bool EXT = true>
+template <class D = NoDiff, bool EXT = true, bool MESH = true>
 DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev* st,
                 D* dx = nullptr, const bool zx = false) {
   switch (c.scat) {
@@ -1360,7 +1366,7 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
       s_finish(c, n, s, ii);
       break;
     case RAMP_S_BEAMSTOP: set_die(n, 1.0f); s_finish(c, n, s, ii); break;
-    case RAMP_S_ATTENUATE: s_attenuate(c, n, s, ii); break;
+    case RAMP_S_ATTENUATE: if constexpr (MESH) s_attenuate(c, n, s, ii); break;
     case RAMP_S_MONO: if constexpr (EXT) s_mono(c, n, s, ii, r); break;
     case RAMP_S_POWDER1: if constexpr (EXT) s_powder1(c, n, s, ii, r); break;
     default: break;
@@ -1372,16 +1378,16 @@ DI void scatter(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDev*
 /* intersect, terminate, scatter, untransform on a live neutron.  The   */
 /* intersection starts at its reset value.                               */
 /* ------------------------------------------------------------------ */
-template <class D = NoDiff, bool EXT = true>
+template <class D = NoDiff, bool EXT = true, bool MESH = true>
 DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st,
                     D* dx = nullptr, const bool zx = false) {
   transform<D::pol>(c, n);
   Is s;
   is_reset(s);
-  if (intersect(c, n, s, st)) ii = c.idx;
+  if (intersect<MESH>(c, n, s, st)) ii = c.idx;
   /* terminate.cl:16-18 */
   if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
-  if (ii == c.idx && !(n.die > 0.f)) scatter<D, EXT>(c, n, s, ii, r, st, dx, zx);
+  if (ii == c.idx && !(n.die > 0.f)) scatter<D, EXT, MESH>(c, n, s, ii, r, st, dx, zx);
   if (zx && n.p == 0.0f) {
     set_die(n, 1.0f);
     return;
@@ -1391,7 +1397,7 @@ DI void comp_linear(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st
 
 /* one non-linear block (mcramp.py:167-217): "multi" rounds of all
  * geometries then all scatters; no termination step. */
-template <class D = NoDiff>
+template <class D = NoDiff, bool EXT = true, bool MESH = true>
 DI void block_nonlinear(const CompDev* comps, int first, int count, int multi, Nt& n,
                         uint32_t& ii, Rng& r, StatusDev* st, D* dx = nullptr) {
   Is s;
@@ -1401,14 +1407,14 @@ DI void block_nonlinear(const CompDev* comps, int first, int count, int multi, N
       if (n.die > 0.f) break;
       const CompDev& c = comps[j];
       transform<D::pol>(c, n);
-      if (intersect(c, n, s, st)) ii = c.idx;
+      if (intersect<MESH>(c, n, s, st)) ii = c.idx;
       untransform<D::pol>(c, n);
     }
     for (int j = first; j < first + count; ++j) {
       if (n.die > 0.f) break;
       const CompDev& c = comps[j];
       transform<D::pol>(c, n);
-      if (ii == c.idx) scatter<D>(c, n, s, ii, r, st, dx);
+      if (ii == c.idx) scatter<D, EXT, MESH>(c, n, s, ii, r, st, dx);
       if (!(n.die > 0.f)) untransform<D::pol>(c, n);
     }
   }

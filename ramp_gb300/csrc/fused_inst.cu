@@ -4,8 +4,8 @@
  * -DFK_MINB (register cap: minimum CTAs per SM), -DFK_MODE (RNG keying),
  * -DFK_BATCHED (one launch, a grid row per variant), -DFK_PHASE (0 whole
  * chain, 1 stage A, 2 stage B, 4 stage B walking a mesh per lane) and
- * -DFK_EXT (extended component kinds), so that the kernels compile in
- * parallel.
+ * -DFK_EXT (kind set: 0 core kinds, 1 everything, 2 core kinds and the
+ * mesh), so that the kernels compile in parallel.
  */
 #include "fused_kernel.cuh"
 
@@ -14,7 +14,7 @@
 #error "fused_inst.cu is compiled with -DFK_MINB, -DFK_MODE, -DFK_BATCHED, -DFK_PHASE, -DFK_EXT"
 #endif
 
-template cudaError_t launch_phase<FK_MINB, FK_MODE, (FK_BATCHED != 0), FK_PHASE, (FK_EXT != 0)>(
+template cudaError_t launch_phase<FK_MINB, FK_MODE, (FK_BATCHED != 0), FK_PHASE, FK_EXT>(
     const FusedArgs&, int, int, cudaStream_t);
 
 #if FK_PHASE == 0 && FK_BATCHED == 0 && FK_EXT == 0

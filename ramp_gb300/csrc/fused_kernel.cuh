@@ -44,7 +44,7 @@
  * buffer (no atomics) and finish in PHASE 2.  The bounds of both loops are kernel parameters, so the loop
  * counters and descriptor addresses stay warp-uniform.
  */
-template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
+template <int MINB, int MODE, bool BATCHED, int PHASE, int KS>
 __global__ void __launch_bounds__(256, MINB)
 k_fused(const FusedArgs a);
 
@@ -55,8 +55,9 @@ k_fused(const FusedArgs a);
  * A survivor is keyed by its own index and variant, so it continues
  * exactly where stage A left it. */
 #define SURV_GROUP 8
-template <int MODE, bool BATCHED, bool EXT>
+template <int MODE, bool BATCHED, int KS>
 DI void fused_tail(const FusedArgs& a) {
+  constexpr bool EXT = KS == 1, MESH = KS != 0;
   const int lane = threadIdx.x & 31;
   const bool carry = (a.carry_sb != nullptr);
   const bool zx = !carry;
@@ -120,10 +121,10 @@ DI void fused_tail(const FusedArgs& a) {
         if (B.linear) {
           for (int k = B.first > K ? B.first : K; k < e; ++k) {
             if (n.die > 0.f) break;
-            comp_linear<TallyOnly, EXT>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
+            comp_linear<TallyOnly, EXT, MESH>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
           }
         } else {
-          block_nonlinear<TallyOnly>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
+          block_nonlinear<TallyOnly, EXT, MESH>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
         }
       }
       if (carry) { a.carry_sb[idx] = n.sb; a.carry_iidx[idx] = ii; }
@@ -136,9 +137,10 @@ DI void fused_tail(const FusedArgs& a) {
  * read it back from its survivor record, bring it into K's frame again
  * (the same operations give the same values), take the walk's records, then
  * the rest of comp_linear of K and the components after it */
-template <int MODE, bool EXT>
+template <int MODE, int KS>
 DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, int64_t slot,
                  MeshWalk& w, int k, bool zx, bool carry) {
+  constexpr bool EXT = KS == 1, MESH = KS != 0;
   const int64_t cap = a.surv_cap;
   const uint32_t* wp = a.surv + slot;
   Nt n;
@@ -163,7 +165,7 @@ DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, i
   if (k == 0 && mesh_end(cK, n, s, w)) ii = cK.idx;
   if (len3(ip2(s)) == 0.0f && cK.restore == 0) set_die(n, 1.f);
   if (ii == cK.idx && !(n.die > 0.f))
-    scatter<TallyOnly, EXT>(cK, n, s, ii, r, a.st, (TallyOnly*)nullptr, zx);
+    scatter<TallyOnly, EXT, MESH>(cK, n, s, ii, r, a.st, (TallyOnly*)nullptr, zx);
   if (zx && n.p == 0.0f) set_die(n, 1.0f);
   else if (!(n.die > 0.f)) untransform<false>(cK, n);
   for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
@@ -173,10 +175,10 @@ DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, i
     if (B.linear) {
       for (int j = B.first > K + 1 ? B.first : K + 1; j < e; ++j) {
         if (n.die > 0.f) break;
-        comp_linear<TallyOnly, EXT>(comps[j], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
+        comp_linear<TallyOnly, EXT, MESH>(comps[j], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
       }
     } else {
-      block_nonlinear<TallyOnly>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
+      block_nonlinear<TallyOnly, EXT, MESH>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
     }
   }
   if (carry) { a.carry_sb[idx] = n.sb; a.carry_iidx[idx] = ii; }
@@ -191,7 +193,7 @@ DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, i
  * it) and takes the next waiting survivor; the warp claims the next group of
  * work items as soon as every survivor of the current one is taken.  Every
  * neutron goes through the same operations as in PHASE 2. */
-template <int MODE, bool BATCHED, bool EXT>
+template <int MODE, bool BATCHED, int KS>
 DI void fused_tail_walk(const FusedArgs& a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -264,7 +266,7 @@ DI void fused_tail_walk(const FusedArgs& a) {
         ray.vy = __uint_as_float(wp[4 * cap]); ray.vz = __uint_as_float(wp[5 * cap]);
         transform<false>(cK, ray);        /* comp_linear of component K */
         if (mesh_begin(cK, ray, w)) walking = true;
-        else walk_end<MODE, EXT>(a, comps, K, slot, w, -2, zx, carry);
+        else walk_end<MODE, KS>(a, comps, K, slot, w, -2, zx, carry);
       }
     }
     const bool more = groups_left || handed < total;   /* survivors still waiting */
@@ -276,7 +278,7 @@ DI void fused_tail_walk(const FusedArgs& a) {
         const int k = mesh_step(cK, w, a.st);
         if (k <= 0) {
           walking = false;
-          walk_end<MODE, EXT>(a, comps, K, slot, w, k, zx, carry);
+          walk_end<MODE, KS>(a, comps, K, slot, w, k, zx, carry);
         }
       }
       const int idle = __popc(__ballot_sync(FULL_MASK, !walking));
@@ -285,14 +287,15 @@ DI void fused_tail_walk(const FusedArgs& a) {
   }
 }
 
-template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
+template <int MINB, int MODE, bool BATCHED, int PHASE, int KS>
 __global__ void __launch_bounds__(256, MINB)
 k_fused(const FusedArgs a) {
+  constexpr bool EXT = KS == 1, MESH = KS != 0;
   if constexpr (PHASE == 2) {
-    fused_tail<MODE, BATCHED, EXT>(a);
+    fused_tail<MODE, BATCHED, KS>(a);
     return;
   } else if constexpr (PHASE == 4) {
-    fused_tail_walk<MODE, BATCHED, EXT>(a);
+    fused_tail_walk<MODE, BATCHED, KS>(a);
     return;
   } else {
     const int lane = threadIdx.x & 31;
@@ -344,10 +347,10 @@ k_fused(const FusedArgs a) {
               const int e = (PHASE == 1 && B.first + B.count > KE) ? KE : B.first + B.count;
               for (int k = B.first; k < e; ++k) {
                 if (n.die > 0.f) break;
-                comp_linear<TallyOnly, EXT>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
+                comp_linear<TallyOnly, EXT, MESH>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
               }
             } else {
-              block_nonlinear<TallyOnly>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
+              block_nonlinear<TallyOnly, EXT, MESH>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
             }
           }
         }
@@ -406,13 +409,13 @@ k_fused(const FusedArgs a) {
 /* one launch of one instantiation; each is compiled in a translation unit
  * of its own (fused_inst.cu, built once per template argument set) and the
  * sequencing of phases lives in fused.cu */
-template <int MINB, int MODE, bool BATCHED, int PHASE, bool EXT>
+template <int MINB, int MODE, bool BATCHED, int PHASE, int KS>
 cudaError_t launch_phase(const FusedArgs& a, int block, int grid, cudaStream_t s) {
   const dim3 g((unsigned)grid, BATCHED ? (unsigned)a.n_variants : 1u);
   size_t smem = 0;
   if (PHASE == 0 && !BATCHED && a.priv_floats > 0)
     smem = (size_t)a.priv_floats * sizeof(float);    /* at most 48 KB: no attribute */
-  k_fused<MINB, MODE, BATCHED, PHASE, EXT><<<g, block, smem, s>>>(a);
+  k_fused<MINB, MODE, BATCHED, PHASE, KS><<<g, block, smem, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -423,7 +426,7 @@ int occ_mm(int block) {
   const int slot = block == 128 ? 1 : 0;
   if (cached[slot] > 0) return cached[slot];
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<MINB, MODE, false, 0, false>, block,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<MINB, MODE, false, 0, 0>, block,
                                                     0) != cudaSuccess || nb <= 0)
     return 1;
   cached[slot] = nb;

@@ -52,9 +52,11 @@ struct FusedArgs {
   int32_t minb;                 /* register cap: the build for 3 or 4 CTAs per SM */
   int32_t walk;                 /* split before the GMesh component `split` (may
                                    be 0): stage B walks the mesh per lane (PHASE 4) */
-  int32_t ext;                  /* the chain uses an extended kind (MISIS source,
-                                   SMonochromator, SPowder1): the kernels built
-                                   with them (split only when not BATCHED) */
+  int32_t ext;                  /* kind set of the kernels to run: 0 the core
+                                   kinds; 1 the chain uses an extended kind
+                                   (MISIS source, SMonochromator, SPowder1):
+                                   everything (split only when not BATCHED);
+                                   2 core kinds and GMesh / SAttenuate */
   int32_t priv_floats;          /* whole chain, one instrument: shared-memory
                                    floats of the private tallies (descriptors
                                    with priv_off >= 0); 0: off */
