@@ -557,7 +557,9 @@ int ramp_run_block(RampPlan* p, int block, const RampState* st, int64_t n, const
   if (B.linear) {
     for (int j = B.first; j < B.first + B.count; ++j) CK(launch_linear_comp(p->comps[j], a, s));
   } else {
-    CK(launch_nonlinear_block(p->comps_dev, B.first, B.count, B.multi, a, s));
+    bool mesh = false;
+    for (int j = B.first; j < B.first + B.count; ++j) mesh = mesh || p->comps[j].geom == RAMP_G_MESH;
+    CK(launch_nonlinear_block(p->comps_dev, B.first, B.count, B.multi, mesh, a, s));
   }
   return RAMP_OK;
 }

@@ -24,7 +24,7 @@ cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_s
                             int32_t seed, cudaStream_t s);
 cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_nonlinear_block(const CompDev* comps_dev, int first, int count, int multi,
-                                   const PlainArgs& a, cudaStream_t s);
+                                   bool mesh, const PlainArgs& a, cudaStream_t s);
 
 struct FusedArgs {
   const VariantDev* variants;   /* device, n_variants entries (one grid row

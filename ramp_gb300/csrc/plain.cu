@@ -58,13 +58,13 @@ DI void scatter_k(const CompDev& c, Nt& n, Is& s, uint32_t& ii, Rng& r, StatusDe
   }
 }
 
-template <int SK>
+template <int SK, bool MESH>
 DI void comp_linear_k(const CompDev& c, Nt& n, uint32_t& ii, Rng& r, StatusDev* st,
                       float* ev = nullptr) {
   transform(c, n);
   Is s;
   is_reset(s);
-  if (intersect(c, n, s, st)) ii = c.idx;
+  if (intersect<MESH>(c, n, s, st)) ii = c.idx;
   if (len3(ip2(s)) == 0.0f && c.restore == 0) set_die(n, 1.f);
   if (ii == c.idx && !(n.die > 0.f)) scatter_k<SK>(c, n, s, ii, r, st, ev);
   if (!(n.die > 0.f)) untransform(c, n);
@@ -86,7 +86,9 @@ k_generate(const __grid_constant__ SrcDev src, const PlainArgs a, int32_t num_si
   }
 }
 
-template <int SK, int MODE>
+/* MESH: the component's geometry is a GMesh (only then is the hierarchy
+ * walk compiled in: its stack raises register pressure in the whole kernel) */
+template <int SK, int MODE, bool MESH>
 __global__ void __launch_bounds__(PLAIN_BLOCK)
 k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
   constexpr bool RD_P = SK == RAMP_S_GUIDE || SK == RAMP_S_ISOTROPIC || SK == RAMP_S_POWDERN ||
@@ -124,7 +126,7 @@ k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
     Rng r;
     rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
     float ev[8];
-    comp_linear_k<SK>(c, n, ii, r, a.st, ev);
+    comp_linear_k<SK, MESH>(c, n, ii, r, a.st, ev);
     if constexpr (SK == RAMP_S_RESCAL) {
       /* the event of a neutron this component scattered (rescal.cl:67) */
       if (n.wr & WR_SC) {
@@ -153,6 +155,7 @@ k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
   }
 }
 
+template <bool MESH>
 __global__ void __launch_bounds__(PLAIN_BLOCK)
 k_nonlinear(const CompDev* __restrict__ comps, int first, int count, int multi, const PlainArgs a) {
   const int64_t st = a.stride;
@@ -167,7 +170,7 @@ k_nonlinear(const CompDev* __restrict__ comps, int first, int count, int multi, 
     uint32_t ii = a.iidx[i];
     Rng r;
     rng_init(r, a.rng.mode, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
-    block_nonlinear(comps, first, count, multi, n, ii, r, a.st);
+    block_nonlinear<NoDiff, true, MESH>(comps, first, count, multi, n, ii, r, a.st);
     STORE_ALL(n, S, st, i);
     a.iidx[i] = ii;
   }
@@ -317,13 +320,23 @@ cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_s
 cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_t s) {
   if (a.n <= 0) return cudaSuccess;
   int g = plain_grid(a.n);
+  const bool mesh = c.geom == RAMP_G_MESH;
   switch (c.scat) {
 /* kinds that draw random numbers get one instantiation per keying mode */
-#define CASE(K) case K: k_linear<K, 0><<<g, PLAIN_BLOCK, 0, s>>>(c, a); break;
-#define CASE2(K)                                                        \
-  case K:                                                               \
-    if (a.rng.mode == 0) k_linear<K, 0><<<g, PLAIN_BLOCK, 0, s>>>(c, a); \
-    else k_linear<K, 1><<<g, PLAIN_BLOCK, 0, s>>>(c, a);                \
+#define CASE(K)                                                               \
+  case K:                                                                     \
+    if (mesh) k_linear<K, 0, true><<<g, PLAIN_BLOCK, 0, s>>>(c, a);           \
+    else k_linear<K, 0, false><<<g, PLAIN_BLOCK, 0, s>>>(c, a);               \
+    break;
+#define CASE2(K)                                                              \
+  case K:                                                                     \
+    if (mesh) {                                                               \
+      if (a.rng.mode == 0) k_linear<K, 0, true><<<g, PLAIN_BLOCK, 0, s>>>(c, a); \
+      else k_linear<K, 1, true><<<g, PLAIN_BLOCK, 0, s>>>(c, a);              \
+    } else {                                                                  \
+      if (a.rng.mode == 0) k_linear<K, 0, false><<<g, PLAIN_BLOCK, 0, s>>>(c, a); \
+      else k_linear<K, 1, false><<<g, PLAIN_BLOCK, 0, s>>>(c, a);             \
+    }                                                                         \
     break;
     CASE(RAMP_S_ARM) CASE(RAMP_S_GUIDE) CASE2(RAMP_S_CHOPPER) CASE2(RAMP_S_ISOTROPIC)
     CASE2(RAMP_S_POWDERN) CASE(RAMP_S_DET1D) CASE(RAMP_S_DET2D) CASE(RAMP_S_COUNTER)
@@ -337,9 +350,10 @@ cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_
 }
 
 cudaError_t launch_nonlinear_block(const CompDev* comps_dev, int first, int count, int multi,
-                                   const PlainArgs& a, cudaStream_t s) {
+                                   bool mesh, const PlainArgs& a, cudaStream_t s) {
   if (a.n <= 0 || multi <= 0 || count <= 0) return cudaSuccess;
-  k_nonlinear<<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(comps_dev, first, count, multi, a);
+  if (mesh) k_nonlinear<true><<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(comps_dev, first, count, multi, a);
+  else k_nonlinear<false><<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(comps_dev, first, count, multi, a);
   return cudaGetLastError();
 }
 
