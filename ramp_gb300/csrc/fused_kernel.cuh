@@ -139,7 +139,7 @@ DI void fused_tail(const FusedArgs& a) {
  * the rest of comp_linear of K and the components after it */
 template <int MODE, int KS>
 DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, int64_t slot,
-                 MeshWalk& w, int k, bool zx, bool carry) {
+                 const MeshRec& w, int k, bool zx, bool carry) {
   constexpr bool EXT = KS == 1, MESH = KS != 0;
   const int64_t cap = a.surv_cap;
   const uint32_t* wp = a.surv + slot;
@@ -188,11 +188,14 @@ DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, i
  * block's), for chains where the walk through the mesh hierarchy is most of
  * the work.  Walk lengths differ a lot between rays (a ray outside the mesh
  * box has none), so with one ray per lane a warp runs at a few lanes.  Here
- * each lane walks its ray one node per pass, and a lane whose walk is over
+ * each lane walks its ray one node visit or one triangle per pass (the warp
+ * runs the kind more of its lanes wait for), and a lane whose walk is over
  * finishes that neutron (the rest of component K and the components after
- * it) and takes the next waiting survivor; the warp claims the next group of
- * work items as soon as every survivor of the current one is taken.  Every
- * neutron goes through the same operations as in PHASE 2. */
+ * it, together with the other lanes done since the last refill) and takes
+ * the next waiting survivor; the warp claims the next group of work items as
+ * soon as every survivor of the current one is taken.  Every neutron goes
+ * through the same operations as in PHASE 2 (the records and the chord do
+ * not depend on the order in which triangles are visited). */
 template <int MODE, bool BATCHED, int KS>
 DI void fused_tail_walk(const FusedArgs& a) {
   const int lane = threadIdx.x & 31;
@@ -219,9 +222,18 @@ DI void fused_tail_walk(const FusedArgs& a) {
   /* this lane's walk: only the ray and the walk state stay live while it
      runs; the neutron is read back from its survivor record when it ends */
   bool walking = false;
+  bool done = false;     /* the walk is over; the neutron finishes with the others */
+  int kres = 0;
   int64_t slot = 0;
   MeshWalk w;
   for (;;) {
+    /* the lanes whose walks ended since the last refill finish their
+       neutrons together (the rest of component K and the components after
+       it), not one at a time inside the walk loop */
+    if (done) {
+      walk_end<MODE, KS>(a, comps, K, slot, mesh_rec(w), kres, zx, carry);
+      done = false;
+    }
     /* hand the waiting survivors to the idle lanes (a lane whose ray misses
        the mesh box finishes it at once and is idle again) */
     for (;;) {
@@ -266,20 +278,29 @@ DI void fused_tail_walk(const FusedArgs& a) {
         ray.vy = __uint_as_float(wp[4 * cap]); ray.vz = __uint_as_float(wp[5 * cap]);
         transform<false>(cK, ray);        /* comp_linear of component K */
         if (mesh_begin(cK, ray, w)) walking = true;
-        else walk_end<MODE, KS>(a, comps, K, slot, w, -2, zx, carry);
+        else walk_end<MODE, KS>(a, comps, K, slot, mesh_rec(w), -2, zx, carry);
       }
     }
     const bool more = groups_left || handed < total;   /* survivors still waiting */
-    if (!more && !__any_sync(FULL_MASK, walking)) break;
+    if (!more && !__any_sync(FULL_MASK, walking || done)) break;
     /* walk until a quarter of the lanes are idle (or, with nothing left
-       to hand out, until every walk is over) */
+       to hand out, until every walk is over).  Each pass runs one kind of
+       work, the kind more lanes wait for: a triangle of each lane's pending
+       leaf range, or an inner node of each lane without one */
     for (;;) {
-      if (walking) {
-        const int k = mesh_step(cK, w, a.st);
-        if (k <= 0) {
-          walking = false;
-          walk_end<MODE, KS>(a, comps, K, slot, w, k, zx, carry);
-        }
+      const bool wt = walking && w.tb < w.te;
+      const unsigned bt = __ballot_sync(FULL_MASK, wt);
+      const unsigned bn = __ballot_sync(FULL_MASK, walking && !wt);
+      bool ok = true;
+      if (__popc(bt) >= __popc(bn)) {
+        if (wt) mesh_tri(cK, w, w.tb++);
+      } else if (walking && !wt) {
+        ok = mesh_visit(cK, w, a.st);
+      }
+      if (walking && (!ok || mesh_walk_over(w))) {
+        walking = false;
+        done = true;
+        kres = ok ? 0 : -1;
       }
       const int idle = __popc(__ballot_sync(FULL_MASK, !walking));
       if (idle == 32 || (more && idle >= 8)) break;

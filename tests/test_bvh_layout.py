@@ -139,6 +139,10 @@ def test_leaves_partition_the_triangles_and_walks_reach_every_hit(builder, nu, n
             if b >= 1:
                 seen[a:a + b] += 1
     assert (seen == 1).all()
+    # sibling leaves hold adjacent triangle ranges: a walk that takes both
+    # leaf children of a node tests one range [a0, a1 + b1)
+    both = (ni[:, 7] >= 1) & (ni[:, 15] >= 1)
+    assert (ni[both, 11] == ni[both, 3] + ni[both, 7]).all()
     hits_total = 0
     for _ in range(150):
         pos = rng.uniform(-0.1, 0.1, 3).astype(np.float32)
