@@ -18,8 +18,9 @@ e2e:   histories/s through the public API including Instrument
 construction (IDF parse, table upload), execute and the histogram readback.
 roofline: the fused kernel is bound by integer issue (Threefry-4x32-20,
 about 150 integer operations per random draw), not by HBM or tensor cores;
-achieved = draws x ops per draw / kernel time, peak = the same operation
-rate measured by a Threefry-only kernel on this GPU.  The DRAM traffic and
+achieved = the moderator's draws (5 per history, the RNG work every history
+needs) x ops per draw / kernel time, peak = the same operation rate measured
+by a Threefry-only kernel on this GPU: a lower bound on the issue used.  The DRAM traffic and
 the instruction count per history come from the ncu capture recorded in
 profiles/ with a hash of the kernel sources; they are reported only when
 that hash equals the sources being run.
@@ -52,6 +53,7 @@ sys.path.insert(0, HERE)
 
 N_HIST = 100_000_000
 THREEFRY_OPS = 148          # integer operations per Threefry-4x32-20 draw
+MCONT_DRAWS = 5             # Threefry blocks the MCont moderator computes per history
 CPU_CHUNK = 2_000_000       # histories per chunk of a CPU-baseline step
 CPU_SECONDS = 12.0          # CPU work per CPU-baseline step (whole chunks)
 NODE_BYTES, TRI_BYTES = 64, 48   # one BVH inner node / triangle as the walk reads them
@@ -125,10 +127,17 @@ def profile_counters(tune):
     if c.get("kernel_source_sha") != kernel_source_sha():
         return None, "recorded capture is of other kernel sources (%s)" % c.get(
             "kernel_source_sha")
-    keys = ("split", "walk", "privatize", "block")
+    keys = ("split", "walk", "privatize", "block", "cull")
     if any(int((tune or {}).get(k, 0)) != int(c.get("tune", {}).get(k, 0)) for k in keys):
         return None, "recorded capture is of another launch configuration"
     return c, None
+
+
+def kernels_per_trace(tune):
+    """Kernels one fused trace launches: two (stage A, stage B) with a
+    split, the mesh walk or the chopper look-ahead, else one."""
+    t = tune or {}
+    return 2 if any(int(t.get(k, 0)) > 0 for k in ("split", "walk", "cull")) else 1
 
 
 # ---------------------------------------------------------------- CPU arm
@@ -367,7 +376,7 @@ def measure_batched(config, steps, warmup, tune_arg="auto", variants=0, plain=Tr
         # the component structure)
         from ramp_gb300 import autotune
         tune = {k: v for k, v in autotune.tune(B.instruments[0], rng="reference").items()
-                if k in ("block", "blocks_per_sm", "split", "walk")}
+                if k in ("block", "blocks_per_sm", "split", "walk", "cull")}
     else:
         tune = json.loads(tune_arg) if tune_arg else None
     for w in range(warmup):
@@ -388,8 +397,7 @@ def measure_batched(config, steps, warmup, tune_arg="auto", variants=0, plain=Tr
     out = {"value": total / (statistics.mean(ms) / 1000.0), "ms_per_step": statistics.mean(ms),
            "steps": steps, "warmup": warmup, "variants": len(counts), "histories_per_step": total,
            "tune": tune, "setup_s": setup_s, "clocks": clk,
-           "gpu_launches_per_step": (2 if (int((tune or {}).get("split", 0)) > 0 or
-                                           int((tune or {}).get("walk", 0)) > 0) else 1) *
+           "gpu_launches_per_step": kernels_per_trace(tune) *
                                     (sum(1 for c in counts if c > 0)
                                      if int((tune or {}).get("streams", 0)) > 1 else 1)}
     if plain:
@@ -698,12 +706,15 @@ def main():
     value = world * n * a.steps / (fused_total_ms / 1000.0)
     plain_value = world * n * len(plain_ms) / (plain_total_ms / 1000.0)
 
-    # ---- roofline of the fused kernel: draws from the plain records ----
+    # ---- roofline of the fused kernel: the moderator's Threefry blocks,
+    # which every history computes (energy, two position and two target
+    # coordinates, cont_mod.cl:36-55; the spin's two draws advance the
+    # counter but nothing reads them, and later draws are not counted) ----
     stream = torch.cuda.current_stream(dev)
     nlast = plain.last_chunk
     random.seed(1000 + len(plain_ms) - 1)
     seed_last = plain.source.next_seed()
-    draws = float((plain.state[_abi.LANE["mc"], :nlast].double() - seed_last).sum())
+    draws = float(MCONT_DRAWS * nlast)
     # neutrons whose last component is the detector: each adds to both of
     # its histograms (sum p, sum p^2), two float atomics per tally
     det_idx = [c["idx"] for name, c in plain.components() if name == "detector"][0]
@@ -854,7 +865,7 @@ def main():
                 "d2h_bytes_per_step": d2h,
                 "includes": "Instrument(...) parse + plan/table upload, execute(tune=\"auto\", "
                             "cached autotuner choice), data() readback"},
-        "gpu_launches": a.steps * (2 if int((tune or {}).get("split", 0)) > 0 else 1),
+        "gpu_launches": a.steps * kernels_per_trace(tune),
         "clocks": clk,
     }
     line.update(extras)

@@ -240,6 +240,20 @@ typedef struct RampTune {
                                    waiting neutron (buffer as for
                                    `split`).  Ignored without such a
                                    component.                            */
+  int32_t cull;                 /* fused path, runs without carry
+                                   buffers: 1 = split before component
+                                   `split` (which may then be 0: stage A
+                                   runs the moderator alone) and let
+                                   stage A also retire every neutron that
+                                   certainly cannot pass the disk
+                                   choppers of the run of on-axis
+                                   components starting there
+                                   (ramp_chopper_run); only tallies are
+                                   observable, and those neutrons would
+                                   add nothing to them.  RAMP_E_INVALID
+                                   without such a run.  Not with `walk`
+                                   or in the one-launch batched layout of
+                                   chains with the extended kinds.       */
 } RampTune;
 
 typedef struct RampPlan RampPlan;
@@ -453,6 +467,26 @@ int ramp_debug_atomic_peak(float* bins, int64_t n_bins, int64_t n_threads, int32
  * bytes of the mesh imaging roofline.                                   */
 int ramp_bvh_walk_counts(const float* pts, int64_t n_tri, const float* rays, int64_t n_rays,
                          int64_t* out);
+
+/* Host helper (no GPU): the length of the chopper look-ahead run that
+ * starts at component k (RampTune.cull), 0 when there is none.  The run:
+ * components of the linear block holding k, each unrotated, centred on the
+ * z axis (pos x = y = 0), with a z-normal GPlane and restore_neutron 0:
+ * at most one straight SGuide (w1 = w2, h1 = h2) first, then at least one
+ * SChopper, at non-decreasing z, the first at or after the guide's exit.
+ * From a neutron's state before such a run, the time and place it meets
+ * each chopper plane follow within tight bounds (vz does not change along
+ * it; the guide folds the transverse motion at its walls).              */
+int ramp_chopper_run(const RampComp* comps, int n_comps, const RampBlock* blocks, int n_blocks,
+                     int k);
+
+/* Host check (no GPU) of the look-ahead bound the device applies: for n
+ * neutron records (16 floats each, stride 16: position, velocity, spin,
+ * weight, time, ...; laboratory frame, before component k) out[i] = 1 when
+ * the neutron certainly cannot pass a chopper of the run at k, else 0.
+ * RAMP_E_INVALID when there is no run at k.                              */
+int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock* blocks,
+                            int n_blocks, int k, const float* records, int64_t n, uint8_t* out);
 
 #ifdef __cplusplus
 }

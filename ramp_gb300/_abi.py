@@ -83,10 +83,10 @@ class RampTune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("chunk", ctypes.c_int32), ("privatize", ctypes.c_int32),
                 ("split", ctypes.c_int32), ("streams", ctypes.c_int32),
-                ("walk", ctypes.c_int32)]
+                ("walk", ctypes.c_int32), ("cull", ctypes.c_int32)]
 
 
-TUNE_KEYS = ("block", "blocks_per_sm", "chunk", "privatize", "split", "streams", "walk")
+TUNE_KEYS = ("block", "blocks_per_sm", "chunk", "privatize", "split", "streams", "walk", "cull")
 
 
 def tune_struct(tune):
@@ -176,6 +176,11 @@ _SIGS = {
                                 ctypes.c_void_p], ctypes.c_int),
     "ramp_bvh_walk_counts": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                               ctypes.c_void_p], ctypes.c_int),
+    "ramp_chopper_run": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                          ctypes.c_int], ctypes.c_int),
+    "ramp_debug_chopper_cull": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
+                                ctypes.c_int),
 }
 
 

@@ -8,8 +8,10 @@ span of neutrons a task covers, whether survivors are compacted into
 full warps before the first component that less than half of the
 histories reach — found by a plain-path pilot, ``survival`` — 128- against
 256-thread CTAs, shared-memory private
-tallies for chains whose detectors fit, and, for chains with a mesh, the
-per-lane mesh walk) and keeps the fastest; results are
+tallies for chains whose detectors fit, for chains with a mesh the
+per-lane mesh walk, and for chains with a run of on-axis disk choppers the
+chopper look-ahead, which retires before the run the neutrons that cannot
+pass it) and keeps the fastest; results are
 cached in a JSON file keyed by GPU name, the instrument's component
 structure and the keying mode.  Tuning uses fixed seeds and restores the
 instrument's tallies afterwards: it leaves no trace in the results or in
@@ -141,6 +143,19 @@ def split_point(inst, alive, threshold=0.5):
     return 0
 
 
+def chopper_run_start(inst):
+    """First component at which a run of on-axis choppers (after at most
+    one straight guide) starts, for the chopper look-ahead
+    (RampTune.cull; ramp_chopper_run), or None."""
+    keep = []
+    _, carr, nc, barr, nb = inst.descriptors(keep)
+    lib = _abi.load()
+    for k in range(nc):
+        if lib.ramp_chopper_run(ctypes.addressof(carr), nc, ctypes.addressof(barr), nb, k) > 0:
+            return k
+    return None
+
+
 def privatizable(inst):
     """Whether a detector of the chain has histograms small enough for the
     shared-memory private tallies of a whole-chain launch (two float
@@ -202,6 +217,10 @@ def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False
             candidates += [dict(c, privatize=1) for c in CANDIDATES]
         if has_mesh(inst):
             candidates += [dict(c, walk=1) for c in CANDIDATES]
+        k0 = chopper_run_start(inst)
+        if k0 is not None:
+            candidates += [dict(c, split=k0, cull=1) for c in CANDIDATES]
+            candidates += [dict(block=128, blocks_per_sm=2 * b, split=k0, cull=1) for b in (3, 4)]
     with torch.cuda.device(inst.device):
         stream = torch.cuda.current_stream(inst.device)
         for cfg in candidates:

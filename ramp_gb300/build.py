@@ -29,7 +29,8 @@ FUSED_INSTANCES = ([(mb, mode, b, ph, ks) for mb in (3, 4) for mode in (0, 1) fo
                     for ks in (0, 1, 2) for ph in (0, 1, 2) if not (b and ks == 1 and ph)]
                    + [(mb, mode, b, 4, 2) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)])
 CPP_SOURCES = ["bvh.cpp"]
-HEADERS = ["device.cuh", "fused_kernel.cuh", "mesh.cuh", "plan.h", "launch.h", "rmath.h", "rconst.h", "bvh.h",
+HEADERS = ["device.cuh", "fused_kernel.cuh", "mesh.cuh", "lookahead.h", "plan.h", "launch.h", "rmath.h",
+           "rconst.h", "bvh.h",
            os.path.join("..", "..", "include", "ramp.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

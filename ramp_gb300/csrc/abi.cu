@@ -22,6 +22,7 @@
 #include "rconst.h"
 #include "plan.h"
 #include "launch.h"
+#include "lookahead.h"
 #include "bvh.h"
 
 static thread_local std::string g_err;
@@ -370,6 +371,9 @@ static int get_bvh(RampPlan* p, const float* pts, int64_t len, const float4** no
   return RAMP_OK;
 }
 
+/* chopper slit period 2 pi / n_slits (chopper.cl:21), per component */
+static float chopper_period(const RampComp& c) { return 2.0f * RC_PI / (float)(uint32_t)c.si[0]; }
+
 /* Convert one caller descriptor into its device form.  Tables (and a mesh's
  * BVH) are uploaded when the plan does not hold them yet; with may_upload
  * false they must already be held (callers that may not allocate). */
@@ -387,8 +391,7 @@ static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo 
   for (int k = 0; k < 6; ++k) d.dslot[k] = -1;
   d.priv_off = -1;
   if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
-  /* chopper slit period 2 pi / n_slits (chopper.cl:21), per component */
-  if (c.scat == RAMP_S_CHOPPER) d.aux[0] = 2.0f * RC_PI / (float)(uint32_t)c.si[0];
+  if (c.scat == RAMP_S_CHOPPER) d.aux[0] = chopper_period(c);
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;   /* the BVH replaces the raw points */
@@ -623,13 +626,78 @@ static int tune_split(const RampPlan* p, const RampTune* tune, int32_t* out) {
   return RAMP_OK;
 }
 
-/* the launch's stage split: RampTune.walk (chains without the extended
- * kinds that hold a GMesh component in a linear block: split before the
- * first such component, which may be component 0, and walk the mesh per
- * lane in stage B), else RampTune.split */
+/* ---- chopper look-ahead (RampTune.cull; the bound is in lookahead.h) ---- */
+static bool on_axis_plane(const RampComp& c) {
+  return c.geom == RAMP_G_PLANE && c.gi[0] == 0 && c.restore == 0 && c.rot[0] == 0.0f &&
+         c.rot[1] == 0.0f && c.rot[2] == 0.0f && c.pos[0] == 0.0f && c.pos[1] == 0.0f &&
+         std::isfinite(c.pos[2]);
+}
+
+/* length of the run of on-axis components at k: at most one straight
+ * guide, then choppers (0: no chopper follows) */
+static int chopper_run(const RampComp* comps, int nc, const RampBlock* blocks, int nb, int k) {
+  if (!comps || !blocks || k < 0 || k >= nc) return 0;
+  int end = -1;
+  for (int b = 0; b < nb; ++b)
+    if (blocks[b].linear && blocks[b].first <= k && k < blocks[b].first + blocks[b].count)
+      end = std::min(blocks[b].first + blocks[b].count, nc);
+  if (end < 0) return 0;
+  int j = k;
+  float zmin = -INFINITY;
+  const RampComp& g = comps[j];
+  if (g.scat == RAMP_S_GUIDE) {
+    if (!on_axis_plane(g) || !(g.sp[0] == g.sp[2]) || !(g.sp[1] == g.sp[3]) ||
+        !(g.sp[0] > 0.0f) || !(g.sp[1] > 0.0f) || !(g.sp[4] > 0.0f) || !std::isfinite(g.sp[4]))
+      return 0;
+    zmin = g.pos[2] + g.sp[4];
+    ++j;
+  }
+  int nch = 0;
+  for (; j < end; ++j) {
+    const RampComp& c = comps[j];
+    if (c.scat != RAMP_S_CHOPPER || !on_axis_plane(c) || !(c.sp[1] > 0.0f) ||
+        (uint32_t)c.si[0] == 0u || !(c.pos[2] >= zmin))
+      break;
+    bool finite = true;
+    for (int q = 0; q < 5; ++q) finite = finite && std::isfinite(c.sp[q]);
+    if (!finite) break;
+    zmin = c.pos[2];
+    ++nch;
+  }
+  return nch > 0 ? j - k : 0;
+}
+
+/* the launch's stage split: RampTune.cull (split before component
+ * `split`, which may be 0, and retire in stage A what the look-ahead
+ * shows cannot pass the chopper run there; every variant must hold the
+ * run), else RampTune.walk (chains without the extended kinds that hold a
+ * GMesh component in a linear block: split before the first such
+ * component, which may be component 0, and walk the mesh per lane in
+ * stage B), else RampTune.split */
 static int tune_stage(const RampPlan* p, const RampTune* tune, bool ext, int32_t* split,
-                      int32_t* walk) {
+                      int32_t* walk, int32_t* cull, const RampVariant* vars = nullptr,
+                      int n_vars = 0) {
   *walk = 0;
+  *cull = 0;
+  if (tune && tune->cull > 0) {
+    if (tune->walk > 0) {
+      set_err("RampTune.cull and RampTune.walk exclude each other");
+      return RAMP_E_INVALID;
+    }
+    const int nc = (int)p->comps.size();
+    const int k = tune->split > 0 ? tune->split : 0;
+    int nl = chopper_run(p->comps_in.data(), nc, p->blocks.data(), (int)p->blocks.size(), k);
+    for (int v = 0; v < n_vars && nl > 0; ++v)
+      nl = std::min(nl, chopper_run(vars[v].comps, nc, p->blocks.data(), (int)p->blocks.size(), k));
+    if (nl == 0) {
+      set_err("RampTune.cull: no run of on-axis choppers (after at most one straight guide) "
+              "starts at component %d", k);
+      return RAMP_E_INVALID;
+    }
+    *split = k;
+    *cull = nl;
+    return RAMP_OK;
+  }
   if (tune && tune->walk > 0 && !ext) {
     for (const RampBlock& B : p->blocks) {
       if (!B.linear) continue;
@@ -857,14 +925,14 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.st = p->status;
   a.workq = &p->status->workq;
   a.workq_b = &p->status->workq_b;
-  int rc = tune_stage(p, tune, p->ext, &a.split, &a.walk);
-  if (!rc && tune && tune->privatize > 0 && a.split == 0 && !a.walk) {
+  int rc = tune_stage(p, tune, p->ext, &a.split, &a.walk, &a.cull);
+  if (!rc && tune && tune->privatize > 0 && a.split == 0 && !a.walk && !a.cull) {
     rc = priv_descriptors(p, s, &a.priv_floats);
     if (!rc && a.priv_floats > 0) a.single.comps = p->priv_dev;
   }
   if (rc) return rc;
   a.ext = kind_set(p->ext, p->mesh);
-  if (a.split > 0 || a.walk) {
+  if (a.split > 0 || a.walk || a.cull) {
     rc = attach_surv(p, a, (n + 127) / 128, s);
     if (rc) return rc;
   }
@@ -881,7 +949,8 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
  * the whole call can be captured in a CUDA graph).  Kernels of different
  * streams fill each other's tails. */
 static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<VariantDev>& vars,
-                           int block, int grid, const RampTune* tune, cudaStream_t s) {
+                           int block, int grid, const RampTune* tune, int32_t split,
+                           int32_t walk, int32_t cull, cudaStream_t s) {
   BatchCache& B = p->batch;
   const size_t nv = vars.size();
   if (B.counters_cap < 2 * nv) {             /* stage A and stage B queues */
@@ -893,14 +962,12 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
   }
   /* split launches: each variant gets its own region of the survivor
      buffer (its items' slots, SoA, and its items' counts) */
-  int32_t split = 0, walk = 0;
-  int rc0 = tune_stage(p, tune, base.ext == 1, &split, &walk);
-  if (rc0) return rc0;
+  int rc0 = RAMP_OK;
   std::vector<int64_t> item_off(nv + 1, 0);
   for (size_t v = 0; v < nv; ++v)
     item_off[v + 1] = item_off[v] + (vars[v].n > 0 ? (vars[v].n + 127) / 128 : 0);
   uint32_t* cnt = nullptr;
-  if ((split > 0 || walk) && item_off[nv] > 0) {
+  if ((split > 0 || walk || cull) && item_off[nv] > 0) {
     rc0 = ensure_surv(p, item_off[nv]);
     if (rc0) return rc0;
     cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS;
@@ -940,6 +1007,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
       const int64_t items = item_off[v + 1] - item_off[v];
       a.split = split;
       a.walk = walk;
+      a.cull = cull;
       a.surv = p->surv + (size_t)item_off[v] * 128 * SURV_WORDS;
       a.surv_cap = items * 128;
       a.surv_cnt = cnt + item_off[v];
@@ -1024,6 +1092,8 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   }
   bool ext = p->ext;
   for (int v = 0; v < n_variants; ++v) ext = ext || ext_source(variants[v].source);
+  int32_t split = 0, walk = 0, cull = 0;
+  if (int rc = tune_stage(p, tune, ext, &split, &walk, &cull, variants, n_variants)) return rc;
   if (use_streams) {
     FusedArgs a;
     memset(&a, 0, sizeof(a));
@@ -1036,7 +1106,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     a.rng.run_seed = rng ? rng->run_seed : 0u;
     a.rng.tid_base = 0u;   /* variants key by their own index */
     a.st = p->status;
-    return batched_streams(p, a, vars, block, grid, tune, s);
+    return batched_streams(p, a, vars, block, grid, tune, split, walk, cull, s);
   }
   /* one launch: grid row v traces variant v from its own work counter
      (two with a split), its survivors in its own range of work items */
@@ -1046,10 +1116,8 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     return RAMP_E_RANGE;
   }
   if (n_max == 0) return RAMP_OK;
-  int32_t split = 0, walk = 0;
-  int rc = tune_stage(p, tune, ext, &split, &walk);
-  if (rc) return rc;
-  if (ext) split = 0;   /* the one-launch kernel runs the extended kinds whole */
+  int rc = RAMP_OK;
+  if (ext) split = cull = 0;   /* the one-launch kernel runs the extended kinds whole */
   int64_t items = 0;
   for (int v = 0; v < n_variants; ++v) {
     vars[v].item_off = items;
@@ -1092,8 +1160,9 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.workq_b = B.counters + n_variants;
   a.split = split;
   a.walk = walk;
+  a.cull = cull;
   a.ext = kind_set(ext, p->mesh);
-  if (a.split > 0 || a.walk) {
+  if (a.split > 0 || a.walk || a.cull) {
     rc = attach_surv(p, a, items, s);
     if (rc) return rc;
   }
@@ -1333,6 +1402,41 @@ int ramp_debug_atomic_peak(float* bins, int64_t n_bins, int64_t n_threads, int32
     return RAMP_E_INVALID;
   }
   CK(launch_debug_atomic_peak(bins, n_bins, n_threads, iters, (cudaStream_t)stream));
+  return RAMP_OK;
+}
+
+int ramp_chopper_run(const RampComp* comps, int n_comps, const RampBlock* blocks, int n_blocks,
+                     int k) {
+  return chopper_run(comps, n_comps, blocks, n_blocks, k);
+}
+
+int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock* blocks,
+                            int n_blocks, int k, const float* records, int64_t n, uint8_t* out) {
+  if (!comps || n_comps <= 0 || n < 0 || (n > 0 && (!records || !out))) {
+    set_err("ramp_debug_chopper_cull: bad arguments");
+    return RAMP_E_INVALID;
+  }
+  const int nl = chopper_run(comps, n_comps, blocks, n_blocks, k);
+  if (nl == 0) {
+    set_err("ramp_debug_chopper_cull: no chopper run at component %d", k);
+    return RAMP_E_INVALID;
+  }
+  /* the descriptor fields the bound reads, as make_comp sets them */
+  std::vector<CompDev> d((size_t)n_comps);
+  for (int j = 0; j < n_comps; ++j) {
+    CompDev& q = d[(size_t)j];
+    memset(&q, 0, sizeof(q));
+    q.geom = comps[j].geom; q.scat = comps[j].scat;
+    memcpy(q.pos, comps[j].pos, sizeof(q.pos));
+    memcpy(q.sp, comps[j].sp, sizeof(q.sp));
+    memcpy(q.si, comps[j].si, sizeof(q.si));
+    if (comps[j].scat == RAMP_S_CHOPPER && (uint32_t)comps[j].si[0] != 0u)
+      q.aux[0] = chopper_period(comps[j]);
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    const float* r = records + 16 * i;
+    out[i] = chopper_run_blocks(d.data(), k, nl, r[0], r[1], r[2], r[3], r[4], r[5], r[10]) ? 1 : 0;
+  }
   return RAMP_OK;
 }
 

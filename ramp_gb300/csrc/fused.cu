@@ -38,7 +38,7 @@ static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream
     }
   }
   if constexpr (!(BATCHED && KS == 1)) {
-    if (a.split > 0) {
+    if (a.split > 0 || a.cull > 0) {
       const cudaError_t e = launch_phase<MB, MODE, BATCHED, 1, KS>(a, block, grid, s);
       if (e != cudaSuccess) return e;
       return launch_phase<MB, MODE, BATCHED, 2, KS>(a, block, grid, s);
@@ -66,7 +66,10 @@ cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s
   if (a.variants ? a.n_variants <= 0 : a.n_tasks <= 0) return cudaSuccess;
   if (a.variants && a.n_variants > 65535) return cudaErrorInvalidValue;   /* grid rows */
   if (a.n_blocks > FUSED_MAX_BLOCKS || a.n_comps > RAMP_MAX_COMPS) return cudaErrorInvalidValue;
-  if (a.split < 0 || (a.split > 0 && (a.split >= a.n_comps || !a.surv))) return cudaErrorInvalidValue;
+  if (a.split < 0 || ((a.split > 0 || a.cull > 0) && (a.split >= a.n_comps || !a.surv)))
+    return cudaErrorInvalidValue;
+  if (a.cull > 0 && (a.walk || a.split + a.cull > a.n_comps || (a.variants && a.ext == 1)))
+    return cudaErrorInvalidValue;
   if (a.walk && (a.ext != 2 || a.split >= a.n_comps || !a.surv)) return cudaErrorInvalidValue;
   /* register cap: 3 or 4 CTAs of 256 threads per SM (at 2 the kernel is
      never faster on GB300) */

@@ -26,6 +26,7 @@
 #define RAMP_FUSED_KERNEL_CUH
 #include "device.cuh"
 #include "launch.h"
+#include "lookahead.h"
 
 #define FUSED_MAX_BLOCKS 32
 #define FUSED_WARP_TASK 128   /* neutrons a warp claims at once */
@@ -374,6 +375,11 @@ k_fused(const FusedArgs a) {
               block_nonlinear<TallyOnly, EXT, MESH>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
             }
           }
+          /* the chopper look-ahead: a neutron that certainly cannot pass
+             the choppers after the split adds nothing to any tally */
+          if (PHASE == 1 && zx && a.cull > 0 && !(n.die > 0.f) &&
+              chopper_run_blocks(comps, KE, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t))
+            n.die = 1.0f;
         }
         if (PHASE == 0) {
           if (carry) { a.carry_sb[i] = n.sb; a.carry_iidx[i] = ii; }

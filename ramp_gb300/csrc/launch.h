@@ -60,6 +60,10 @@ struct FusedArgs {
   int32_t priv_floats;          /* whole chain, one instrument: shared-memory
                                    floats of the private tallies (descriptors
                                    with priv_off >= 0); 0: off */
+  int32_t cull;                 /* split launch: components of the chopper run
+                                   at `split` (lookahead.h); stage A retires
+                                   the neutrons that cannot pass it (without
+                                   carry buffers).  0: off */
 };
 #define RAMP_PRIV_FLOATS 12288  /* shared memory for private tallies: 48 KB per CTA */
 #define SURV_WORDS 18           /* 15 record lanes (die is 0), iidx, index, variant */

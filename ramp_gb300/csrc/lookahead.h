@@ -1,0 +1,143 @@
+/*
+ * lookahead.h — the chopper look-ahead of split fused launches
+ * (RampTune.cull).  From a neutron's state before a run of on-axis
+ * components (at most one straight guide, then disk choppers) it bounds
+ * when and where the neutron meets each chopper's plane and tells whether
+ * some chopper certainly stops it.  Compiled for the device (the end of
+ * stage A) and for the host (ramp_debug_chopper_cull, with which the
+ * bound is checked against the CPU restatement of the reference kernels).
+ *
+ * The run (checked by chopper_run in abi.cu): components of one linear
+ * block, each unrotated, centred on the z axis (x = y = 0), with a
+ * z-normal GPlane and no restore; first at most one SGuide with w1 = w2
+ * and h1 = h2, then SChopper components at non-decreasing z, the first at
+ * or after the guide's exit.  Why the bounds hold there:
+ *  - time.  Nothing in the run changes vz: the frame transforms are the
+ *    identity on velocities; a straight guide's wall normals have no z
+ *    component (guide.cl:39-43 with w1 = w2: ww = hh = 0, so the bounce
+ *    leaves vz - d * 0 = vz); planes and choppers do not touch velocities.
+ *    So the time at a chopper plane is t + (zc - z) / vz, up to the
+ *    rounding of the segment times and z steps the kernels add up.
+ *  - transverse position.  Inside a straight guide of half-width a the
+ *    motion is the unfolded line u(z) = x_e + (vx / vz)(z - z_e) reflected
+ *    at x = +-a (the bounce loop, guide.cl:49-135, reflects at one wall at
+ *    a time, x and y independently); after the exit the neutron flies on
+ *    from its last bounce along the folded line.  A reflection changes
+ *    |vx| by a few ulp (about 5e-7 relative); when the folded exit point
+ *    lies within the slack of a wall, the last bounce may fall on either
+ *    side of the exit plane, and both signs of vx after the exit are
+ *    allowed.
+ *  - the chopper (chopper.cl:4-59): the neutron passes only if the
+ *    distance from freq (t - |phase|) + e - atan2(x, y + R), e in
+ *    [-jitter, jitter), to the nearest multiple of 2 pi / n_slits is at
+ *    most atan2(w, y + R) / 2.  atan2(x, Y) is monotone in x and in Y for
+ *    Y > 0, so its range over the box of (x, y) is taken at corners, and
+ *    atan2(w, Y) <= w / Y.
+ * Every slack is far above the rounding it covers (time: 1e-5 relative
+ * plus a micrometre of z per bounce; position: 2e-5 m plus 4e-6 of the
+ * guide path per bounce; angle: 1e-4 rad plus 1e-6 relative).  A neutron
+ * outside the assumptions (vz <= 0, at the guide entrance within the slack
+ * of a wall, y + R not clearly positive, angles beyond 1e4 rad) gets no
+ * claim.  A neutron that would instead miss a plane, leave the guide at
+ * zero weight or exceed its bounce limit dies in the reference as well,
+ * so with only tallies observable it may be retired either way.
+ */
+#ifndef RAMP_LOOKAHEAD_H
+#define RAMP_LOOKAHEAD_H
+
+#include "rmath.h"
+#include "plan.h"
+
+#if defined(__CUDACC__)
+#define LA_FN static __host__ __device__ __forceinline__
+#else
+#define LA_FN static inline
+#endif
+
+/* the folded position of the unfolded coordinate u in a guide of
+ * half-width a, x = a - |((u + a) mod 4a) - 2a|; *sgn is +1 where the
+ * neutron moves along the unfolded line, -1 against it; *amb when x lies
+ * within `slack` of a wall */
+LA_FN float la_fold(float u, float a, float slack, float* sgn, bool* amb) {
+  const float p = 4.0f * a;
+  float m = u + a;
+  m = m - p * floorf(m / p);
+  if (m < 0.0f) m += p;
+  if (m >= p) m -= p;
+  const bool up = m < 2.0f * a;
+  const float x = up ? m - a : 3.0f * a - m;
+  *sgn = up ? 1.0f : -1.0f;
+  *amb = !(a - fabsf(x) > slack);
+  return x;
+}
+
+/* true: the neutron at (x, y, z) with velocity (vx, vy, vz) and time t,
+ * in the laboratory frame before component k, cannot pass every chopper
+ * of the run comps[k .. k + nl) */
+LA_FN bool chopper_run_blocks(const CompDev* comps, int k, int nl, float x, float y, float z,
+                              float vx, float vy, float vz, float t) {
+  if (!(vz > 0.0f) || nl <= 0) return false;
+  const float sx = vx / vz, sy = vy / vz;
+  /* the reference line after the guide: x(zz) = x0 + mx (zz - z0), with
+     slope uncertainty ux when the sign after the exit is ambiguous */
+  float x0 = x, y0 = y, z0 = z, mx = sx, my = sy, ux = 0.0f, uy = 0.0f;
+  float ex = 2e-5f, ey = 2e-5f;   /* position slack (m) */
+  float nb = 0.0f;                /* bounces, for the time slack */
+  int j = k;
+  if (comps[j].scat == RAMP_S_GUIDE) {
+    const CompDev& g = comps[j];
+    const float zg = g.pos[2], l = g.sp[4];
+    const float a = 0.5f * g.sp[0], b = 0.5f * g.sp[1];
+    const float dz = zg - z;
+    if (!(dz >= 0.0f)) return false;
+    const float xe = x + sx * dz, ye = y + sy * dz;
+    if (!(fabsf(xe) < a - 2e-5f) || !(fabsf(ye) < b - 2e-5f)) return false;
+    const float dux = sx * l, duy = sy * l;
+    const float nbx = floorf(fabsf(dux) / (2.0f * a)) + 1.0f;
+    const float nby = floorf(fabsf(duy) / (2.0f * b)) + 1.0f;
+    if (!(nbx < 1e4f) || !(nby < 1e4f)) return false;
+    nb = nbx + nby;
+    ex += 4e-6f * nbx * (fabsf(dux) + a);
+    ey += 4e-6f * nby * (fabsf(duy) + b);
+    float gx, gy;
+    bool ax, ay;
+    x0 = la_fold(xe + dux, a, ex, &gx, &ax);
+    y0 = la_fold(ye + duy, b, ey, &gy, &ay);
+    z0 = zg + l;
+    mx = ax ? 0.0f : gx * sx;
+    ux = ax ? fabsf(sx) : 0.0f;
+    my = ay ? 0.0f : gy * sy;
+    uy = ay ? fabsf(sy) : 0.0f;
+    ++j;
+  }
+  for (; j < k + nl; ++j) {
+    const CompDev& c = comps[j];
+    const float zc = c.pos[2];
+    const float dzc = zc - z0;
+    if (!(dzc >= -1e-6f)) return false;
+    const float xc = x0 + mx * dzc, yc = y0 + my * dzc;
+    /* the slope error of the bounces carries on after the exit */
+    const float exc = ex + (ux + 4e-6f * nb * fabsf(sx)) * fabsf(dzc) + 1e-6f * fabsf(xc);
+    const float eyc = ey + (uy + 4e-6f * nb * fabsf(sy)) * fabsf(dzc) + 1e-6f * fabsf(yc);
+    const float tc = t + (zc - z) / vz;
+    const float et = 1e-5f * fabsf(tc) + (1e-5f * fabsf(zc - z) + 1e-6f * (nb + 10.0f)) / vz + 1e-9f;
+    const float sw = c.sp[0], R = c.sp[1], freq = c.sp[2], phase = c.sp[3], jit = c.sp[4];
+    const float Tg = c.aux[0];
+    const float Ylo = yc - eyc + R, Yhi = yc + eyc + R;
+    if (!(Ylo > 1e-3f) || !(Tg > 0.0f)) continue;
+    const float xlo = xc - exc, xhi = xc + exc;
+    const float th_hi = rm_atan2f(xhi, xhi >= 0.0f ? Ylo : Yhi);
+    const float th_lo = rm_atan2f(xlo, xlo >= 0.0f ? Yhi : Ylo);
+    const float c0 = freq * (tc - et - fabsf(phase)), c1 = freq * (tc + et - fabsf(phase));
+    const float dlo = fminf(c0, c1) - fabsf(jit) - th_hi;
+    const float dhi = fmaxf(c0, c1) + fabsf(jit) - th_lo;
+    if (!(fabsf(dlo) < 1e4f) || !(fabsf(dhi) < 1e4f)) continue;
+    const float h = 0.5f * fabsf(sw) / Ylo + 1e-4f + 1e-6f * fmaxf(fabsf(dlo), fabsf(dhi));
+    /* no multiple of the slit period within [dlo - h, dhi + h] */
+    const float klo = ceilf((dlo - h) / Tg), khi = floorf((dhi + h) / Tg);
+    if (klo > khi) return true;
+  }
+  return false;
+}
+
+#endif /* RAMP_LOOKAHEAD_H */

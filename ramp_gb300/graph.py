@@ -130,8 +130,8 @@ def capture(inst, N, path="fused", rng="reference", run_seed=0, tune=None, chunk
         rngd.mode = {"reference": 0, "native": 1}[rng]
         rngd.run_seed = int(run_seed) & 0xffffffff
         rngd.seed_dev = seed_buf.data_ptr()
-        if path == "fused" and tune and (int(tune.get("split", 0)) > 0
-                                         or int(tune.get("walk", 0)) > 0):
+        if path == "fused" and tune and any(int(tune.get(k, 0)) > 0
+                                            for k in ("split", "walk", "cull")):
             _abi.check(lib, lib.ramp_plan_reserve(plan, first), "ramp_plan_reserve")
         stream = inst.queue if inst.queue is not None else torch.cuda.Stream(dev)
         torch.cuda.synchronize(dev)

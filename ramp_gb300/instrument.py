@@ -217,8 +217,9 @@ class Instrument:
         rng  : "reference" reproduces the reference's per-draw Threefry
                stream; "native" uses all four words of each block.
         tune : fused launch configuration: a dict of RampTune fields
-               (blocks_per_sm, chunk, split, streams) or "auto" for the
-               cached autotuner choice (ramp_gb300.autotune).
+               (block, blocks_per_sm, chunk, privatize, split, streams,
+               walk, cull) or "auto" for the cached autotuner choice
+               (ramp_gb300.autotune).
         chunk: override the chunk size (default max_mem_alloc / 256).
         shard: (rank, world) — trace only this rank's contiguous slice of
                every chunk, keyed by global index and weighted by the full

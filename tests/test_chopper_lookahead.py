@@ -1,0 +1,116 @@
+"""The chopper look-ahead of split fused launches (RampTune.cull,
+ramp_gb300/csrc/lookahead.h), on the CPU.
+
+Soundness: the bound is evaluated on each neutron's state after the
+moderator (the oracle's records of a moderator + arm chain) and compared
+with what the oracle's trace of moderator -> guide -> chopper -> chopper
+does with the same neutrons (same keys, same seeds): no neutron that
+passes both choppers (mcramp/scat/chopper.cl:4-59) may be retired.
+Efficiency: the bound retires most of those that do not pass.  The run
+detection (ramp_chopper_run) accepts only on-axis, unrotated, straight
+runs."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+import ramp_gb300 as m
+from ramp_gb300 import _abi
+
+MOD = '''
+    "mod": {"source": true, "position": [0.0, 0.0, 0.0],
+      "moderator_kernel": {"name": "MCont", "mod_dim": [0.1, 0.1], "target_dim": [0.04, 0.04],
+        "target_dist": 1.7, "E_min": 1.1, "E_max": 9.0, "T1": 40.0, "I1": 1.0,
+        "T2": 40.0, "I2": 0.0, "T3": 40.0, "I3": 0.0}}'''
+
+RUN = '''
+    "guide1": {"position": [0.0, 0.0, 1.7],
+      "geom_kernel": {"name": "GPlane", "width": 0.04, "height": 0.04},
+      "scat_kernel": {"name": "SGuide", "w1": 0.04, "h1": 0.04, "w2": $gw2$, "h2": 0.04,
+        "l": 6.05, "R0": 0.99, "Qc": 0.0219, "alpha": 3.0, "m": 2, "W": 0.003}},
+    "chopper1": {"position": [0.0, $cy$, 7.8],
+      "geom_kernel": {"name": "GPlane", "width": 0.6, "height": 0.6},
+      "scat_kernel": {"name": "SChopper", "radius": 0.28, "freq": 1884.955592, "n_slits": 6,
+        "jitter": 7e-07, "slit_width": 0.04, "phase": $7.80 / (437.393*Ei**0.5)$}},
+    "chopper2": {"position": [0.0, 0.0, 8.4],
+      "geom_kernel": {"name": "GPlane", "width": 0.6, "height": 0.6},
+      "scat_kernel": {"name": "SChopper", "radius": 0.28, "freq": 62.831853, "n_slits": 1,
+        "jitter": 7e-07, "slit_width": 0.04, "phase": $8.40 / (437.393*Ei**0.5)$}}'''
+
+ARM = '''
+    "arm": {"position": [0.0, 0.0, 0.0], "geom_kernel": {"name": "GArm"},
+      "scat_kernel": {"name": "SArm"}}'''
+
+
+def instrument(tmp_path, name, body, **kw):
+    fn = tmp_path / name
+    fn.write_text('{"all": {"linear": true,%s}}' % body)
+    return m.Instrument(str(fn), "cpu", **kw)
+
+
+def run_length(inst, k):
+    keep = []
+    _, carr, nc, barr, nb = inst.descriptors(keep)
+    return _abi.load().ramp_chopper_run(ctypes.addressof(carr), nc, ctypes.addressof(barr), nb, k)
+
+
+def culled(inst, k, records):
+    keep = []
+    _, carr, nc, barr, nb = inst.descriptors(keep)
+    rec = np.ascontiguousarray(records, dtype=np.float32)
+    out = np.zeros(len(rec), np.uint8)
+    lib = _abi.load()
+    rc = lib.ramp_debug_chopper_cull(ctypes.addressof(carr), nc, ctypes.addressof(barr), nb, k,
+                                     rec.ctypes.data, len(rec), out.ctypes.data)
+    _abi.check(lib, rc, "ramp_debug_chopper_cull")
+    return out.astype(bool)
+
+
+@pytest.mark.parametrize("Ei", [1.5, 3.7, 8.0])
+def test_lookahead_never_retires_a_neutron_that_passes(tmp_path, Ei):
+    N = 400_000
+    kw = dict(Ei=Ei, gw2=0.04, cy=0.0)
+    full = instrument(tmp_path, "run.json", MOD + "," + RUN, **kw)
+    arm = instrument(tmp_path, "arm.json", MOD + "," + ARM, **kw)
+    assert run_length(full, 0) == 3          # the guide and both choppers
+    seeds = [1234]
+    after_mod = oracle.run(arm, N, seeds=seeds).neutrons
+    traced = oracle.run(full, N, seeds=seeds).neutrons
+    passed = traced[:, 15] == 0.0
+    # the same neutrons: a neutron through both choppers drew twice more
+    assert np.array_equal(after_mod[passed, 11] + 2, traced[passed, 11])
+    cut = culled(full, 0, after_mod)
+    assert passed.sum() > 100
+    assert not (cut & passed).any(), "a neutron that passes the choppers was retired"
+    # most of those that do not pass are retired before the guide
+    assert cut.sum() >= 0.8 * (~passed).sum()
+
+
+def test_lookahead_run_detection(tmp_path):
+    kw = dict(Ei=3.7, gw2=0.04, cy=0.0)
+    full = instrument(tmp_path, "run.json", MOD + "," + RUN, **kw)
+    assert run_length(full, 0) == 3
+    assert run_length(full, 1) == 2          # from chopper 1: both choppers, no guide
+    assert run_length(full, 2) == 1
+    # a tapered guide, or a chopper off the axis, ends the run before it
+    taper = instrument(tmp_path, "taper.json", MOD + "," + RUN, **dict(kw, gw2=0.03))
+    assert run_length(taper, 0) == 0
+    assert run_length(taper, 1) == 2
+    off = instrument(tmp_path, "off.json", MOD + "," + RUN, **dict(kw, cy=0.01))
+    assert run_length(off, 0) == 0
+    assert run_length(off, 2) == 1
+    # the bound is only offered where there is a run
+    lib = _abi.load()
+    keep = []
+    _, carr, nc, barr, nb = off.descriptors(keep)
+    rec = np.zeros((1, 16), np.float32)
+    out = np.zeros(1, np.uint8)
+    assert lib.ramp_debug_chopper_cull(ctypes.addressof(carr), nc, ctypes.addressof(barr), nb, 0,
+                                       rec.ctypes.data, 1, out.ctypes.data) == _abi.E_INVALID
+
+
+def test_let_like_chain_has_a_run_after_the_moderator():
+    from ramp_gb300 import instruments as I
+    inst = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
+    assert run_length(inst, 0) == 3

@@ -416,7 +416,8 @@ def test_autotune_survival_and_split_point(cuda_lib, tmp_path, monkeypatch):
     assert autotune.split_point(inst, alive) == 2
     before = [t.clone() for t in inst.tallies()]
     cfg = autotune.tune(inst, n_probe=200_000)
-    assert set(cfg) <= set(("block", "blocks_per_sm", "chunk", "split", "privatize"))
+    assert set(cfg) <= set(("block", "blocks_per_sm", "chunk", "split", "privatize", "cull"))
+    assert autotune.chopper_run_start(inst) == 0
     for t, b in zip(inst.tallies(), before):
         assert torch.equal(t, b)
 
