@@ -371,8 +371,12 @@ static int get_bvh(RampPlan* p, const float* pts, int64_t len, const float4** no
   return RAMP_OK;
 }
 
-/* chopper slit period 2 pi / n_slits (chopper.cl:21), per component */
-static float chopper_period(const RampComp& c) { return 2.0f * RC_PI / (float)(uint32_t)c.si[0]; }
+/* chopper constants: aux[0] the slit period 2 pi / n_slits (chopper.cl:21),
+ * aux[1] its reciprocal (for the look-ahead bound of lookahead.h) */
+static void chopper_aux(const RampComp& c, float* aux) {
+  aux[0] = 2.0f * RC_PI / (float)(uint32_t)c.si[0];
+  aux[1] = 1.0f / aux[0];
+}
 
 /* Convert one caller descriptor into its device form.  Tables (and a mesh's
  * BVH) are uploaded when the plan does not hold them yet; with may_upload
@@ -391,7 +395,7 @@ static int make_comp(RampPlan* p, const RampComp& c, CompDev& d, HashMemo* memo 
   for (int k = 0; k < 6; ++k) d.dslot[k] = -1;
   d.priv_off = -1;
   if (c.scat == RAMP_S_GUIDE) guide_aux(c, d.aux);
-  if (c.scat == RAMP_S_CHOPPER) d.aux[0] = chopper_period(c);
+  if (c.scat == RAMP_S_CHOPPER) chopper_aux(c, d.aux);   /* no slits: period inf, as 2 pi / 0 */
   for (int k = 0; k < RAMP_NTAB; ++k) {
     d.tab_len[k] = c.table_len[k];
     if (c.geom == RAMP_G_MESH && k == 0) continue;   /* the BVH replaces the raw points */
@@ -1431,7 +1435,7 @@ int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock*
     memcpy(q.sp, comps[j].sp, sizeof(q.sp));
     memcpy(q.si, comps[j].si, sizeof(q.si));
     if (comps[j].scat == RAMP_S_CHOPPER && (uint32_t)comps[j].si[0] != 0u)
-      q.aux[0] = chopper_period(comps[j]);
+      chopper_aux(comps[j], q.aux);
   }
   for (int64_t i = 0; i < n; ++i) {
     const float* r = records + 16 * i;

@@ -55,7 +55,21 @@ k_fused(const FusedArgs a);
  * SURV_GROUP items at a time and deals their survivors out 32 to a pass.
  * A survivor is keyed by its own index and variant, so it continues
  * exactly where stage A left it. */
-#define SURV_GROUP 8
+#define SURV_GROUP 32   /* one work item per lane */
+
+/* the item of the current group that holds survivor q: the last item whose
+ * first survivor (excl, one item per lane, non-decreasing over the lanes)
+ * is at or before q, by binary search over the lanes; *base is that first
+ * survivor.  Every lane of the warp takes part. */
+DI int surv_item(int excl, int q, int* base) {
+  int lo = 0;
+  for (int step = 16; step >= 1; step >>= 1) {
+    const int e = __shfl_sync(FULL_MASK, excl, lo + step);
+    if (e <= q) lo += step;
+  }
+  *base = __shfl_sync(FULL_MASK, excl, lo);
+  return lo;
+}
 template <int MODE, bool BATCHED, int KS>
 DI void fused_tail(const FusedArgs& a) {
   constexpr bool EXT = KS == 1, MESH = KS != 0;
@@ -91,12 +105,8 @@ DI void fused_tail(const FusedArgs& a) {
     const int total = __shfl_sync(FULL_MASK, incl, SURV_GROUP - 1);
     for (int q0 = 0; q0 < total; q0 += 32) {
       const int q = q0 + lane;
-      int item = 0, base = 0;
-      for (int k = 0; k < SURV_GROUP; ++k) {   /* last item starting at or before q */
-        const int ek = __shfl_sync(FULL_MASK, excl, k);
-        const int ck = __shfl_sync(FULL_MASK, c, k);
-        if (ck > 0 && ek <= q) { item = k; base = ek; }
-      }
+      int base = 0;
+      const int item = surv_item(excl, q, &base);
       if (q >= total) continue;
       const int64_t s = (item0 + t0 + item) * FUSED_WARP_TASK + (q - base);
       const uint32_t* w = a.surv + s;
@@ -263,12 +273,8 @@ DI void fused_tail_walk(const FusedArgs& a) {
         continue;
       }
       const int qk = handed + __popc(m & lt);
-      int item = 0, base = 0;
-      for (int k = 0; k < SURV_GROUP; ++k) {   /* last item starting at or before qk */
-        const int ek = __shfl_sync(FULL_MASK, excl, k);
-        const int ck = __shfl_sync(FULL_MASK, c, k);
-        if (ck > 0 && ek <= qk) { item = k; base = ek; }
-      }
+      int base = 0;
+      const int item = surv_item(excl, qk, &base);
       handed = (handed + __popc(m) < total) ? handed + __popc(m) : total;
       if (!walking && qk < total) {
         slot = (item0 + t0 + item) * FUSED_WARP_TASK + (qk - base);

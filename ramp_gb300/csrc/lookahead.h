@@ -35,7 +35,8 @@
  *    atan2(w, Y) <= w / Y.
  * Every slack is far above the rounding it covers (time: 1e-5 relative
  * plus a micrometre of z per bounce; position: 2e-5 m plus 4e-6 of the
- * guide path per bounce; angle: 1e-4 rad plus 1e-6 relative).  A neutron
+ * guide path per bounce; angle: 1e-4 rad plus 1e-6 relative, which also
+ * covers the truncated atan series and products with reciprocals).  A neutron
  * outside the assumptions (vz <= 0, at the guide entrance within the slack
  * of a wall, y + R not clearly positive, angles beyond 1e4 rad) gets no
  * claim.  A neutron that would instead miss a plane, leave the guide at
@@ -55,13 +56,13 @@
 #endif
 
 /* the folded position of the unfolded coordinate u in a guide of
- * half-width a, x = a - |((u + a) mod 4a) - 2a|; *sgn is +1 where the
- * neutron moves along the unfolded line, -1 against it; *amb when x lies
- * within `slack` of a wall */
-LA_FN float la_fold(float u, float a, float slack, float* sgn, bool* amb) {
+ * half-width a (ia = 1/a), x = a - |((u + a) mod 4a) - 2a|; *sgn is +1
+ * where the neutron moves along the unfolded line, -1 against it; *amb
+ * when x lies within `slack` of a wall */
+LA_FN float la_fold(float u, float a, float ia, float slack, float* sgn, bool* amb) {
   const float p = 4.0f * a;
   float m = u + a;
-  m = m - p * floorf(m / p);
+  m = m - p * floorf(m * (0.25f * ia));
   if (m < 0.0f) m += p;
   if (m >= p) m -= p;
   const bool up = m < 2.0f * a;
@@ -71,13 +72,27 @@ LA_FN float la_fold(float u, float a, float slack, float* sgn, bool* amb) {
   return x;
 }
 
+/* atan(r): for |r| <= 1/4 the alternating series to r^7, whose error is
+ * below the next term, r^9/9 < 5e-7 (the angle slack covers it), else the
+ * library's atan2 */
+LA_FN float la_atan(float r) {
+  if (fabsf(r) <= 0.25f) {
+    const float r2 = r * r;
+    return r * (1.0f - r2 * (0.333333343f - r2 * (0.2f - r2 * 0.142857149f)));
+  }
+  return rm_atan2f(r, 1.0f);
+}
+
 /* true: the neutron at (x, y, z) with velocity (vx, vy, vz) and time t,
  * in the laboratory frame before component k, cannot pass every chopper
- * of the run comps[k .. k + nl) */
+ * of the run comps[k .. k + nl).  Divisions are replaced by products with
+ * reciprocals where the slack covers their extra rounding; a chopper's
+ * aux[0] is its slit period and aux[1] the reciprocal of it. */
 LA_FN bool chopper_run_blocks(const CompDev* comps, int k, int nl, float x, float y, float z,
                               float vx, float vy, float vz, float t) {
   if (!(vz > 0.0f) || nl <= 0) return false;
-  const float sx = vx / vz, sy = vy / vz;
+  const float ivz = 1.0f / vz;
+  const float sx = vx * ivz, sy = vy * ivz;
   /* the reference line after the guide: x(zz) = x0 + mx (zz - z0), with
      slope uncertainty ux when the sign after the exit is ambiguous */
   float x0 = x, y0 = y, z0 = z, mx = sx, my = sy, ux = 0.0f, uy = 0.0f;
@@ -92,17 +107,18 @@ LA_FN bool chopper_run_blocks(const CompDev* comps, int k, int nl, float x, floa
     if (!(dz >= 0.0f)) return false;
     const float xe = x + sx * dz, ye = y + sy * dz;
     if (!(fabsf(xe) < a - 2e-5f) || !(fabsf(ye) < b - 2e-5f)) return false;
+    const float ia = 1.0f / a, ib = 1.0f / b;
     const float dux = sx * l, duy = sy * l;
-    const float nbx = floorf(fabsf(dux) / (2.0f * a)) + 1.0f;
-    const float nby = floorf(fabsf(duy) / (2.0f * b)) + 1.0f;
+    const float nbx = floorf(fabsf(dux) * (0.5f * ia)) + 2.0f;
+    const float nby = floorf(fabsf(duy) * (0.5f * ib)) + 2.0f;
     if (!(nbx < 1e4f) || !(nby < 1e4f)) return false;
     nb = nbx + nby;
     ex += 4e-6f * nbx * (fabsf(dux) + a);
     ey += 4e-6f * nby * (fabsf(duy) + b);
     float gx, gy;
     bool ax, ay;
-    x0 = la_fold(xe + dux, a, ex, &gx, &ax);
-    y0 = la_fold(ye + duy, b, ey, &gy, &ay);
+    x0 = la_fold(xe + dux, a, ia, ex, &gx, &ax);
+    y0 = la_fold(ye + duy, b, ib, ey, &gy, &ay);
     z0 = zg + l;
     mx = ax ? 0.0f : gx * sx;
     ux = ax ? fabsf(sx) : 0.0f;
@@ -119,22 +135,23 @@ LA_FN bool chopper_run_blocks(const CompDev* comps, int k, int nl, float x, floa
     /* the slope error of the bounces carries on after the exit */
     const float exc = ex + (ux + 4e-6f * nb * fabsf(sx)) * fabsf(dzc) + 1e-6f * fabsf(xc);
     const float eyc = ey + (uy + 4e-6f * nb * fabsf(sy)) * fabsf(dzc) + 1e-6f * fabsf(yc);
-    const float tc = t + (zc - z) / vz;
-    const float et = 1e-5f * fabsf(tc) + (1e-5f * fabsf(zc - z) + 1e-6f * (nb + 10.0f)) / vz + 1e-9f;
+    const float tc = t + (zc - z) * ivz;
+    const float et = 1e-5f * fabsf(tc) + (1e-5f * fabsf(zc - z) + 1e-6f * (nb + 10.0f)) * ivz + 1e-9f;
     const float sw = c.sp[0], R = c.sp[1], freq = c.sp[2], phase = c.sp[3], jit = c.sp[4];
-    const float Tg = c.aux[0];
+    const float iTg = c.aux[1];
     const float Ylo = yc - eyc + R, Yhi = yc + eyc + R;
-    if (!(Ylo > 1e-3f) || !(Tg > 0.0f)) continue;
+    if (!(Ylo > 1e-3f) || !(iTg > 0.0f)) continue;
+    const float iYlo = 1.0f / Ylo, iYhi = 1.0f / Yhi;
     const float xlo = xc - exc, xhi = xc + exc;
-    const float th_hi = rm_atan2f(xhi, xhi >= 0.0f ? Ylo : Yhi);
-    const float th_lo = rm_atan2f(xlo, xlo >= 0.0f ? Yhi : Ylo);
+    const float th_hi = la_atan(xhi * (xhi >= 0.0f ? iYlo : iYhi));
+    const float th_lo = la_atan(xlo * (xlo >= 0.0f ? iYhi : iYlo));
     const float c0 = freq * (tc - et - fabsf(phase)), c1 = freq * (tc + et - fabsf(phase));
     const float dlo = fminf(c0, c1) - fabsf(jit) - th_hi;
     const float dhi = fmaxf(c0, c1) + fabsf(jit) - th_lo;
     if (!(fabsf(dlo) < 1e4f) || !(fabsf(dhi) < 1e4f)) continue;
-    const float h = 0.5f * fabsf(sw) / Ylo + 1e-4f + 1e-6f * fmaxf(fabsf(dlo), fabsf(dhi));
+    const float h = 0.5f * fabsf(sw) * iYlo + 1e-4f + 1e-6f * fmaxf(fabsf(dlo), fabsf(dhi));
     /* no multiple of the slit period within [dlo - h, dhi + h] */
-    const float klo = ceilf((dlo - h) / Tg), khi = floorf((dhi + h) / Tg);
+    const float klo = ceilf((dlo - h) * iTg), khi = floorf((dhi + h) * iTg);
     if (klo > khi) return true;
   }
   return false;
