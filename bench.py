@@ -117,20 +117,26 @@ def kernel_source_sha():
 
 def profile_counters(tune):
     """Per-history DRAM bytes and warp instructions of the fused launch
-    from the recorded ncu capture, when it was made from these kernel
-    sources with this launch configuration; else None with the reason."""
+    from the recorded ncu captures (one per launch configuration), when one
+    was made from these kernel sources with this launch configuration;
+    else None with the reason."""
     try:
         with open(COUNTERS) as f:
             c = json.load(f)
     except (OSError, ValueError):
         return None, "no recorded capture"
-    if c.get("kernel_source_sha") != kernel_source_sha():
-        return None, "recorded capture is of other kernel sources (%s)" % c.get(
-            "kernel_source_sha")
+    sha = kernel_source_sha()
     keys = ("split", "walk", "privatize", "block", "cull")
-    if any(int((tune or {}).get(k, 0)) != int(c.get("tune", {}).get(k, 0)) for k in keys):
-        return None, "recorded capture is of another launch configuration"
-    return c, None
+    why = None
+    for cap in c.get("captures", [c]):
+        if cap.get("kernel_source_sha") != sha:
+            why = "recorded capture is of other kernel sources (%s)" % cap.get("kernel_source_sha")
+            continue
+        if any(int((tune or {}).get(k, 0)) != int(cap.get("tune", {}).get(k, 0)) for k in keys):
+            why = why or "recorded capture is of another launch configuration"
+            continue
+        return cap, None
+    return None, why or "no recorded capture"
 
 
 def kernels_per_trace(tune):

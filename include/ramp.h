@@ -468,6 +468,19 @@ int ramp_debug_atomic_peak(float* bins, int64_t n_bins, int64_t n_threads, int32
 int ramp_bvh_walk_counts(const float* pts, int64_t n_tri, const float* rays, int64_t n_rays,
                          int64_t* out);
 
+/* Bytes of the survivor buffer that a split fused launch (RampTune.split,
+ * walk, cull) of n histories uses: 72 per history, rounded up to work
+ * items of 128 histories, plus 4 per work item.                           */
+int64_t ramp_survivor_bytes(int64_t n);
+
+/* Let the plan's split launches keep their survivors in caller-owned
+ * device memory (buf, 16-byte aligned, `bytes` long) instead of a buffer
+ * the plan allocates; a launch that needs more than `bytes` uses the
+ * plan's own.  buf NULL goes back to plan-owned buffers.  The memory must
+ * stay valid while launches that use it run (a caching allocator keeps a
+ * multi-gigabyte buffer from being allocated again for every new plan). */
+int ramp_plan_set_survivors(RampPlan* p, void* buf, int64_t bytes);
+
 /* Host helper (no GPU): the length of the chopper look-ahead run that
  * starts at component k (RampTune.cull), 0 when there is none.  The run:
  * components of the linear block holding k, each unrotated, centred on the

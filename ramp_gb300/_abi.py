@@ -176,6 +176,8 @@ _SIGS = {
                                 ctypes.c_void_p], ctypes.c_int),
     "ramp_bvh_walk_counts": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                               ctypes.c_void_p], ctypes.c_int),
+    "ramp_survivor_bytes": ([ctypes.c_int64], ctypes.c_int64),
+    "ramp_plan_set_survivors": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
     "ramp_chopper_run": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                           ctypes.c_int], ctypes.c_int),
     "ramp_debug_chopper_cull": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,

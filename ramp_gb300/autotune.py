@@ -28,7 +28,9 @@ import torch
 
 from . import _abi
 
-CANDIDATES = [dict(blocks_per_sm=b, chunk=c) for b in (3, 4) for c in (0, 4096)]
+# the default register cap (4 CTAs per SM) first: near-ties keep the earlier candidate
+CANDIDATES = [dict(blocks_per_sm=b, chunk=c) for b in (4, 3) for c in (0, 4096)]
+TIE = 0.01        # candidates within 1 % of the fastest count as tied
 
 
 def cache_path():
@@ -190,7 +192,7 @@ def _time_config(lib, plan, n, rng, cfg, stream, reps=2):
     return best
 
 
-def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False):
+def tune(inst, n_probe=40_000_000, rng="reference", candidates=None, force=False):
     """Best fused launch configuration for ``inst`` (a dict for
     Instrument.execute(tune=...)); measured once per GPU and instrument
     structure, then read from the cache."""
@@ -229,9 +231,12 @@ def tune(inst, n_probe=10_000_000, rng="reference", candidates=None, force=False
         for t, s in zip(inst.tallies(), saved):
             t.copy_(s)
         inst._check_status(lib, plan)
+    fastest = min(ms for ms, _ in results)
+    # the first candidate (in the order above) within TIE of the fastest:
+    # short probes cannot tell near-ties apart
+    best_ms, best = next((ms, c) for ms, c in results if ms <= fastest * (1.0 + TIE))
     results.sort(key=lambda x: x[0])
-    best = results[0][1]
-    cache[key] = {"config": best, "ms": results[0][0], "n_probe": n_probe, "split_candidate": split,
+    cache[key] = {"config": best, "ms": best_ms, "n_probe": n_probe, "split_candidate": split,
                   "all": [[ms, c] for ms, c in results]}
     _save(cache)
     _MEMO[key] = dict(best)

@@ -101,6 +101,9 @@ struct RampPlan {
   CompDev* priv_dev = nullptr;       /* descriptors of a private-tally launch */
   uint32_t* surv = nullptr;          /* survivor buffer of split launches */
   int64_t surv_cap = 0;              /* slots (128 per work item) */
+  bool surv_owned = false;           /* surv was allocated by the plan */
+  uint32_t* surv_ext = nullptr;      /* caller's buffer (ramp_plan_set_survivors) */
+  int64_t surv_ext_bytes = 0;
   StreamSet streams;
   bool plain_only = false;           /* a component writes per-index output */
   bool ext = false;                  /* an extended kind: MISIS, SMonochromator, SPowder1 */
@@ -455,7 +458,7 @@ int ramp_plan_destroy(RampPlan* p) {
   for (void* a : p->allocs) cudaFree(a);
   if (p->batch.comps_dev) cudaFree(p->batch.comps_dev);
   if (p->batch.vars_dev) cudaFree(p->batch.vars_dev);
-  if (p->surv) cudaFree(p->surv);
+  if (p->surv && p->surv_owned) cudaFree(p->surv);
   if (p->adj_list) cudaFree(p->adj_list);
   if (p->batch.counters) cudaFree(p->batch.counters);
   if (p->streams.ready) {
@@ -756,16 +759,31 @@ static int priv_descriptors(RampPlan* p, cudaStream_t s, int32_t* floats) {
   return RAMP_OK;
 }
 
-/* survivor buffer for split launches covering up to n_items work items
- * of 128 neutrons: SURV_WORDS words per slot plus one count per item
- * (grows, never shrinks) */
+/* bytes of the survivor buffer for n_items work items of 128 neutrons:
+ * SURV_WORDS words per slot plus one count per item */
+static size_t surv_bytes(int64_t n_items) {
+  return ((size_t)n_items * 128 * SURV_WORDS + (size_t)n_items) * sizeof(uint32_t);
+}
+
+/* survivor buffer for split launches covering up to n_items work items:
+ * the caller's (ramp_plan_set_survivors) when it is large enough, else one
+ * of the plan's own (grows, never shrinks) */
 static int ensure_surv(RampPlan* p, int64_t n_items) {
   const int64_t slots = n_items * 128;
-  if (slots <= p->surv_cap) return RAMP_OK;
-  if (p->surv) { cudaFree(p->surv); p->surv = nullptr; p->surv_cap = 0; }
+  if (p->surv_ext && surv_bytes(n_items) <= (size_t)p->surv_ext_bytes) {
+    if (p->surv && p->surv_owned) cudaFree(p->surv);
+    p->surv = p->surv_ext;
+    p->surv_cap = slots;
+    p->surv_owned = false;
+    return RAMP_OK;
+  }
+  if (p->surv && p->surv_owned && slots <= p->surv_cap) return RAMP_OK;
+  if (p->surv && p->surv_owned) cudaFree(p->surv);
+  p->surv = nullptr;
+  p->surv_cap = 0;
+  p->surv_owned = false;
   void* d = nullptr;
-  const size_t bytes = ((size_t)slots * SURV_WORDS + (size_t)n_items) * sizeof(uint32_t);
-  cudaError_t e = cudaMalloc(&d, bytes);
+  cudaError_t e = cudaMalloc(&d, surv_bytes(n_items));
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_err("survivor buffer for %lld histories: %s", (long long)slots, cudaGetErrorString(e));
@@ -773,6 +791,7 @@ static int ensure_surv(RampPlan* p, int64_t n_items) {
   }
   p->surv = (uint32_t*)d;
   p->surv_cap = slots;
+  p->surv_owned = true;
   return RAMP_OK;
 }
 
@@ -874,6 +893,21 @@ int ramp_plan_set_buffer(RampPlan* p, int32_t comp, float* buf, int64_t len) {
 int ramp_plan_reserve(RampPlan* p, int64_t n) {
   if (!p || n < 0) { set_err("ramp_plan_reserve: bad arguments"); return RAMP_E_INVALID; }
   return ensure_surv(p, (n + 127) / 128);
+}
+
+int64_t ramp_survivor_bytes(int64_t n) {
+  return n > 0 ? (int64_t)surv_bytes((n + 127) / 128) : 0;
+}
+
+int ramp_plan_set_survivors(RampPlan* p, void* buf, int64_t bytes) {
+  if (!p || bytes < 0 || (buf && ((uintptr_t)buf & 15))) {
+    set_err("ramp_plan_set_survivors: a 16-byte aligned device buffer and its size");
+    return RAMP_E_INVALID;
+  }
+  if (p->surv && !p->surv_owned) { p->surv = nullptr; p->surv_cap = 0; }
+  p->surv_ext = buf ? (uint32_t*)buf : nullptr;
+  p->surv_ext_bytes = buf ? bytes : 0;
+  return RAMP_OK;
 }
 
 /* span size for n histories: about eight spans per resident CTA, in

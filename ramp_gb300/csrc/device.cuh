@@ -374,11 +374,22 @@ DI float cont_weight(const SrcDev& s, float E_val, int32_t num_sim, D* dx) {
   return M / (float)num_sim;
 }
 
+/* the weight of a flat or MCont history of energy E_val (flat_mod.cl:26,
+ * cont_mod.cl:39-47) */
+template <class D = NoDiff>
+DI float source_weight(const SrcDev& s, float E_val, int32_t num_sim, D* dx = nullptr) {
+  return (s.kind == RAMP_SRC_CONT) ? cont_weight<D>(s, E_val, num_sim, dx)
+                                   : 1.0f / (float)num_sim;
+}
+
 /* generate_neutrons — flat_mod.cl:4-50, cont_mod.cl:11-72, isis_mod.cl:15-104.
  * EXT = false compiles the kernel without the extended kinds (the MISIS
  * source here, the TAS components in scatter): a smaller whole-chain
- * kernel for chains that do not use them. */
-template <class D = NoDiff, bool EXT = true>
+ * kernel for chains that do not use them.  WEIGHT = false (flat and MCont
+ * sources only) leaves the energy in n.p for source_weight to turn into the
+ * weight later, with the same operations: a kernel that may retire the
+ * history first skips the weight for those it retires. */
+template <class D = NoDiff, bool EXT = true, bool WEIGHT = true>
 DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t seed, Rng& r,
                  D* dx = nullptr) {
   n.x = n.y = n.z = n.vx = n.vy = n.vz = n.px = n.py = n.pz = 0.0f;
@@ -393,8 +404,7 @@ DI void generate(const SrcDev& s, Nt& n, float old_sb, int32_t num_sim, int32_t 
     const float E_min = s.p[5], E_max = s.p[6];
     float E_range = (E_max - E_min);
     E_val = E_min + E_range * draw(n, r);
-    n.p = (s.kind == RAMP_SRC_CONT) ? cont_weight<D>(s, E_val, num_sim, dx)
-                                    : 1.0f / (float)num_sim;
+    n.p = WEIGHT ? source_weight<D>(s, E_val, num_sim, dx) : E_val;
   }
   n.x = s.p[0] * (0.5f - draw(n, r));
   n.y = s.p[1] * (0.5f - draw(n, r));

@@ -19,6 +19,7 @@
   PH(MB, MODE, false, 0, 2) PH(MB, MODE, false, 1, 2) PH(MB, MODE, false, 2, 2)             \
   PH(MB, MODE, true, 0, 2) PH(MB, MODE, true, 1, 2) PH(MB, MODE, true, 2, 2)                \
   PH(MB, MODE, false, 4, 2) PH(MB, MODE, true, 4, 2)                                        \
+  PH(MB, MODE, false, 3, 0) PH(MB, MODE, true, 3, 0)                                        \
   extern template int occ_mm<MB, MODE>(int);
 ONE_MODE(3, 0)
 ONE_MODE(3, 1)
@@ -27,7 +28,9 @@ ONE_MODE(4, 1)
 
 /* one register cap, keying mode, layout and kind set: the whole chain, or
  * stage A then stage B of a split launch (the batched one-launch layout
- * runs the extended kinds whole; the mesh walk runs with the mesh kind set) */
+ * runs the extended kinds whole; the mesh walk runs with the mesh kind set;
+ * a split before component 0 of a core-kind chain, which only the chopper
+ * look-ahead makes, has a stage A of its own without the component code) */
 template <int MB, int MODE, bool BATCHED, int KS>
 static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream_t s) {
   if constexpr (KS == 2) {
@@ -39,7 +42,11 @@ static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream
   }
   if constexpr (!(BATCHED && KS == 1)) {
     if (a.split > 0 || a.cull > 0) {
-      const cudaError_t e = launch_phase<MB, MODE, BATCHED, 1, KS>(a, block, grid, s);
+      cudaError_t e;
+      if (KS == 0 && a.split == 0)     /* the moderator alone: the lean stage A */
+        e = launch_phase<MB, MODE, BATCHED, 3, 0>(a, block, grid, s);
+      else
+        e = launch_phase<MB, MODE, BATCHED, 1, KS>(a, block, grid, s);
       if (e != cudaSuccess) return e;
       return launch_phase<MB, MODE, BATCHED, 2, KS>(a, block, grid, s);
     }

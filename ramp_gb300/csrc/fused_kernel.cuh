@@ -42,7 +42,9 @@
  * PHASE 0: the whole chain per neutron.  PHASE 1: stage A of a split
  * launch — the moderator and components [0, split); the survivors of work
  * item t are stored at slots [128 t, 128 t + cnt[t]) of the survivor
- * buffer (no atomics) and finish in PHASE 2.  The bounds of both loops are kernel parameters, so the loop
+ * buffer (no atomics) and finish in PHASE 2.  PHASE 3: stage A of a launch
+ * split before component 0 (the moderator and the chopper look-ahead),
+ * compiled without the component code.  The bounds of both loops are kernel parameters, so the loop
  * counters and descriptor addresses stay warp-uniform.
  */
 template <int MINB, int MODE, bool BATCHED, int PHASE, int KS>
@@ -328,7 +330,8 @@ k_fused(const FusedArgs a) {
   } else {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    const int KE = PHASE == 1 ? a.split : a.n_comps;
+    constexpr bool STAGE_A = PHASE == 1 || PHASE == 3;
+    const int KE = PHASE == 3 ? 0 : (PHASE == 1 ? a.split : a.n_comps);
     const int var = BATCHED ? (int)blockIdx.y : a.var_key;
     const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
     /* batched: CTAs past what this row's variant can use leave at once */
@@ -355,7 +358,7 @@ k_fused(const FusedArgs a) {
       const bool zx = !carry;
       int kept = 0;      /* PHASE 1: survivors of this item so far (warp-uniform) */
       /* PHASE 1 keeps the whole warp in the loop for the ballot */
-      const int jend = PHASE == 1 ? (int)((count + 31) & ~31ll) : (int)count;
+      const int jend = STAGE_A ? (int)((count + 31) & ~31ll) : (int)count;
       for (int j = lane; j < jend; j += 32) {
         const bool live = j < count;
         const int64_t i = start + j;
@@ -366,26 +369,36 @@ k_fused(const FusedArgs a) {
           rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
           const float old_sb = carry ? a.carry_sb[i] : 0.0f;
           ii = carry ? a.carry_iidx[i] : 0u;
-          generate<TallyOnly, EXT>(V->src, n, old_sb, num_sim, seed, r);
-          if (zx && n.p == 0.0f) n.die = 1.0f;
-          for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
-            const RampBlock B = a.blocks[b];
-            if (PHASE == 1 && B.first >= KE) break;
-            if (B.linear) {
-              const int e = (PHASE == 1 && B.first + B.count > KE) ? KE : B.first + B.count;
-              for (int k = B.first; k < e; ++k) {
-                if (n.die > 0.f) break;
-                comp_linear<TallyOnly, EXT, MESH>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr, zx);
+          /* the lean stage A (core kinds: flat or MCont source) weighs a
+             history only once the look-ahead has kept it */
+          generate<TallyOnly, EXT, PHASE != 3>(V->src, n, old_sb, num_sim, seed, r);
+          if (PHASE != 3 && zx && n.p == 0.0f) n.die = 1.0f;
+          if constexpr (PHASE != 3) {
+            for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
+              const RampBlock B = a.blocks[b];
+              if (PHASE == 1 && B.first >= KE) break;
+              if (B.linear) {
+                const int e = (PHASE == 1 && B.first + B.count > KE) ? KE : B.first + B.count;
+                for (int k = B.first; k < e; ++k) {
+                  if (n.die > 0.f) break;
+                  comp_linear<TallyOnly, EXT, MESH>(comps[k], n, ii, r, a.st, (TallyOnly*)nullptr,
+                                                    zx);
+                }
+              } else {
+                block_nonlinear<TallyOnly, EXT, MESH>(comps, B.first, B.count, B.multi, n, ii, r,
+                                                      a.st);
               }
-            } else {
-              block_nonlinear<TallyOnly, EXT, MESH>(comps, B.first, B.count, B.multi, n, ii, r, a.st);
             }
           }
           /* the chopper look-ahead: a neutron that certainly cannot pass
              the choppers after the split adds nothing to any tally */
-          if (PHASE == 1 && zx && a.cull > 0 && !(n.die > 0.f) &&
+          if (STAGE_A && zx && a.cull > 0 && !(n.die > 0.f) &&
               chopper_run_blocks(comps, KE, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t))
             n.die = 1.0f;
+          if (PHASE == 3 && !(n.die > 0.f)) {
+            n.p = source_weight<TallyOnly>(V->src, n.p, num_sim);
+            if (zx && n.p == 0.0f) n.die = 1.0f;
+          }
         }
         if (PHASE == 0) {
           if (carry) { a.carry_sb[i] = n.sb; a.carry_iidx[i] = ii; }
@@ -414,7 +427,7 @@ k_fused(const FusedArgs a) {
         w[14 * cap] = __float_as_uint(n.se);
         w[15 * cap] = ii; w[16 * cap] = (uint32_t)i; w[17 * cap] = (uint32_t)var;
       }
-      if (PHASE == 1 && lane == 0 && item0 + (int64_t)t < a.surv_items)
+      if (STAGE_A && lane == 0 && item0 + (int64_t)t < a.surv_items)
         a.surv_cnt[item0 + t] = (uint32_t)kept;
     }
     if (priv) {                   /* merge the private tallies, nonzero bins only */

@@ -132,7 +132,7 @@ def capture(inst, N, path="fused", rng="reference", run_seed=0, tune=None, chunk
         rngd.seed_dev = seed_buf.data_ptr()
         if path == "fused" and tune and any(int(tune.get(k, 0)) > 0
                                             for k in ("split", "walk", "cull")):
-            _abi.check(lib, lib.ramp_plan_reserve(plan, first), "ramp_plan_reserve")
+            keep.append(inst._survivors(lib, plan, first))   # allocated before the capture
         stream = inst.queue if inst.queue is not None else torch.cuda.Stream(dev)
         torch.cuda.synchronize(dev)
         g = torch.cuda.CUDAGraph()

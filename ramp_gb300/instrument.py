@@ -198,6 +198,25 @@ class Instrument:
         s = self.queue if self.queue is not None else torch.cuda.current_stream(self.device)
         return _abi.ctypes.c_void_p(s.cuda_stream)
 
+    def _survivors(self, lib, plan, n):
+        """The survivor buffer of split fused launches of up to n histories
+        (RampTune split, walk, cull): device memory from PyTorch's caching
+        allocator, allocated on this instrument's stream and handed to the
+        plan (ramp_plan_set_survivors), so that a new Instrument reuses the
+        memory of an earlier one instead of allocating gigabytes again."""
+        need = int(lib.ramp_survivor_bytes(int(n)))
+        buf = getattr(self, "_surv_buf", None)
+        if buf is None or buf.numel() < need:
+            if self.queue is not None:
+                with torch.cuda.stream(self.queue):
+                    buf = torch.empty(need, dtype=torch.uint8, device=self.device)
+            else:
+                buf = torch.empty(need, dtype=torch.uint8, device=self.device)
+            _abi.check(lib, lib.ramp_plan_set_survivors(plan, _abi.ctypes.c_void_p(buf.data_ptr()),
+                                                        buf.numel()), "ramp_plan_set_survivors")
+            self._surv_buf = buf       # the previous buffer, if any, is released after the swap
+        return self._surv_buf
+
     def _alloc_state(self, n):
         stride = (n + 31) // 32 * 32
         self.state = torch.zeros((_abi.NLANES, stride), dtype=torch.float32, device=self.device)
@@ -263,6 +282,8 @@ class Instrument:
                 st = self._alloc_state(first)
             elif path == "fused":
                 carry = None
+                if tune and any(int(tune.get(k, 0)) > 0 for k in ("split", "walk", "cull")):
+                    self._survivors(lib, plan, first)
                 if N > buf_max:
                     # per index: final RNG counter (float) and index buffer (uint32)
                     carry = torch.zeros((2, first), dtype=torch.float32, device=self.device)

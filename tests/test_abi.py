@@ -14,7 +14,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 
 def declared():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^int\s+(ramp_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:int|int64_t)\s+(ramp_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")

@@ -436,13 +436,17 @@ def _chi2_two_sample(h1, e1, h2, e2, min_count=0.0):
     return stat, dof, float(chi2.sf(stat, dof))
 
 
-@pytest.mark.parametrize("fn,kw,N,shape,min_count", [
+@pytest.mark.parametrize("fn,kw,N,shape,min_count,tune", [
     # 500 x 500 (2theta x TOF) detector rebinned to 50 x 50: both axes kept
-    ("small_chain.json", "small", 10_000_000, (50, 10, 50, 10), 5.0),
+    ("small_chain.json", "small", 10_000_000, (50, 10, 50, 10), 5.0, None),
     # the LET-like detector at its full 50-us TOF resolution (the axis the
     # five choppers shape) and 2.5-degree angle bins
-    ("let_like.json", "let", 200_000_000, (72, 10, 1000, 1), 3.0)])
-def test_fused_agrees_with_oracle_on_independent_streams(cuda_lib, fn, kw, N, shape, min_count):
+    ("let_like.json", "let", 200_000_000, (72, 10, 1000, 1), 3.0, None),
+    # the same with the chopper look-ahead (one chunk per call: it stands
+    # aside when RNG counters are carried between chunks)
+    ("let_like.json", "let", 200_000_000, (72, 10, 1000, 1), 3.0, {"split": 0, "cull": 1})])
+def test_fused_agrees_with_oracle_on_independent_streams(cuda_lib, fn, kw, N, shape, min_count,
+                                                         tune):
     """Different chunk seeds (independent random streams): the fused GPU
     histogram and the oracle's pass a two-sample chi-square test, p > 0.01,
     on a two-dimensional (angle x time-of-flight) rebinning of the
@@ -451,7 +455,11 @@ def test_fused_agrees_with_oracle_on_independent_streams(cuda_lib, fn, kw, N, sh
     gi = m.Instrument(I.path(fn), "cuda", **kws)
     chunk = 10_000_000             # the same chunk weights 1/N_chunk on both sides
     random.seed(101)
-    gi.execute(N, path="fused", chunk=chunk)
+    if tune is None:
+        gi.execute(N, path="fused", chunk=chunk)
+    else:
+        for _ in range(N // chunk):
+            gi.execute(chunk, path="fused", tune=tune)
     torch.cuda.synchronize()
     ci = m.Instrument(I.path(fn), "cpu", **kws)
     random.seed(202)
