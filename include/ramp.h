@@ -218,8 +218,10 @@ typedef struct RampTune {
                                    component (0: off; not inside a
                                    non-linear block).  Stage A appends the
                                    neutrons alive there to a survivor
-                                   buffer in HBM (about 72 B per history of the
-                                   launch, owned by the plan) and stage B
+                                   buffer in HBM (96 B per history of the
+                                   launch, owned by the plan unless the
+                                   caller sets one with
+                                   ramp_plan_set_survivors) and stage B
                                    traces them 32 to a warp.  Ignored by
                                    ramp_trace_batched_noalloc.           */
   int32_t streams;              /* ramp_trace_batched: 0 or 1 = one
@@ -469,8 +471,9 @@ int ramp_bvh_walk_counts(const float* pts, int64_t n_tri, const float* rays, int
                          int64_t* out);
 
 /* Bytes of the survivor buffer that a split fused launch (RampTune.split,
- * walk, cull) of n histories uses: 72 per history, rounded up to work
- * items of 128 histories, plus 4 per work item.                           */
+ * walk, cull) of n histories uses: 96 per history (a 72-byte record and,
+ * after a mesh walk, its 24-byte result), rounded up to work items of 128
+ * histories, plus 4 per work item.                                        */
 int64_t ramp_survivor_bytes(int64_t n);
 
 /* Let the plan's split launches keep their survivors in caller-owned

@@ -24,13 +24,15 @@ CU_SOURCES = ["plain.cu", "fused.cu", "adjoint.cu", "abi.cu"]
 # batched one-launch layout, phase, kind set); kind sets: 0 core kinds, 1
 # everything (extended kinds and the mesh), 2 core kinds and the mesh.  The
 # batched layout runs the extended kinds whole (phase 0 only); phase 4
-# (stage B walking a mesh per lane) exists for kind set 2, phase 3 (stage A
+# (stage B walking a mesh per lane) and phase 5 (finishing the walked
+# survivors) exist for kind set 2, phase 3 (stage A
 # of a split before component 0: the moderator and the chopper look-ahead)
 # for kind set 0
 FUSED_INSTANCES = ([(mb, mode, b, ph, ks) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)
                     for ks in (0, 1, 2) for ph in (0, 1, 2) if not (b and ks == 1 and ph)]
                    + [(mb, mode, b, 4, 2) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)]
-                   + [(mb, mode, b, 3, 0) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)])
+                   + [(mb, mode, b, 3, 0) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)]
+                   + [(mb, mode, b, 5, 2) for mb in (3, 4) for mode in (0, 1) for b in (0, 1)])
 CPP_SOURCES = ["bvh.cpp"]
 HEADERS = ["device.cuh", "fused_kernel.cuh", "mesh.cuh", "lookahead.h", "plan.h", "launch.h", "rmath.h",
            "rconst.h", "bvh.h",

@@ -760,9 +760,10 @@ static int priv_descriptors(RampPlan* p, cudaStream_t s, int32_t* floats) {
 }
 
 /* bytes of the survivor buffer for n_items work items of 128 neutrons:
- * SURV_WORDS words per slot plus one count per item */
+ * SURV_WORDS_WALK words per slot (the record and, after a mesh walk, its
+ * result) plus one count per item */
 static size_t surv_bytes(int64_t n_items) {
-  return ((size_t)n_items * 128 * SURV_WORDS + (size_t)n_items) * sizeof(uint32_t);
+  return ((size_t)n_items * 128 * SURV_WORDS_WALK + (size_t)n_items) * sizeof(uint32_t);
 }
 
 /* survivor buffer for split launches covering up to n_items work items:
@@ -801,7 +802,7 @@ static int attach_surv(RampPlan* p, FusedArgs& a, int64_t n_items, cudaStream_t 
   if (rc) return rc;
   a.surv = p->surv;
   a.surv_cap = p->surv_cap;
-  a.surv_cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS;
+  a.surv_cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS_WALK;
   a.surv_items = n_items;
   CK(cudaMemsetAsync(a.surv_cnt, 0, (size_t)n_items * sizeof(uint32_t), s));
   return RAMP_OK;
@@ -963,6 +964,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.st = p->status;
   a.workq = &p->status->workq;
   a.workq_b = &p->status->workq_b;
+  a.workq_c = &p->status->workq_c;
   int rc = tune_stage(p, tune, p->ext, &a.split, &a.walk, &a.cull);
   if (!rc && tune && tune->privatize > 0 && a.split == 0 && !a.walk && !a.cull) {
     rc = priv_descriptors(p, s, &a.priv_floats);
@@ -974,7 +976,8 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
     rc = attach_surv(p, a, (n + 127) / 128, s);
     if (rc) return rc;
   }
-  CK(cudaMemsetAsync(&p->status->workq, 0, 3 * sizeof(unsigned long long), s));
+  /* workq, surv, workq_b and workq_c */
+  CK(cudaMemsetAsync(&p->status->workq, 0, 4 * sizeof(unsigned long long), s));
   CK(launch_fused(a, block, fused_grid(a.n_tasks, grid), s));
   return RAMP_OK;
 }
@@ -991,12 +994,12 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
                            int32_t walk, int32_t cull, cudaStream_t s) {
   BatchCache& B = p->batch;
   const size_t nv = vars.size();
-  if (B.counters_cap < 2 * nv) {             /* stage A and stage B queues */
+  if (B.counters_cap < 3 * nv) {   /* stage A, stage B and walk-finishing queues */
     if (B.counters) cudaFree(B.counters);
     B.counters = nullptr;
     B.counters_cap = 0;
-    CK(cudaMalloc(&B.counters, 2 * nv * sizeof(unsigned long long)));
-    B.counters_cap = 2 * nv;
+    CK(cudaMalloc(&B.counters, 3 * nv * sizeof(unsigned long long)));
+    B.counters_cap = 3 * nv;
   }
   /* split launches: each variant gets its own region of the survivor
      buffer (its items' slots, SoA, and its items' counts) */
@@ -1008,7 +1011,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
   if ((split > 0 || walk || cull) && item_off[nv] > 0) {
     rc0 = ensure_surv(p, item_off[nv]);
     if (rc0) return rc0;
-    cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS;
+    cnt = p->surv + (size_t)p->surv_cap * SURV_WORDS_WALK;
     CK(cudaMemsetAsync(cnt, 0, (size_t)item_off[nv] * sizeof(uint32_t), s));
   }
   StreamSet& S = p->streams;
@@ -1022,7 +1025,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
   }
   const int ns = (tune && tune->streams > 1 && tune->streams < RAMP_BATCH_STREAMS)
                      ? tune->streams : RAMP_BATCH_STREAMS;
-  CK(cudaMemsetAsync(B.counters, 0, 2 * nv * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(B.counters, 0, 3 * nv * sizeof(unsigned long long), s));
   CK(cudaEventRecord(S.fork, s));
   for (int k = 0; k < ns; ++k) CK(cudaStreamWaitEvent(S.st[k], S.fork, 0));
   std::vector<int> order(nv);
@@ -1039,6 +1042,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
     a.var_key = v;
     a.workq = B.counters + v;
     a.workq_b = B.counters + nv + v;
+    a.workq_c = B.counters + 2 * nv + v;
     a.task_size = auto_task(vars[v].n, grid, 0);
     a.n_tasks = (vars[v].n + a.task_size - 1) / a.task_size;
     if (cnt) {
@@ -1046,7 +1050,7 @@ static int batched_streams(RampPlan* p, FusedArgs base, const std::vector<Varian
       a.split = split;
       a.walk = walk;
       a.cull = cull;
-      a.surv = p->surv + (size_t)item_off[v] * 128 * SURV_WORDS;
+      a.surv = p->surv + (size_t)item_off[v] * 128 * SURV_WORDS_WALK;
       a.surv_cap = items * 128;
       a.surv_cnt = cnt + item_off[v];
       a.surv_items = items;
@@ -1175,12 +1179,12 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
                   cudaMemcpyHostToDevice));
     B.vars_host = vars;
   }
-  if (B.counters_cap < 2 * (size_t)n_variants) {
+  if (B.counters_cap < 3 * (size_t)n_variants) {
     if (B.counters) cudaFree(B.counters);
     B.counters = nullptr;
     B.counters_cap = 0;
-    CK(cudaMalloc(&B.counters, 2 * (size_t)n_variants * sizeof(unsigned long long)));
-    B.counters_cap = 2 * (size_t)n_variants;
+    CK(cudaMalloc(&B.counters, 3 * (size_t)n_variants * sizeof(unsigned long long)));
+    B.counters_cap = 3 * (size_t)n_variants;
   }
   FusedArgs a;
   memset(&a, 0, sizeof(a));
@@ -1196,6 +1200,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.st = p->status;
   a.workq = B.counters;
   a.workq_b = B.counters + n_variants;
+  a.workq_c = B.counters + 2 * n_variants;
   a.split = split;
   a.walk = walk;
   a.cull = cull;
@@ -1204,7 +1209,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     rc = attach_surv(p, a, items, s);
     if (rc) return rc;
   }
-  CK(cudaMemsetAsync(B.counters, 0, 2 * (size_t)n_variants * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(B.counters, 0, 3 * (size_t)n_variants * sizeof(unsigned long long), s));
   CK(launch_fused(a, block, batched_grid(n_max, grid), s));
   return RAMP_OK;
 }

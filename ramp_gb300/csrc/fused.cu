@@ -19,6 +19,7 @@
   PH(MB, MODE, false, 0, 2) PH(MB, MODE, false, 1, 2) PH(MB, MODE, false, 2, 2)             \
   PH(MB, MODE, true, 0, 2) PH(MB, MODE, true, 1, 2) PH(MB, MODE, true, 2, 2)                \
   PH(MB, MODE, false, 4, 2) PH(MB, MODE, true, 4, 2)                                        \
+  PH(MB, MODE, false, 5, 2) PH(MB, MODE, true, 5, 2)                                        \
   PH(MB, MODE, false, 3, 0) PH(MB, MODE, true, 3, 0)                                        \
   extern template int occ_mm<MB, MODE>(int);
 ONE_MODE(3, 0)
@@ -34,10 +35,12 @@ ONE_MODE(4, 1)
 template <int MB, int MODE, bool BATCHED, int KS>
 static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream_t s) {
   if constexpr (KS == 2) {
-    if (a.walk) {
-      const cudaError_t e = launch_phase<MB, MODE, BATCHED, 1, 2>(a, block, grid, s);
+    if (a.walk) {      /* stage A, the walk, then the rest of the chain */
+      cudaError_t e = launch_phase<MB, MODE, BATCHED, 1, 2>(a, block, grid, s);
       if (e != cudaSuccess) return e;
-      return launch_phase<MB, MODE, BATCHED, 4, 2>(a, block, grid, s);
+      e = launch_phase<MB, MODE, BATCHED, 4, 2>(a, block, grid, s);
+      if (e != cudaSuccess) return e;
+      return launch_phase<MB, MODE, BATCHED, 5, 2>(a, block, grid, s);
     }
   }
   if constexpr (!(BATCHED && KS == 1)) {
@@ -77,7 +80,8 @@ cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s
     return cudaErrorInvalidValue;
   if (a.cull > 0 && (a.walk || a.split + a.cull > a.n_comps || (a.variants && a.ext == 1)))
     return cudaErrorInvalidValue;
-  if (a.walk && (a.ext != 2 || a.split >= a.n_comps || !a.surv)) return cudaErrorInvalidValue;
+  if (a.walk && (a.ext != 2 || a.split >= a.n_comps || !a.surv || !a.workq_c))
+    return cudaErrorInvalidValue;
   /* register cap: 3 or 4 CTAs of 256 threads per SM (at 2 the kernel is
      never faster on GB300) */
   if (a.minb != 3)

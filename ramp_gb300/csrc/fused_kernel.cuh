@@ -59,6 +59,25 @@ k_fused(const FusedArgs a);
  * exactly where stage A left it. */
 #define SURV_GROUP 32   /* one work item per lane */
 
+template <int MODE, int KS>
+DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, int64_t slot,
+                 const MeshRec& w, int k, bool zx, bool carry);
+
+/* the result of a finished mesh walk (k = 0: the walk ended, -1: the stack
+ * overflowed, -2: the ray missed the mesh box), kept beside the survivor's
+ * record for PHASE 5 */
+DI void walk_store(const FusedArgs& a, int64_t slot, const MeshRec& r, int k) {
+  uint32_t* wp = a.surv + slot;
+  const int64_t cap = a.surv_cap;
+  const unsigned long long cb = (unsigned long long)__double_as_longlong(r.chord);
+  wp[18 * cap] = __float_as_uint(r.o3);
+  wp[19 * cap] = __float_as_uint(r.o7);
+  wp[20 * cap] = (uint32_t)cb;
+  wp[21 * cap] = (uint32_t)(cb >> 32);
+  wp[22 * cap] = r.num_intersections;
+  wp[23 * cap] = (uint32_t)k;
+}
+
 /* the item of the current group that holds survivor q: the last item whose
  * first survivor (excl, one item per lane, non-decreasing over the lanes)
  * is at or before q, by binary search over the lanes; *base is that first
@@ -72,7 +91,7 @@ DI int surv_item(int excl, int q, int* base) {
   *base = __shfl_sync(FULL_MASK, excl, lo);
   return lo;
 }
-template <int MODE, bool BATCHED, int KS>
+template <int MODE, bool BATCHED, int KS, bool FINISH = false>
 DI void fused_tail(const FusedArgs& a) {
   constexpr bool EXT = KS == 1, MESH = KS != 0;
   const int lane = threadIdx.x & 31;
@@ -90,7 +109,7 @@ DI void fused_tail(const FusedArgs& a) {
     return;
   }
   const CompDev* __restrict__ comps = V->comps;
-  unsigned long long* const q_b = a.workq_b + (BATCHED ? var : 0);
+  unsigned long long* const q_b = (FINISH ? a.workq_c : a.workq_b) + (BATCHED ? var : 0);
   for (;;) {
     unsigned long long g = 0;
     if (lane == 0) g = atomicAdd(q_b, 1ull);
@@ -112,6 +131,16 @@ DI void fused_tail(const FusedArgs& a) {
       if (q >= total) continue;
       const int64_t s = (item0 + t0 + item) * FUSED_WARP_TASK + (q - base);
       const uint32_t* w = a.surv + s;
+      if constexpr (FINISH) {   /* PHASE 5: the rest of the chain after a mesh walk */
+        MeshRec rec;
+        rec.o3 = __uint_as_float(w[18 * cap]);
+        rec.o7 = __uint_as_float(w[19 * cap]);
+        rec.chord = __longlong_as_double(
+            (long long)(((unsigned long long)w[21 * cap] << 32) | (unsigned long long)w[20 * cap]));
+        rec.num_intersections = w[22 * cap];
+        walk_end<MODE, KS>(a, comps, K, s, rec, (int)w[23 * cap], zx, carry);
+        continue;
+      }
       Nt n;
       n.x = __uint_as_float(w[0 * cap]);   n.y = __uint_as_float(w[1 * cap]);
       n.z = __uint_as_float(w[2 * cap]);   n.vx = __uint_as_float(w[3 * cap]);
@@ -203,18 +232,19 @@ DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, i
  * box has none), so with one ray per lane a warp runs at a few lanes.  Here
  * each lane walks its ray one node visit or one triangle per pass (the warp
  * runs the kind more of its lanes wait for), and a lane whose walk is over
- * finishes that neutron (the rest of component K and the components after
- * it, together with the other lanes done since the last refill) and takes
- * the next waiting survivor; the warp claims the next group of work items as
- * soon as every survivor of the current one is taken.  Every neutron goes
- * through the same operations as in PHASE 2 (the records and the chord do
- * not depend on the order in which triangles are visited). */
+ * stores its result beside the survivor's record and takes the next waiting
+ * survivor; the warp claims the next group of work items as soon as every
+ * survivor of the current one is taken.  PHASE 5 then finishes every
+ * survivor 32 to a warp (the rest of component K and the components after
+ * it): kept out of the walk's loop, that code would otherwise make the loop
+ * spill (1.5 KB of spill stores per thread at 64 registers; none without
+ * it).  Every neutron goes through the same operations as in PHASE 2 (the
+ * records and the chord do not depend on the order in which triangles are
+ * visited). */
 template <int MODE, bool BATCHED, int KS>
 DI void fused_tail_walk(const FusedArgs& a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const bool carry = (a.carry_sb != nullptr);
-  const bool zx = !carry;
   const int K = a.split;
   const int64_t cap = a.surv_cap;
   const int var = BATCHED ? (int)blockIdx.y : a.var_key;
@@ -235,18 +265,9 @@ DI void fused_tail_walk(const FusedArgs& a) {
   /* this lane's walk: only the ray and the walk state stay live while it
      runs; the neutron is read back from its survivor record when it ends */
   bool walking = false;
-  bool done = false;     /* the walk is over; the neutron finishes with the others */
-  int kres = 0;
   int64_t slot = 0;
   MeshWalk w;
   for (;;) {
-    /* the lanes whose walks ended since the last refill finish their
-       neutrons together (the rest of component K and the components after
-       it), not one at a time inside the walk loop */
-    if (done) {
-      walk_end<MODE, KS>(a, comps, K, slot, mesh_rec(w), kres, zx, carry);
-      done = false;
-    }
     /* hand the waiting survivors to the idle lanes (a lane whose ray misses
        the mesh box finishes it at once and is idle again) */
     for (;;) {
@@ -287,11 +308,11 @@ DI void fused_tail_walk(const FusedArgs& a) {
         ray.vy = __uint_as_float(wp[4 * cap]); ray.vz = __uint_as_float(wp[5 * cap]);
         transform<false>(cK, ray);        /* comp_linear of component K */
         if (mesh_begin(cK, ray, w)) walking = true;
-        else walk_end<MODE, KS>(a, comps, K, slot, mesh_rec(w), -2, zx, carry);
+        else walk_store(a, slot, mesh_rec(w), -2);
       }
     }
     const bool more = groups_left || handed < total;   /* survivors still waiting */
-    if (!more && !__any_sync(FULL_MASK, walking || done)) break;
+    if (!more && !__any_sync(FULL_MASK, walking)) break;
     /* walk until a quarter of the lanes are idle (or, with nothing left
        to hand out, until every walk is over).  Each pass runs one kind of
        work, the kind more lanes wait for: a triangle of each lane's pending
@@ -308,8 +329,7 @@ DI void fused_tail_walk(const FusedArgs& a) {
       }
       if (walking && (!ok || mesh_walk_over(w))) {
         walking = false;
-        done = true;
-        kres = ok ? 0 : -1;
+        walk_store(a, slot, mesh_rec(w), ok ? 0 : -1);
       }
       const int idle = __popc(__ballot_sync(FULL_MASK, !walking));
       if (idle == 32 || (more && idle >= 8)) break;
@@ -321,8 +341,8 @@ template <int MINB, int MODE, bool BATCHED, int PHASE, int KS>
 __global__ void __launch_bounds__(256, MINB)
 k_fused(const FusedArgs a) {
   constexpr bool EXT = KS == 1, MESH = KS != 0;
-  if constexpr (PHASE == 2) {
-    fused_tail<MODE, BATCHED, KS>(a);
+  if constexpr (PHASE == 2 || PHASE == 5) {
+    fused_tail<MODE, BATCHED, KS, PHASE == 5>(a);
     return;
   } else if constexpr (PHASE == 4) {
     fused_tail_walk<MODE, BATCHED, KS>(a);

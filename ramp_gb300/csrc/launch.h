@@ -48,6 +48,8 @@ struct FusedArgs {
   unsigned long long* workq;    /* work-queue counter of this launch (batched:
                                    one per variant) */
   unsigned long long* workq_b;  /* stage-B work-queue counter(s) (split) */
+  unsigned long long* workq_c;  /* the walk's finishing stage: work-queue
+                                   counter(s) of PHASE 5 */
   int32_t var_key;              /* single variant: its index in the RNG key */
   int32_t minb;                 /* register cap: the build for 3 or 4 CTAs per SM */
   int32_t walk;                 /* split before the GMesh component `split` (may
@@ -67,6 +69,9 @@ struct FusedArgs {
 };
 #define RAMP_PRIV_FLOATS 12288  /* shared memory for private tallies: 48 KB per CTA */
 #define SURV_WORDS 18           /* 15 record lanes (die is 0), iidx, index, variant */
+#define SURV_WORDS_WALK 24      /* and, after a mesh walk, its result: t of the
+                                   two records, the chord (a double, two words),
+                                   the crossing count and how the walk ended */
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s);
 int fused_max_blocks_per_sm(int block, int minb);

@@ -32,29 +32,36 @@
 
 #define RAMP_BVH_STACK 64
 
-struct Shear { int kx, ky, kz; float Sx, Sy, Sz; };
+/* the ray's shear: axis indices kx | ky << 2 | kz << 4 in one word (fewer
+ * live registers in the walk), and the three shear factors */
+struct Shear { int k; float Sx, Sy, Sz; };
+DI int shear_kx(const Shear& S) { return S.k & 3; }
+DI int shear_ky(const Shear& S) { return (S.k >> 2) & 3; }
+DI int shear_kz(const Shear& S) { return S.k >> 4; }
 
 DI float comp3(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 
 DI Shear make_shear(V3 d) {
   float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   Shear S;
-  S.kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
-  S.kx = (S.kz + 1) % 3; S.ky = (S.kx + 1) % 3;
-  if (comp3(d, S.kz) < 0.0f) { int t = S.kx; S.kx = S.ky; S.ky = t; }
-  S.Sx = comp3(d, S.kx) / comp3(d, S.kz);
-  S.Sy = comp3(d, S.ky) / comp3(d, S.kz);
-  S.Sz = 1.0f / comp3(d, S.kz);
+  const int kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+  int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+  if (comp3(d, kz) < 0.0f) { int t = kx; kx = ky; ky = t; }
+  S.k = kx | (ky << 2) | (kz << 4);
+  S.Sx = comp3(d, kx) / comp3(d, kz);
+  S.Sy = comp3(d, ky) / comp3(d, kz);
+  S.Sz = 1.0f / comp3(d, kz);
   return S;
 }
 
 /* watertight crossing parameter t, NaN when the ray misses the face */
 DI float watertight_t(const Shear& S, V3 org, V3 v0, V3 v1, V3 v2) {
   V3 A = sub(v0, org), B = sub(v1, org), C = sub(v2, org);
-  float Akz = comp3(A, S.kz), Bkz = comp3(B, S.kz), Ckz = comp3(C, S.kz);
-  float Ax = comp3(A, S.kx) - S.Sx * Akz, Ay = comp3(A, S.ky) - S.Sy * Akz;
-  float Bx = comp3(B, S.kx) - S.Sx * Bkz, By = comp3(B, S.ky) - S.Sy * Bkz;
-  float Cx = comp3(C, S.kx) - S.Sx * Ckz, Cy = comp3(C, S.ky) - S.Sy * Ckz;
+  const int kx = shear_kx(S), ky = shear_ky(S), kz = shear_kz(S);
+  float Akz = comp3(A, kz), Bkz = comp3(B, kz), Ckz = comp3(C, kz);
+  float Ax = comp3(A, kx) - S.Sx * Akz, Ay = comp3(A, ky) - S.Sy * Akz;
+  float Bx = comp3(B, kx) - S.Sx * Bkz, By = comp3(B, ky) - S.Sy * Bkz;
+  float Cx = comp3(C, kx) - S.Sx * Ckz, Cy = comp3(C, ky) - S.Sy * Ckz;
   float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
   if (U == 0.0f || V == 0.0f || W == 0.0f) {
     U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
@@ -77,6 +84,11 @@ DI float watertight_t(const Shear& S, V3 org, V3 v0, V3 v1, V3 v2) {
  * range [tb, te) (the triangles of sibling leaves are adjacent, so one range
  * covers both); mesh_tri tests one triangle of that range.  Such a walk is
  * over when the range is empty and no node is left (mesh_walk_over). */
+/* per component: the walk needs every crossing (interior parity or a
+ * chord) / accumulates SAttenuate's chord */
+DI bool mesh_all(const CompDev& c) { return (c.gi[0] == 1) || (c.scat == RAMP_S_ATTENUATE); }
+DI bool mesh_chord(const CompDev& c) { return c.scat == RAMP_S_ATTENUATE; }
+
 struct MeshWalk {
   V3 pos, vel;
   float ix, iy, iz;
@@ -84,7 +96,6 @@ struct MeshWalk {
   double chord;
   uint32_t num_intersections;
   int sp, node, tb, te;
-  bool need_all, want_chord;
   Shear S;
   int stack[RAMP_BVH_STACK];
 };
@@ -111,12 +122,10 @@ DI bool mesh_begin(const CompDev& c, const Nt& n, MeshWalk& w) {
   if (tmax < 0.0f || tmin > tmax) return false;
   w.pos = pos;
   w.vel = vel;
-  w.need_all = (c.gi[0] == 1) || (c.scat == RAMP_S_ATTENUATE);
   w.num_intersections = 0;
   w.o3 = 1e8f;
   w.o7 = 1e8f;
-  w.want_chord = (c.scat == RAMP_S_ATTENUATE);
-  if (w.want_chord) w.S = make_shear(vel);
+  if (mesh_chord(c)) w.S = make_shear(vel);
   w.chord = 0.0;
   w.ix = 1.0f / vel.x; w.iy = 1.0f / vel.y; w.iz = 1.0f / vel.z;
   w.sp = 0;
@@ -134,7 +143,7 @@ DI void mesh_tri(const CompDev& c, MeshWalk& w, int k) {
   float4 q0 = __ldg(tris + 3 * k), q1 = __ldg(tris + 3 * k + 1), q2 = __ldg(tris + 3 * k + 2);
   V3 v0 = v3(q0.x, q0.y, q0.z), v1 = v3(q1.x, q1.y, q1.z), v2 = v3(q2.x, q2.y, q2.z);
   V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
-  if (w.want_chord) {
+  if (mesh_chord(c)) {
     float tw = watertight_t(w.S, pos, v0, v1, v2);
     if (tw > eps) {
       float nvw = dot(cross(e1, e2), vel);
@@ -165,6 +174,7 @@ DI void mesh_tri(const CompDev& c, MeshWalk& w, int k) {
 struct MeshKids { int r0, c0, r1, c1; float tn0, tn1; bool h0, h1; };
 
 DI MeshKids mesh_kids(const CompDev& c, const MeshWalk& w) {
+  const bool all = mesh_all(c);
   const V3 pos = w.pos;
   const float ix = w.ix, iy = w.iy, iz = w.iz;
   const float4* q = c.bvh_nodes + 4 * w.node;
@@ -180,7 +190,7 @@ DI MeshKids mesh_kids(const CompDev& c, const MeshWalk& w) {
     float tz0 = (a0.z - pos.z) * iz, tz1 = (b0.z - pos.z) * iz;
     K.tn0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
     float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-    K.h0 = !(K.tn0 > tf || tf < -1e-6f) && (w.need_all || !(K.tn0 > fmaxf(w.o3, w.o7)));
+    K.h0 = !(K.tn0 > tf || tf < -1e-6f) && (all || !(K.tn0 > fmaxf(w.o3, w.o7)));
   }
   if (K.c1 >= 0) {
     float tx0 = (a1.x - pos.x) * ix, tx1 = (b1.x - pos.x) * ix;
@@ -188,7 +198,7 @@ DI MeshKids mesh_kids(const CompDev& c, const MeshWalk& w) {
     float tz0 = (a1.z - pos.z) * iz, tz1 = (b1.z - pos.z) * iz;
     K.tn1 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
     float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-    K.h1 = !(K.tn1 > tf || tf < -1e-6f) && (w.need_all || !(K.tn1 > fmaxf(w.o3, w.o7)));
+    K.h1 = !(K.tn1 > tf || tf < -1e-6f) && (all || !(K.tn1 > fmaxf(w.o3, w.o7)));
   }
   return K;
 }

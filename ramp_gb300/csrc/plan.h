@@ -80,7 +80,7 @@ struct StatusDev {
   unsigned long long workq;    /* work-queue head of the persistent kernel */
   unsigned long long surv;     /* survivors appended by a split launch's stage A */
   unsigned long long workq_b;  /* work-queue head of its stage B */
-  unsigned long long pad2;
+  unsigned long long workq_c;  /* the mesh walk's finishing stage (PHASE 5) */
 };
 
 #define RAMP_MAX_COMPS 64
