@@ -29,6 +29,13 @@
 #include "lookahead.h"
 
 #define FUSED_MAX_BLOCKS 32
+/* the mesh walk (PHASE 4) holds only the ray and the walk state: it is
+ * compiled for more resident CTAs per SM than the other phases (40
+ * registers at 6 CTAs of 256 threads, against 64 at 4), and its
+ * single-instrument grid fills that occupancy */
+#ifndef WALK_MINB
+#define WALK_MINB 6
+#endif
 #define FUSED_WARP_TASK 128   /* neutrons a warp claims at once */
 #define FULL_MASK 0xffffffffu
 
@@ -48,7 +55,7 @@
  * counters and descriptor addresses stay warp-uniform.
  */
 template <int MINB, int MODE, bool BATCHED, int PHASE, int KS>
-__global__ void __launch_bounds__(256, MINB)
+__global__ void __launch_bounds__(256, PHASE == 4 ? WALK_MINB : MINB)
 k_fused(const FusedArgs a);
 
 /* PHASE 2: the survivors of stage A through components [split, end).
@@ -338,7 +345,7 @@ DI void fused_tail_walk(const FusedArgs& a) {
 }
 
 template <int MINB, int MODE, bool BATCHED, int PHASE, int KS>
-__global__ void __launch_bounds__(256, MINB)
+__global__ void __launch_bounds__(256, PHASE == 4 ? WALK_MINB : MINB)
 k_fused(const FusedArgs a) {
   constexpr bool EXT = KS == 1, MESH = KS != 0;
   if constexpr (PHASE == 2 || PHASE == 5) {
@@ -477,6 +484,22 @@ k_fused(const FusedArgs a) {
  * sequencing of phases lives in fused.cu */
 template <int MINB, int MODE, bool BATCHED, int PHASE, int KS>
 cudaError_t launch_phase(const FusedArgs& a, int block, int grid, cudaStream_t s) {
+  if constexpr (PHASE == 4 && !BATCHED) {   /* the walk's own occupancy: CTAs x SMs */
+    static int cached[2] = {0, 0};         /* 256- and 128-thread CTAs */
+    int& nb = cached[block == 128 ? 1 : 0];
+    if (nb == 0) {
+      int dev = 0, sms = 0, per_sm = 0;
+      if (cudaGetDevice(&dev) == cudaSuccess &&
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused<MINB, MODE, false, 4, KS>,
+                                                        block, 0) == cudaSuccess &&
+          per_sm > 0)
+        nb = sms * per_sm;
+      else
+        nb = -1;
+    }
+    if (nb > grid) grid = nb;
+  }
   const dim3 g((unsigned)grid, BATCHED ? (unsigned)a.n_variants : 1u);
   size_t smem = 0;
   if (PHASE == 0 && !BATCHED && a.priv_floats > 0)
