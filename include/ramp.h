@@ -248,8 +248,9 @@ typedef struct RampTune {
                                    runs the moderator alone) and let
                                    stage A also retire every neutron that
                                    certainly cannot pass the disk
-                                   choppers of the run of on-axis
-                                   components starting there
+                                   choppers (or misses a guide) of the
+                                   run of on-axis straight guides and
+                                   choppers starting there
                                    (ramp_chopper_run); only tallies are
                                    observable, and those neutrons would
                                    add nothing to them.  RAMP_E_INVALID
@@ -487,12 +488,13 @@ int ramp_plan_set_survivors(RampPlan* p, void* buf, int64_t bytes);
 /* Host helper (no GPU): the length of the chopper look-ahead run that
  * starts at component k (RampTune.cull), 0 when there is none.  The run:
  * components of the linear block holding k, each unrotated, centred on the
- * z axis (pos x = y = 0), with a z-normal GPlane and restore_neutron 0:
- * at most one straight SGuide (w1 = w2, h1 = h2) first, then at least one
- * SChopper, at non-decreasing z, the first at or after the guide's exit.
- * From a neutron's state before such a run, the time and place it meets
- * each chopper plane follow within tight bounds (vz does not change along
- * it; the guide folds the transverse motion at its walls).              */
+ * z axis (pos x = y = 0), with a z-normal GPlane and restore_neutron 0,
+ * non-overlapping at non-decreasing z: straight SGuides (w1 = w2, h1 = h2)
+ * and SChoppers in any order, up to the last chopper before the first
+ * component that is neither.  From a neutron's state before such a run,
+ * the time and place it meets each component's plane follow within tight
+ * bounds (vz does not change along it; the guides fold the transverse
+ * motion at their walls).                                                 */
 int ramp_chopper_run(const RampComp* comps, int n_comps, const RampBlock* blocks, int n_blocks,
                      int k);
 

@@ -146,9 +146,9 @@ def split_point(inst, alive, threshold=0.5):
 
 
 def chopper_run_start(inst):
-    """First component at which a run of on-axis choppers (after at most
-    one straight guide) starts, for the chopper look-ahead
-    (RampTune.cull; ramp_chopper_run), or None."""
+    """First component at which a run of on-axis straight guides and disk
+    choppers starts, for the chopper look-ahead (RampTune.cull;
+    ramp_chopper_run), or None."""
     keep = []
     _, carr, nc, barr, nb = inst.descriptors(keep)
     lib = _abi.load()

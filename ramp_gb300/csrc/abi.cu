@@ -640,8 +640,9 @@ static bool on_axis_plane(const RampComp& c) {
          std::isfinite(c.pos[2]);
 }
 
-/* length of the run of on-axis components at k: at most one straight
- * guide, then choppers (0: no chopper follows) */
+/* length of the run of on-axis components at k: straight guides and disk
+ * choppers in any order, non-overlapping at non-decreasing z, up to the
+ * last chopper before the first component that is neither (0: no chopper) */
 static int chopper_run(const RampComp* comps, int nc, const RampBlock* blocks, int nb, int k) {
   if (!comps || !blocks || k < 0 || k >= nc) return 0;
   int end = -1;
@@ -649,29 +650,29 @@ static int chopper_run(const RampComp* comps, int nc, const RampBlock* blocks, i
     if (blocks[b].linear && blocks[b].first <= k && k < blocks[b].first + blocks[b].count)
       end = std::min(blocks[b].first + blocks[b].count, nc);
   if (end < 0) return 0;
-  int j = k;
   float zmin = -INFINITY;
-  const RampComp& g = comps[j];
-  if (g.scat == RAMP_S_GUIDE) {
-    if (!on_axis_plane(g) || !(g.sp[0] == g.sp[2]) || !(g.sp[1] == g.sp[3]) ||
-        !(g.sp[0] > 0.0f) || !(g.sp[1] > 0.0f) || !(g.sp[4] > 0.0f) || !std::isfinite(g.sp[4]))
-      return 0;
-    zmin = g.pos[2] + g.sp[4];
-    ++j;
-  }
-  int nch = 0;
-  for (; j < end; ++j) {
+  int last = -1;
+  for (int j = k; j < end; ++j) {
     const RampComp& c = comps[j];
-    if (c.scat != RAMP_S_CHOPPER || !on_axis_plane(c) || !(c.sp[1] > 0.0f) ||
-        (uint32_t)c.si[0] == 0u || !(c.pos[2] >= zmin))
+    if (!on_axis_plane(c) || !(c.pos[2] >= zmin)) break;
+    if (c.scat == RAMP_S_GUIDE) {
+      if (!(c.sp[0] == c.sp[2]) || !(c.sp[1] == c.sp[3]) || !(c.sp[0] > 0.0f) ||
+          !(c.sp[1] > 0.0f) || !(c.sp[4] > 0.0f) || !std::isfinite(c.sp[4]) ||
+          !std::isfinite(c.sp[0]) || !std::isfinite(c.sp[1]) || !(c.gp[0] > 0.0f) ||
+          !(c.gp[1] > 0.0f))
+        break;
+      zmin = c.pos[2] + c.sp[4];
+    } else if (c.scat == RAMP_S_CHOPPER) {
+      bool finite = true;
+      for (int q = 0; q < 5; ++q) finite = finite && std::isfinite(c.sp[q]);
+      if (!finite || !(c.sp[1] > 0.0f) || (uint32_t)c.si[0] == 0u) break;
+      zmin = c.pos[2];
+      last = j;
+    } else {
       break;
-    bool finite = true;
-    for (int q = 0; q < 5; ++q) finite = finite && std::isfinite(c.sp[q]);
-    if (!finite) break;
-    zmin = c.pos[2];
-    ++nch;
+    }
   }
-  return nch > 0 ? j - k : 0;
+  return last >= 0 ? last - k + 1 : 0;
 }
 
 /* the launch's stage split: RampTune.cull (split before component
@@ -697,7 +698,7 @@ static int tune_stage(const RampPlan* p, const RampTune* tune, bool ext, int32_t
     for (int v = 0; v < n_vars && nl > 0; ++v)
       nl = std::min(nl, chopper_run(vars[v].comps, nc, p->blocks.data(), (int)p->blocks.size(), k));
     if (nl == 0) {
-      set_err("RampTune.cull: no run of on-axis choppers (after at most one straight guide) "
+      set_err("RampTune.cull: no run of on-axis straight guides and choppers "
               "starts at component %d", k);
       return RAMP_E_INVALID;
     }
@@ -1471,6 +1472,7 @@ int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock*
     memset(&q, 0, sizeof(q));
     q.geom = comps[j].geom; q.scat = comps[j].scat;
     memcpy(q.pos, comps[j].pos, sizeof(q.pos));
+    memcpy(q.gp, comps[j].gp, sizeof(q.gp));
     memcpy(q.sp, comps[j].sp, sizeof(q.sp));
     memcpy(q.si, comps[j].si, sizeof(q.si));
     if (comps[j].scat == RAMP_S_CHOPPER && (uint32_t)comps[j].si[0] != 0u)

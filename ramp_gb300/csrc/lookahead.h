@@ -1,17 +1,18 @@
 /*
  * lookahead.h — the chopper look-ahead of split fused launches
  * (RampTune.cull).  From a neutron's state before a run of on-axis
- * components (at most one straight guide, then disk choppers) it bounds
- * when and where the neutron meets each chopper's plane and tells whether
- * some chopper certainly stops it.  Compiled for the device (the end of
- * stage A) and for the host (ramp_debug_chopper_cull, with which the
- * bound is checked against the CPU restatement of the reference kernels).
+ * components (straight guides and disk choppers) it bounds when and where
+ * the neutron meets each component's plane, and tells whether some chopper
+ * certainly stops it or it certainly misses a guide's entrance.  Compiled
+ * for the device (the end of stage A) and for the host
+ * (ramp_debug_chopper_cull, with which the bound is checked against the CPU
+ * restatement of the reference kernels).
  *
  * The run (checked by chopper_run in abi.cu): components of one linear
- * block, each unrotated, centred on the z axis (x = y = 0), with a
- * z-normal GPlane and no restore; first at most one SGuide with w1 = w2
- * and h1 = h2, then SChopper components at non-decreasing z, the first at
- * or after the guide's exit.  Why the bounds hold there:
+ * block, each unrotated, centred on the z axis (x = y = 0), with a z-normal
+ * GPlane and no restore, at non-decreasing z without overlaps: straight
+ * SGuides (w1 = w2, h1 = h2) and SChopper components in any order, ending
+ * with a chopper.  Why the bounds hold there:
  *  - time.  Nothing in the run changes vz: the frame transforms are the
  *    identity on velocities; a straight guide's wall normals have no z
  *    component (guide.cl:39-43 with w1 = w2: ww = hh = 0, so the bounce
@@ -22,26 +23,29 @@
  *    motion is the unfolded line u(z) = x_e + (vx / vz)(z - z_e) reflected
  *    at x = +-a (the bounce loop, guide.cl:49-135, reflects at one wall at
  *    a time, x and y independently); after the exit the neutron flies on
- *    from its last bounce along the folded line.  A reflection changes
- *    |vx| by a few ulp (about 5e-7 relative); when the folded exit point
- *    lies within the slack of a wall, the last bounce may fall on either
- *    side of the exit plane, and both signs of vx after the exit are
- *    allowed.
- *  - the chopper (chopper.cl:4-59): the neutron passes only if the
- *    distance from freq (t - |phase|) + e - atan2(x, y + R), e in
- *    [-jitter, jitter), to the nearest multiple of 2 pi / n_slits is at
- *    most atan2(w, y + R) / 2.  atan2(x, Y) is monotone in x and in Y for
- *    Y > 0, so its range over the box of (x, y) is taken at corners, and
+ *    from its last bounce along the folded line to the next component.  A
+ *    reflection changes |vx| by a few ulp (about 5e-7 relative); when the
+ *    folded exit point lies within the slack of a wall, the last bounce may
+ *    fall on either side of the exit plane, and both signs of vx after the
+ *    exit are allowed (a later guide then ends the look-ahead).
+ *  - a guide entrance (plane.cl:3-52): a neutron whose line meets the plane
+ *    outside its rectangle by more than the slack misses it and dies.
+ *  - a chopper (chopper.cl:4-59): the neutron passes only if the distance
+ *    from freq (t - |phase|) + e - atan2(x, y + R), e in [-jitter, jitter),
+ *    to the nearest multiple of 2 pi / n_slits is at most
+ *    atan2(w, y + R) / 2.  atan2(x, Y) is monotone in x and in Y for Y > 0,
+ *    so its range over the box of (x, y) is taken at corners, and
  *    atan2(w, Y) <= w / Y.
  * Every slack is far above the rounding it covers (time: 1e-5 relative
  * plus a micrometre of z per bounce; position: 2e-5 m plus 4e-6 of the
- * guide path per bounce; angle: 1e-4 rad plus 1e-6 relative, which also
- * covers the truncated atan series and products with reciprocals).  A neutron
- * outside the assumptions (vz <= 0, at the guide entrance within the slack
- * of a wall, y + R not clearly positive, angles beyond 1e4 rad) gets no
- * claim.  A neutron that would instead miss a plane, leave the guide at
- * zero weight or exceed its bounce limit dies in the reference as well,
- * so with only tallies observable it may be retired either way.
+ * guide path per bounce so far; angle: 1e-4 rad plus 1e-6 relative, which
+ * also covers the truncated atan series and products with reciprocals).  A
+ * neutron outside the assumptions (vz <= 0, at a guide entrance within the
+ * slack of a wall, y + R not clearly positive, angles beyond 1e4 rad) gets
+ * no claim from there on.  A neutron that would instead miss a plane,
+ * leave a guide at zero weight or exceed its bounce limit dies in the
+ * reference as well, so with only tallies observable it may be retired
+ * either way.
  */
 #ifndef RAMP_LOOKAHEAD_H
 #define RAMP_LOOKAHEAD_H
@@ -85,56 +89,58 @@ LA_FN float la_atan(float r) {
 
 /* true: the neutron at (x, y, z) with velocity (vx, vy, vz) and time t,
  * in the laboratory frame before component k, cannot pass every chopper
- * of the run comps[k .. k + nl).  Divisions are replaced by products with
- * reciprocals where the slack covers their extra rounding; a chopper's
- * aux[0] is its slit period and aux[1] the reciprocal of it. */
+ * of the run comps[k .. k + nl) (or misses a guide entrance of it, which
+ * kills it as well).  Divisions are replaced by products with reciprocals
+ * where the slack covers their extra rounding; a chopper's aux[0] is its
+ * slit period and aux[1] the reciprocal of it. */
 LA_FN bool chopper_run_blocks(const CompDev* comps, int k, int nl, float x, float y, float z,
                               float vx, float vy, float vz, float t) {
   if (!(vz > 0.0f) || nl <= 0) return false;
   const float ivz = 1.0f / vz;
   const float sx = vx * ivz, sy = vy * ivz;
-  /* the reference line after the guide: x(zz) = x0 + mx (zz - z0), with
-     slope uncertainty ux when the sign after the exit is ambiguous */
+  /* the neutron's line: (x0, y0) at z0 with slopes (mx, my); after a guide
+     exit near a wall the sign of a slope is open (mx = 0, ux = |sx|) */
   float x0 = x, y0 = y, z0 = z, mx = sx, my = sy, ux = 0.0f, uy = 0.0f;
   float ex = 2e-5f, ey = 2e-5f;   /* position slack (m) */
-  float nb = 0.0f;                /* bounces, for the time slack */
-  int j = k;
-  if (comps[j].scat == RAMP_S_GUIDE) {
-    const CompDev& g = comps[j];
-    const float zg = g.pos[2], l = g.sp[4];
-    const float a = 0.5f * g.sp[0], b = 0.5f * g.sp[1];
-    const float dz = zg - z;
-    if (!(dz >= 0.0f)) return false;
-    const float xe = x + sx * dz, ye = y + sy * dz;
-    if (!(fabsf(xe) < a - 2e-5f) || !(fabsf(ye) < b - 2e-5f)) return false;
-    const float ia = 1.0f / a, ib = 1.0f / b;
-    const float dux = sx * l, duy = sy * l;
-    const float nbx = floorf(fabsf(dux) * (0.5f * ia)) + 2.0f;
-    const float nby = floorf(fabsf(duy) * (0.5f * ib)) + 2.0f;
-    if (!(nbx < 1e4f) || !(nby < 1e4f)) return false;
-    nb = nbx + nby;
-    ex += 4e-6f * nbx * (fabsf(dux) + a);
-    ey += 4e-6f * nby * (fabsf(duy) + b);
-    float gx, gy;
-    bool ax, ay;
-    x0 = la_fold(xe + dux, a, ia, ex, &gx, &ax);
-    y0 = la_fold(ye + duy, b, ib, ey, &gy, &ay);
-    z0 = zg + l;
-    mx = ax ? 0.0f : gx * sx;
-    ux = ax ? fabsf(sx) : 0.0f;
-    my = ay ? 0.0f : gy * sy;
-    uy = ay ? fabsf(sy) : 0.0f;
-    ++j;
-  }
-  for (; j < k + nl; ++j) {
+  float nb = 0.0f;                /* bounces so far, for the slope and time slack */
+  for (int j = k; j < k + nl; ++j) {
     const CompDev& c = comps[j];
     const float zc = c.pos[2];
-    const float dzc = zc - z0;
-    if (!(dzc >= -1e-6f)) return false;
-    const float xc = x0 + mx * dzc, yc = y0 + my * dzc;
-    /* the slope error of the bounces carries on after the exit */
-    const float exc = ex + (ux + 4e-6f * nb * fabsf(sx)) * fabsf(dzc) + 1e-6f * fabsf(xc);
-    const float eyc = ey + (uy + 4e-6f * nb * fabsf(sy)) * fabsf(dzc) + 1e-6f * fabsf(yc);
+    const float dz = zc - z0;
+    if (!(dz >= -1e-6f)) return false;
+    /* where the line meets this component's plane; the slope error of
+       earlier bounces carries on over dz */
+    const float xc = x0 + mx * dz, yc = y0 + my * dz;
+    const float exc = ex + (ux + 4e-6f * nb * fabsf(sx)) * fabsf(dz) + 1e-6f * fabsf(xc);
+    const float eyc = ey + (uy + 4e-6f * nb * fabsf(sy)) * fabsf(dz) + 1e-6f * fabsf(yc);
+    if (c.scat == RAMP_S_GUIDE) {
+      /* a neutron that certainly misses the entrance plane dies there
+         (plane.cl:3-52: |x| < width/2 and |y| < height/2 to hit it) */
+      if (fabsf(xc) - exc >= 0.5f * c.gp[0] || fabsf(yc) - eyc >= 0.5f * c.gp[1]) return true;
+      /* folding needs known slopes and an entry inside the walls */
+      const float a = 0.5f * c.sp[0], b = 0.5f * c.sp[1], l = c.sp[4];
+      if (ux > 0.0f || uy > 0.0f) return false;
+      if (!(fabsf(xc) < a - exc) || !(fabsf(yc) < b - eyc)) return false;
+      const float ia = 1.0f / a, ib = 1.0f / b;
+      const float dux = mx * l, duy = my * l;
+      const float nbx = floorf(fabsf(dux) * (0.5f * ia)) + 2.0f;
+      const float nby = floorf(fabsf(duy) * (0.5f * ib)) + 2.0f;
+      if (!(nbx < 1e4f) || !(nby < 1e4f)) return false;
+      ex = exc + 4e-6f * (nb + nbx) * (fabsf(dux) + a);
+      ey = eyc + 4e-6f * (nb + nby) * (fabsf(duy) + b);
+      nb += nbx + nby;
+      float gx, gy;
+      bool ax, ay;
+      x0 = la_fold(xc + dux, a, ia, ex, &gx, &ax);
+      y0 = la_fold(yc + duy, b, ib, ey, &gy, &ay);
+      z0 = zc + l;
+      ux = ax ? fabsf(mx) : 0.0f;
+      mx = ax ? 0.0f : gx * mx;
+      uy = ay ? fabsf(my) : 0.0f;
+      my = ay ? 0.0f : gy * my;
+      continue;
+    }
+    /* a disk chopper */
     const float tc = t + (zc - z) * ivz;
     const float et = 1e-5f * fabsf(tc) + (1e-5f * fabsf(zc - z) + 1e-6f * (nb + 10.0f)) * ivz + 1e-9f;
     const float sw = c.sp[0], R = c.sp[1], freq = c.sp[2], phase = c.sp[3], jit = c.sp[4];

@@ -38,6 +38,24 @@ RUN = '''
       "scat_kernel": {"name": "SChopper", "radius": 0.28, "freq": 62.831853, "n_slits": 1,
         "jitter": 7e-07, "slit_width": 0.04, "phase": $8.40 / (437.393*Ei**0.5)$}}'''
 
+RUN2 = '''
+    "guide2": {"position": [0.0, 0.0, 8.45],
+      "geom_kernel": {"name": "GPlane", "width": 0.04, "height": 0.04},
+      "scat_kernel": {"name": "SGuide", "w1": 0.04, "h1": 0.04, "w2": 0.04, "h2": 0.04,
+        "l": 3.3, "R0": 0.99, "Qc": 0.0219, "alpha": 3.0, "m": 2, "W": 0.003}},
+    "chopper3": {"position": [0.0, 0.0, 11.8],
+      "geom_kernel": {"name": "GPlane", "width": 0.6, "height": 0.6},
+      "scat_kernel": {"name": "SChopper", "radius": 0.28, "freq": 942.477796, "n_slits": 2,
+        "jitter": 7e-07, "slit_width": 0.04, "phase": $11.80 / (437.393*Ei**0.5)$}},
+    "guide3": {"position": [0.0, 0.0, 11.85],
+      "geom_kernel": {"name": "GPlane", "width": 0.03, "height": 0.04},
+      "scat_kernel": {"name": "SGuide", "w1": 0.03, "h1": 0.04, "w2": 0.03, "h2": 0.04,
+        "l": 3.8, "R0": 0.99, "Qc": 0.0219, "alpha": 3.0, "m": 2, "W": 0.003}},
+    "chopper4": {"position": [0.0, 0.0, 15.7],
+      "geom_kernel": {"name": "GPlane", "width": 0.6, "height": 0.6},
+      "scat_kernel": {"name": "SChopper", "radius": 0.28, "freq": 942.477796, "n_slits": 6,
+        "jitter": 7e-07, "slit_width": 0.04, "phase": $15.70 / (437.393*Ei**0.5)$}}'''
+
 ARM = '''
     "arm": {"position": [0.0, 0.0, 0.0], "geom_kernel": {"name": "GArm"},
       "scat_kernel": {"name": "SArm"}}'''
@@ -87,6 +105,25 @@ def test_lookahead_never_retires_a_neutron_that_passes(tmp_path, Ei):
     assert cut.sum() >= 0.8 * (~passed).sum()
 
 
+@pytest.mark.parametrize("Ei", [2.0, 3.7])
+def test_lookahead_through_several_guides_never_retires_a_neutron_that_passes(tmp_path, Ei):
+    """The run guide, chopper, chopper, guide, chopper, guide (narrower than
+    the ones before it, so some neutrons miss its entrance), chopper."""
+    N = 400_000
+    kw = dict(Ei=Ei, gw2=0.04, cy=0.0)
+    full = instrument(tmp_path, "run2.json", MOD + "," + RUN + "," + RUN2, **kw)
+    arm = instrument(tmp_path, "arm.json", MOD + "," + ARM, **kw)
+    assert run_length(full, 0) == 7
+    seeds = [77]
+    after_mod = oracle.run(arm, N, seeds=seeds).neutrons
+    traced = oracle.run(full, N, seeds=seeds).neutrons
+    passed = traced[:, 15] == 0.0
+    cut = culled(full, 0, after_mod)
+    assert passed.sum() > 20
+    assert not (cut & passed).any(), "a neutron that passes the run was retired"
+    assert cut.sum() >= 0.9 * (~passed).sum()
+
+
 def test_lookahead_run_detection(tmp_path):
     kw = dict(Ei=3.7, gw2=0.04, cy=0.0)
     full = instrument(tmp_path, "run.json", MOD + "," + RUN, **kw)
@@ -113,4 +150,5 @@ def test_lookahead_run_detection(tmp_path):
 def test_let_like_chain_has_a_run_after_the_moderator():
     from ramp_gb300 import instruments as I
     inst = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
-    assert run_length(inst, 0) == 3
+    assert run_length(inst, 0) == 9       # guide 1 .. chopper 5
+    assert run_length(inst, 3) == 6       # guide 2 .. chopper 5
