@@ -274,6 +274,8 @@ DI void fused_tail_walk(const FusedArgs& a) {
   bool walking = false;
   int64_t slot = 0;
   MeshWalk w;
+  /* this thread's column of the shared-memory part of the walk stack */
+  int* const sstack = reinterpret_cast<int*>(ramp_dyn_smem) + threadIdx.x;
   for (;;) {
     /* hand the waiting survivors to the idle lanes (a lane whose ray misses
        the mesh box finishes it at once and is idle again) */
@@ -332,7 +334,7 @@ DI void fused_tail_walk(const FusedArgs& a) {
       if (__popc(bt) >= __popc(bn)) {
         if (wt) mesh_tri(cK, w, w.tb++);
       } else if (walking && !wt) {
-        ok = mesh_visit(cK, w, a.st);
+        ok = mesh_visit(cK, w, a.st, sstack, (int)blockDim.x);
       }
       if (walking && (!ok || mesh_walk_over(w))) {
         walking = false;
@@ -491,8 +493,9 @@ cudaError_t launch_phase(const FusedArgs& a, int block, int grid, cudaStream_t s
       int dev = 0, sms = 0, per_sm = 0;
       if (cudaGetDevice(&dev) == cudaSuccess &&
           cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused<MINB, MODE, false, 4, KS>,
-                                                        block, 0) == cudaSuccess &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &per_sm, k_fused<MINB, MODE, false, 4, KS>, block,
+              (size_t)RAMP_BVH_SSTACK * block * sizeof(int)) == cudaSuccess &&
           per_sm > 0)
         nb = sms * per_sm;
       else
@@ -504,6 +507,7 @@ cudaError_t launch_phase(const FusedArgs& a, int block, int grid, cudaStream_t s
   size_t smem = 0;
   if (PHASE == 0 && !BATCHED && a.priv_floats > 0)
     smem = (size_t)a.priv_floats * sizeof(float);    /* at most 48 KB: no attribute */
+  if (PHASE == 4) smem = (size_t)RAMP_BVH_SSTACK * block * sizeof(int);   /* 16 KB */
   k_fused<MINB, MODE, BATCHED, PHASE, KS><<<g, block, smem, s>>>(a);
   return cudaGetLastError();
 }

@@ -31,6 +31,9 @@
 #define RAMP_MESH_CUH
 
 #define RAMP_BVH_STACK 64
+/* stack entries a walk kernel keeps per thread in shared memory (the rest
+ * go to the thread's local array) */
+#define RAMP_BVH_SSTACK 16
 
 /* the ray's shear: axis indices kx | ky << 2 | kz << 4 in one word (fewer
  * live registers in the walk), and the three shear factors */
@@ -203,22 +206,38 @@ DI MeshKids mesh_kids(const CompDev& c, const MeshWalk& w) {
   return K;
 }
 
+/* The walk's stack.  With ss set (a walk kernel: this thread's column of
+ * a shared-memory array, entry d at ss[d * bd], bd the threads of the CTA,
+ * so lanes at different depths never share a bank) its first
+ * RAMP_BVH_SSTACK entries live there and the rest in w.stack; without,
+ * all of it is in w.stack. */
+DI void stack_push(MeshWalk& w, int* ss, int bd, int v) {
+  if (ss && w.sp < RAMP_BVH_SSTACK) ss[w.sp * bd] = v;
+  else w.stack[w.sp] = v;
+  ++w.sp;
+}
+DI int stack_pop(MeshWalk& w, int* ss, int bd) {
+  --w.sp;
+  return (ss && w.sp < RAMP_BVH_SSTACK) ? ss[w.sp * bd] : w.stack[w.sp];
+}
+
 /* continue into the nearer hit inner child and keep the other on the stack;
  * with none, take the next node off the stack (-1 when it is empty).
  * false: the stack would overflow (the status flag is raised) */
-DI bool mesh_descend(MeshWalk& w, const MeshKids& K, StatusDev* st) {
+DI bool mesh_descend(MeshWalk& w, const MeshKids& K, StatusDev* st, int* ss = nullptr,
+                     int bd = 0) {
   const bool i0 = K.h0 && K.c0 == 0, i1 = K.h1 && K.c1 == 0;
   if (i0 && i1) {
     if (w.sp + 1 > RAMP_BVH_STACK) { raise_flag(st, RAMP_F_BVH_STACK); return false; }
     const bool first0 = !(K.tn1 < K.tn0);
-    w.stack[w.sp++] = first0 ? K.r1 : K.r0;
+    stack_push(w, ss, bd, first0 ? K.r1 : K.r0);
     w.node = first0 ? K.r0 : K.r1;
   } else if (i0) {
     w.node = K.r0;
   } else if (i1) {
     w.node = K.r1;
   } else {
-    w.node = w.sp > 0 ? w.stack[--w.sp] : -1;
+    w.node = w.sp > 0 ? stack_pop(w, ss, bd) : -1;
   }
   return true;
 }
@@ -239,14 +258,14 @@ DI int mesh_step(const CompDev& c, MeshWalk& w, StatusDev* st) {
 /* one inner node without its triangles: the hit leaf children's triangles
  * become the range [tb, te), to be tested by mesh_tri.  The caller visits
  * only with an empty range and a node left.  false: stack overflow */
-DI bool mesh_visit(const CompDev& c, MeshWalk& w, StatusDev* st) {
+DI bool mesh_visit(const CompDev& c, MeshWalk& w, StatusDev* st, int* ss = nullptr, int bd = 0) {
   const MeshKids K = mesh_kids(c, w);
   const int n0 = (K.h0 && K.c0 > 0) ? K.c0 : 0, n1 = (K.h1 && K.c1 > 0) ? K.c1 : 0;
   /* sibling leaves: the second's triangles follow the first's (r1 = r0 + c0) */
   w.tb = n0 > 0 ? K.r0 : K.r1;
   w.te = n1 > 0 ? K.r1 + n1 : K.r0 + n0;
   if (n0 == 0 && n1 == 0) w.te = w.tb;
-  return mesh_descend(w, K, st);
+  return mesh_descend(w, K, st, ss, bd);
 }
 
 DI bool mesh_walk_over(const MeshWalk& w) { return w.tb >= w.te && w.node < 0; }
