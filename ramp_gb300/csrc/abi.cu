@@ -1317,6 +1317,8 @@ static int adjoint_args(RampPlan* p, const SrcDev& src, int n_params, int64_t n,
   a.grad = grad;
   a.lr = lr;
   a.st = p->status;
+  a.cull = chopper_run(p->comps_in.data(), (int)p->comps.size(), p->blocks.data(),
+                       (int)p->blocks.size(), 0);
   if (p->adj_cap < n) {                  /* n indices and one counter */
     if (p->adj_list) cudaFree(p->adj_list);
     p->adj_list = nullptr;

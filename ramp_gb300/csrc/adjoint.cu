@@ -7,14 +7,18 @@
  * loss detector.  The replay is the checkpoint: a neutron's state at every
  * component boundary is recomputed exactly, nothing per neutron is stored.
  * Only neutrons the loss detector counts carry a term, so a first pass
- * (no tallies, no derivatives) lists their indices and the second replays
- * just those with the derivative context.
+ * (no derivatives) lists their indices and the second replays just those
+ * with the derivative context.  The first pass retires after the moderator
+ * the neutrons that certainly cannot pass the chopper run the chain starts
+ * with (lookahead.h): they add nothing to a tally and are never counted.
  */
 #include "device.cuh"
 #include "launch.h"
+#include "lookahead.h"
 
-/* one neutron through the chain with context D */
-template <class D, int MODE>
+/* one neutron through the chain with context D (CULL: with the chopper
+ * look-ahead after the moderator) */
+template <class D, int MODE, bool CULL = false>
 DI void adj_trace(const AdjointArgs& a, uint32_t i, D& dx) {
   Nt n;
   Rng r;
@@ -23,6 +27,9 @@ DI void adj_trace(const AdjointArgs& a, uint32_t i, D& dx) {
   generate<D>(a.src, n, 0.0f, a.num_sim, a.rng.seed_dev ? *a.rng.seed_dev : a.seed, r, &dx);
   /* a zero-weight neutron contributes dL/dH * p * dlog p = 0: retired */
   if (n.p == 0.0f) n.die = 1.0f;
+  if (CULL && a.cull > 0 && !(n.die > 0.f) &&
+      chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t))
+    n.die = 1.0f;
   for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
     const RampBlock B = a.blocks[b];
     if (B.linear) {
@@ -48,7 +55,7 @@ __global__ void __launch_bounds__(256) k_adjoint_record(const AdjointArgs a) {
     dx.list = a.list;
     dx.count = a.list_count;
     dx.cap = a.list_cap;
-    adj_trace<RecorderT<TALLY>, MODE>(a, (uint32_t)i, dx);
+    adj_trace<RecorderT<TALLY>, MODE, true>(a, (uint32_t)i, dx);
   }
 }
 

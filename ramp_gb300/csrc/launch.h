@@ -92,6 +92,8 @@ struct AdjointArgs {
   uint32_t* list;               /* pass 1 output: indices the loss detector counts */
   unsigned long long* list_count;
   int64_t list_cap;
+  int32_t cull;                 /* pass 1: components of the chopper run at
+                                   component 0 (lookahead.h), 0: none */
 };
 
 cudaError_t launch_adjoint(const AdjointArgs& a, int grid, int passes, cudaStream_t s);
