@@ -100,12 +100,18 @@ def peaks_file():
         return {}
 
 
+# the fused kernels' compile inputs: their translation units, the headers
+# those include, the ABI header and the build recipe (flags, instances)
+FUSED_SOURCES = ["fused_inst.cu", "fused.cu", "fused_kernel.cuh", "device.cuh", "mesh.cuh",
+                 "lookahead.h", "plan.h", "launch.h", "rmath.h", "rconst.h"]
+
+
 def kernel_source_sha():
-    """Hash of the sources and build recipe of libramp_cuda.so."""
+    """Hash of the fused kernels' sources and build recipe (the files the
+    recorded ncu counters depend on)."""
     h = hashlib.sha256()
     csrc = os.path.join(HERE, "ramp_gb300", "csrc")
-    files = sorted(os.path.join(csrc, f) for f in os.listdir(csrc)
-                   if f.endswith((".cu", ".cuh", ".h", ".cpp")))
+    files = [os.path.join(csrc, f) for f in FUSED_SOURCES]
     files += [os.path.join(HERE, "include", "ramp.h"),
               os.path.join(HERE, "ramp_gb300", "build.py")]
     for f in files:

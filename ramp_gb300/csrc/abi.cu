@@ -1319,12 +1319,12 @@ static int adjoint_args(RampPlan* p, const SrcDev& src, int n_params, int64_t n,
   a.st = p->status;
   a.cull = chopper_run(p->comps_in.data(), (int)p->comps.size(), p->blocks.data(),
                        (int)p->blocks.size(), 0);
-  if (p->adj_cap < n) {                  /* n indices and one counter */
+  if (p->adj_cap < n) {   /* two lists of n indices (counted, kept) and two counters */
     if (p->adj_list) cudaFree(p->adj_list);
     p->adj_list = nullptr;
     p->adj_cap = 0;
     void* d = nullptr;
-    if (cudaMalloc(&d, (size_t)n * sizeof(uint32_t) + 2 * sizeof(unsigned long long)) !=
+    if (cudaMalloc(&d, 2 * (size_t)n * sizeof(uint32_t) + 3 * sizeof(unsigned long long)) !=
         cudaSuccess) {
       cudaGetLastError();
       set_err("ramp_adjoint: no room for %lld recorded indices", (long long)n);
@@ -1336,7 +1336,10 @@ static int adjoint_args(RampPlan* p, const SrcDev& src, int n_params, int64_t n,
   }
   a.list = p->adj_list;
   a.list_cap = p->adj_cap;
-  a.list_count = (unsigned long long*)(((uintptr_t)(p->adj_list + p->adj_cap) + 7) & ~(uintptr_t)7);
+  a.keep = p->adj_list + p->adj_cap;
+  a.list_count = (unsigned long long*)(((uintptr_t)(p->adj_list + 2 * p->adj_cap) + 7) &
+                                       ~(uintptr_t)7);
+  a.keep_count = a.list_count + 1;
   int64_t g = (n + 255) / 256;
   int64_t cap = (int64_t)p->sm_count * 8;
   grid = (int)(g < cap ? g : cap);

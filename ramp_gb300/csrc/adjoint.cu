@@ -8,17 +8,19 @@
  * component boundary is recomputed exactly, nothing per neutron is stored.
  * Only neutrons the loss detector counts carry a term, so a first pass
  * (no derivatives) lists their indices and the second replays just those
- * with the derivative context.  The first pass retires after the moderator
- * the neutrons that certainly cannot pass the chopper run the chain starts
- * with (lookahead.h): they add nothing to a tally and are never counted.
+ * with the derivative context.  When the chain starts with a chopper run
+ * (lookahead.h), the first pass is split in two: the moderator and the
+ * look-ahead for every neutron, keeping the indices of those that may pass
+ * (the others add nothing to a tally and are never counted), then the
+ * whole chain for the kept ones, 32 to a warp, each regenerated from its
+ * key (the same operations, so the same neutron).
  */
 #include "device.cuh"
 #include "launch.h"
 #include "lookahead.h"
 
-/* one neutron through the chain with context D (CULL: with the chopper
- * look-ahead after the moderator) */
-template <class D, int MODE, bool CULL = false>
+/* one neutron through the chain with context D */
+template <class D, int MODE>
 DI void adj_trace(const AdjointArgs& a, uint32_t i, D& dx) {
   Nt n;
   Rng r;
@@ -27,9 +29,6 @@ DI void adj_trace(const AdjointArgs& a, uint32_t i, D& dx) {
   generate<D>(a.src, n, 0.0f, a.num_sim, a.rng.seed_dev ? *a.rng.seed_dev : a.seed, r, &dx);
   /* a zero-weight neutron contributes dL/dH * p * dlog p = 0: retired */
   if (n.p == 0.0f) n.die = 1.0f;
-  if (CULL && a.cull > 0 && !(n.die > 0.f) &&
-      chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t))
-    n.die = 1.0f;
   for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
     const RampBlock B = a.blocks[b];
     if (B.linear) {
@@ -43,19 +42,57 @@ DI void adj_trace(const AdjointArgs& a, uint32_t i, D& dx) {
   }
 }
 
-/* pass 1: every neutron, the indices the loss detector counts (with TALLY,
- * also the forward histograms) */
-template <int MODE, bool TALLY>
+/* pass 1: every neutron (KEPT: the neutrons of the kept list), the
+ * indices the loss detector counts (with TALLY, also the forward
+ * histograms) */
+template <int MODE, bool TALLY, bool KEPT>
 __global__ void __launch_bounds__(256) k_adjoint_record(const AdjointArgs a) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  int64_t m = a.n;
+  if (KEPT) {
+    m = (int64_t)*a.keep_count;
+    if (m > a.list_cap) m = a.list_cap;
+  }
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = KEPT ? a.keep[j] : (uint32_t)j;
     RecorderT<TALLY> dx;
-    dx.idx = (uint32_t)i;
+    dx.idx = i;
     dx.done = false;
     dx.list = a.list;
     dx.count = a.list_count;
     dx.cap = a.list_cap;
-    adj_trace<RecorderT<TALLY>, MODE, true>(a, (uint32_t)i, dx);
+    adj_trace<RecorderT<TALLY>, MODE>(a, i, dx);
+  }
+}
+
+/* pass 1, first half: the moderator and the chopper look-ahead for every
+ * neutron; the indices of those it keeps are appended to a.keep (one
+ * atomic per warp) */
+template <int MODE>
+__global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  for (int64_t base = i0; base < a.n; base += stride) {   /* warp-uniform */
+    const int64_t i = base + lane;
+    bool kept = false;
+    if (i < a.n) {
+      Nt n;
+      Rng r;
+      rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+      generate<TallyOnly, true, false>(a.src, n, 0.0f, a.num_sim,
+                                       a.rng.seed_dev ? *a.rng.seed_dev : a.seed, r);
+      kept = !chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, kept);
+    if (m == 0u) continue;
+    unsigned long long at = 0;
+    if (lane == 0) at = atomicAdd(a.keep_count, (unsigned long long)__popc(m));
+    at = __shfl_sync(0xffffffffu, at, 0);
+    if (kept) {
+      const int64_t k = (int64_t)at + __popc(m & ((1u << lane) - 1u));
+      if (k < a.list_cap) a.keep[k] = (uint32_t)i;
+    }
   }
 }
 
@@ -79,12 +116,24 @@ cudaError_t launch_adjoint(const AdjointArgs& a, int grid, int passes, cudaStrea
     cudaError_t e = cudaMemsetAsync(a.list_count, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     const bool t = (passes & 4) != 0;
-    if (a.rng.mode == 0) {
-      if (t) k_adjoint_record<0, true><<<grid, 256, 0, s>>>(a);
-      else k_adjoint_record<0, false><<<grid, 256, 0, s>>>(a);
+    if (a.cull > 0) {          /* keep, then trace the kept neutrons */
+      e = cudaMemsetAsync(a.keep_count, 0, sizeof(unsigned long long), s);
+      if (e != cudaSuccess) return e;
+      if (a.rng.mode == 0) {
+        k_adjoint_keep<0><<<grid, 256, 0, s>>>(a);
+        if (t) k_adjoint_record<0, true, true><<<grid, 256, 0, s>>>(a);
+        else k_adjoint_record<0, false, true><<<grid, 256, 0, s>>>(a);
+      } else {
+        k_adjoint_keep<1><<<grid, 256, 0, s>>>(a);
+        if (t) k_adjoint_record<1, true, true><<<grid, 256, 0, s>>>(a);
+        else k_adjoint_record<1, false, true><<<grid, 256, 0, s>>>(a);
+      }
+    } else if (a.rng.mode == 0) {
+      if (t) k_adjoint_record<0, true, false><<<grid, 256, 0, s>>>(a);
+      else k_adjoint_record<0, false, false><<<grid, 256, 0, s>>>(a);
     } else {
-      if (t) k_adjoint_record<1, true><<<grid, 256, 0, s>>>(a);
-      else k_adjoint_record<1, false><<<grid, 256, 0, s>>>(a);
+      if (t) k_adjoint_record<1, true, false><<<grid, 256, 0, s>>>(a);
+      else k_adjoint_record<1, false, false><<<grid, 256, 0, s>>>(a);
     }
   }
   if (passes & 2) {

@@ -36,6 +36,11 @@
 #ifndef WALK_MINB
 #define WALK_MINB 6
 #endif
+/* the walk hands waiting rays to idle lanes once this many of a warp's 32
+ * lanes are idle (or when none is left walking) */
+#ifndef WALK_REFILL
+#define WALK_REFILL 8
+#endif
 #define FUSED_WARP_TASK 128   /* neutrons a warp claims at once */
 #define FULL_MASK 0xffffffffu
 
@@ -322,7 +327,7 @@ DI void fused_tail_walk(const FusedArgs& a) {
     }
     const bool more = groups_left || handed < total;   /* survivors still waiting */
     if (!more && !__any_sync(FULL_MASK, walking)) break;
-    /* walk until a quarter of the lanes are idle (or, with nothing left
+    /* walk until WALK_REFILL lanes are idle (or, with nothing left
        to hand out, until every walk is over).  Each pass runs one kind of
        work, the kind more lanes wait for: a triangle of each lane's pending
        leaf range, or an inner node of each lane without one */
@@ -341,7 +346,7 @@ DI void fused_tail_walk(const FusedArgs& a) {
         walk_store(a, slot, mesh_rec(w), ok ? 0 : -1);
       }
       const int idle = __popc(__ballot_sync(FULL_MASK, !walking));
-      if (idle == 32 || (more && idle >= 8)) break;
+      if (idle == 32 || (more && idle >= WALK_REFILL)) break;
     }
   }
 }

@@ -94,6 +94,8 @@ struct AdjointArgs {
   int64_t list_cap;
   int32_t cull;                 /* pass 1: components of the chopper run at
                                    component 0 (lookahead.h), 0: none */
+  uint32_t* keep;               /* with cull: the indices the look-ahead keeps */
+  unsigned long long* keep_count;
 };
 
 cudaError_t launch_adjoint(const AdjointArgs& a, int grid, int passes, cudaStream_t s);

@@ -85,3 +85,46 @@ def test_cull_in_a_captured_graph(cuda_lib):
     ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
     oracle.run(ci, N, seeds=seeds)
     tallies_close(gi, ci)
+
+
+def test_caller_survivor_buffer_reuse_and_fallback(cuda_lib):
+    """Split launches keep their survivors in the caller's buffer
+    (ramp_plan_set_survivors) when it is large enough and in one of the
+    plan's own otherwise; Instrument grows its buffer with the trace.  Each
+    run equals the oracle's."""
+    import ctypes
+    from ramp_gb300 import _abi
+    kw = I.let_like_kwargs()
+    tune = {"split": 0, "cull": 1}
+    lib = _abi.load()
+    assert lib.ramp_survivor_bytes(0) == 0
+    assert lib.ramp_survivor_bytes(1) == 128 * 96 + 4
+    # a caller buffer far too small for the trace: the plan uses its own
+    gi = m.Instrument(I.path("let_like.json"), "cuda", **kw)
+    plan = gi.plan()
+    small = torch.empty(4096, dtype=torch.uint8, device="cuda")
+    assert lib.ramp_plan_set_survivors(plan, ctypes.c_void_p(small.data_ptr()), small.numel()) == 0
+    rng = _abi.RampRng(0, 0, 0, 0)
+    t = _abi.tune_struct(tune)
+    s = torch.cuda.current_stream()
+    _abi.check(lib, lib.ramp_trace_fused(plan, 300_000, 300_000, 1234, ctypes.byref(rng), None,
+                                         None, ctypes.byref(t), ctypes.c_void_p(s.cuda_stream)),
+               "ramp_trace_fused")
+    torch.cuda.synchronize()
+    ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
+    oracle.run(ci, 300_000, seeds=[1234])
+    tallies_close(gi, ci)
+    # through Instrument: a buffer sized for the trace, larger for a larger one
+    gi = m.Instrument(I.path("let_like.json"), "cuda", **kw)
+    random.seed(41)
+    gi.execute(300_000, path="fused", tune=tune)
+    first = gi._surv_buf.numel()
+    assert first >= lib.ramp_survivor_bytes(300_000)
+    gi.execute(700_000, path="fused", tune=tune)
+    torch.cuda.synchronize()
+    assert gi._surv_buf.numel() >= lib.ramp_survivor_bytes(700_000) > first
+    ci = m.Instrument(I.path("let_like.json"), "cpu", **kw)
+    random.seed(41)
+    oracle.run(ci, 300_000)
+    oracle.run(ci, 700_000)
+    tallies_close(gi, ci)
