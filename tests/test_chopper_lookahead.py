@@ -152,3 +152,66 @@ def test_let_like_chain_has_a_run_after_the_moderator():
     inst = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
     assert run_length(inst, 0) == 9       # guide 1 .. chopper 5
     assert run_length(inst, 3) == 6       # guide 2 .. chopper 5
+
+
+def _random_run(rng):
+    """IDF text of a random on-axis run behind a flat moderator: guides of
+    random aperture and length and choppers of random frequency (either
+    sign), slit count, slit width, radius, phase and jitter, at random
+    gaps; and the moderator energy range."""
+    z = float(rng.uniform(0.5, 2.0))
+    mod = {"mod_dim": [float(rng.uniform(0.02, 0.12)), float(rng.uniform(0.02, 0.12))],
+           "target_dim": [float(rng.uniform(0.01, 0.06)), float(rng.uniform(0.01, 0.06))],
+           "target_dist": z, "E_min": float(rng.uniform(0.5, 3.0))}
+    mod["E_max"] = mod["E_min"] + float(rng.uniform(0.5, 15.0))
+    parts = ['"mod": {"source": true, "position": [0.0, 0.0, 0.0], "moderator_kernel": '
+             '{"name": "MFlat", "mod_dim": %s, "target_dim": %s, "target_dist": %r, '
+             '"E_min": %r, "E_max": %r}}' % (mod["mod_dim"], mod["target_dim"], z,
+                                             mod["E_min"], mod["E_max"])]
+    # every chopper phased for one design energy, as on an instrument, so
+    # that a fair share of the neutrons passes the whole run
+    v0 = 437.393 * np.sqrt(float(rng.uniform(mod["E_min"], mod["E_max"])))
+    kinds = ["guide"] + list(rng.choice(["guide", "chopper"], size=3)) + ["chopper"]
+    for j, kind in enumerate(kinds):
+        if kind == "guide":
+            w, h = float(rng.uniform(0.01, 0.06)), float(rng.uniform(0.01, 0.06))
+            l = float(rng.uniform(0.5, 8.0))
+            parts.append('"c%d": {"position": [0.0, 0.0, %r], "geom_kernel": {"name": "GPlane", '
+                         '"width": %r, "height": %r}, "scat_kernel": {"name": "SGuide", "w1": %r, '
+                         '"h1": %r, "w2": %r, "h2": %r, "l": %r, "R0": 0.99, "Qc": 0.0219, '
+                         '"alpha": 3.0, "m": 2, "W": 0.003}}' % (j, z, w, h, w, h, w, h, l))
+            z += l + float(rng.uniform(0.0, 0.5))
+        else:
+            parts.append('"c%d": {"position": [0.0, 0.0, %r], "geom_kernel": {"name": "GPlane", '
+                         '"width": 0.6, "height": 0.6}, "scat_kernel": {"name": "SChopper", '
+                         '"radius": %r, "freq": %r, "n_slits": %d, "jitter": %r, '
+                         '"slit_width": %r, "phase": %r}}'
+                         % (j, z, float(rng.uniform(0.1, 0.5)),
+                            float(rng.choice([-1, 1]) * rng.uniform(30.0, 600.0)),
+                            int(rng.integers(1, 7)), float(rng.choice([7e-7, 1e-4, 3e-3])),
+                            float(rng.uniform(0.02, 0.12)),
+                            float(rng.choice([-1, 1]) * z / v0)))
+            z += float(rng.uniform(0.0, 0.8))
+    return ",".join(parts), len(kinds)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_lookahead_sound_on_random_runs(tmp_path, seed):
+    """Random guide and chopper runs (a flat moderator, apertures, lengths,
+    gaps, frequencies of either sign, slit counts and widths, radii, jitter
+    up to 3e-3, all choppers phased for one random design energy): no
+    neutron that passes the whole run in the oracle is retired by the
+    bound."""
+    rng = np.random.default_rng(1000 + seed)
+    body, n = _random_run(rng)
+    full = instrument(tmp_path, "rand.json", body)
+    arm_body = body.split(',"c0"')[0] + "," + ARM
+    arm = instrument(tmp_path, "arm.json", arm_body)
+    assert run_length(full, 0) == n
+    N = 200_000
+    after_mod = oracle.run(arm, N, seeds=[seed]).neutrons
+    traced = oracle.run(full, N, seeds=[seed]).neutrons
+    passed = traced[:, 15] == 0.0
+    cut = culled(full, 0, after_mod)
+    assert passed.sum() > 50
+    assert not (cut & passed).any(), "a neutron that passes the run was retired"
