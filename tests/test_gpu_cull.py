@@ -128,3 +128,25 @@ def test_caller_survivor_buffer_reuse_and_fallback(cuda_lib):
     oracle.run(ci, 300_000)
     oracle.run(ci, 700_000)
     tallies_close(gi, ci)
+
+
+@pytest.mark.parametrize("seed", [3, 6, 11])
+def test_fused_cull_on_random_runs_matches_oracle(cuda_lib, tmp_path, seed):
+    """Random guide and chopper runs (the generator of the CPU soundness
+    test) ending in time-of-flight and x-y monitors: the fused launch with
+    the look-ahead equals the oracle's tallies."""
+    import numpy as np
+    from test_chopper_lookahead import _random_run
+    body, n = _random_run(np.random.default_rng(1000 + seed))
+    body += (',"m_tof": {"position": [0.0, 0.0, 60.0], "geom_kernel": {"name": "GPlane", '
+             '"width": 1.0, "height": 1.0}, "scat_kernel": {"name": "SDetector1D", '
+             '"binning": [0.0, 20.0, 60000.0], "var": "tof", "restore_neutron": true}}'
+             ',"m_xy": {"position": [0.0, 0.0, 60.1], "geom_kernel": {"name": "GPlane", '
+             '"width": 1.0, "height": 1.0}, "scat_kernel": {"name": "SDetector2D", '
+             '"axis1_binning": [-0.2, 0.004, 0.2], "axis2_binning": [-0.2, 0.004, 0.2], '
+             '"axis1_var": "x", "axis2_var": "y"}}')
+    fn = tmp_path / "rand_mon.json"
+    fn.write_text('{"all": {"linear": true,%s}}' % body)
+    gi, ci, r = pair(str(fn), {}, 1_000_000, path="fused", tune={"split": 0, "cull": 1})
+    tallies_close(gi, ci)
+    assert float(sum(t.abs().sum() for t in ci.tallies())) > 0
