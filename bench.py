@@ -24,7 +24,8 @@ by a Threefry-only kernel on this GPU: a lower bound on the issue used.  The DRA
 the instruction count per history come from the ncu capture recorded in
 profiles/ with a hash of the kernel sources; they are reported only when
 that hash equals the sources being run.
-Beside the headline (one GPU, unless --no-extra): the batched scan of 256
+Beside the headline: the same step without the chopper look-ahead
+(fused_without_lookahead), and (one GPU, unless --no-extra) the batched scan of 256
 variants (config 3), gradients of a histogram loss (config 4, grads/s) and
 the mesh imaging workload (config 5, rays/s with an L2 roofline from the
 walk's counted node and triangle reads), the tallies' L2 atomics against a
@@ -780,6 +781,35 @@ def main():
                  "peak_source": "measured (copy bandwidth)" if hbm_peak else None}
 
     extras = {}
+    if world == 1 and int((tune or {}).get("cull", 0)) > 0:
+        # ---- the same step without the chopper look-ahead (split where
+        # fewer than half the histories are alive), to show what it adds ----
+        from ramp_gb300.autotune import split_point
+        nl_tune = {k: v for k, v in tune.items() if k not in ("cull", "split")}
+        nl_tune["split"] = split_point(plain, alive)
+        nl = m.Instrument(fn, dev, **kw)
+        nl_ms = []
+        for w in range(max(1, min(a.warmup, 2))):
+            random.seed(10 + w)
+            nl.execute(n, path="fused", tune=nl_tune)
+        torch.cuda.synchronize()
+        for k in range(max(2, a.steps // 2)):
+            flush.fill_(float(k))
+            s, e = _events()
+            random.seed(1000 + k)
+            s.record()
+            nl.execute(n, path="fused", tune=nl_tune)
+            e.record()
+            e.synchronize()
+            nl_ms.append(s.elapsed_time(e))
+        nl_value = n / (statistics.mean(nl_ms) / 1000.0)
+        extras["fused_without_lookahead"] = {
+            "value": nl_value, "unit": "histories/s", "ms_per_step": statistics.mean(nl_ms),
+            "tune": nl_tune, "fused_over_plain": nl_value / plain_value,
+            "note": "the same fused kernels and step with the chopper look-ahead off: every "
+                    "history is traced through guide 1, survivors compacted before the first "
+                    "component fewer than half of them reach"}
+        del nl
     if not a.no_extra and world == 1:
         # ---- tallies: float atomics into L2 against a measured peak ----
         ap, ap_how = atomic_peak(lib, dev)
