@@ -506,6 +506,16 @@ int ramp_chopper_run(const RampComp* comps, int n_comps, const RampBlock* blocks
 int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock* blocks,
                             int n_blocks, int k, const float* records, int64_t n, uint8_t* out);
 
+/* Host check (no GPU) of the speed-only bound of the lean stage A: a flat
+ * or MCont moderator with parameters source_p (moderator width and
+ * height, target width and height, target distance: RampSource.p[0..4]);
+ * out[i] = 1 when no neutron of speed speeds[i] (m/s) from it can pass the
+ * choppers of the run at component k (the run must start where the
+ * moderator's neutrons enter the chain), else 0.                          */
+int ramp_debug_speed_cull(const RampComp* comps, int n_comps, const RampBlock* blocks,
+                          int n_blocks, int k, const float* source_p, const float* speeds,
+                          int64_t n, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

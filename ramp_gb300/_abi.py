@@ -180,6 +180,9 @@ _SIGS = {
     "ramp_plan_set_survivors": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
     "ramp_chopper_run": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                           ctypes.c_int], ctypes.c_int),
+    "ramp_debug_speed_cull": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                               ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                               ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_chopper_cull": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
                                 ctypes.c_int),

@@ -1490,6 +1490,36 @@ int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock*
   return RAMP_OK;
 }
 
+int ramp_debug_speed_cull(const RampComp* comps, int n_comps, const RampBlock* blocks,
+                          int n_blocks, int k, const float* source_p, const float* speeds,
+                          int64_t n, uint8_t* out) {
+  if (!comps || n_comps <= 0 || !source_p || n < 0 || (n > 0 && (!speeds || !out))) {
+    set_err("ramp_debug_speed_cull: bad arguments");
+    return RAMP_E_INVALID;
+  }
+  const int nl = chopper_run(comps, n_comps, blocks, n_blocks, k);
+  if (nl == 0) {
+    set_err("ramp_debug_speed_cull: no chopper run at component %d", k);
+    return RAMP_E_INVALID;
+  }
+  std::vector<CompDev> d((size_t)n_comps);
+  for (int j = 0; j < n_comps; ++j) {
+    CompDev& q = d[(size_t)j];
+    memset(&q, 0, sizeof(q));
+    q.geom = comps[j].geom; q.scat = comps[j].scat;
+    memcpy(q.pos, comps[j].pos, sizeof(q.pos));
+    memcpy(q.gp, comps[j].gp, sizeof(q.gp));
+    memcpy(q.sp, comps[j].sp, sizeof(q.sp));
+    memcpy(q.si, comps[j].si, sizeof(q.si));
+    if (comps[j].scat == RAMP_S_CHOPPER && (uint32_t)comps[j].si[0] != 0u)
+      chopper_aux(comps[j], q.aux);
+  }
+  for (int64_t i = 0; i < n; ++i)
+    out[i] = speed_run_blocks(d.data(), k, nl, speeds[i], source_p[0], source_p[1], source_p[2],
+                              source_p[3], source_p[4]) ? 1 : 0;
+  return RAMP_OK;
+}
+
 }  // extern "C"
 
 /* ======================================================================

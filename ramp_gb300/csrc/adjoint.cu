@@ -9,11 +9,11 @@
  * Only neutrons the loss detector counts carry a term, so a first pass
  * (no derivatives) lists their indices and the second replays just those
  * with the derivative context.  When the chain starts with a chopper run
- * (lookahead.h), the first pass is split in two: the moderator and the
- * look-ahead for every neutron, keeping the indices of those that may pass
- * (the others add nothing to a tally and are never counted), then the
- * whole chain for the kept ones, 32 to a warp, each regenerated from its
- * key (the same operations, so the same neutron).
+ * (lookahead.h), the first pass is split in two: every neutron's first draw
+ * and the speed look-ahead, keeping the indices of those that may pass (the
+ * others add nothing to a tally and are never counted), then the whole
+ * chain for the kept ones, 32 to a warp, each regenerated from its key (the
+ * same operations, so the same neutron).
  */
 #include "device.cuh"
 #include "launch.h"
@@ -65,9 +65,10 @@ __global__ void __launch_bounds__(256) k_adjoint_record(const AdjointArgs a) {
   }
 }
 
-/* pass 1, first half: the moderator and the chopper look-ahead for every
- * neutron; the indices of those it keeps are appended to a.keep (one
- * atomic per warp) */
+/* pass 1, first half: for every neutron its first draw (the energy, hence
+ * the speed) and the speed look-ahead (speed_run_blocks; with a source
+ * other than flat or MCont the moderator and the full look-ahead); the
+ * indices of those it keeps are appended to a.keep (one atomic per warp) */
 template <int MODE>
 __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
   const int lane = threadIdx.x & 31;
@@ -80,9 +81,17 @@ __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
       Nt n;
       Rng r;
       rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
-      generate<TallyOnly, true, false>(a.src, n, 0.0f, a.num_sim,
-                                       a.rng.seed_dev ? *a.rng.seed_dev : a.seed, r);
-      kept = !chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t);
+      const int32_t seed = a.rng.seed_dev ? *a.rng.seed_dev : a.seed;
+      if (a.src.kind == RAMP_SRC_FLAT || a.src.kind == RAMP_SRC_CONT) {
+        n.sb = (float)seed + 0.0f;      /* generate's first draw and speed */
+        const float E_val = a.src.p[5] + (a.src.p[6] - a.src.p[5]) * draw(n, r);
+        const float v = RC_SE2V * sqrtf(E_val);
+        kept = !speed_run_blocks(a.comps, 0, a.cull, v, a.src.p[0], a.src.p[1], a.src.p[2],
+                                 a.src.p[3], a.src.p[4]);
+      } else {
+        generate<TallyOnly, true, false>(a.src, n, 0.0f, a.num_sim, seed, r);
+        kept = !chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t);
+      }
     }
     const unsigned m = __ballot_sync(0xffffffffu, kept);
     if (m == 0u) continue;

@@ -27,6 +27,57 @@ ONE_MODE(3, 1)
 ONE_MODE(4, 0)
 ONE_MODE(4, 1)
 
+/* ---- before the lean stage A: the speed look-ahead -------------------
+ * Every history's first draw (its energy, hence its speed) is made here
+ * and the speed-only bound (speed_run_blocks) applied; the indices of the
+ * histories that may pass are appended, one atomic per warp, to a list in
+ * word 18 of the variant's survivor slots (free until a walk uses it), its
+ * length in the variant's workq_c.  The lean stage A then traces only the
+ * listed histories, each regenerated from its key (the same operations,
+ * so the same neutron).  Without carry buffers only; with a source other
+ * than flat or MCont every history is listed. */
+template <int MODE, bool BATCHED>
+__global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
+  const int var = BATCHED ? (int)blockIdx.y : a.var_key;
+  const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
+  const int64_t n = V->n;
+  const int64_t item0 = BATCHED ? V->item_off : 0;
+  if (BATCHED && item0 + (n + FUSED_WARP_TASK - 1) / FUSED_WARP_TASK > a.surv_items) return;
+  const SrcDev& src = V->src;
+  const bool speed = (src.kind == RAMP_SRC_FLAT || src.kind == RAMP_SRC_CONT) &&
+                     a.carry_sb == nullptr && a.cull > 0;
+  uint32_t* const keep = a.surv + (size_t)18 * a.surv_cap + item0 * FUSED_WARP_TASK;
+  unsigned long long* const kc = a.workq_c + (BATCHED ? var : 0);
+  const int32_t seed = (a.rng.seed_dev && !BATCHED) ? *a.rng.seed_dev : V->seed;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
+       base += stride) {                                   /* warp-uniform */
+    const int64_t i = base + lane;
+    bool kept = false;
+    if (i < n) {
+      kept = true;
+      if (speed) {
+        /* generate's first draw and speed (flat_mod.cl, cont_mod.cl:36) */
+        Rng r;
+        rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
+        Nt nn;
+        nn.sb = (float)seed + 0.0f;
+        const float E_val = src.p[5] + (src.p[6] - src.p[5]) * draw(nn, r);
+        const float v = RC_SE2V * sqrtf(E_val);
+        kept = !speed_run_blocks(V->comps, 0, a.cull, v, src.p[0], src.p[1], src.p[2],
+                                 src.p[3], src.p[4]);
+      }
+    }
+    const unsigned m = __ballot_sync(FULL_MASK, kept);
+    if (m == 0u) continue;
+    unsigned long long at = 0;
+    if (lane == 0) at = atomicAdd(kc, (unsigned long long)__popc(m));
+    at = __shfl_sync(FULL_MASK, at, 0);
+    if (kept) keep[at + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+  }
+}
+
 /* one register cap, keying mode, layout and kind set: the whole chain, or
  * stage A then stage B of a split launch (the batched one-launch layout
  * runs the extended kinds whole; the mesh walk runs with the mesh kind set;
@@ -46,9 +97,13 @@ static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream
   if constexpr (!(BATCHED && KS == 1)) {
     if (a.split > 0 || a.cull > 0) {
       cudaError_t e;
-      if (KS == 0 && a.split == 0)     /* the moderator alone: the lean stage A */
+      if (KS == 0 && a.split == 0) {   /* the moderator alone: the lean stage A */
+        const dim3 g((unsigned)grid, BATCHED ? (unsigned)a.n_variants : 1u);
+        k_speed_keep<MODE, BATCHED><<<g, 256, 0, s>>>(a);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
         e = launch_phase<MB, MODE, BATCHED, 3, 0>(a, block, grid, s);
-      else
+      } else
         e = launch_phase<MB, MODE, BATCHED, 1, KS>(a, block, grid, s);
       if (e != cudaSuccess) return e;
       return launch_phase<MB, MODE, BATCHED, 2, KS>(a, block, grid, s);

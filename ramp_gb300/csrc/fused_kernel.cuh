@@ -368,9 +368,18 @@ k_fused(const FusedArgs a) {
     const int KE = PHASE == 3 ? 0 : (PHASE == 1 ? a.split : a.n_comps);
     const int var = BATCHED ? (int)blockIdx.y : a.var_key;
     const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
-    /* batched: CTAs past what this row's variant can use leave at once */
-    if (BATCHED && (int64_t)blockIdx.x * (blockDim.x / 32) * FUSED_WARP_TASK >= V->n) return;
     const int64_t item0 = BATCHED ? V->item_off : 0;
+    /* the lean stage A traces the histories the speed look-ahead listed
+       (k_speed_keep in fused.cu: their indices in word 18 of the survivor
+       slots, their number in workq_c); the other phases every history */
+    const uint32_t* __restrict__ listed = a.surv + (size_t)18 * a.surv_cap + item0 * FUSED_WARP_TASK;
+    int64_t n_work = V->n;
+    if (PHASE == 3) {
+      const int64_t m = (int64_t)a.workq_c[BATCHED ? var : 0];
+      if (m < n_work) n_work = m;
+    }
+    /* batched: CTAs past what this row's variant can use leave at once */
+    if (BATCHED && (int64_t)blockIdx.x * (blockDim.x / 32) * FUSED_WARP_TASK >= n_work) return;
     unsigned long long* const q_a = a.workq + (BATCHED ? var : 0);
     const bool priv = PHASE == 0 && !BATCHED && a.priv_floats > 0;
     if (priv) {                   /* the CTA's private tallies start at zero */
@@ -382,8 +391,8 @@ k_fused(const FusedArgs a) {
       if (lane == 0) t = atomicAdd(q_a, 1ull);
       t = __shfl_sync(FULL_MASK, t, 0);
       const int64_t start = (int64_t)t * FUSED_WARP_TASK;
-      if (start >= V->n) break;
-      int64_t count = V->n - start;
+      if (start >= n_work) break;
+      int64_t count = n_work - start;
       if (count > FUSED_WARP_TASK) count = FUSED_WARP_TASK;
       const CompDev* __restrict__ comps = V->comps;
       const int32_t num_sim = V->num_sim;
@@ -395,7 +404,7 @@ k_fused(const FusedArgs a) {
       const int jend = STAGE_A ? (int)((count + 31) & ~31ll) : (int)count;
       for (int j = lane; j < jend; j += 32) {
         const bool live = j < count;
-        const int64_t i = start + j;
+        const int64_t i = (PHASE == 3 && live) ? (int64_t)listed[start + j] : start + j;
         Nt n;
         Rng r;
         uint32_t ii = 0u;

@@ -85,6 +85,22 @@ def culled(inst, k, records):
     return out.astype(bool)
 
 
+def speed_culled(inst, k, records):
+    """The speed-only bound (ramp_debug_speed_cull) for each neutron's
+    speed after the moderator."""
+    keep = []
+    src, carr, nc, barr, nb = inst.descriptors(keep)
+    rec = np.asarray(records, dtype=np.float64)
+    v = np.ascontiguousarray(np.sqrt((rec[:, 3:6] ** 2).sum(axis=1)), dtype=np.float32)
+    p = np.ascontiguousarray(np.array(src.p[0:5], dtype=np.float32))
+    out = np.zeros(len(v), np.uint8)
+    lib = _abi.load()
+    rc = lib.ramp_debug_speed_cull(ctypes.addressof(carr), nc, ctypes.addressof(barr), nb, k,
+                                   p.ctypes.data, v.ctypes.data, len(v), out.ctypes.data)
+    _abi.check(lib, rc, "ramp_debug_speed_cull")
+    return out.astype(bool)
+
+
 @pytest.mark.parametrize("Ei", [1.5, 3.7, 8.0])
 def test_lookahead_never_retires_a_neutron_that_passes(tmp_path, Ei):
     N = 400_000
@@ -103,6 +119,10 @@ def test_lookahead_never_retires_a_neutron_that_passes(tmp_path, Ei):
     assert not (cut & passed).any(), "a neutron that passes the choppers was retired"
     # most of those that do not pass are retired before the guide
     assert cut.sum() >= 0.8 * (~passed).sum()
+    # the speed-only bound retires a subset of those, and no passing one
+    scut = speed_culled(full, 0, after_mod)
+    assert not (scut & passed).any(), "the speed bound retired a neutron that passes"
+    assert scut.sum() > 0.3 * (~passed).sum()
 
 
 @pytest.mark.parametrize("Ei", [2.0, 3.7])
@@ -122,6 +142,8 @@ def test_lookahead_through_several_guides_never_retires_a_neutron_that_passes(tm
     assert passed.sum() > 20
     assert not (cut & passed).any(), "a neutron that passes the run was retired"
     assert cut.sum() >= 0.9 * (~passed).sum()
+    scut = speed_culled(full, 0, after_mod)
+    assert not (scut & passed).any(), "the speed bound retired a neutron that passes"
 
 
 def test_lookahead_run_detection(tmp_path):
@@ -215,3 +237,5 @@ def test_lookahead_sound_on_random_runs(tmp_path, seed):
     cut = culled(full, 0, after_mod)
     assert passed.sum() > 50
     assert not (cut & passed).any(), "a neutron that passes the run was retired"
+    scut = speed_culled(full, 0, after_mod)
+    assert not (scut & passed).any(), "the speed bound retired a neutron that passes"
