@@ -1514,9 +1514,10 @@ int ramp_debug_speed_cull(const RampComp* comps, int n_comps, const RampBlock* b
     if (comps[j].scat == RAMP_S_CHOPPER && (uint32_t)comps[j].si[0] != 0u)
       chopper_aux(comps[j], q.aux);
   }
-  for (int64_t i = 0; i < n; ++i)
-    out[i] = speed_run_blocks(d.data(), k, nl, speeds[i], source_p[0], source_p[1], source_p[2],
-                              source_p[3], source_p[4]) ? 1 : 0;
+  SpeedRun run;
+  speed_run_prepare(d.data(), k, nl, source_p[0], source_p[1], source_p[2], source_p[3],
+                    source_p[4], &run);
+  for (int64_t i = 0; i < n; ++i) out[i] = speed_run_blocks(run, speeds[i]) ? 1 : 0;
   return RAMP_OK;
 }
 

@@ -71,6 +71,15 @@ __global__ void __launch_bounds__(256) k_adjoint_record(const AdjointArgs a) {
  * indices of those it keeps are appended to a.keep (one atomic per warp) */
 template <int MODE>
 __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
+  const bool speed = a.src.kind == RAMP_SRC_FLAT || a.src.kind == RAMP_SRC_CONT;
+  /* the run's per-chopper constants for the speed look-ahead, once per CTA */
+  __shared__ SpeedRun run;
+  if (threadIdx.x == 0) {
+    run.n = 0;
+    if (speed) speed_run_prepare(a.comps, 0, a.cull, a.src.p[0], a.src.p[1], a.src.p[2],
+                                 a.src.p[3], a.src.p[4], &run);
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
@@ -82,12 +91,10 @@ __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
       Rng r;
       rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
       const int32_t seed = a.rng.seed_dev ? *a.rng.seed_dev : a.seed;
-      if (a.src.kind == RAMP_SRC_FLAT || a.src.kind == RAMP_SRC_CONT) {
+      if (speed) {
         n.sb = (float)seed + 0.0f;      /* generate's first draw and speed */
         const float E_val = a.src.p[5] + (a.src.p[6] - a.src.p[5]) * draw(n, r);
-        const float v = RC_SE2V * sqrtf(E_val);
-        kept = !speed_run_blocks(a.comps, 0, a.cull, v, a.src.p[0], a.src.p[1], a.src.p[2],
-                                 a.src.p[3], a.src.p[4]);
+        kept = !speed_run_blocks(run, RC_SE2V * sqrtf(E_val));
       } else {
         generate<TallyOnly, true, false>(a.src, n, 0.0f, a.num_sim, seed, r);
         kept = !chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t);

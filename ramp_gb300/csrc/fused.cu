@@ -49,6 +49,14 @@ __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
   uint32_t* const keep = a.surv + (size_t)18 * a.surv_cap + item0 * FUSED_WARP_TASK;
   unsigned long long* const kc = a.workq_c + (BATCHED ? var : 0);
   const int32_t seed = (a.rng.seed_dev && !BATCHED) ? *a.rng.seed_dev : V->seed;
+  /* the run's per-chopper constants, once per CTA */
+  __shared__ SpeedRun run;
+  if (threadIdx.x == 0) {
+    run.n = 0;
+    if (speed) speed_run_prepare(V->comps, 0, a.cull, src.p[0], src.p[1], src.p[2], src.p[3],
+                                 src.p[4], &run);
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
@@ -57,16 +65,14 @@ __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
     bool kept = false;
     if (i < n) {
       kept = true;
-      if (speed) {
+      if (speed && run.n > 0) {
         /* generate's first draw and speed (flat_mod.cl, cont_mod.cl:36) */
         Rng r;
         rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
         Nt nn;
         nn.sb = (float)seed + 0.0f;
         const float E_val = src.p[5] + (src.p[6] - src.p[5]) * draw(nn, r);
-        const float v = RC_SE2V * sqrtf(E_val);
-        kept = !speed_run_blocks(V->comps, 0, a.cull, v, src.p[0], src.p[1], src.p[2],
-                                 src.p[3], src.p[4]);
+        kept = !speed_run_blocks(run, RC_SE2V * sqrtf(E_val));
       }
     }
     const unsigned m = __ballot_sync(FULL_MASK, kept);

@@ -163,63 +163,92 @@ LA_FN bool chopper_run_blocks(const CompDev* comps, int k, int nl, float x, floa
   return false;
 }
 
-/* true: no neutron of speed v from a flat or MCont moderator can pass every
- * chopper of the run comps[k .. k + nl).  Such a moderator (flat_mod.cl,
- * cont_mod.cl:11-72) emits at time 0 from a uniform point of a p0 x p1
+/* The speed look-ahead.  For a flat or MCont moderator (flat_mod.cl,
+ * cont_mod.cl:11-72: emission at time 0 from a uniform point of a p0 x p1
  * rectangle at z = 0 towards a uniform point of a p2 x p3 target window at
- * distance p4, so before its other draws a neutron's speed is known and its
+ * distance p4) a neutron's speed v is known after its first draw, and its
  * direction lies in a cone: |vx / vz| <= (|p0| + |p2|) / (2 p4), likewise
  * y, and vz >= v / sqrt(1 + sx^2 + sy^2).  Along the run vz does not change
  * (see above), so the time at a chopper plane lies in [z / v, z / vz_min];
  * the transverse position is within the moderator rectangle widened by the
  * cone before the first guide, within a guide's walls inside it, and within
  * the walls widened by the cone after its exit.  A chopper whose slits are
- * closed over all of that stops the neutron. */
-LA_FN bool speed_run_blocks(const CompDev* comps, int k, int nl, float v, float p0, float p1,
-                            float p2, float p3, float p4) {
-  if (!(v > 0.0f) || !(p4 > 0.0f) || nl <= 0) return false;
+ * closed over all of that stops the neutron.  Everything but v is the same
+ * for every neutron of a launch: speed_run_prepare computes it once per
+ * chopper, speed_run_blocks applies it to one speed. */
+#define SPEED_RUN_MAX 16          /* choppers of a run the bound uses */
+struct SpeedRun {
+  int n;                          /* choppers prepared */
+  float a0[SPEED_RUN_MAX];        /* earliest time x v (with its slack) */
+  float a1[SPEED_RUN_MAX];        /* latest time x v (with its slack) */
+  float ph[SPEED_RUN_MAX];        /* |phase| */
+  float fr[SPEED_RUN_MAX];        /* freq */
+  float wide[SPEED_RUN_MAX];      /* |jitter| + the largest |atan2(x, y + R)| */
+  float hb[SPEED_RUN_MAX];        /* half the largest slit angle, plus slack */
+  float iTg[SPEED_RUN_MAX];       /* 1 / slit period */
+};
+
+LA_FN void speed_run_prepare(const CompDev* comps, int k, int nl, float p0, float p1, float p2,
+                             float p3, float p4, SpeedRun* R) {
+  R->n = 0;
+  if (!(p4 > 0.0f) || nl <= 0) return;
   const float sx = 0.5f * (fabsf(p0) + fabsf(p2)) / p4, sy = 0.5f * (fabsf(p1) + fabsf(p3)) / p4;
   const float cmin = (1.0f - 1e-5f) / sqrtf(1.0f + sx * sx + sy * sy);
-  if (!(cmin > 0.0f)) return false;
-  const float iv = 1.0f / v, ivmin = iv / cmin;
+  if (!(cmin > 0.0f)) return;
+  const float icmin = 1.0f / cmin;
   /* |x| <= X + sx |z - z0| (and y) beyond the last guide exit z0 */
   float X = 0.5f * fabsf(p0), Y = 0.5f * fabsf(p1), z0 = 0.0f;
   float nb = 0.0f;                /* bounces the guides can take, for the time slack */
-  for (int j = k; j < k + nl; ++j) {
+  for (int j = k; j < k + nl && R->n < SPEED_RUN_MAX; ++j) {
     const CompDev& c = comps[j];
     const float zc = c.pos[2];
     const float dz = zc - z0;
-    if (!(dz >= -1e-6f)) return false;
+    if (!(dz >= -1e-6f)) return;
     const float Xc = X + sx * fabsf(dz), Yc = Y + sy * fabsf(dz);
     if (c.scat == RAMP_S_GUIDE) {
       const float a = 0.5f * c.sp[0], b = 0.5f * c.sp[1], l = c.sp[4];
       /* a neutron entering beside the walls (an entrance plane wider than
-         the guide) is not bounded by them: no claim */
-      if (!(0.5f * c.gp[0] <= a) || !(0.5f * c.gp[1] <= b)) return false;
+         the guide) is not bounded by them: the later choppers get no claim */
+      if (!(0.5f * c.gp[0] <= a) || !(0.5f * c.gp[1] <= b)) return;
       nb += floorf(sx * l / (2.0f * a)) + floorf(sy * l / (2.0f * b)) + 4.0f;
-      if (!(nb < 1e6f)) return false;
+      if (!(nb < 1e6f)) return;
       X = a + 2e-5f;
       Y = b + 2e-5f;
       z0 = zc + l;
       continue;
     }
-    /* a disk chopper (chopper.cl:4-59): the time in [zc / v, zc / vz_min],
-       the angle atan2(x, y + R) within +-atan(Xc / (R - Yc)) */
+    /* a disk chopper (chopper.cl:4-59): the time in [zc / v, zc / vz_min]
+       widened by 1e-5 of it and a micrometre of z per bounce, the angle
+       atan2(x, y + R) within +-atan(Xc / (R - Yc)) */
     const float ex = 2e-5f + 1e-6f * Xc, ey = 2e-5f + 1e-6f * Yc;
-    const float tlo = zc * iv, thi = zc * ivmin;
-    const float et = 1e-5f * thi + (1e-5f * zc + 1e-6f * (nb + 10.0f)) * ivmin + 1e-9f;
-    const float sw = c.sp[0], R = c.sp[1], freq = c.sp[2], phase = c.sp[3], jit = c.sp[4];
-    const float iTg = c.aux[1];
-    const float Ylo = R - Yc - ey;
-    if (!(Ylo > 1e-3f) || !(iTg > 0.0f)) continue;
-    const float iYlo = 1.0f / Ylo;
-    const float th = la_atan((Xc + ex) * iYlo);
-    const float c0 = freq * (tlo - et - fabsf(phase)), c1 = freq * (thi + et - fabsf(phase));
-    const float dlo = fminf(c0, c1) - fabsf(jit) - th;
-    const float dhi = fmaxf(c0, c1) + fabsf(jit) + th;
+    const float sw = c.sp[0], Rr = c.sp[1];
+    const float Ylo = Rr - Yc - ey;
+    if (!(Ylo > 1e-3f) || !(c.aux[1] > 0.0f)) continue;
+    const float e1 = (1e-5f * zc * icmin + (1e-5f * zc + 1e-6f * (nb + 10.0f)) * icmin);
+    const int q = R->n++;
+    R->a0[q] = zc - e1;
+    R->a1[q] = zc * icmin + e1;
+    R->ph[q] = fabsf(c.sp[3]);
+    R->fr[q] = c.sp[2];
+    R->wide[q] = fabsf(c.sp[4]) + la_atan((Xc + ex) / Ylo);
+    R->hb[q] = 0.5f * fabsf(sw) / Ylo + 1e-4f;
+    R->iTg[q] = c.aux[1];
+  }
+}
+
+/* true: no neutron of speed v can pass every chopper of the prepared run */
+LA_FN bool speed_run_blocks(const SpeedRun& R, float v) {
+  if (!(v > 0.0f)) return false;
+  const float iv = 1.0f / v;
+  for (int q = 0; q < R.n; ++q) {
+    const float t0 = iv * R.a0[q] - 1e-9f, t1 = iv * R.a1[q] + 1e-9f;
+    const float c0 = R.fr[q] * (t0 - R.ph[q]), c1 = R.fr[q] * (t1 - R.ph[q]);
+    const float dlo = fminf(c0, c1) - R.wide[q];
+    const float dhi = fmaxf(c0, c1) + R.wide[q];
     if (!(fabsf(dlo) < 1e4f) || !(fabsf(dhi) < 1e4f)) continue;
-    const float h = 0.5f * fabsf(sw) * iYlo + 1e-4f + 1e-6f * fmaxf(fabsf(dlo), fabsf(dhi));
-    const float klo = ceilf((dlo - h) * iTg), khi = floorf((dhi + h) * iTg);
+    const float h = R.hb[q] + 1e-6f * fmaxf(fabsf(dlo), fabsf(dhi));
+    /* no multiple of the slit period within [dlo - h, dhi + h] */
+    const float klo = ceilf((dlo - h) * R.iTg[q]), khi = floorf((dhi + h) * R.iTg[q]);
     if (klo > khi) return true;
   }
   return false;
