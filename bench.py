@@ -16,11 +16,13 @@ value: histories/s over all ranks, device-timed (CUDA events per step, L2
 flushed between steps by writing a 256 MiB buffer outside the events).
 e2e:   histories/s through the public API including Instrument
 construction (IDF parse, table upload), execute and the histogram readback.
-roofline: the fused kernel is bound by integer issue (Threefry-4x32-20,
+roofline: the fused kernels are bound by integer issue (Threefry-4x32-20,
 about 150 integer operations per random draw), not by HBM or tensor cores;
-achieved = the moderator's draws (5 per history, the RNG work every history
-needs) x ops per draw / kernel time, peak = the same operation rate measured
-by a Threefry-only kernel on this GPU: a lower bound on the issue used.  The DRAM traffic and
+achieved = the moderator's Threefry blocks the step needs x ops per block /
+kernel time: with the speed look-ahead one per history (its energy) plus
+four per history the look-ahead keeps (2.8 % here), else five per history;
+peak = the same operation rate measured by a Threefry-only kernel on this
+GPU: a lower bound on the issue used.  The DRAM traffic and
 the instruction count per history come from the ncu capture recorded in
 profiles/ with a hash of the kernel sources; they are reported only when
 that hash equals the sources being run.
@@ -147,10 +149,17 @@ def profile_counters(tune):
 
 
 def kernels_per_trace(tune):
-    """Kernels one fused trace launches: two (stage A, stage B) with a
-    split, the mesh walk or the chopper look-ahead, else one."""
+    """Kernels one fused trace of a chain of the core kinds launches: four
+    with the chopper look-ahead from the moderator (the speed table, the
+    keep pass, the lean stage A, stage B), three with the mesh walk (stage
+    A, the walk, the finish), two with another split (stage A, stage B),
+    else one."""
     t = tune or {}
-    return 2 if any(int(t.get(k, 0)) > 0 for k in ("split", "walk", "cull")) else 1
+    if int(t.get("walk", 0)) > 0:
+        return 3
+    if int(t.get("cull", 0)) > 0 and int(t.get("split", 0)) == 0:
+        return 4
+    return 2 if any(int(t.get(k, 0)) > 0 for k in ("split", "cull")) else 1
 
 
 # ---------------------------------------------------------------- CPU arm
@@ -537,7 +546,7 @@ def run_gradients(a):
                                    "720x1000 detector, 22 parameters, fused forward + adjoint",
                        "histories": r["histories"]},
             "histories_per_s_forward_and_adjoint": r["histories_per_s_forward_and_adjoint"],
-            "gpu_launches": a.steps * 2, "clocks": r["clocks"],
+            "gpu_launches": a.steps * 3, "clocks": r["clocks"],
             "gradient_vs_central_fd": r.get("gradient_vs_central_fd")}
     print(json.dumps(line), flush=True)
 
@@ -727,7 +736,13 @@ def main():
     nlast = plain.last_chunk
     random.seed(1000 + len(plain_ms) - 1)
     seed_last = plain.source.next_seed()
-    draws = float(MCONT_DRAWS * nlast)
+    # with the speed look-ahead (split at the moderator) every history
+    # needs its first block (the energy) and only the kept ones the other
+    # four of the moderator
+    from ramp_gb300.autotune import speed_kept_fraction
+    speed_la = int((tune or {}).get("cull", 0)) > 0 and int((tune or {}).get("split", 0)) == 0
+    kept_frac = speed_kept_fraction(plain) if speed_la else 1.0
+    draws = float(nlast * (1.0 + (MCONT_DRAWS - 1) * kept_frac))
     # neutrons whose last component is the detector: each adds to both of
     # its histograms (sum p, sum p^2), two float atomics per tally
     det_idx = [c["idx"] for name, c in plain.components() if name == "detector"][0]
@@ -896,7 +911,8 @@ def main():
                                         "history of the capture recorded for these kernel "
                                         "sources, times the histories of the launch"
                                         if counters else stale),
-                     "kernel": "k_fused", "kernel_ms": kern_ms, "draws_per_launch": draws,
+                     "kernel": "k_speed_keep + k_fused" if speed_la else "k_fused", "kernel_ms": kern_ms,
+                     "draws_per_launch": draws, "lookahead_kept_fraction": kept_frac,
                      "ops_per_draw": THREEFRY_OPS,
                      "peak_source": "measured: Threefry-only kernel (ramp_debug_rng_peak), "
                                     "%d threads x %d x 2 blocks" % (out.numel(), iters),

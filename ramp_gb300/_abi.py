@@ -182,7 +182,7 @@ _SIGS = {
                           ctypes.c_int], ctypes.c_int),
     "ramp_debug_speed_cull": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
-                               ctypes.c_void_p], ctypes.c_int),
+                               ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "ramp_debug_chopper_cull": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
                                 ctypes.c_int),

@@ -3,6 +3,7 @@
  * creation (descriptor validation, frame matrices, table and BVH upload),
  * the plain and fused launchers, status readback and error messages.
  */
+#include <memory>
 #include <climits>
 #include <cmath>
 #include <cstdarg>
@@ -1492,7 +1493,7 @@ int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock*
 
 int ramp_debug_speed_cull(const RampComp* comps, int n_comps, const RampBlock* blocks,
                           int n_blocks, int k, const float* source_p, const float* speeds,
-                          int64_t n, uint8_t* out) {
+                          int64_t n, uint8_t* out, int64_t* table_check) {
   if (!comps || n_comps <= 0 || !source_p || n < 0 || (n > 0 && (!speeds || !out))) {
     set_err("ramp_debug_speed_cull: bad arguments");
     return RAMP_E_INVALID;
@@ -1514,10 +1515,57 @@ int ramp_debug_speed_cull(const RampComp* comps, int n_comps, const RampBlock* b
     if (comps[j].scat == RAMP_S_CHOPPER && (uint32_t)comps[j].si[0] != 0u)
       chopper_aux(comps[j], q.aux);
   }
-  SpeedRun run;
+  std::unique_ptr<SpeedTab> T(new SpeedTab);
+  SpeedRun& run = T->run;
   speed_run_prepare(d.data(), k, nl, source_p[0], source_p[1], source_p[2], source_p[3],
                     source_p[4], &run);
-  for (int64_t i = 0; i < n; ++i) out[i] = speed_run_blocks(run, speeds[i]) ? 1 : 0;
+  /* the choppers ordered as the device orders them, by how many of a
+     sample of speeds (here the first 256 given) each one blocks */
+  int blocked[SPEED_RUN_MAX] = {0};
+  for (int64_t i = 0; i < n && i < 256; ++i)
+    for (int q = 0; q < run.n; ++q)
+      if (speeds[i] > 0.0f && speed_chopper_blocks(run, q, 1.0f / speeds[i])) ++blocked[q];
+  speed_run_sort(&run, blocked);
+  /* the device's speed table, its cells spread over the given speeds */
+  float iv_a = 0.0f, iv_b = 0.0f;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(speeds[i] > 0.0f)) continue;
+    const float iv = 1.0f / speeds[i];
+    if (iv_a == 0.0f || iv < iv_a) iv_a = iv;
+    if (iv > iv_b) iv_b = iv;
+  }
+  speed_tab_range(T.get(), iv_a, iv_b);
+  for (int c = 0; c < T->ncell; ++c) {
+    float lo, hi;
+    speed_cell_bounds(T->iv0, T->w, c, &lo, &hi);
+    T->cell[c] = (uint8_t)speed_cell_verdict(run, lo, hi);
+  }
+  int64_t nm = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    bool by_table = false, by_run = false;
+    if (speeds[i] > 0.0f) {
+      const float iv = 1.0f / speeds[i];
+      by_table = speed_tab_blocks(*T, iv);
+      by_run = speed_run_blocks(run, iv);
+    }
+    out[i] = by_table ? 1 : 0;
+    nm += by_table != by_run;
+  }
+  if (table_check) {
+    int64_t dec = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      if (!(speeds[i] > 0.0f) || T->ncell == 0) continue;
+      const float iv = 1.0f / speeds[i];
+      const float f = (iv - T->iv0) * T->iw;
+      if (!(f >= 0.0f && f < (float)T->ncell)) continue;
+      const int c = (int)f;
+      float lo, hi;
+      speed_cell_bounds(T->iv0, T->w, c, &lo, &hi);
+      if (iv >= lo && iv <= hi && T->cell[c] != SPEED_MIXED) ++dec;
+    }
+    table_check[0] = dec;
+    table_check[1] = nm;
+  }
   return RAMP_OK;
 }
 

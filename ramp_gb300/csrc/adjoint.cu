@@ -68,19 +68,17 @@ __global__ void __launch_bounds__(256) k_adjoint_record(const AdjointArgs a) {
 /* pass 1, first half: for every neutron its first draw (the energy, hence
  * the speed) and the speed look-ahead (speed_run_blocks; with a source
  * other than flat or MCont the moderator and the full look-ahead); the
- * indices of those it keeps are appended to a.keep (one atomic per warp) */
+ * indices of those it keeps are appended to a.keep (warp_list_add) */
 template <int MODE>
 __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
   const bool speed = a.src.kind == RAMP_SRC_FLAT || a.src.kind == RAMP_SRC_CONT;
   /* the run's per-chopper constants for the speed look-ahead, once per CTA */
   __shared__ SpeedRun run;
-  if (threadIdx.x == 0) {
-    run.n = 0;
-    if (speed) speed_run_prepare(a.comps, 0, a.cull, a.src.p[0], a.src.p[1], a.src.p[2],
-                                 a.src.p[3], a.src.p[4], &run);
-  }
-  __syncthreads();
+  __shared__ int blocked[SPEED_RUN_MAX];
+  speed_run_setup(&run, blocked, speed, a.comps, a.cull, a.src.p);
   const int lane = threadIdx.x & 31;
+  __shared__ uint32_t stage[256 / 32][64];
+  int held = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
   for (int64_t base = i0; base < a.n; base += stride) {   /* warp-uniform */
@@ -94,22 +92,16 @@ __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
       if (speed) {
         n.sb = (float)seed + 0.0f;      /* generate's first draw and speed */
         const float E_val = a.src.p[5] + (a.src.p[6] - a.src.p[5]) * draw(n, r);
-        kept = !speed_run_blocks(run, RC_SE2V * sqrtf(E_val));
+        kept = !speed_run_blocks(run, rsqrtf(E_val) * (1.0f / RC_SE2V));
       } else {
         generate<TallyOnly, true, false>(a.src, n, 0.0f, a.num_sim, seed, r);
         kept = !chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t);
       }
     }
-    const unsigned m = __ballot_sync(0xffffffffu, kept);
-    if (m == 0u) continue;
-    unsigned long long at = 0;
-    if (lane == 0) at = atomicAdd(a.keep_count, (unsigned long long)__popc(m));
-    at = __shfl_sync(0xffffffffu, at, 0);
-    if (kept) {
-      const int64_t k = (int64_t)at + __popc(m & ((1u << lane) - 1u));
-      if (k < a.list_cap) a.keep[k] = (uint32_t)i;
-    }
+    warp_list_add(kept, (uint32_t)i, stage[threadIdx.x >> 5], held, a.keep_count, a.keep,
+                  a.list_cap);
   }
+  warp_list_flush(stage[threadIdx.x >> 5], held, a.keep_count, a.keep, a.list_cap);
 }
 
 /* pass 2: the recorded neutrons, replayed with d log p / d theta */

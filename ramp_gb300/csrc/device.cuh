@@ -1430,4 +1430,44 @@ DI void block_nonlinear(const CompDev* comps, int first, int count, int multi, N
   }
 }
 
+/* ---- appending indices to a list shared by the whole grid -------------
+ * (an atomic counter and its array).  Each warp gathers its entries in 64
+ * words of shared memory (`stage`) and reserves list slots 32 at a time:
+ * the counter takes one atomic per 32 entries, not one per warp pass.
+ * `held` (warp-uniform, below 32 between calls) counts the gathered
+ * entries; all 32 lanes call both functions.  Entries at or beyond `cap`
+ * are dropped; the counter still counts them. */
+__device__ __forceinline__ void warp_list_add(bool put, uint32_t v, uint32_t* stage, int& held,
+                                              unsigned long long* count, uint32_t* list,
+                                              int64_t cap) {
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(0xffffffffu, put);
+  if (m == 0u) return;
+  if (put) stage[held + __popc(m & ((1u << lane) - 1u))] = v;
+  held += __popc(m);                                    /* at most 31 + 32 */
+  if (held < 32) return;
+  __syncwarp();
+  unsigned long long at = 0;
+  if (lane == 0) at = atomicAdd(count, 32ull);
+  at = __shfl_sync(0xffffffffu, at, 0);
+  if ((int64_t)(at + lane) < cap) list[at + lane] = stage[lane];
+  held -= 32;
+  const uint32_t rest = stage[32 + lane];
+  __syncwarp();
+  if (lane < held) stage[lane] = rest;
+  __syncwarp();
+}
+
+__device__ __forceinline__ void warp_list_flush(const uint32_t* stage, int held,
+                                                unsigned long long* count, uint32_t* list,
+                                                int64_t cap) {
+  if (held == 0) return;
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  unsigned long long at = 0;
+  if (lane == 0) at = atomicAdd(count, (unsigned long long)held);
+  at = __shfl_sync(0xffffffffu, at, 0);
+  if (lane < held && (int64_t)(at + lane) < cap) list[at + lane] = stage[lane];
+}
+
 #endif /* RAMP_DEVICE_CUH */

@@ -28,14 +28,72 @@ ONE_MODE(4, 0)
 ONE_MODE(4, 1)
 
 /* ---- before the lean stage A: the speed look-ahead -------------------
- * Every history's first draw (its energy, hence its speed) is made here
- * and the speed-only bound (speed_run_blocks) applied; the indices of the
- * histories that may pass are appended, one atomic per warp, to a list in
- * word 18 of the variant's survivor slots (free until a walk uses it), its
- * length in the variant's workq_c.  The lean stage A then traces only the
- * listed histories, each regenerated from its key (the same operations,
- * so the same neutron).  Without carry buffers only; with a source other
- * than flat or MCont every history is listed. */
+ * The speed table of a variant (lookahead.h: the run's constants, ordered,
+ * and a verdict for each cell of 1 / speed) lives in word 19 of the
+ * variant's survivor slots, free on this path; a variant without the speed
+ * look-ahead, or with fewer slots than the table takes, has none. */
+template <bool BATCHED>
+DI uint32_t* speed_tab_slot(const FusedArgs& a, const VariantDev* V) {
+  const int64_t n = V->n;
+  const int64_t item0 = BATCHED ? V->item_off : 0;
+  const int64_t items = (n + FUSED_WARP_TASK - 1) / FUSED_WARP_TASK;
+  const bool speed = (V->src.kind == RAMP_SRC_FLAT || V->src.kind == RAMP_SRC_CONT) &&
+                     a.carry_sb == nullptr && a.cull > 0;
+  if (!speed || item0 + items > a.surv_items || items * FUSED_WARP_TASK < SPEED_TAB_WORDS)
+    return nullptr;
+  return a.surv + (size_t)19 * a.surv_cap + item0 * FUSED_WARP_TASK;
+}
+
+/* the speed table of each variant: one grid row per variant, SPEED_CELLS /
+ * 256 CTAs of 256 threads a row, each CTA preparing and ordering the run
+ * and deciding 256 cells; CTA 0 also writes the run and the cell layout.
+ * The cells cover 1 / speed of the moderator's energy range (flat_mod.cl,
+ * cont_mod.cl:36: v = SE2V sqrt(E), E uniform in [E_min, E_max]) widened
+ * by 1e-5 of it; a history outside them takes speed_run_blocks. */
+template <bool BATCHED>
+__global__ void __launch_bounds__(256) k_speed_table(const FusedArgs a) {
+  const int var = BATCHED ? (int)blockIdx.y : a.var_key;
+  const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
+  uint32_t* const dst = speed_tab_slot<BATCHED>(a, V);
+  if (dst == nullptr) return;
+  __shared__ SpeedTab T;
+  __shared__ int blocked[SPEED_RUN_MAX];
+  speed_run_setup(&T.run, blocked, true, V->comps, a.cull, V->src.p);
+  if (threadIdx.x == 0) {
+    const float e_lo = fminf(V->src.p[5], V->src.p[6]), e_hi = fmaxf(V->src.p[5], V->src.p[6]);
+    if (e_lo > 0.0f)
+      speed_tab_range(&T, rsqrtf(e_hi) * (1.0f / RC_SE2V) * (1.0f - 1e-5f),
+                      rsqrtf(e_lo) * (1.0f / RC_SE2V) * (1.0f + 1e-5f));
+    else
+      speed_tab_range(&T, 0.0f, 0.0f);
+  }
+  __syncthreads();
+  const int c = (int)blockIdx.x * (int)blockDim.x + (int)threadIdx.x;
+  if (c < SPEED_CELLS) {
+    int v = SPEED_MIXED;
+    if (T.ncell > 0) {
+      float lo, hi;
+      speed_cell_bounds(T.iv0, T.w, c, &lo, &hi);
+      v = speed_cell_verdict(T.run, lo, hi);
+    }
+    reinterpret_cast<uint8_t*>(dst)[offsetof(SpeedTab, cell) + c] = (uint8_t)v;
+  }
+  if (blockIdx.x == 0) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(&T);
+    for (int k = threadIdx.x; k < (int)(offsetof(SpeedTab, cell) / 4); k += blockDim.x)
+      dst[k] = w[k];
+  }
+}
+
+/* Every history's first draw (its energy, hence its speed) is made here
+ * and the speed-only bound applied (speed_tab_blocks, with the variant's
+ * speed table; without one, speed_run_blocks with the run prepared here);
+ * the indices of the histories that may pass are appended (warp_list_add)
+ * to a list in word 18 of the variant's survivor slots (free until a walk
+ * uses it), its length in the variant's workq_c.  The lean stage A then
+ * traces only the listed histories, each regenerated from its key (the
+ * same operations, so the same neutron).  Without carry buffers only; with
+ * a source other than flat or MCont every history is listed. */
 template <int MODE, bool BATCHED>
 __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
   const int var = BATCHED ? (int)blockIdx.y : a.var_key;
@@ -49,15 +107,22 @@ __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
   uint32_t* const keep = a.surv + (size_t)18 * a.surv_cap + item0 * FUSED_WARP_TASK;
   unsigned long long* const kc = a.workq_c + (BATCHED ? var : 0);
   const int32_t seed = (a.rng.seed_dev && !BATCHED) ? *a.rng.seed_dev : V->seed;
-  /* the run's per-chopper constants, once per CTA */
-  __shared__ SpeedRun run;
-  if (threadIdx.x == 0) {
-    run.n = 0;
-    if (speed) speed_run_prepare(V->comps, 0, a.cull, src.p[0], src.p[1], src.p[2], src.p[3],
-                                 src.p[4], &run);
+  /* the variant's speed table, or the run prepared here without cells */
+  __shared__ SpeedTab tab;
+  const uint32_t* const tsrc = speed_tab_slot<BATCHED>(a, V);
+  if (tsrc != nullptr) {
+    uint32_t* w = reinterpret_cast<uint32_t*>(&tab);
+    for (int k = threadIdx.x; k < SPEED_TAB_WORDS; k += blockDim.x) w[k] = tsrc[k];
+    __syncthreads();
+  } else {
+    __shared__ int blocked[SPEED_RUN_MAX];
+    speed_run_setup(&tab.run, blocked, speed, V->comps, a.cull, src.p);
+    if (threadIdx.x == 0) speed_tab_range(&tab, 0.0f, 0.0f);
+    __syncthreads();
   }
-  __syncthreads();
   const int lane = threadIdx.x & 31;
+  __shared__ uint32_t stage[256 / 32][64];
+  int held = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
        base += stride) {                                   /* warp-uniform */
@@ -65,23 +130,19 @@ __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
     bool kept = false;
     if (i < n) {
       kept = true;
-      if (speed && run.n > 0) {
+      if (speed && tab.run.n > 0) {
         /* generate's first draw and speed (flat_mod.cl, cont_mod.cl:36) */
         Rng r;
         rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
         Nt nn;
         nn.sb = (float)seed + 0.0f;
         const float E_val = src.p[5] + (src.p[6] - src.p[5]) * draw(nn, r);
-        kept = !speed_run_blocks(run, RC_SE2V * sqrtf(E_val));
+        kept = !speed_tab_blocks(tab, rsqrtf(E_val) * (1.0f / RC_SE2V));
       }
     }
-    const unsigned m = __ballot_sync(FULL_MASK, kept);
-    if (m == 0u) continue;
-    unsigned long long at = 0;
-    if (lane == 0) at = atomicAdd(kc, (unsigned long long)__popc(m));
-    at = __shfl_sync(FULL_MASK, at, 0);
-    if (kept) keep[at + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    warp_list_add(kept, (uint32_t)i, stage[threadIdx.x >> 5], held, kc, keep, n);
   }
+  warp_list_flush(stage[threadIdx.x >> 5], held, kc, keep, n);
 }
 
 /* one register cap, keying mode, layout and kind set: the whole chain, or
@@ -104,8 +165,9 @@ static cudaError_t launch_fk(const FusedArgs& a, int block, int grid, cudaStream
     if (a.split > 0 || a.cull > 0) {
       cudaError_t e;
       if (KS == 0 && a.split == 0) {   /* the moderator alone: the lean stage A */
-        const dim3 g((unsigned)grid, BATCHED ? (unsigned)a.n_variants : 1u);
-        k_speed_keep<MODE, BATCHED><<<g, 256, 0, s>>>(a);
+        const unsigned rows = BATCHED ? (unsigned)a.n_variants : 1u;
+        k_speed_table<BATCHED><<<dim3(SPEED_CELLS / 256, rows), 256, 0, s>>>(a);
+        k_speed_keep<MODE, BATCHED><<<dim3((unsigned)grid, rows), 256, 0, s>>>(a);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         e = launch_phase<MB, MODE, BATCHED, 3, 0>(a, block, grid, s);

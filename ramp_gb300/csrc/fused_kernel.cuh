@@ -66,7 +66,9 @@ k_fused(const FusedArgs a);
 /* PHASE 2: the survivors of stage A through components [split, end).
  * Stage A leaves the survivors of work item t at slots [128 t, 128 t +
  * cnt[t]) (batched: item item_off + t of its variant's row); a warp claims
- * SURV_GROUP items at a time and deals their survivors out 32 to a pass.
+ * up to SURV_GROUP items at a time (fewer when there are too few items to
+ * give every warp of the grid two claims) and deals their survivors out 32
+ * to a pass.
  * A survivor is keyed by its own index and variant, so it continues
  * exactly where stage A left it. */
 #define SURV_GROUP 32   /* one work item per lane */
@@ -115,20 +117,31 @@ DI void fused_tail(const FusedArgs& a) {
   const int var = BATCHED ? (int)blockIdx.y : a.var_key;
   const VariantDev* __restrict__ V = BATCHED ? a.variants + var : &a.single;
   const int64_t item0 = BATCHED ? V->item_off : 0;
-  const int64_t n_items = BATCHED ? (V->n + FUSED_WARP_TASK - 1) / FUSED_WARP_TASK : a.surv_items;
+  int64_t n_items = BATCHED ? (V->n + FUSED_WARP_TASK - 1) / FUSED_WARP_TASK : a.surv_items;
   if (BATCHED && item0 + n_items > a.surv_items) {   /* host sized the buffer for every row */
     if (lane == 0) raise_flag(a.st, RAMP_F_WORKQ);
     return;
   }
+  /* after the lean stage A only the items of the listed histories hold
+     survivors (their number in workq_c, written by k_speed_keep) */
+  if (!FINISH && KS == 0 && K == 0 && a.cull > 0) {
+    const int64_t used = ((int64_t)a.workq_c[BATCHED ? var : 0] + FUSED_WARP_TASK - 1) /
+                         FUSED_WARP_TASK;
+    if (used < n_items) n_items = used;
+  }
+  /* items per grab: about two grabs per warp of the grid, at most one item
+     per lane */
+  const int64_t per = n_items / (2 * (int64_t)gridDim.x * (blockDim.x >> 5));
+  const int G = per < 1 ? 1 : (per > SURV_GROUP ? SURV_GROUP : (int)per);
   const CompDev* __restrict__ comps = V->comps;
   unsigned long long* const q_b = (FINISH ? a.workq_c : a.workq_b) + (BATCHED ? var : 0);
   for (;;) {
     unsigned long long g = 0;
     if (lane == 0) g = atomicAdd(q_b, 1ull);
     g = __shfl_sync(FULL_MASK, g, 0);
-    const int64_t t0 = (int64_t)g * SURV_GROUP;
+    const int64_t t0 = (int64_t)g * G;
     if (t0 >= n_items) break;
-    const int c = (lane < SURV_GROUP && t0 + lane < n_items) ? (int)a.surv_cnt[item0 + t0 + lane] : 0;
+    const int c = (lane < G && t0 + lane < n_items) ? (int)a.surv_cnt[item0 + t0 + lane] : 0;
     int incl = c;
     for (int d = 1; d < SURV_GROUP; d <<= 1) {
       const int y = __shfl_up_sync(FULL_MASK, incl, d);

@@ -236,22 +236,176 @@ LA_FN void speed_run_prepare(const CompDev* comps, int k, int nl, float p0, floa
   }
 }
 
-/* true: no neutron of speed v can pass every chopper of the prepared run */
-LA_FN bool speed_run_blocks(const SpeedRun& R, float v) {
-  if (!(v > 0.0f)) return false;
-  const float iv = 1.0f / v;
-  for (int q = 0; q < R.n; ++q) {
-    const float t0 = iv * R.a0[q] - 1e-9f, t1 = iv * R.a1[q] + 1e-9f;
-    const float c0 = R.fr[q] * (t0 - R.ph[q]), c1 = R.fr[q] * (t1 - R.ph[q]);
-    const float dlo = fminf(c0, c1) - R.wide[q];
-    const float dhi = fmaxf(c0, c1) + R.wide[q];
-    if (!(fabsf(dlo) < 1e4f) || !(fabsf(dhi) < 1e4f)) continue;
-    const float h = R.hb[q] + 1e-6f * fmaxf(fabsf(dlo), fabsf(dhi));
-    /* no multiple of the slit period within [dlo - h, dhi + h] */
-    const float klo = ceilf((dlo - h) * R.iTg[q]), khi = floorf((dhi + h) * R.iTg[q]);
-    if (klo > khi) return true;
-  }
+/* true: no neutron with 1 / speed = iv can pass chopper q of the run */
+LA_FN bool speed_chopper_blocks(const SpeedRun& R, int q, float iv) {
+  const float t0 = iv * R.a0[q] - 1e-9f, t1 = iv * R.a1[q] + 1e-9f;
+  const float c0 = R.fr[q] * (t0 - R.ph[q]), c1 = R.fr[q] * (t1 - R.ph[q]);
+  const float dlo = fminf(c0, c1) - R.wide[q];
+  const float dhi = fmaxf(c0, c1) + R.wide[q];
+  if (!(fabsf(dlo) < 1e4f) || !(fabsf(dhi) < 1e4f)) return false;
+  const float h = R.hb[q] + 1e-6f * fmaxf(fabsf(dlo), fabsf(dhi));
+  /* no multiple of the slit period within [dlo - h, dhi + h] */
+  const float klo = ceilf((dlo - h) * R.iTg[q]), khi = floorf((dhi + h) * R.iTg[q]);
+  return klo > khi;
+}
+
+/* true: no neutron with 1 / speed = iv can pass every chopper of the
+ * prepared run.  iv may carry a relative error of a few 1e-7 (an
+ * approximate reciprocal square root): the time slack is 1e-5 of it. */
+LA_FN bool speed_run_blocks(const SpeedRun& R, float iv) {
+  if (!(iv > 0.0f) || !(iv < 1e30f)) return false;
+  for (int q = 0; q < R.n; ++q)
+    if (speed_chopper_blocks(R, q, iv)) return true;
   return false;
 }
+
+/* reorder the prepared choppers by blocked[q] (how many of a sample of
+ * speeds chopper q blocks), the most first, so that the histories the run
+ * retires leave the test loop early; the answer of speed_run_blocks does
+ * not depend on the order */
+LA_FN void speed_run_sort(SpeedRun* R, const int* blocked) {
+  int key[SPEED_RUN_MAX];
+  for (int q = 0; q < R->n; ++q) key[q] = blocked[q];
+  for (int q = 1; q < R->n; ++q)          /* insertion sort, stable */
+    for (int j = q; j > 0 && key[j] > key[j - 1]; --j) {
+      const int kk = key[j]; key[j] = key[j - 1]; key[j - 1] = kk;
+      float* arr[7] = {R->a0, R->a1, R->ph, R->fr, R->wide, R->hb, R->iTg};
+      for (int f = 0; f < 7; ++f) {
+        const float x = arr[f][j]; arr[f][j] = arr[f][j - 1]; arr[f][j - 1] = x;
+      }
+    }
+}
+
+/* ---- the speed table: verdicts for cells of 1 / speed ------------------
+ * speed_chopper_blocks is, for a fixed chopper, a chain of correctly
+ * rounded float operations each monotone in its operands (products and
+ * sums with constants, min, max, |.| of a monotone value, ceil, floor), so
+ * over a cell [lo, hi] of iv every intermediate value lies between bounds
+ * taken from its values at lo and hi.  From those bounds a cell gets
+ * SPEED_BLOCKED when every iv in it is blocked by one chopper,
+ * SPEED_KEPT when no chopper blocks any iv in it, else SPEED_MIXED; a
+ * history in a BLOCKED or KEPT cell gets from the table exactly the answer
+ * speed_run_blocks would give it, and the others take speed_run_blocks. */
+#define SPEED_CELLS 4096
+#define SPEED_MIXED 0
+#define SPEED_BLOCKED 1
+#define SPEED_KEPT 2
+
+struct SpeedTab {
+  SpeedRun run;                   /* ordered (speed_run_sort) */
+  float iv0, w;                   /* cell c: [iv0 + c w, iv0 + (c + 1) w] */
+  float iw;                       /* about 1 / w (finds the cell; its bounds decide) */
+  int ncell;                      /* 0: no cells, every history takes speed_run_blocks */
+  uint8_t cell[SPEED_CELLS];
+};
+#define SPEED_TAB_WORDS ((int)(sizeof(SpeedTab) / 4))
+
+LA_FN void speed_cell_bounds(float iv0, float w, int c, float* lo, float* hi) {
+  *lo = iv0 + (float)c * w;
+  *hi = iv0 + (float)(c + 1) * w;
+}
+
+/* SPEED_BLOCKED, SPEED_KEPT or SPEED_MIXED for chopper q over iv in [lo, hi] */
+LA_FN int speed_chopper_range(const SpeedRun& R, int q, float lo, float hi) {
+  float c0[2], c1[2];
+  for (int e = 0; e < 2; ++e) {
+    const float iv = e ? hi : lo;
+    const float t0 = iv * R.a0[q] - 1e-9f, t1 = iv * R.a1[q] + 1e-9f;
+    c0[e] = R.fr[q] * (t0 - R.ph[q]);
+    c1[e] = R.fr[q] * (t1 - R.ph[q]);
+  }
+  const float c0n = fminf(c0[0], c0[1]), c0x = fmaxf(c0[0], c0[1]);
+  const float c1n = fminf(c1[0], c1[1]), c1x = fmaxf(c1[0], c1[1]);
+  const float dlo_n = fminf(c0n, c1n) - R.wide[q], dlo_x = fminf(c0x, c1x) - R.wide[q];
+  const float dhi_n = fmaxf(c0n, c1n) + R.wide[q], dhi_x = fmaxf(c0x, c1x) + R.wide[q];
+  if (!(dlo_n == dlo_n) || !(dlo_x == dlo_x) || !(dhi_n == dhi_n) || !(dhi_x == dhi_x))
+    return SPEED_MIXED;
+  const float mlo = fmaxf(fabsf(dlo_n), fabsf(dlo_x)), mhi = fmaxf(fabsf(dhi_n), fabsf(dhi_x));
+  const float hb = R.hb[q], hx = R.hb[q] + 1e-6f * fmaxf(mlo, mhi);
+  const float T = R.iTg[q];
+  /* every iv of the cell blocked: the widest window holds no multiple of
+     the period, and no iv of the cell falls out through the 1e4 guard */
+  if (mlo < 1e4f && mhi < 1e4f && ceilf((dlo_n - hx) * T) > floorf((dhi_x + hx) * T))
+    return SPEED_BLOCKED;
+  /* no iv of the cell blocked: the narrowest window holds a multiple */
+  if (ceilf((dlo_x - hb) * T) <= floorf((dhi_n + hb) * T)) return SPEED_KEPT;
+  return SPEED_MIXED;
+}
+
+/* the verdict of a cell over the whole run */
+LA_FN int speed_cell_verdict(const SpeedRun& R, float lo, float hi) {
+  if (!(lo > 0.0f) || !(hi < 1e30f) || !(lo <= hi)) return SPEED_MIXED;
+  bool all_kept = true;
+  for (int q = 0; q < R.n; ++q) {
+    const int v = speed_chopper_range(R, q, lo, hi);
+    if (v == SPEED_BLOCKED) return SPEED_BLOCKED;
+    if (v != SPEED_KEPT) all_kept = false;
+  }
+  return all_kept ? SPEED_KEPT : SPEED_MIXED;
+}
+
+/* cells spread over [iv_a, iv_b] */
+LA_FN void speed_tab_range(SpeedTab* T, float iv_a, float iv_b) {
+  T->ncell = 0;
+  T->iv0 = 0.0f;
+  T->w = 0.0f;
+  T->iw = 0.0f;
+  if (!(iv_a > 0.0f) || !(iv_b > iv_a) || !(iv_b < 1e30f)) return;
+  T->iv0 = iv_a;
+  T->w = (iv_b - iv_a) / (float)SPEED_CELLS;
+  if (!(T->w > 0.0f)) return;
+  T->iw = 1.0f / T->w;
+  T->ncell = SPEED_CELLS;
+}
+
+/* true: no neutron with 1 / speed = iv can pass the run (the table's
+ * answer where its cell has one, else speed_run_blocks) */
+LA_FN bool speed_tab_blocks(const SpeedTab& T, float iv) {
+  if (T.ncell > 0) {
+    const float f = (iv - T.iv0) * T.iw;
+    if (f >= 0.0f && f < (float)T.ncell) {
+      const int c = (int)f;
+      float lo, hi;
+      speed_cell_bounds(T.iv0, T.w, c, &lo, &hi);
+      if (iv >= lo && iv <= hi) {
+        const int v = T.cell[c];
+        if (v == SPEED_BLOCKED) return true;
+        if (v == SPEED_KEPT) return false;
+      }
+    }
+  }
+  return speed_run_blocks(T.run, iv);
+}
+
+#ifdef __CUDACC__
+/* Called by every thread of a CTA of blockDim.x (a multiple of 32) threads,
+ * R and blocked (SPEED_RUN_MAX ints) in shared memory: thread 0 prepares
+ * the run at component 0 for a flat or MCont source with parameters p
+ * (RampSource.p: p[0..4] the geometry, p[5..6] the energy range); each
+ * thread then takes one energy of an even grid over the range and counts
+ * the choppers that block it, and thread 0 orders the choppers by those
+ * counts.  R->n = 0 when `on` is false. */
+__device__ __forceinline__ void speed_run_setup(SpeedRun* R, int* blocked, bool on,
+                                                const CompDev* comps, int nl, const float* p) {
+  if (threadIdx.x == 0) {
+    R->n = 0;
+    if (on) speed_run_prepare(comps, 0, nl, p[0], p[1], p[2], p[3], p[4], R);
+  }
+  if (threadIdx.x < SPEED_RUN_MAX) blocked[threadIdx.x] = 0;
+  __syncthreads();
+  const int nq = R->n;
+  if (nq > 1) {
+    const float e = p[5] + (p[6] - p[5]) * (((float)threadIdx.x + 0.5f) / (float)blockDim.x);
+    const float iv = rsqrtf(e) * (1.0f / RC_SE2V);
+    for (int q = 0; q < nq; ++q) {
+      const unsigned m = __ballot_sync(0xffffffffu, speed_chopper_blocks(*R, q, iv));
+      if ((threadIdx.x & 31) == 0 && m != 0u) atomicAdd(&blocked[q], __popc(m));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && nq > 1) speed_run_sort(R, blocked);
+  __syncthreads();
+}
+#endif
 
 #endif /* RAMP_LOOKAHEAD_H */

@@ -94,11 +94,56 @@ def speed_culled(inst, k, records):
     v = np.ascontiguousarray(np.sqrt((rec[:, 3:6] ** 2).sum(axis=1)), dtype=np.float32)
     p = np.ascontiguousarray(np.array(src.p[0:5], dtype=np.float32))
     out = np.zeros(len(v), np.uint8)
+    check = np.zeros(2, np.int64)
     lib = _abi.load()
     rc = lib.ramp_debug_speed_cull(ctypes.addressof(carr), nc, ctypes.addressof(barr), nb, k,
-                                   p.ctypes.data, v.ctypes.data, len(v), out.ctypes.data)
+                                   p.ctypes.data, v.ctypes.data, len(v), out.ctypes.data,
+                                   check.ctypes.data)
     _abi.check(lib, rc, "ramp_debug_speed_cull")
+    assert check[1] == 0          # the speed table agrees with the per-chopper test
     return out.astype(bool)
+
+
+def test_speed_table_equals_the_per_chopper_test():
+    """The cells of the speed table (lookahead.h) decide most speeds, and
+    every speed they decide gets the per-chopper test's answer, also at and
+    a few ulp either side of every cell boundary."""
+    import ramp_gb300 as m
+    from ramp_gb300 import instruments as I
+    inst = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
+    src, carr, nc, barr, nb = inst.descriptors([])
+    e0, e1 = float(src.p[5]), float(src.p[6])
+    rng = np.random.default_rng(5)
+    E = rng.uniform(e0, e1, 1_000_000).astype(np.float32)
+    v = (np.float32(437.393377) * np.sqrt(E)).astype(np.float32)
+    v[0] = np.float32(437.393377) * np.sqrt(np.float32(e0))
+    v[1] = np.float32(437.393377) * np.sqrt(np.float32(e1))
+    # speeds whose 1 / v lands on and beside the cell boundaries (the host
+    # spreads the cells over [min 1/v, max 1/v], as the device's layout)
+    iv = (np.float32(1.0) / v).astype(np.float32)
+    a, b = iv.min(), iv.max()
+    w = np.float32((b - a) / np.float32(4096))
+    lo = (a + np.arange(1, 4096, dtype=np.float32) * w).astype(np.float32)
+    s0 = (np.float32(1.0) / lo).astype(np.float32)
+    extra = [s0]
+    for k in range(1, 4):
+        extra += [np.nextafter(extra[-1] if k > 1 else s0, np.float32(np.inf)).astype(np.float32)]
+    down = s0
+    for k in range(1, 4):
+        down = np.nextafter(down, np.float32(0)).astype(np.float32)
+        extra.append(down)
+    v = np.ascontiguousarray(np.concatenate([v] + extra), dtype=np.float32)
+    p = np.ascontiguousarray(np.array(src.p[0:5], dtype=np.float32))
+    out = np.zeros(len(v), np.uint8)
+    check = np.zeros(2, np.int64)
+    lib = _abi.load()
+    _abi.check(lib, lib.ramp_debug_speed_cull(ctypes.addressof(carr), nc, ctypes.addressof(barr),
+                                              nb, 0, p.ctypes.data, v.ctypes.data, len(v),
+                                              out.ctypes.data, check.ctypes.data),
+               "ramp_debug_speed_cull")
+    assert check[1] == 0
+    assert check[0] > 0.9 * len(v)
+    assert 0.01 < 1.0 - out[:1_000_000].mean() < 0.05     # about 2.8 % kept
 
 
 @pytest.mark.parametrize("Ei", [1.5, 3.7, 8.0])
