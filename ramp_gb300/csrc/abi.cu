@@ -438,6 +438,7 @@ static PlainArgs plain_args(RampPlan* p, const RampState* st, int64_t n, const R
   a.n = n;
   a.rng.mode = rng ? rng->mode : 0;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.one = 1u;
   a.rng.tid_base = rng ? rng->tid_base : 0u;
   a.rng.seed_dev = rng ? rng->seed_dev : nullptr;
   a.st = p->status;
@@ -959,6 +960,7 @@ int ramp_trace_fused(RampPlan* p, int64_t n, int32_t num_sim, int32_t seed, cons
   a.n_comps = (int32_t)p->comps.size();
   a.rng.mode = rng ? rng->mode : 0;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.one = 1u;
   a.rng.tid_base = rng ? rng->tid_base : 0u;
   a.rng.seed_dev = rng ? rng->seed_dev : nullptr;
   a.carry_sb = sb_carry;
@@ -1148,6 +1150,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
     a.n_comps = nc;
     a.rng.mode = rng ? rng->mode : 1;
     a.rng.run_seed = rng ? rng->run_seed : 0u;
+    a.rng.one = 1u;
     a.rng.tid_base = 0u;   /* variants key by their own index */
     a.st = p->status;
     return batched_streams(p, a, vars, block, grid, tune, split, walk, cull, s);
@@ -1198,6 +1201,7 @@ int ramp_trace_batched(RampPlan* p, const RampVariant* variants, int n_variants,
   a.n_comps = nc;
   a.rng.mode = rng ? rng->mode : 1;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.one = 1u;
   a.rng.tid_base = 0u;   /* variants key by their own index */
   a.st = p->status;
   a.workq = B.counters;
@@ -1313,6 +1317,7 @@ static int adjoint_args(RampPlan* p, const SrcDev& src, int n_params, int64_t n,
   a.seed = seed;
   a.rng.mode = rng ? rng->mode : 0;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.one = 1u;
   a.rng.tid_base = rng ? rng->tid_base : 0u;
   a.rng.seed_dev = rng ? rng->seed_dev : nullptr;
   a.grad = grad;
@@ -1728,6 +1733,7 @@ extern "C" int ramp_trace_batched_noalloc(RampPlan* p, const RampVariant* varian
   a.n_comps = nc;
   a.rng.mode = rng ? rng->mode : 1;
   a.rng.run_seed = rng ? rng->run_seed : 0u;
+  a.rng.one = 1u;
   a.rng.tid_base = 0u;
   a.st = p->status;             /* allocated with the plan: read by ramp_plan_status */
   a.workq = D->counters;

@@ -24,7 +24,7 @@ template <class D, int MODE>
 DI void adj_trace(const AdjointArgs& a, uint32_t i, D& dx) {
   Nt n;
   Rng r;
-  rng_init(r, MODE, a.rng.tid_base + i, 0u, a.rng.run_seed);
+  rng_init(r, MODE, a.rng.tid_base + i, 0u, a.rng.run_seed, a.rng.one);
   uint32_t ii = 0;
   generate<D>(a.src, n, 0.0f, a.num_sim, a.rng.seed_dev ? *a.rng.seed_dev : a.seed, r, &dx);
   /* a zero-weight neutron contributes dL/dH * p * dlog p = 0: retired */
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
     if (i < a.n) {
       Nt n;
       Rng r;
-      rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+      rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed, a.rng.one);
       const int32_t seed = a.rng.seed_dev ? *a.rng.seed_dev : a.seed;
       if (speed) {
         n.sb = (float)seed + 0.0f;      /* generate's first draw and speed */
@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
 
 /* passes: bit 1 record (bit 4: with tallies), bit 2 replay */
 cudaError_t launch_adjoint(const AdjointArgs& a, int grid, int passes, cudaStream_t s) {
+  if (a.rng.one != 1u) return cudaErrorInvalidValue;   /* tf20 */
   if (a.n <= 0) return cudaSuccess;
   if (passes & 1) {
     cudaError_t e = cudaMemsetAsync(a.list_count, 0, sizeof(unsigned long long), s);

@@ -78,17 +78,23 @@ DI V3 ip2(const Is& s) { return v3(s.x2, s.y2, s.z2); }
 /* ------------------------------------------------------------------ */
 /* Threefry-4x32-20 (Salmon et al., SC'11), written for the GPU: the key */
 /* schedule is built once per neutron and the constant key and counter  */
-/* words fold into immediates.                                           */
+/* words fold into immediates.  Its adds are written x * one + y, with  */
+/* `one` a kernel argument equal to 1 that the compiler cannot fold, so */
+/* that they issue as integer multiply-adds on the FMA pipe, beside the */
+/* rotates and xors on the ALU pipe; mod 2^32 the value is x + y.        */
 /* ------------------------------------------------------------------ */
 DI uint32_t rotl(uint32_t x, int r) { return __funnelshift_l(x, x, r); }
 
-#define TF_E(a, b) x0 += x1; x1 = rotl(x1, a) ^ x0; x2 += x3; x3 = rotl(x3, b) ^ x2;
-#define TF_O(a, b) x0 += x3; x3 = rotl(x3, a) ^ x0; x2 += x1; x1 = rotl(x1, b) ^ x2;
-#define TF_INJ(s, k0, k1, k2, k3) x0 += k0; x1 += k1; x2 += k2; x3 += k3 + (s);
+#define TF_E(a, b) x0 = x1 * one + x0; x1 = rotl(x1, a) ^ x0; \
+                   x2 = x3 * one + x2; x3 = rotl(x3, b) ^ x2;
+#define TF_O(a, b) x0 = x3 * one + x0; x3 = rotl(x3, a) ^ x0; \
+                   x2 = x1 * one + x2; x1 = rotl(x1, b) ^ x2;
+#define TF_INJ(s, k0, k1, k2, k3) x0 = (k0) * one + x0; x1 = (k1) * one + x1; \
+                                  x2 = (k2) * one + x2; x3 = ((k3) + (s)) * one + x3;
 
 DI void tf20(uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t& x3, uint32_t K0, uint32_t K1,
-             uint32_t K2, uint32_t K3, uint32_t K4) {
-  x0 += K0; x1 += K1; x2 += K2; x3 += K3;
+             uint32_t K2, uint32_t K3, uint32_t K4, uint32_t one) {
+  x0 = K0 * one + x0; x1 = K1 * one + x1; x2 = K2 * one + x2; x3 = K3 * one + x3;
   TF_E(10, 26) TF_O(11, 21) TF_E(13, 27) TF_O(23, 5) TF_INJ(1u, K1, K2, K3, K4)
   TF_E(6, 20) TF_O(17, 11) TF_E(25, 10) TF_O(18, 20) TF_INJ(2u, K2, K3, K4, K0)
   TF_E(10, 26) TF_O(11, 21) TF_E(13, 27) TF_O(23, 5) TF_INJ(3u, K3, K4, K0, K1)
@@ -105,9 +111,9 @@ DI void tf20(uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t& x3, uint32_t K0
 #define TF_PARITY 0x1BD11BDAu
 
 /* word x of threefry4x32({c0,C1,C2,C3}, {tid,K1,K2,K3}) (rand.h:7-16) */
-DI uint32_t tf_ref_x(uint32_t c0, uint32_t tid, uint32_t k4) {
+DI uint32_t tf_ref_x(uint32_t c0, uint32_t tid, uint32_t k4, uint32_t one) {
   uint32_t x0 = c0, x1 = TF_C1, x2 = TF_C2, x3 = TF_C3;
-  tf20(x0, x1, x2, x3, tid, TF_K1, TF_K2, TF_K3, k4);
+  tf20(x0, x1, x2, x3, tid, TF_K1, TF_K2, TF_K3, k4, one);
   return x0;
 }
 
@@ -118,14 +124,17 @@ DI float u01cc(uint32_t i) {
 
 struct Rng {
   uint32_t tid, k1, k2, k4;   /* key words 0..2 and the parity word */
+  uint32_t one;               /* 1 (tf20) */
   int mode;
   uint32_t blk;               /* native mode: cached block index       */
   uint32_t w0, w1, w2, w3;
 };
 
-DI void rng_init(Rng& r, int mode, uint32_t tid, uint32_t variant, uint32_t run_seed) {
+DI void rng_init(Rng& r, int mode, uint32_t tid, uint32_t variant, uint32_t run_seed,
+                 uint32_t one) {
   r.mode = mode;
   r.tid = tid;
+  r.one = one;
   if (mode == 0) {
     r.k1 = TF_K1; r.k2 = TF_K2;
   } else {
@@ -142,12 +151,12 @@ DI float draw(Nt& n, Rng& r) {
   uint32_t c = (uint32_t)n.sb;
   uint32_t x;
   if (r.mode == 0) {
-    x = tf_ref_x(c, r.tid, r.k4);
+    x = tf_ref_x(c, r.tid, r.k4, r.one);
   } else {
     uint32_t b = c >> 2;
     if (b != r.blk) {
       uint32_t x0 = b, x1 = TF_C1, x2 = TF_C2, x3 = TF_C3;
-      tf20(x0, x1, x2, x3, r.tid, r.k1, r.k2, TF_K3, r.k4);
+      tf20(x0, x1, x2, x3, r.tid, r.k1, r.k2, TF_K3, r.k4, r.one);
       r.w0 = x0; r.w1 = x1; r.w2 = x2; r.w3 = x3;
       r.blk = b;
     }

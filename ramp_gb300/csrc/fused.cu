@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
       if (speed && tab.run.n > 0) {
         /* generate's first draw and speed (flat_mod.cl, cont_mod.cl:36) */
         Rng r;
-        rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
+        rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed,
+                 a.rng.one);
         Nt nn;
         nn.sb = (float)seed + 0.0f;
         const float E_val = src.p[5] + (src.p[6] - src.p[5]) * draw(nn, r);
@@ -196,6 +197,7 @@ static cudaError_t launch_m(const FusedArgs& a, int block, int grid, cudaStream_
 }
 
 cudaError_t launch_fused(const FusedArgs& a, int block, int grid, cudaStream_t s) {
+  if (a.rng.one != 1u) return cudaErrorInvalidValue;   /* tf20 */
   if (a.variants ? a.n_variants <= 0 : a.n_tasks <= 0) return cudaSuccess;
   if (a.variants && a.n_variants > 65535) return cudaErrorInvalidValue;   /* grid rows */
   if (a.n_blocks > FUSED_MAX_BLOCKS || a.n_comps > RAMP_MAX_COMPS) return cudaErrorInvalidValue;

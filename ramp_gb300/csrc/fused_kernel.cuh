@@ -180,7 +180,7 @@ DI void fused_tail(const FusedArgs& a) {
       uint32_t ii = w[15 * cap];
       const uint32_t idx = w[16 * cap];
       Rng r;
-      rng_init(r, MODE, a.rng.tid_base + idx, w[17 * cap], a.rng.run_seed);
+      rng_init(r, MODE, a.rng.tid_base + idx, w[17 * cap], a.rng.run_seed, a.rng.one);
       for (int b = 0; b < a.n_blocks && !(n.die > 0.f); ++b) {
         const RampBlock B = a.blocks[b];
         const int e = B.first + B.count;
@@ -224,7 +224,7 @@ DI void walk_end(const FusedArgs& a, const CompDev* __restrict__ comps, int K, i
   uint32_t ii = wp[15 * cap];
   const uint32_t idx = wp[16 * cap];
   Rng r;
-  rng_init(r, MODE, a.rng.tid_base + idx, wp[17 * cap], a.rng.run_seed);
+  rng_init(r, MODE, a.rng.tid_base + idx, wp[17 * cap], a.rng.run_seed, a.rng.one);
   const CompDev& cK = comps[K];
   transform<false>(cK, n);
   Is s;
@@ -422,7 +422,8 @@ k_fused(const FusedArgs a) {
         Rng r;
         uint32_t ii = 0u;
         if (live) {
-          rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed);
+          rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed,
+                   a.rng.one);
           const float old_sb = carry ? a.carry_sb[i] : 0.0f;
           ii = carry ? a.carry_iidx[i] : 0u;
           /* the lean stage A (core kinds: flat or MCont source) weighs a

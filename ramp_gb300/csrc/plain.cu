@@ -80,7 +80,7 @@ k_generate(const __grid_constant__ SrcDev src, const PlainArgs a, int32_t num_si
     float old_sb = S[RAMP_MC * st + i];
     Nt n;
     Rng r;
-    rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed, a.rng.one);
     generate(src, n, old_sb, num_sim, a.rng.seed_dev ? *a.rng.seed_dev : seed, r);
     STORE_ALL(n, S, st, i);
   }
@@ -124,7 +124,7 @@ k_linear(const __grid_constant__ CompDev c, const PlainArgs a) {
     const uint32_t ii0 = a.iidx[i];
     uint32_t ii = ii0;
     Rng r;
-    rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed, a.rng.one);
     float ev[8];
     comp_linear_k<SK, MESH>(c, n, ii, r, a.st, ev);
     if constexpr (SK == RAMP_S_RESCAL) {
@@ -169,7 +169,7 @@ k_nonlinear(const CompDev* __restrict__ comps, int first, int count, int multi, 
     n.wr = 0;
     uint32_t ii = a.iidx[i];
     Rng r;
-    rng_init(r, a.rng.mode, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed);
+    rng_init(r, a.rng.mode, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed, a.rng.one);
     block_nonlinear<NoDiff, true, MESH>(comps, first, count, multi, n, ii, r, a.st);
     STORE_ALL(n, S, st, i);
     a.iidx[i] = ii;
@@ -223,6 +223,7 @@ k_leave(const __grid_constant__ CompDev c, const PlainArgs a) {
 }
 
 cudaError_t launch_host_half(const CompDev& c, const PlainArgs& a, int leave, cudaStream_t s) {
+  if (a.rng.one != 1u) return cudaErrorInvalidValue;   /* tf20 */
   if (a.n <= 0) return cudaSuccess;
   if (leave) k_leave<<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(c, a);
   else k_enter<<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(c, a);
@@ -311,6 +312,7 @@ cudaError_t launch_gather_alive(const PlainArgs& a, uint32_t lanes, float* out, 
 
 cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_sim, int32_t seed,
                             cudaStream_t s) {
+  if (a.rng.one != 1u) return cudaErrorInvalidValue;   /* tf20 */
   if (a.n <= 0) return cudaSuccess;
   if (a.rng.mode == 0) k_generate<0><<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(src, a, num_sim, seed);
   else k_generate<1><<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(src, a, num_sim, seed);
@@ -318,6 +320,7 @@ cudaError_t launch_generate(const SrcDev& src, const PlainArgs& a, int32_t num_s
 }
 
 cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_t s) {
+  if (a.rng.one != 1u) return cudaErrorInvalidValue;   /* tf20 */
   if (a.n <= 0) return cudaSuccess;
   int g = plain_grid(a.n);
   const bool mesh = c.geom == RAMP_G_MESH;
@@ -351,6 +354,7 @@ cudaError_t launch_linear_comp(const CompDev& c, const PlainArgs& a, cudaStream_
 
 cudaError_t launch_nonlinear_block(const CompDev* comps_dev, int first, int count, int multi,
                                    bool mesh, const PlainArgs& a, cudaStream_t s) {
+  if (a.rng.one != 1u) return cudaErrorInvalidValue;   /* tf20 */
   if (a.n <= 0 || multi <= 0 || count <= 0) return cudaSuccess;
   if (mesh) k_nonlinear<true><<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(comps_dev, first, count, multi, a);
   else k_nonlinear<false><<<plain_grid(a.n), PLAIN_BLOCK, 0, s>>>(comps_dev, first, count, multi, a);
@@ -360,11 +364,12 @@ cudaError_t launch_nonlinear_block(const CompDev* comps_dev, int first, int coun
 /* ------------------------------------------------------------------ */
 /* debug kernels used by the parity tests                               */
 /* ------------------------------------------------------------------ */
-__global__ void k_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out, int64_t n) {
+__global__ void k_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out, int64_t n,
+                                 uint32_t one) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t t = tid[i];
-  out[i] = tf_ref_x(c0[i], t, TF_PARITY ^ t ^ TF_K1 ^ TF_K2 ^ TF_K3);
+  out[i] = tf_ref_x(c0[i], t, TF_PARITY ^ t ^ TF_K1 ^ TF_K2 ^ TF_K3, one);
 }
 
 __global__ void k_debug_math(int fn, const float* a, const float* b, float* out, int64_t n) {
@@ -387,22 +392,23 @@ __global__ void k_debug_math(int fn, const float* a, const float* b, float* out,
   out[i] = r;
 }
 
-__global__ void __launch_bounds__(256) k_debug_rng_peak(int32_t iters, uint32_t* out, int64_t n) {
+__global__ void __launch_bounds__(256) k_debug_rng_peak(int32_t iters, uint32_t* out, int64_t n,
+                                                        uint32_t one) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t tid = (uint32_t)i;
   uint32_t k4 = TF_PARITY ^ tid ^ TF_K1 ^ TF_K2 ^ TF_K3;
   uint32_t a = tid, b = tid ^ 0x9e3779b9u;
   for (int k = 0; k < iters; ++k) {
-    a = tf_ref_x(a, tid, k4);
-    b = tf_ref_x(b, tid, k4);
+    a = tf_ref_x(a, tid, k4, one);
+    b = tf_ref_x(b, tid, k4, one);
   }
   out[i] = a ^ b;
 }
 
 cudaError_t launch_debug_rng_peak(int64_t n, int32_t iters, uint32_t* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_debug_rng_peak<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(iters, out, n);
+  k_debug_rng_peak<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(iters, out, n, 1u);
   return cudaGetLastError();
 }
 
@@ -471,7 +477,7 @@ cudaError_t launch_seed_advance(int32_t* seed_dev, cudaStream_t s) {
 cudaError_t launch_debug_threefry(const uint32_t* c0, const uint32_t* tid, uint32_t* out,
                                   int64_t n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_debug_threefry<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c0, tid, out, n);
+  k_debug_threefry<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c0, tid, out, n, 1u);
   return cudaGetLastError();
 }
 

@@ -68,7 +68,9 @@ struct RngDev {
   int32_t mode;
   uint32_t run_seed;
   uint32_t tid_base;
-  uint32_t pad;
+  uint32_t one;              /* 1, set by the host (Threefry's multiplier of
+                                its adds, device.cuh: the launchers refuse
+                                any other value) */
   const int32_t* seed_dev;   /* when set, the chunk seed is read here */
 };
 
