@@ -85,6 +85,46 @@ __global__ void __launch_bounds__(256) k_speed_table(const FusedArgs a) {
   }
 }
 
+/* 1 / sqrt(x), the PTX approximation (relative error below 2^-22): the
+ * speed bound's time slack is 1e-5 of the time */
+DI float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+/* the keep pass over histories [0, n) of one variant (index type I: 32-bit
+ * when the grid's strides stay below 2^31); `test` false lists every one */
+template <typename I, int MODE>
+DI void keep_histories(const FusedArgs& a, const SrcDev& src, const SpeedTab& tab, bool test,
+                       int var, int32_t seed, I n, uint32_t* keep, unsigned long long* kc,
+                       uint32_t* stage) {
+  const int lane = threadIdx.x & 31;
+  int held = 0;
+  const I stride = (I)gridDim.x * (I)blockDim.x;
+  const float e0 = src.p[5], de = src.p[6] - src.p[5];
+  for (I base = (I)blockIdx.x * (I)blockDim.x + (I)(threadIdx.x & ~31); base < n;
+       base += stride) {                                   /* warp-uniform */
+    const I i = base + (I)lane;
+    bool kept = false;
+    if (i < n) {
+      kept = true;
+      if (test) {
+        /* generate's first draw and speed (flat_mod.cl, cont_mod.cl:36) */
+        Rng r;
+        rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed,
+                 a.rng.one);
+        Nt nn;
+        nn.sb = (float)seed + 0.0f;
+        const float E_val = e0 + de * draw(nn, r);
+        kept = !speed_tab_blocks(tab, rsqrt_approx(E_val) * (1.0f / RC_SE2V));
+      }
+    }
+    warp_list_add(kept, (uint32_t)i, stage, held, kc, keep, (int64_t)n);
+  }
+  warp_list_flush(stage, held, kc, keep, (int64_t)n);
+}
+
 /* Every history's first draw (its energy, hence its speed) is made here
  * and the speed-only bound applied (speed_tab_blocks, with the variant's
  * speed table; without one, speed_run_blocks with the run prepared here);
@@ -120,30 +160,15 @@ __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
     if (threadIdx.x == 0) speed_tab_range(&tab, 0.0f, 0.0f);
     __syncthreads();
   }
-  const int lane = threadIdx.x & 31;
   __shared__ uint32_t stage[256 / 32][64];
-  int held = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-       base += stride) {                                   /* warp-uniform */
-    const int64_t i = base + lane;
-    bool kept = false;
-    if (i < n) {
-      kept = true;
-      if (speed && tab.run.n > 0) {
-        /* generate's first draw and speed (flat_mod.cl, cont_mod.cl:36) */
-        Rng r;
-        rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, (uint32_t)var, a.rng.run_seed,
-                 a.rng.one);
-        Nt nn;
-        nn.sb = (float)seed + 0.0f;
-        const float E_val = src.p[5] + (src.p[6] - src.p[5]) * draw(nn, r);
-        kept = !speed_tab_blocks(tab, rsqrtf(E_val) * (1.0f / RC_SE2V));
-      }
-    }
-    warp_list_add(kept, (uint32_t)i, stage[threadIdx.x >> 5], held, kc, keep, n);
-  }
-  warp_list_flush(stage[threadIdx.x >> 5], held, kc, keep, n);
+  const bool test = speed && tab.run.n > 0;
+  if (n + stride <= (int64_t)INT32_MAX)
+    keep_histories<int32_t, MODE>(a, src, tab, test, var, seed, (int32_t)n, keep, kc,
+                                  stage[threadIdx.x >> 5]);
+  else
+    keep_histories<int64_t, MODE>(a, src, tab, test, var, seed, n, keep, kc,
+                                  stage[threadIdx.x >> 5]);
 }
 
 /* one register cap, keying mode, layout and kind set: the whole chain, or

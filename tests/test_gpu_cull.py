@@ -27,10 +27,12 @@ pytestmark = pytest.mark.gpu
     ("let_like.json", dict(Ei=8.0), 1_000_000, {"split": 1, "cull": 1}, "reference"),
     ("let_like.json", dict(Ei=3.7), 1_000_000,
      {"split": 0, "cull": 1, "block": 128, "blocks_per_sm": 8}, "reference"),
-    ("let_like_misis.json", dict(Ei=3.7), 400_000, {"split": 0, "cull": 1}, "reference")])
+    ("let_like_misis.json", dict(Ei=3.7), 400_000, {"split": 0, "cull": 1}, "reference"),
+    ("let_like.json", dict(Ei=3.7), 1_000_003, {"split": 0, "cull": 1}, "reference")])
 def test_fused_cull_matches_oracle(cuda_lib, fn, kw, N, tune, rng):
     """Split before guide 1 (stage A: the moderator alone) or before
-    chopper 1, with the look-ahead; also with the MISIS source."""
+    chopper 1, with the look-ahead; also with the MISIS source and with a
+    history count that is not a whole number of work items."""
     kws = (I.let_like_misis_kwargs if "misis" in fn else I.let_like_kwargs)(**kw)
     gi, ci, r = pair(I.path(fn), kws, N, path="fused", rng=rng, tune=tune)
     tallies_close(gi, ci)
