@@ -1325,13 +1325,14 @@ static int adjoint_args(RampPlan* p, const SrcDev& src, int n_params, int64_t n,
   a.st = p->status;
   a.cull = chopper_run(p->comps_in.data(), (int)p->comps.size(), p->blocks.data(),
                        (int)p->blocks.size(), 0);
-  if (p->adj_cap < n) {   /* two lists of n indices (counted, kept) and two counters */
+  if (p->adj_cap < n) {   /* two lists of n indices (counted, kept), three
+                             counters and the keep pass's speed table */
     if (p->adj_list) cudaFree(p->adj_list);
     p->adj_list = nullptr;
     p->adj_cap = 0;
     void* d = nullptr;
-    if (cudaMalloc(&d, 2 * (size_t)n * sizeof(uint32_t) + 3 * sizeof(unsigned long long)) !=
-        cudaSuccess) {
+    if (cudaMalloc(&d, 2 * (size_t)n * sizeof(uint32_t) + 3 * sizeof(unsigned long long) +
+                           sizeof(SpeedTab)) != cudaSuccess) {
       cudaGetLastError();
       set_err("ramp_adjoint: no room for %lld recorded indices", (long long)n);
       return RAMP_E_NOMEM;

@@ -65,17 +65,31 @@ __global__ void __launch_bounds__(256) k_adjoint_record(const AdjointArgs a) {
   }
 }
 
+/* the speed table of the keep pass (lookahead.h) lives after the three
+ * counters of the index lists */
+DI uint32_t* adjoint_speed_tab(const AdjointArgs& a) {
+  return reinterpret_cast<uint32_t*>(a.list_count + 3);
+}
+
+/* pass 1, before the keep pass, for a flat or MCont source: the speed
+ * table, SPEED_CELLS / 256 CTAs */
+__global__ void __launch_bounds__(256) k_adjoint_table(const AdjointArgs a) {
+  __shared__ SpeedTab T;
+  __shared__ int blocked[SPEED_RUN_MAX];
+  speed_tab_build(adjoint_speed_tab(a), &T, blocked, a.comps, a.cull, a.src.p,
+                  (int)blockIdx.x);
+}
+
 /* pass 1, first half: for every neutron its first draw (the energy, hence
- * the speed) and the speed look-ahead (speed_run_blocks; with a source
- * other than flat or MCont the moderator and the full look-ahead); the
- * indices of those it keeps are appended to a.keep (warp_list_add) */
+ * the speed) and the speed look-ahead (speed_tab_blocks with the table of
+ * k_adjoint_table; with a source other than flat or MCont the moderator
+ * and the full look-ahead); the indices of those it keeps are appended to
+ * a.keep (warp_list_add) */
 template <int MODE>
 __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
   const bool speed = a.src.kind == RAMP_SRC_FLAT || a.src.kind == RAMP_SRC_CONT;
-  /* the run's per-chopper constants for the speed look-ahead, once per CTA */
-  __shared__ SpeedRun run;
-  __shared__ int blocked[SPEED_RUN_MAX];
-  speed_run_setup(&run, blocked, speed, a.comps, a.cull, a.src.p);
+  __shared__ SpeedTab tab;
+  if (speed) speed_tab_load(&tab, adjoint_speed_tab(a));
   const int lane = threadIdx.x & 31;
   __shared__ uint32_t stage[256 / 32][64];
   int held = 0;
@@ -92,7 +106,7 @@ __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
       if (speed) {
         n.sb = (float)seed + 0.0f;      /* generate's first draw and speed */
         const float E_val = a.src.p[5] + (a.src.p[6] - a.src.p[5]) * draw(n, r);
-        kept = !speed_run_blocks(run, rsqrtf(E_val) * (1.0f / RC_SE2V));
+        kept = !speed_tab_blocks(tab, rsqrtf(E_val) * (1.0f / RC_SE2V));
       } else {
         generate<TallyOnly, true, false>(a.src, n, 0.0f, a.num_sim, seed, r);
         kept = !chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t);
@@ -128,6 +142,8 @@ cudaError_t launch_adjoint(const AdjointArgs& a, int grid, int passes, cudaStrea
     if (a.cull > 0) {          /* keep, then trace the kept neutrons */
       e = cudaMemsetAsync(a.keep_count, 0, sizeof(unsigned long long), s);
       if (e != cudaSuccess) return e;
+      if (a.src.kind == RAMP_SRC_FLAT || a.src.kind == RAMP_SRC_CONT)
+        k_adjoint_table<<<SPEED_CELLS / 256, 256, 0, s>>>(a);
       if (a.rng.mode == 0) {
         k_adjoint_keep<0><<<grid, 256, 0, s>>>(a);
         if (t) k_adjoint_record<0, true, true><<<grid, 256, 0, s>>>(a);

@@ -58,31 +58,7 @@ __global__ void __launch_bounds__(256) k_speed_table(const FusedArgs a) {
   if (dst == nullptr) return;
   __shared__ SpeedTab T;
   __shared__ int blocked[SPEED_RUN_MAX];
-  speed_run_setup(&T.run, blocked, true, V->comps, a.cull, V->src.p);
-  if (threadIdx.x == 0) {
-    const float e_lo = fminf(V->src.p[5], V->src.p[6]), e_hi = fmaxf(V->src.p[5], V->src.p[6]);
-    if (e_lo > 0.0f)
-      speed_tab_range(&T, rsqrtf(e_hi) * (1.0f / RC_SE2V) * (1.0f - 1e-5f),
-                      rsqrtf(e_lo) * (1.0f / RC_SE2V) * (1.0f + 1e-5f));
-    else
-      speed_tab_range(&T, 0.0f, 0.0f);
-  }
-  __syncthreads();
-  const int c = (int)blockIdx.x * (int)blockDim.x + (int)threadIdx.x;
-  if (c < SPEED_CELLS) {
-    int v = SPEED_MIXED;
-    if (T.ncell > 0) {
-      float lo, hi;
-      speed_cell_bounds(T.iv0, T.w, c, &lo, &hi);
-      v = speed_cell_verdict(T.run, lo, hi);
-    }
-    reinterpret_cast<uint8_t*>(dst)[offsetof(SpeedTab, cell) + c] = (uint8_t)v;
-  }
-  if (blockIdx.x == 0) {
-    const uint32_t* w = reinterpret_cast<const uint32_t*>(&T);
-    for (int k = threadIdx.x; k < (int)(offsetof(SpeedTab, cell) / 4); k += blockDim.x)
-      dst[k] = w[k];
-  }
+  speed_tab_build(dst, &T, blocked, V->comps, a.cull, V->src.p, (int)blockIdx.x);
 }
 
 /* 1 / sqrt(x), the PTX approximation (relative error below 2^-22): the
@@ -151,9 +127,7 @@ __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
   __shared__ SpeedTab tab;
   const uint32_t* const tsrc = speed_tab_slot<BATCHED>(a, V);
   if (tsrc != nullptr) {
-    uint32_t* w = reinterpret_cast<uint32_t*>(&tab);
-    for (int k = threadIdx.x; k < SPEED_TAB_WORDS; k += blockDim.x) w[k] = tsrc[k];
-    __syncthreads();
+    speed_tab_load(&tab, tsrc);
   } else {
     __shared__ int blocked[SPEED_RUN_MAX];
     speed_run_setup(&tab.run, blocked, speed, V->comps, a.cull, src.p);

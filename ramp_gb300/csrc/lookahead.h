@@ -406,6 +406,51 @@ __device__ __forceinline__ void speed_run_setup(SpeedRun* R, int* blocked, bool 
   if (threadIdx.x == 0 && nq > 1) speed_run_sort(R, blocked);
   __syncthreads();
 }
+
+/* One CTA's share of a speed table written to dst (SPEED_TAB_WORDS words):
+ * SPEED_CELLS / blockDim.x CTAs, CTA `cta` deciding cells [cta blockDim.x,
+ * (cta + 1) blockDim.x) and CTA 0 also writing the run and the cell
+ * layout; T and blocked in shared memory.  The run is the one at component
+ * 0 (nl components) for a flat or MCont source with parameters p; the
+ * cells cover 1 / speed of the source's energy range (flat_mod.cl,
+ * cont_mod.cl:36: v = SE2V sqrt(E), E uniform in [E_min, E_max]) widened
+ * by 1e-5 of it. */
+__device__ __forceinline__ void speed_tab_build(uint32_t* dst, SpeedTab* T, int* blocked,
+                                                const CompDev* comps, int nl, const float* p,
+                                                int cta) {
+  speed_run_setup(&T->run, blocked, true, comps, nl, p);
+  if (threadIdx.x == 0) {
+    const float e_lo = fminf(p[5], p[6]), e_hi = fmaxf(p[5], p[6]);
+    if (e_lo > 0.0f)
+      speed_tab_range(T, rsqrtf(e_hi) * (1.0f / RC_SE2V) * (1.0f - 1e-5f),
+                      rsqrtf(e_lo) * (1.0f / RC_SE2V) * (1.0f + 1e-5f));
+    else
+      speed_tab_range(T, 0.0f, 0.0f);
+  }
+  __syncthreads();
+  const int c = cta * (int)blockDim.x + (int)threadIdx.x;
+  if (c < SPEED_CELLS) {
+    int v = SPEED_MIXED;
+    if (T->ncell > 0) {
+      float lo, hi;
+      speed_cell_bounds(T->iv0, T->w, c, &lo, &hi);
+      v = speed_cell_verdict(T->run, lo, hi);
+    }
+    reinterpret_cast<uint8_t*>(dst)[offsetof(SpeedTab, cell) + c] = (uint8_t)v;
+  }
+  if (cta == 0) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(T);
+    for (int k = threadIdx.x; k < (int)(offsetof(SpeedTab, cell) / 4); k += blockDim.x)
+      dst[k] = w[k];
+  }
+}
+
+/* a speed table from dst into shared memory T, every thread of the CTA */
+__device__ __forceinline__ void speed_tab_load(SpeedTab* T, const uint32_t* src) {
+  uint32_t* w = reinterpret_cast<uint32_t*>(T);
+  for (int k = threadIdx.x; k < SPEED_TAB_WORDS; k += blockDim.x) w[k] = src[k];
+  __syncthreads();
+}
 #endif
 
 #endif /* RAMP_LOOKAHEAD_H */
