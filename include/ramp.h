@@ -491,10 +491,13 @@ int ramp_plan_set_survivors(RampPlan* p, void* buf, int64_t bytes);
  * z axis (pos x = y = 0), with a z-normal GPlane and restore_neutron 0,
  * non-overlapping at non-decreasing z: straight SGuides (w1 = w2, h1 = h2)
  * and SChoppers in any order, up to the last chopper before the first
- * component that is neither.  From a neutron's state before such a run,
- * the time and place it meets each component's plane follow within tight
- * bounds (vz does not change along it; the guides fold the transverse
- * motion at their walls).                                                 */
+ * component that is neither; then, when the component right after that
+ * chopper is an on-axis, unrotated GCylinderExt with restore_neutron 0
+ * starting beyond it, that cylinder as the run's target (a neutron whose
+ * line certainly misses its box dies there).  From a neutron's state
+ * before such a run, the time and place it meets each component's plane
+ * follow within tight bounds (vz does not change along it; the guides fold
+ * the transverse motion at their walls).                                  */
 int ramp_chopper_run(const RampComp* comps, int n_comps, const RampBlock* blocks, int n_blocks,
                      int k);
 

@@ -644,7 +644,10 @@ static bool on_axis_plane(const RampComp& c) {
 
 /* length of the run of on-axis components at k: straight guides and disk
  * choppers in any order, non-overlapping at non-decreasing z, up to the
- * last chopper before the first component that is neither (0: no chopper) */
+ * last chopper before the first component that is neither (0: no
+ * chopper); when the component right after that chopper is an on-axis,
+ * unrotated GCylinderExt without restore that starts beyond it, the run
+ * takes it as its target (its last component) */
 static int chopper_run(const RampComp* comps, int nc, const RampBlock* blocks, int nb, int k) {
   if (!comps || !blocks || k < 0 || k >= nc) return 0;
   int end = -1;
@@ -674,7 +677,16 @@ static int chopper_run(const RampComp* comps, int nc, const RampBlock* blocks, i
       break;
     }
   }
-  return last >= 0 ? last - k + 1 : 0;
+  if (last < 0) return 0;
+  if (last + 1 < end) {
+    const RampComp& c = comps[last + 1];
+    if (c.geom == RAMP_G_CYL_EXT && c.restore == 0 && c.rot[0] == 0.0f && c.rot[1] == 0.0f &&
+        c.rot[2] == 0.0f && c.pos[0] == 0.0f && c.pos[1] == 0.0f && std::isfinite(c.pos[2]) &&
+        c.gp[0] > 0.0f && std::isfinite(c.gp[0]) && c.gp[1] > 0.0f && std::isfinite(c.gp[1]) &&
+        c.pos[2] - c.gp[0] >= comps[last].pos[2])
+      return last - k + 2;
+  }
+  return last - k + 1;
 }
 
 /* the launch's stage split: RampTune.cull (split before component

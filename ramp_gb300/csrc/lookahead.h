@@ -12,7 +12,9 @@
  * block, each unrotated, centred on the z axis (x = y = 0), with a z-normal
  * GPlane and no restore, at non-decreasing z without overlaps: straight
  * SGuides (w1 = w2, h1 = h2) and SChopper components in any order, ending
- * with a chopper.  Why the bounds hold there:
+ * with a chopper, and then, where the next component is one, an on-axis
+ * unrotated GCylinderExt without restore as its target.  Why the bounds
+ * hold there:
  *  - time.  Nothing in the run changes vz: the frame transforms are the
  *    identity on velocities; a straight guide's wall normals have no z
  *    component (guide.cl:39-43 with w1 = w2: ww = hh = 0, so the bounce
@@ -30,6 +32,9 @@
  *    exit are allowed (a later guide then ends the look-ahead).
  *  - a guide entrance (plane.cl:3-52): a neutron whose line meets the plane
  *    outside its rectangle by more than the slack misses it and dies.
+ *  - the target (cylinder_ext.cl:3-53): the cylinder accepts a neutron
+ *    only where its line crosses the cylinder's box; one it does not
+ *    accept dies there (terminate.cl: no intersection, no restore).
  *  - a chopper (chopper.cl:4-59): the neutron passes only if the distance
  *    from freq (t - |phase|) + e - atan2(x, y + R), e in [-jitter, jitter),
  *    to the nearest multiple of 2 pi / n_slits is at most
@@ -40,9 +45,10 @@
  * plus a micrometre of z per bounce; position: 2e-5 m plus 4e-6 of the
  * guide path per bounce so far; angle: 1e-4 rad plus 1e-6 relative, which
  * also covers the truncated atan series and products with reciprocals).  A
- * neutron outside the assumptions (vz <= 0, at a guide entrance within the
- * slack of a wall, y + R not clearly positive, angles beyond 1e4 rad) gets
- * no claim from there on.  A neutron that would instead miss a plane,
+ * neutron outside the assumptions (vz <= 0, within the slack of a wall at
+ * the entrance of a guide whose entrance plane is wider than the guide, y
+ * + R not clearly positive, angles beyond 1e4 rad) gets no claim from
+ * there on.  A neutron that would instead miss a plane,
  * leave a guide at zero weight or exceed its bounce limit dies in the
  * reference as well, so with only tallies observable it may be retired
  * either way.
@@ -113,14 +119,41 @@ LA_FN bool chopper_run_blocks(const CompDev* comps, int k, int nl, float x, floa
     const float xc = x0 + mx * dz, yc = y0 + my * dz;
     const float exc = ex + (ux + 4e-6f * nb * fabsf(sx)) * fabsf(dz) + 1e-6f * fabsf(xc);
     const float eyc = ey + (uy + 4e-6f * nb * fabsf(sy)) * fabsf(dz) + 1e-6f * fabsf(yc);
+    if (c.geom == RAMP_G_CYL_EXT) {
+      /* the run's target, after its last chopper: a cylinder of radius r
+         about the y axis through (0, 0, zc), height h.  It accepts a
+         neutron only where its line meets x^2 + (z - zc)^2 < r^2 with the
+         exit point at |y| < h/2 (cylinder_ext.cl:3-53), so within the box
+         |x| < r, |y| < h/2, |z - zc| <= r; one whose line certainly stays
+         outside that box over z in [zc - r, zc + r] dies there */
+      const float r = c.gp[0], hh = 0.5f * c.gp[1];
+      float xlo = 1e30f, xhi = -1e30f, ylo = 1e30f, yhi = -1e30f;
+      for (int e = 0; e < 2; ++e) {
+        const float ze = e ? zc + r : zc - r;
+        const float de = ze - z0;
+        const float xe = x0 + mx * de, ye = y0 + my * de;
+        const float exe = ex + (ux + 4e-6f * nb * fabsf(sx)) * fabsf(de) + 1e-6f * fabsf(xe);
+        const float eye = ey + (uy + 4e-6f * nb * fabsf(sy)) * fabsf(de) + 1e-6f * fabsf(ye);
+        xlo = fminf(xlo, xe - exe); xhi = fmaxf(xhi, xe + exe);
+        ylo = fminf(ylo, ye - eye); yhi = fmaxf(yhi, ye + eye);
+      }
+      return xlo >= r || xhi <= -r || ylo >= hh || yhi <= -hh;
+    }
     if (c.scat == RAMP_S_GUIDE) {
       /* a neutron that certainly misses the entrance plane dies there
          (plane.cl:3-52: |x| < width/2 and |y| < height/2 to hit it) */
       if (fabsf(xc) - exc >= 0.5f * c.gp[0] || fabsf(yc) - eyc >= 0.5f * c.gp[1]) return true;
-      /* folding needs known slopes and an entry inside the walls */
+      /* folding needs known slopes and an entry inside the walls.  With an
+         entrance no wider than the guide every neutron the plane accepts
+         starts inside them (|x| < width/2 <= a); one within the slack of a
+         wall folds there too: the bounce loop takes the wall it flies
+         towards at once, whatever the sign of that time (guide.cl:66-85),
+         and the fold moves the point by less than the slack */
       const float a = 0.5f * c.sp[0], b = 0.5f * c.sp[1], l = c.sp[4];
       if (ux > 0.0f || uy > 0.0f) return false;
-      if (!(fabsf(xc) < a - exc) || !(fabsf(yc) < b - eyc)) return false;
+      if ((0.5f * c.gp[0] > a || 0.5f * c.gp[1] > b) &&
+          (!(fabsf(xc) < a - exc) || !(fabsf(yc) < b - eyc)))
+        return false;
       const float ia = 1.0f / a, ib = 1.0f / b;
       const float dux = mx * l, duy = my * l;
       const float nbx = floorf(fabsf(dux) * (0.5f * ia)) + 2.0f;
@@ -217,6 +250,7 @@ LA_FN void speed_run_prepare(const CompDev* comps, int k, int nl, float p0, floa
       z0 = zc + l;
       continue;
     }
+    if (c.scat != RAMP_S_CHOPPER) continue;   /* the run's target: no speed bound */
     /* a disk chopper (chopper.cl:4-59): the time in [zc / v, zc / vz_min]
        widened by 1e-5 of it and a micrometre of z per bounce, the angle
        atan2(x, y + R) within +-atan(Xc / (R - Yc)) */
