@@ -129,9 +129,16 @@ DI void fused_tail(const FusedArgs& a) {
                          FUSED_WARP_TASK;
     if (used < n_items) n_items = used;
   }
-  /* items per grab: about two grabs per warp of the grid, at most one item
-     per lane */
-  const int64_t per = n_items / (2 * (int64_t)gridDim.x * (blockDim.x >> 5));
+  /* items per grab: about two grabs per warp of the grid, or (after the
+     lean stage A of one instrument, whose survivors are counted) enough
+     items for about 32 survivors when that is more; at most one item per
+     lane */
+  int64_t per = n_items / (2 * (int64_t)gridDim.x * (blockDim.x >> 5));
+  if (!FINISH && !BATCHED && KS == 0 && K == 0 && a.cull > 0) {
+    const int64_t tot = (int64_t)a.st->surv;
+    const int64_t fill = tot > 0 ? (32 * n_items + tot - 1) / tot : SURV_GROUP;
+    if (fill > per) per = fill;
+  }
   const int G = per < 1 ? 1 : (per > SURV_GROUP ? SURV_GROUP : (int)per);
   const CompDev* __restrict__ comps = V->comps;
   unsigned long long* const q_b = (FINISH ? a.workq_c : a.workq_b) + (BATCHED ? var : 0);
@@ -486,6 +493,9 @@ k_fused(const FusedArgs a) {
       }
       if (STAGE_A && lane == 0 && item0 + (int64_t)t < a.surv_items)
         a.surv_cnt[item0 + t] = (uint32_t)kept;
+      /* the lean stage A's survivors in all (stage B sizes its claims by it) */
+      if (PHASE == 3 && !BATCHED && lane == 0 && kept > 0)
+        atomicAdd(&a.st->surv, (unsigned long long)kept);
     }
     if (priv) {                   /* merge the private tallies, nonzero bins only */
       __syncthreads();
