@@ -28,11 +28,14 @@ pytestmark = pytest.mark.gpu
     ("let_like.json", dict(Ei=3.7), 1_000_000,
      {"split": 0, "cull": 1, "block": 128, "blocks_per_sm": 8}, "reference"),
     ("let_like_misis.json", dict(Ei=3.7), 400_000, {"split": 0, "cull": 1}, "reference"),
-    ("let_like.json", dict(Ei=3.7), 1_000_003, {"split": 0, "cull": 1}, "reference")])
+    ("let_like.json", dict(Ei=3.7), 1_000_003, {"split": 0, "cull": 1}, "reference"),
+    ("let_like.json", dict(Ei=3.7), 700, {"split": 0, "cull": 1}, "reference")])
 def test_fused_cull_matches_oracle(cuda_lib, fn, kw, N, tune, rng):
     """Split before guide 1 (stage A: the moderator alone) or before
-    chopper 1, with the look-ahead; also with the MISIS source and with a
-    history count that is not a whole number of work items."""
+    chopper 1, with the look-ahead; also with the MISIS source, with a
+    history count that is not a whole number of work items, and with too
+    few histories for the speed table (the keep pass prepares the run
+    itself and applies the per-chopper test to every history)."""
     kws = (I.let_like_misis_kwargs if "misis" in fn else I.let_like_kwargs)(**kw)
     gi, ci, r = pair(I.path(fn), kws, N, path="fused", rng=rng, tune=tune)
     tallies_close(gi, ci)
@@ -52,10 +55,12 @@ def test_fused_cull_with_carry_buffers(cuda_lib):
 @pytest.mark.parametrize("tune", [{"split": 0, "cull": 1},
                                   {"split": 0, "cull": 1, "streams": 4}])
 def test_batched_cull_matches_single_runs(cuda_lib, tune):
-    """Variants with different Ei (so different chopper phases): one launch
-    with a grid row per variant, or per-variant launches on streams."""
-    variants = [I.let_like_kwargs(Ei=3.7), I.let_like_kwargs(Ei=8.0), I.let_like_kwargs(Ei=2.5)]
-    counts, seeds = [300_000, 123_457, 200_003], [11, 2222, 4000]
+    """Variants with different Ei (so different chopper phases), one of
+    them too short for a speed table: one launch with a grid row per
+    variant, or per-variant launches on streams."""
+    variants = [I.let_like_kwargs(Ei=3.7), I.let_like_kwargs(Ei=8.0), I.let_like_kwargs(Ei=2.5),
+                I.let_like_kwargs(Ei=5.0)]
+    counts, seeds = [300_000, 123_457, 200_003, 900], [11, 2222, 4000, 77]
     B = BatchedInstrument(I.path("let_like.json"), variants, ctx="cuda")
     B.execute(counts, rng="native", seeds=seeds, tune=tune)
     torch.cuda.synchronize()
@@ -132,11 +137,13 @@ def test_caller_survivor_buffer_reuse_and_fallback(cuda_lib):
     tallies_close(gi, ci)
 
 
-@pytest.mark.parametrize("seed", [3, 6, 11])
-def test_fused_cull_on_random_runs_matches_oracle(cuda_lib, tmp_path, seed):
+@pytest.mark.parametrize("seed,N", [(3, 1_000_000), (6, 1_000_000), (11, 1_000_000),
+                                    (20, 1000), (11, 1000)])
+def test_fused_cull_on_random_runs_matches_oracle(cuda_lib, tmp_path, seed, N):
     """Random guide and chopper runs (the generator of the CPU soundness
     test) ending in time-of-flight and x-y monitors: the fused launch with
-    the look-ahead equals the oracle's tallies."""
+    the look-ahead equals the oracle's tallies (at 1000 histories without
+    a speed table: the keep pass prepares the run itself)."""
     import numpy as np
     from test_chopper_lookahead import _random_run
     body, n = _random_run(np.random.default_rng(1000 + seed))
@@ -149,6 +156,6 @@ def test_fused_cull_on_random_runs_matches_oracle(cuda_lib, tmp_path, seed):
              '"axis1_var": "x", "axis2_var": "y"}}')
     fn = tmp_path / "rand_mon.json"
     fn.write_text('{"all": {"linear": true,%s}}' % body)
-    gi, ci, r = pair(str(fn), {}, 1_000_000, path="fused", tune={"split": 0, "cull": 1})
+    gi, ci, r = pair(str(fn), {}, N, path="fused", tune={"split": 0, "cull": 1})
     tallies_close(gi, ci)
     assert float(sum(t.abs().sum() for t in ci.tallies())) > 0
