@@ -25,18 +25,24 @@ class BatchedInstrument:
         base = self.instruments[0]
         self.device = base.device
         self.queue = queue
-        kinds = self._kinds(base)
-        for k, inst in enumerate(self.instruments[1:], 1):
-            if self._kinds(inst) != kinds:
-                raise ValueError("variant %d has a different component structure" % k)
+        # the variants' descriptors, built once here (a variant's parameters
+        # are fixed at construction, as an Instrument's plan is) and kept,
+        # with the host tables they point to, for every execute
         self._keep = []
-
-    @staticmethod
-    def _kinds(inst):
-        src, carr, nc, barr, nb = inst.descriptors([])
-        return ([(carr[j].geom, carr[j].scat) for j in range(nc)],
-                [(barr[k].first, barr[k].count, barr[k].linear, barr[k].multi)
-                 for k in range(nb)])
+        self._variants = (_abi.RampVariant * len(self.instruments))()
+        kinds = None
+        for k, inst in enumerate(self.instruments):
+            src, carr, nc, barr, nb = inst.descriptors(self._keep)
+            self._keep.append(carr)
+            kk = ([(carr[j].geom, carr[j].scat) for j in range(nc)],
+                  [(barr[b].first, barr[b].count, barr[b].linear, barr[b].multi)
+                   for b in range(nb)])
+            if kinds is None:
+                kinds = kk
+            elif kk != kinds:
+                raise ValueError("variant %d has a different component structure" % k)
+            self._variants[k].comps = ctypes.cast(carr, ctypes.POINTER(_abi.RampComp))
+            self._variants[k].source = src
 
     def execute(self, counts, rng="native", run_seed=0, seeds=None, tune=None):
         """Trace counts[v] histories of variant v, all in one launch."""
@@ -45,22 +51,16 @@ class BatchedInstrument:
         base = self.instruments[0]
         lib = base._lib()
         plan = base.plan()
-        keep = []
         nv = len(self.instruments)
-        variants = (_abi.RampVariant * nv)()
+        variants = self._variants
         chunk = base.chunk_size()
         for v, inst in enumerate(self.instruments):
             n = int(counts[v])
             if n > chunk:
                 raise ValueError("variant %d: %d histories exceed one chunk (%d)" % (v, n, chunk))
-            src, carr, nc, barr, nb = inst.descriptors(keep)
-            keep.append(carr)
-            variants[v].comps = ctypes.cast(carr, ctypes.POINTER(_abi.RampComp))
-            variants[v].source = src
             variants[v].n = n
             variants[v].num_sim = max(n, 1)
             variants[v].seed = int(seeds[v]) if seeds is not None else inst.source.next_seed()
-        self._keep = keep
         rngd = _abi.RampRng()
         rngd.mode = {"reference": 0, "native": 1}[rng]
         rngd.run_seed = int(run_seed) & 0xffffffff
