@@ -88,8 +88,9 @@ struct RampPlan {
   std::vector<RampBlock> blocks;
   RampBlock* blocks_dev = nullptr;
   StatusDev* status = nullptr;
-  std::vector<void*> allocs;
+  std::vector<std::pair<void*, size_t>> allocs;   /* small buffers (plan_alloc) */
   int sm_count = 0;
+  int device = 0;                    /* the device the plan's buffers live on */
   BatchCache batch;
   std::map<TabKey, std::pair<void*, void*>> tabs;
   std::vector<CompDev> adj_host;     /* descriptors of the last adjoint   */
@@ -194,10 +195,60 @@ static void guide_aux(const RampComp& c, float* aux) {
   aux[15] = (m <= 0 || Qc <= 0 || R0 <= 0) ? 1.0f : 0.0f;
 }
 
-static int upload(const void* host, size_t bytes, void** dev, std::vector<void*>& owner) {
+/* Device memory of plans' small buffers (descriptors, tables, status),
+ * kept by size in a per-process pool once their plan is destroyed and
+ * handed to the next plan: an Instrument built per run would otherwise
+ * pay a cudaMalloc and a cudaFree per buffer.  ramp_plan_destroy waits
+ * for the device before it returns buffers here, as cudaFree would, so
+ * no kernel still reads one when it is reused.  At most 64 MB is kept. */
+static std::mutex g_pool_mu;
+static std::multimap<std::pair<int, size_t>, void*> g_pool;   /* (device, bytes) */
+static size_t g_pool_bytes = 0;
+static const size_t POOL_MAX = (size_t)64 << 20;
+
+static size_t pool_round(size_t bytes) { return ((bytes > 0 ? bytes : 16) + 255) & ~(size_t)255; }
+
+/* on the current device */
+static cudaError_t plan_alloc(size_t bytes, void** dev,
+                              std::vector<std::pair<void*, size_t>>& owner) {
+  const size_t b = pool_round(bytes);
+  int d = 0;
+  cudaError_t e = cudaGetDevice(&d);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto it = g_pool.find(std::make_pair(d, b));
+    if (it != g_pool.end()) {
+      *dev = it->second;
+      g_pool.erase(it);
+      g_pool_bytes -= b;
+      owner.push_back(std::make_pair(*dev, b));
+      return cudaSuccess;
+    }
+  }
+  e = cudaMalloc(dev, b);
+  if (e == cudaSuccess) owner.push_back(std::make_pair(*dev, b));
+  return e;
+}
+
+/* the buffers of a plan on device d, no longer read by any kernel */
+static void plan_release(int d, std::vector<std::pair<void*, size_t>>& owner) {
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  for (auto& a : owner) {
+    if (g_pool_bytes + a.second <= POOL_MAX) {
+      g_pool.insert(std::make_pair(std::make_pair(d, a.second), a.first));
+      g_pool_bytes += a.second;
+    } else {
+      cudaFree(a.first);
+    }
+  }
+  owner.clear();
+}
+
+static int upload(const void* host, size_t bytes, void** dev,
+                  std::vector<std::pair<void*, size_t>>& owner) {
   void* p = nullptr;
-  CK(cudaMalloc(&p, bytes > 0 ? bytes : 16));
-  owner.push_back(p);
+  CK(plan_alloc(bytes, &p, owner));
   if (bytes) CK(cudaMemcpy(p, host, bytes, cudaMemcpyHostToDevice));
   *dev = p;
   return RAMP_OK;
@@ -457,7 +508,14 @@ int ramp_last_error(char* buf, int len) {
 
 int ramp_plan_destroy(RampPlan* p) {
   if (!p) return RAMP_OK;
-  for (void* a : p->allocs) cudaFree(a);
+  if (!p->allocs.empty()) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (prev != p->device) cudaSetDevice(p->device);
+    cudaDeviceSynchronize();      /* as cudaFree would: no kernel reads them any more */
+    plan_release(p->device, p->allocs);
+    if (prev != p->device) cudaSetDevice(prev);
+  }
   if (p->batch.comps_dev) cudaFree(p->batch.comps_dev);
   if (p->batch.vars_dev) cudaFree(p->batch.vars_dev);
   if (p->surv && p->surv_owned) cudaFree(p->surv);
@@ -483,6 +541,7 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
   }
   *out = nullptr;
   RampPlan* p = new RampPlan();
+  cudaGetDevice(&p->device);
   p->src_in = *source;
   int rc = make_src(p, *source, p->src);
   if (rc) { ramp_plan_destroy(p); return rc; }   /* frees any table it uploaded */
@@ -527,9 +586,7 @@ int ramp_plan_create(const RampSource* source, const RampComp* comps, int n_comp
   rc = upload(&zero, sizeof(zero), &d, p->allocs);
   if (rc) { ramp_plan_destroy(p); return rc; }
   p->status = (StatusDev*)d;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, p->device);
   if (p->sm_count <= 0) p->sm_count = 1;
   *out = p;
   return RAMP_OK;
@@ -754,14 +811,13 @@ static int priv_descriptors(RampPlan* p, cudaStream_t s, int32_t* floats) {
   if (used == 0) return RAMP_OK;
   if (!p->priv_dev) {
     void* d = nullptr;
-    cudaError_t e = cudaMalloc(&d, c.size() * sizeof(CompDev));
+    cudaError_t e = plan_alloc(c.size() * sizeof(CompDev), &d, p->allocs);
     if (e != cudaSuccess) {
       cudaGetLastError();
       set_err("private-tally descriptors: %s", cudaGetErrorString(e));
       return RAMP_E_NOMEM;
     }
     p->priv_dev = (CompDev*)d;
-    p->allocs.push_back(d);
   }
   /* pageable source: the copy is staged before cudaMemcpyAsync returns */
   cudaError_t e = cudaMemcpyAsync(p->priv_dev, c.data(), c.size() * sizeof(CompDev),
