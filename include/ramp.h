@@ -275,9 +275,6 @@ int ramp_last_error(char* buf, int len);
 int ramp_plan_create(const RampSource* source, const RampComp* comps,
                      int n_comps, const RampBlock* blocks, int n_blocks,
                      RampPlan** out);
-/* Waits for the plan's device, then frees the plan; its small device
- * buffers (descriptors, tables, status) go to a per-process pool (at most
- * 64 MB) that the next ramp_plan_create on the same device draws from.   */
 int ramp_plan_destroy(RampPlan* plan);
 
 /* Run linear components [k0, k1) over neutrons [0, n) (each a k_linear
