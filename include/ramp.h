@@ -511,17 +511,17 @@ int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock*
 
 /* Host check (no GPU) of the speed-only bound of the lean stage A: a flat
  * or MCont moderator with parameters source_p (moderator width and
- * height, target width and height, target distance: RampSource.p[0..4]);
- * out[i] = 1 when no neutron of speed speeds[i] (m/s) from it can pass the
- * choppers of the run at component k (the run must start where the
- * moderator's neutrons enter the chain), else 0.  The answers come, as on
- * the device, from a table of cells of 1 / speed (here spread over the
- * given speeds) and, outside its decided cells, the per-chopper test.
- * table_check (may be NULL): [0] the speeds a table cell decided, [1] the
- * speeds where the table's answer differs from the per-chopper test's
- * (0 unless the table is wrong).                                          */
+ * height, target width and height, target distance, E_min, E_max:
+ * RampSource.p[0..6]); out[i] = 1 when no neutron whose energy draw gave
+ * the Threefry word words[i] can pass the choppers of the run at
+ * component k (the run must start where the moderator's neutrons enter
+ * the chain), else 0.  The answers come, as on the device, from a table
+ * of cells of the word and, outside its decided cells, the per-chopper
+ * test.  table_check (may be NULL): [0] the words a table cell decided,
+ * [1] the words where the table's answer differs from the per-chopper
+ * test's (0 unless the table is wrong).                                   */
 int ramp_debug_speed_cull(const RampComp* comps, int n_comps, const RampBlock* blocks,
-                          int n_blocks, int k, const float* source_p, const float* speeds,
+                          int n_blocks, int k, const float* source_p, const uint32_t* words,
                           int64_t n, uint8_t* out, int64_t* table_check);
 
 #ifdef __cplusplus

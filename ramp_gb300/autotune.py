@@ -161,9 +161,10 @@ def chopper_run_start(inst):
 def speed_kept_fraction(inst, n_grid=1 << 20):
     """Fraction of the histories the speed look-ahead of a split launch at
     component 0 keeps (the lean stage A regenerates those): the energies of
-    a flat or MCont moderator are uniform on [E_min, E_max], so this is the
-    share of a uniform energy grid whose speeds ramp_debug_speed_cull does
-    not rule out.  1.0 with another source or without a run at component 0."""
+    a flat or MCont moderator come from one uniform Threefry word each, so
+    this is the share of an even grid of words whose energies
+    ramp_debug_speed_cull does not rule out.  1.0 with another source or
+    without a run at component 0."""
     import numpy as np
     keep = []
     src, carr, nc, barr, nb = inst.descriptors(keep)
@@ -171,13 +172,12 @@ def speed_kept_fraction(inst, n_grid=1 << 20):
     if src.kind not in (_abi.SRC_FLAT, _abi.SRC_CONT) or nc == 0 or \
             lib.ramp_chopper_run(ctypes.addressof(carr), nc, ctypes.addressof(barr), nb, 0) <= 0:
         return 1.0
-    e0, e1 = float(src.p[5]), float(src.p[6])
-    E = np.float32(e0) + np.float32(e1 - e0) * ((np.arange(n_grid, dtype=np.float32) + 0.5) / n_grid)
-    v = np.ascontiguousarray(np.float32(437.393377) * np.sqrt(E), dtype=np.float32)
-    p = np.ascontiguousarray(np.array(src.p[0:5], dtype=np.float32))
+    words = np.ascontiguousarray((np.arange(n_grid, dtype=np.uint64) * (1 << 31) // n_grid
+                                  + (1 << 30) // n_grid).astype(np.uint32))
+    p = np.ascontiguousarray(np.array(src.p[0:7], dtype=np.float32))
     out = np.zeros(n_grid, np.uint8)
     _abi.check(lib, lib.ramp_debug_speed_cull(ctypes.addressof(carr), nc, ctypes.addressof(barr),
-                                              nb, 0, p.ctypes.data, v.ctypes.data, n_grid,
+                                              nb, 0, p.ctypes.data, words.ctypes.data, n_grid,
                                               out.ctypes.data, None), "ramp_debug_speed_cull")
     return float(1.0 - out.mean())
 

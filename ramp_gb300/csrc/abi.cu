@@ -1566,9 +1566,9 @@ int ramp_debug_chopper_cull(const RampComp* comps, int n_comps, const RampBlock*
 }
 
 int ramp_debug_speed_cull(const RampComp* comps, int n_comps, const RampBlock* blocks,
-                          int n_blocks, int k, const float* source_p, const float* speeds,
+                          int n_blocks, int k, const float* source_p, const uint32_t* words,
                           int64_t n, uint8_t* out, int64_t* table_check) {
-  if (!comps || n_comps <= 0 || !source_p || n < 0 || (n > 0 && (!speeds || !out))) {
+  if (!comps || n_comps <= 0 || !source_p || n < 0 || (n > 0 && (!words || !out))) {
     set_err("ramp_debug_speed_cull: bad arguments");
     return RAMP_E_INVALID;
   }
@@ -1593,51 +1593,35 @@ int ramp_debug_speed_cull(const RampComp* comps, int n_comps, const RampBlock* b
   SpeedRun& run = T->run;
   speed_run_prepare(d.data(), k, nl, source_p[0], source_p[1], source_p[2], source_p[3],
                     source_p[4], &run);
+  const float e0 = source_p[5], de = source_p[6] - source_p[5];
   /* the choppers ordered as the device orders them, by how many of a
-     sample of speeds (here the first 256 given) each one blocks */
+     sample of speeds (here those of the first 256 words) each one blocks */
   int blocked[SPEED_RUN_MAX] = {0};
-  for (int64_t i = 0; i < n && i < 256; ++i)
+  for (int64_t i = 0; i < n && i < 256; ++i) {
+    const float iv = speed_iv_of_word(words[i], e0, de);
     for (int q = 0; q < run.n; ++q)
-      if (speeds[i] > 0.0f && speed_chopper_blocks(run, q, 1.0f / speeds[i])) ++blocked[q];
-  speed_run_sort(&run, blocked);
-  /* the device's speed table, its cells spread over the given speeds */
-  float iv_a = 0.0f, iv_b = 0.0f;
-  for (int64_t i = 0; i < n; ++i) {
-    if (!(speeds[i] > 0.0f)) continue;
-    const float iv = 1.0f / speeds[i];
-    if (iv_a == 0.0f || iv < iv_a) iv_a = iv;
-    if (iv > iv_b) iv_b = iv;
+      if (iv > 0.0f && iv < 1e30f && speed_chopper_blocks(run, q, iv)) ++blocked[q];
   }
-  speed_tab_range(T.get(), iv_a, iv_b);
+  speed_run_sort(&run, blocked);
+  /* the device's speed table */
+  speed_tab_range(T.get(), e0, de);
   for (int c = 0; c < T->ncell; ++c) {
     float lo, hi;
-    speed_cell_bounds(T->iv0, T->w, c, &lo, &hi);
+    speed_word_cell(c, e0, de, &lo, &hi);
     T->cell[c] = (uint8_t)speed_cell_verdict(run, lo, hi);
   }
-  int64_t nm = 0;
+  int64_t nd = 0, nm = 0;
   for (int64_t i = 0; i < n; ++i) {
-    bool by_table = false, by_run = false;
-    if (speeds[i] > 0.0f) {
-      const float iv = 1.0f / speeds[i];
-      by_table = speed_tab_blocks(*T, iv);
-      by_run = speed_run_blocks(run, iv);
-    }
+    const bool by_table = speed_tab_blocks(*T, words[i]);
+    const bool by_run = speed_run_blocks(run, speed_iv_of_word(words[i], e0, de));
     out[i] = by_table ? 1 : 0;
     nm += by_table != by_run;
+    if (T->ncell > 0 &&
+        T->cell[(words[i] >> SPEED_CELL_SHIFT) & (SPEED_CELLS - 1)] != SPEED_MIXED)
+      ++nd;
   }
   if (table_check) {
-    int64_t dec = 0;
-    for (int64_t i = 0; i < n; ++i) {
-      if (!(speeds[i] > 0.0f) || T->ncell == 0) continue;
-      const float iv = 1.0f / speeds[i];
-      const float f = (iv - T->iv0) * T->iw;
-      if (!(f >= 0.0f && f < (float)T->ncell)) continue;
-      const int c = (int)f;
-      float lo, hi;
-      speed_cell_bounds(T->iv0, T->w, c, &lo, &hi);
-      if (iv >= lo && iv <= hi && T->cell[c] != SPEED_MIXED) ++dec;
-    }
-    table_check[0] = dec;
+    table_check[0] = nd;
     table_check[1] = nm;
   }
   return RAMP_OK;

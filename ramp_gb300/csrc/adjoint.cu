@@ -104,9 +104,8 @@ __global__ void __launch_bounds__(256) k_adjoint_keep(const AdjointArgs a) {
       rng_init(r, MODE, a.rng.tid_base + (uint32_t)i, 0u, a.rng.run_seed, a.rng.one);
       const int32_t seed = a.rng.seed_dev ? *a.rng.seed_dev : a.seed;
       if (speed) {
-        n.sb = (float)seed + 0.0f;      /* generate's first draw and speed */
-        const float E_val = a.src.p[5] + (a.src.p[6] - a.src.p[5]) * draw(n, r);
-        kept = !speed_tab_blocks(tab, rsqrtf(E_val) * (1.0f / RC_SE2V));
+        n.sb = (float)seed + 0.0f;      /* generate's first draw */
+        kept = !speed_tab_blocks(tab, draw_word(n, r));
       } else {
         generate<TallyOnly, true, false>(a.src, n, 0.0f, a.num_sim, seed, r);
         kept = !chopper_run_blocks(a.comps, 0, a.cull, n.x, n.y, n.z, n.vx, n.vy, n.vz, n.t);

@@ -146,8 +146,9 @@ DI void rng_init(Rng& r, int mode, uint32_t tid, uint32_t variant, uint32_t run_
 }
 
 /* rand() — mcramp/include/rand.h:4-21: counter word 0 is (uint)sb, sb is
- * advanced by one.  Native mode reads word (sb & 3) of block sb >> 2. */
-DI float draw(Nt& n, Rng& r) {
+ * advanced by one.  Native mode reads word (sb & 3) of block sb >> 2.
+ * draw_word gives the Threefry word, draw the number rand() returns. */
+DI uint32_t draw_word(Nt& n, Rng& r) {
   uint32_t c = (uint32_t)n.sb;
   uint32_t x;
   if (r.mode == 0) {
@@ -164,8 +165,9 @@ DI float draw(Nt& n, Rng& r) {
     x = (j == 0) ? r.w0 : (j == 1) ? r.w1 : (j == 2) ? r.w2 : r.w3;
   }
   n.sb += 1.0f;
-  return u01cc(x);
+  return x;
 }
+DI float draw(Nt& n, Rng& r) { return u01cc(draw_word(n, r)); }
 
 /* ------------------------------------------------------------------ */
 /* status                                                               */

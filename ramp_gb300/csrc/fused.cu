@@ -61,14 +61,6 @@ __global__ void __launch_bounds__(256) k_speed_table(const FusedArgs a) {
   speed_tab_build(dst, &T, blocked, V->comps, a.cull, V->src.p, (int)blockIdx.x);
 }
 
-/* 1 / sqrt(x), the PTX approximation (relative error below 2^-22): the
- * speed bound's time slack is 1e-5 of the time */
-DI float rsqrt_approx(float x) {
-  float y;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
 /* the keep pass over histories [0, n) of one variant (index type I: 32-bit
  * when the grid's strides stay below 2^31); `test` false lists every one */
 template <typename I, int MODE>
@@ -78,7 +70,6 @@ DI void keep_histories(const FusedArgs& a, const SrcDev& src, const SpeedTab& ta
   const int lane = threadIdx.x & 31;
   int held = 0;
   const I stride = (I)gridDim.x * (I)blockDim.x;
-  const float e0 = src.p[5], de = src.p[6] - src.p[5];
   for (I base = (I)blockIdx.x * (I)blockDim.x + (I)(threadIdx.x & ~31); base < n;
        base += stride) {                                   /* warp-uniform */
     const I i = base + (I)lane;
@@ -92,8 +83,7 @@ DI void keep_histories(const FusedArgs& a, const SrcDev& src, const SpeedTab& ta
                  a.rng.one);
         Nt nn;
         nn.sb = (float)seed + 0.0f;
-        const float E_val = e0 + de * draw(nn, r);
-        kept = !speed_tab_blocks(tab, rsqrt_approx(E_val) * (1.0f / RC_SE2V));
+        kept = !speed_tab_blocks(tab, draw_word(nn, r));
       }
     }
     warp_list_add(kept, (uint32_t)i, stage, held, kc, keep, (int64_t)n);
@@ -102,8 +92,9 @@ DI void keep_histories(const FusedArgs& a, const SrcDev& src, const SpeedTab& ta
 }
 
 /* Every history's first draw (its energy, hence its speed) is made here
- * and the speed-only bound applied (speed_tab_blocks, with the variant's
- * speed table; without one, speed_run_blocks with the run prepared here);
+ * and the speed-only bound applied (speed_tab_blocks on the draw's word,
+ * with the variant's speed table; without one, speed_run_blocks with the
+ * run prepared here);
  * the indices of the histories that may pass are appended (warp_list_add)
  * to a list in word 18 of the variant's survivor slots (free until a walk
  * uses it), its length in the variant's workq_c.  The lean stage A then
@@ -131,7 +122,10 @@ __global__ void __launch_bounds__(256) k_speed_keep(const FusedArgs a) {
   } else {
     __shared__ int blocked[SPEED_RUN_MAX];
     speed_run_setup(&tab.run, blocked, speed, V->comps, a.cull, src.p);
-    if (threadIdx.x == 0) speed_tab_range(&tab, 0.0f, 0.0f);
+    if (threadIdx.x == 0) {
+      speed_tab_range(&tab, src.p[5], src.p[6] - src.p[5]);
+      tab.ncell = 0;                 /* no cells: every history takes the run */
+    }
     __syncthreads();
   }
   __shared__ uint32_t stage[256 / 32][64];

@@ -310,33 +310,60 @@ LA_FN void speed_run_sort(SpeedRun* R, const int* blocked) {
     }
 }
 
-/* ---- the speed table: verdicts for cells of 1 / speed ------------------
- * speed_chopper_blocks is, for a fixed chopper, a chain of correctly
- * rounded float operations each monotone in its operands (products and
+/* ---- the speed table: verdicts for cells of the energy draw ------------
+ * A flat or MCont moderator draws a neutron's energy first:
+ * E = E_min + (E_max - E_min) u with u the reference's u01 of one Threefry
+ * word x (flat_mod.cl, cont_mod.cl:36; u01fixedpt_closed_closed_32_24 reads
+ * bits 6-30 of x and is non-decreasing in them), and 1 / speed is
+ * 1 / (SE2V sqrt(E)).  A cell is the set of words with the same bits 19-30
+ * (SPEED_CELLS cells); u, E and 1 / speed are each a chain of correctly
+ * rounded operations monotone in those bits, so the 1 / speed of every word
+ * of a cell lies between the values at its two ends.  speed_chopper_blocks
+ * is likewise a chain of monotone operations in 1 / speed (products and
  * sums with constants, min, max, |.| of a monotone value, ceil, floor), so
- * over a cell [lo, hi] of iv every intermediate value lies between bounds
- * taken from its values at lo and hi.  From those bounds a cell gets
- * SPEED_BLOCKED when every iv in it is blocked by one chopper,
- * SPEED_KEPT when no chopper blocks any iv in it, else SPEED_MIXED; a
- * history in a BLOCKED or KEPT cell gets from the table exactly the answer
- * speed_run_blocks would give it, and the others take speed_run_blocks. */
+ * over the cell's range every intermediate value lies between bounds taken
+ * at the range's ends.  From those bounds a cell gets SPEED_BLOCKED when
+ * every 1 / speed in it is blocked by one chopper, SPEED_KEPT when no
+ * chopper blocks any, else SPEED_MIXED; a history in a BLOCKED or KEPT cell
+ * gets from the table exactly the answer speed_run_blocks would give it,
+ * and the others compute their speed and take speed_run_blocks. */
 #define SPEED_CELLS 4096
+#define SPEED_CELL_SHIFT 19         /* cell = bits 19-30 of the word */
 #define SPEED_MIXED 0
 #define SPEED_BLOCKED 1
 #define SPEED_KEPT 2
 
 struct SpeedTab {
   SpeedRun run;                   /* ordered (speed_run_sort) */
-  float iv0, w;                   /* cell c: [iv0 + c w, iv0 + (c + 1) w] */
-  float iw;                       /* about 1 / w (finds the cell; its bounds decide) */
+  float e0, de;                   /* E_min and E_max - E_min of the cells */
   int ncell;                      /* 0: no cells, every history takes speed_run_blocks */
+  int pad;
   uint8_t cell[SPEED_CELLS];
 };
 #define SPEED_TAB_WORDS ((int)(sizeof(SpeedTab) / 4))
 
-LA_FN void speed_cell_bounds(float iv0, float w, int c, float* lo, float* hi) {
-  *lo = iv0 + (float)c * w;
-  *hi = iv0 + (float)(c + 1) * w;
+/* u01fixedpt_closed_closed_32_24 (Random123 u01fixedpt.h:137-140), as the
+ * moderator's draw computes it */
+LA_FN float la_u01(uint32_t i) {
+  return (float)((i & 0x7fffffc0u) + (i & 0x40u)) * (1.0f / 2147483648.0f);
+}
+
+/* 1 / speed of a neutron of energy e (meV): correctly rounded square root
+ * and division, both monotone */
+LA_FN float speed_iv(float e) { return 1.0f / (RC_SE2V * sqrtf(e)); }
+
+/* 1 / speed of the energy drawn from word x */
+LA_FN float speed_iv_of_word(uint32_t x, float e0, float de) {
+  return speed_iv(e0 + de * la_u01(x));
+}
+
+/* the 1 / speed range [*lo, *hi] of the words of cell c */
+LA_FN void speed_word_cell(int c, float e0, float de, float* lo, float* hi) {
+  const uint32_t first = (uint32_t)c << SPEED_CELL_SHIFT;
+  const uint32_t last = first | ((1u << SPEED_CELL_SHIFT) - 1u);   /* bit 31 is not read */
+  const float a = speed_iv_of_word(first, e0, de), b = speed_iv_of_word(last, e0, de);
+  *lo = fminf(a, b);
+  *hi = fmaxf(a, b);
 }
 
 /* SPEED_BLOCKED, SPEED_KEPT or SPEED_MIXED for chopper q over iv in [lo, hi] */
@@ -366,7 +393,7 @@ LA_FN int speed_chopper_range(const SpeedRun& R, int q, float lo, float hi) {
   return SPEED_MIXED;
 }
 
-/* the verdict of a cell over the whole run */
+/* the verdict of a range of iv over the whole run */
 LA_FN int speed_cell_verdict(const SpeedRun& R, float lo, float hi) {
   if (!(lo > 0.0f) || !(hi < 1e30f) || !(lo <= hi)) return SPEED_MIXED;
   bool all_kept = true;
@@ -378,37 +405,22 @@ LA_FN int speed_cell_verdict(const SpeedRun& R, float lo, float hi) {
   return all_kept ? SPEED_KEPT : SPEED_MIXED;
 }
 
-/* cells spread over [iv_a, iv_b] */
-LA_FN void speed_tab_range(SpeedTab* T, float iv_a, float iv_b) {
-  T->ncell = 0;
-  T->iv0 = 0.0f;
-  T->w = 0.0f;
-  T->iw = 0.0f;
-  if (!(iv_a > 0.0f) || !(iv_b > iv_a) || !(iv_b < 1e30f)) return;
-  T->iv0 = iv_a;
-  T->w = (iv_b - iv_a) / (float)SPEED_CELLS;
-  if (!(T->w > 0.0f)) return;
-  T->iw = 1.0f / T->w;
-  T->ncell = SPEED_CELLS;
+/* cells over the energies [e0, e0 + de] (none unless both are finite) */
+LA_FN void speed_tab_range(SpeedTab* T, float e0, float de) {
+  T->e0 = e0;
+  T->de = de;
+  T->ncell = (e0 == e0 && de == de && fabsf(e0) < 1e30f && fabsf(de) < 1e30f) ? SPEED_CELLS : 0;
 }
 
-/* true: no neutron with 1 / speed = iv can pass the run (the table's
- * answer where its cell has one, else speed_run_blocks) */
-LA_FN bool speed_tab_blocks(const SpeedTab& T, float iv) {
+/* true: no neutron whose energy draw gave word x can pass the run (the
+ * table's answer where its cell has one, else speed_run_blocks) */
+LA_FN bool speed_tab_blocks(const SpeedTab& T, uint32_t x) {
   if (T.ncell > 0) {
-    const float f = (iv - T.iv0) * T.iw;
-    if (f >= 0.0f && f < (float)T.ncell) {
-      const int c = (int)f;
-      float lo, hi;
-      speed_cell_bounds(T.iv0, T.w, c, &lo, &hi);
-      if (iv >= lo && iv <= hi) {
-        const int v = T.cell[c];
-        if (v == SPEED_BLOCKED) return true;
-        if (v == SPEED_KEPT) return false;
-      }
-    }
+    const int v = T.cell[(x >> SPEED_CELL_SHIFT) & (SPEED_CELLS - 1)];
+    if (v == SPEED_BLOCKED) return true;
+    if (v == SPEED_KEPT) return false;
   }
-  return speed_run_blocks(T.run, iv);
+  return speed_run_blocks(T.run, speed_iv_of_word(x, T.e0, T.de));
 }
 
 #ifdef __CUDACC__
@@ -430,7 +442,7 @@ __device__ __forceinline__ void speed_run_setup(SpeedRun* R, int* blocked, bool 
   const int nq = R->n;
   if (nq > 1) {
     const float e = p[5] + (p[6] - p[5]) * (((float)threadIdx.x + 0.5f) / (float)blockDim.x);
-    const float iv = rsqrtf(e) * (1.0f / RC_SE2V);
+    const float iv = speed_iv(e);
     for (int q = 0; q < nq; ++q) {
       const unsigned m = __ballot_sync(0xffffffffu, speed_chopper_blocks(*R, q, iv));
       if ((threadIdx.x & 31) == 0 && m != 0u) atomicAdd(&blocked[q], __popc(m));
@@ -446,28 +458,19 @@ __device__ __forceinline__ void speed_run_setup(SpeedRun* R, int* blocked, bool 
  * (cta + 1) blockDim.x) and CTA 0 also writing the run and the cell
  * layout; T and blocked in shared memory.  The run is the one at component
  * 0 (nl components) for a flat or MCont source with parameters p; the
- * cells cover 1 / speed of the source's energy range (flat_mod.cl,
- * cont_mod.cl:36: v = SE2V sqrt(E), E uniform in [E_min, E_max]) widened
- * by 1e-5 of it. */
+ * cells are those of the energy draw's word over [E_min, E_max]. */
 __device__ __forceinline__ void speed_tab_build(uint32_t* dst, SpeedTab* T, int* blocked,
                                                 const CompDev* comps, int nl, const float* p,
                                                 int cta) {
   speed_run_setup(&T->run, blocked, true, comps, nl, p);
-  if (threadIdx.x == 0) {
-    const float e_lo = fminf(p[5], p[6]), e_hi = fmaxf(p[5], p[6]);
-    if (e_lo > 0.0f)
-      speed_tab_range(T, rsqrtf(e_hi) * (1.0f / RC_SE2V) * (1.0f - 1e-5f),
-                      rsqrtf(e_lo) * (1.0f / RC_SE2V) * (1.0f + 1e-5f));
-    else
-      speed_tab_range(T, 0.0f, 0.0f);
-  }
+  if (threadIdx.x == 0) speed_tab_range(T, p[5], p[6] - p[5]);
   __syncthreads();
   const int c = cta * (int)blockDim.x + (int)threadIdx.x;
   if (c < SPEED_CELLS) {
     int v = SPEED_MIXED;
     if (T->ncell > 0) {
       float lo, hi;
-      speed_cell_bounds(T->iv0, T->w, c, &lo, &hi);
+      speed_word_cell(c, T->e0, T->de, &lo, &hi);
       v = speed_cell_verdict(T->run, lo, hi);
     }
     reinterpret_cast<uint8_t*>(dst)[offsetof(SpeedTab, cell) + c] = (uint8_t)v;

@@ -85,19 +85,20 @@ def culled(inst, k, records):
     return out.astype(bool)
 
 
-def speed_culled(inst, k, records):
-    """The speed-only bound (ramp_debug_speed_cull) for each neutron's
-    speed after the moderator."""
+def speed_culled(inst, k, n, seed):
+    """The speed-only bound (ramp_debug_speed_cull) for neutrons 0..n-1 of
+    a reference-keyed run with this chunk seed: neutron i's energy draw is
+    the Threefry word of counter seed and index i."""
     keep = []
     src, carr, nc, barr, nb = inst.descriptors(keep)
-    rec = np.asarray(records, dtype=np.float64)
-    v = np.ascontiguousarray(np.sqrt((rec[:, 3:6] ** 2).sum(axis=1)), dtype=np.float32)
-    p = np.ascontiguousarray(np.array(src.p[0:5], dtype=np.float32))
-    out = np.zeros(len(v), np.uint8)
+    words = np.ascontiguousarray(oracle.threefry(np.full(n, seed, np.uint32),
+                                                 np.arange(n, dtype=np.uint32)))
+    p = np.ascontiguousarray(np.array(src.p[0:7], dtype=np.float32))
+    out = np.zeros(n, np.uint8)
     check = np.zeros(2, np.int64)
     lib = _abi.load()
     rc = lib.ramp_debug_speed_cull(ctypes.addressof(carr), nc, ctypes.addressof(barr), nb, k,
-                                   p.ctypes.data, v.ctypes.data, len(v), out.ctypes.data,
+                                   p.ctypes.data, words.ctypes.data, n, out.ctypes.data,
                                    check.ctypes.data)
     _abi.check(lib, rc, "ramp_debug_speed_cull")
     assert check[1] == 0          # the speed table agrees with the per-chopper test
@@ -105,44 +106,29 @@ def speed_culled(inst, k, records):
 
 
 def test_speed_table_equals_the_per_chopper_test():
-    """The cells of the speed table (lookahead.h) decide most speeds, and
-    every speed they decide gets the per-chopper test's answer, also at and
-    a few ulp either side of every cell boundary."""
+    """The cells of the speed table (lookahead.h) decide most energy draws,
+    and every draw they decide gets the per-chopper test's answer, also for
+    the first and last words of every cell and their neighbours."""
     import ramp_gb300 as m
     from ramp_gb300 import instruments as I
     inst = m.Instrument(I.path("let_like.json"), "cpu", **I.let_like_kwargs())
     src, carr, nc, barr, nb = inst.descriptors([])
-    e0, e1 = float(src.p[5]), float(src.p[6])
     rng = np.random.default_rng(5)
-    E = rng.uniform(e0, e1, 1_000_000).astype(np.float32)
-    v = (np.float32(437.393377) * np.sqrt(E)).astype(np.float32)
-    v[0] = np.float32(437.393377) * np.sqrt(np.float32(e0))
-    v[1] = np.float32(437.393377) * np.sqrt(np.float32(e1))
-    # speeds whose 1 / v lands on and beside the cell boundaries (the host
-    # spreads the cells over [min 1/v, max 1/v], as the device's layout)
-    iv = (np.float32(1.0) / v).astype(np.float32)
-    a, b = iv.min(), iv.max()
-    w = np.float32((b - a) / np.float32(4096))
-    lo = (a + np.arange(1, 4096, dtype=np.float32) * w).astype(np.float32)
-    s0 = (np.float32(1.0) / lo).astype(np.float32)
-    extra = [s0]
-    for k in range(1, 4):
-        extra += [np.nextafter(extra[-1] if k > 1 else s0, np.float32(np.inf)).astype(np.float32)]
-    down = s0
-    for k in range(1, 4):
-        down = np.nextafter(down, np.float32(0)).astype(np.float32)
-        extra.append(down)
-    v = np.ascontiguousarray(np.concatenate([v] + extra), dtype=np.float32)
-    p = np.ascontiguousarray(np.array(src.p[0:5], dtype=np.float32))
-    out = np.zeros(len(v), np.uint8)
+    rand = rng.integers(0, 1 << 32, 1_000_000, dtype=np.uint64).astype(np.uint32)
+    first = (np.arange(4096, dtype=np.uint64) << 19).astype(np.uint32)
+    edges = [first, first + np.uint32(1), first + np.uint32(64), first - np.uint32(1),
+             first - np.uint32(64), first | np.uint32(1 << 31)]
+    words = np.ascontiguousarray(np.concatenate([rand] + edges), dtype=np.uint32)
+    p = np.ascontiguousarray(np.array(src.p[0:7], dtype=np.float32))
+    out = np.zeros(len(words), np.uint8)
     check = np.zeros(2, np.int64)
     lib = _abi.load()
     _abi.check(lib, lib.ramp_debug_speed_cull(ctypes.addressof(carr), nc, ctypes.addressof(barr),
-                                              nb, 0, p.ctypes.data, v.ctypes.data, len(v),
-                                              out.ctypes.data, check.ctypes.data),
+                                              nb, 0, p.ctypes.data, words.ctypes.data,
+                                              len(words), out.ctypes.data, check.ctypes.data),
                "ramp_debug_speed_cull")
     assert check[1] == 0
-    assert check[0] > 0.9 * len(v)
+    assert check[0] > 0.99 * len(words)
     assert 0.01 < 1.0 - out[:1_000_000].mean() < 0.05     # about 2.8 % kept
 
 
@@ -165,7 +151,7 @@ def test_lookahead_never_retires_a_neutron_that_passes(tmp_path, Ei):
     # most of those that do not pass are retired before the guide
     assert cut.sum() >= 0.8 * (~passed).sum()
     # the speed-only bound retires a subset of those, and no passing one
-    scut = speed_culled(full, 0, after_mod)
+    scut = speed_culled(full, 0, N, seeds[0])
     assert not (scut & passed).any(), "the speed bound retired a neutron that passes"
     assert scut.sum() > 0.3 * (~passed).sum()
 
@@ -187,7 +173,7 @@ def test_lookahead_through_several_guides_never_retires_a_neutron_that_passes(tm
     assert passed.sum() > 20
     assert not (cut & passed).any(), "a neutron that passes the run was retired"
     assert cut.sum() >= 0.9 * (~passed).sum()
-    scut = speed_culled(full, 0, after_mod)
+    scut = speed_culled(full, 0, N, seeds[0])
     assert not (scut & passed).any(), "the speed bound retired a neutron that passes"
 
 
@@ -350,5 +336,5 @@ def test_lookahead_sound_on_random_runs(tmp_path, seed):
     cut = culled(full, 0, after_mod)
     assert passed.sum() > 50
     assert not (cut & passed).any(), "a neutron that passes the run was retired"
-    scut = speed_culled(full, 0, after_mod)
+    scut = speed_culled(full, 0, N, seed)
     assert not (scut & passed).any(), "the speed bound retired a neutron that passes"
